@@ -1,0 +1,205 @@
+"""Bindings of the CPU oracle (oracle/_build) and of the reference compiled as
+host code (oracle/_ref), and helpers that run a case through either.  Test
+infrastructure: used by tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline leg only."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import sys
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent.parent
+sys.path.insert(0, str(REPO / "mf-lbm-cuda_gb300"))
+sys.path.insert(0, str(REPO))
+
+from mflbm import abi  # noqa: E402
+from mflbm.abi import Layout, ptr  # noqa: E402
+from mflbm.cases import write_case_dir  # noqa: E402
+from oracle import build as obuild  # noqa: E402
+
+VP = C.c_void_p
+FLOAT_FIELDS = ["pdf", "phi", "cn_x", "cn_y", "cn_z", "c_norm", "curv", "W_in",
+                "f_convec_bc", "g_convec_bc", "phi_convec_bc", "s_nx", "s_ny", "s_nz"]
+STATE_FIELDS = ["pdf", "phi", "cn_x", "cn_y", "cn_z", "c_norm", "curv",
+                "f_convec_bc", "g_convec_bc", "phi_convec_bc"]
+
+
+def dtype_of(precision):
+    return np.float32 if precision == abi.MFLBM_FP32 else np.float64
+
+
+def suffix(precision):
+    return "f32" if precision == abi.MFLBM_FP32 else "f64"
+
+
+_ORACLE = None
+
+
+def oracle_lib():
+    global _ORACLE
+    if _ORACLE is None:
+        lib = C.CDLL(str(obuild.build_oracle()))
+        for s in ("f32", "f64"):
+            getattr(lib, f"orc_geometry_preprocess_{s}").argtypes = [VP] * 8
+            getattr(lib, f"orc_params_from_control_{s}").argtypes = [VP, C.c_int, VP, VP]
+            getattr(lib, f"orc_inlet_profile_{s}").argtypes = [VP, VP]
+            getattr(lib, f"orc_init_fields_{s}").argtypes = [VP, C.c_int, C.c_double] + [VP] * 5
+            getattr(lib, f"orc_color_gradient_{s}").argtypes = [VP] * 12
+            getattr(lib, f"orc_step_{s}").argtypes = [VP, C.c_int] + [VP] * 16
+            getattr(lib, f"orc_run_{s}").argtypes = [VP, C.c_int, C.c_int] + [VP] * 16
+            getattr(lib, f"orc_collide_{s}").argtypes = [VP, C.c_int] + [VP] * 8
+            getattr(lib, f"orc_macro_vars_{s}").argtypes = [VP] * 13
+            getattr(lib, f"orc_monitor_{s}").argtypes = [VP] * 9 + [C.c_int, C.c_int, VP]
+        lib.orc_set_walls.argtypes = [VP, VP, VP]
+        lib.orc_max_threads.restype = C.c_int
+        _ORACLE = lib
+    return _ORACLE
+
+
+class OracleState:
+    """A complete host state of one case in the reference layouts."""
+
+    def __init__(self, case, precision, fp_mode=abi.MFLBM_STRICT, geometry=None):
+        self.case = case
+        self.precision = precision
+        self.T = dtype_of(precision)
+        self.s = suffix(precision)
+        self.lib = oracle_lib()
+        self.control = case.control(precision)
+        nx, ny, nz = case.shape
+        self.L = L = Layout(nx, ny, nz)
+        self.geometry = case.geometry_bytes() if geometry is None else geometry
+        self.a = {}
+        for n in FLOAT_FIELDS:
+            self.a[n] = L.empty(abi.FIELD_KINDS[n], self.T)
+        for n in ("walls", "walls_type", "walls_global"):
+            self.a[n] = L.empty(abi.FIELD_KINDS[n], np.int32)
+        self.params = abi.Params()
+        self.derived = abi.Derived()
+        self.counts = abi.GeometryCounts()
+        f = lambda name: getattr(self.lib, f"orc_{name}_{self.s}")
+        self.lib.orc_set_walls(C.byref(self.control), ptr(np.ascontiguousarray(self.geometry)),
+                               ptr(self.a["walls_global"]))
+        f("geometry_preprocess")(C.byref(self.control), ptr(self.a["walls_global"]), ptr(self.a["walls"]),
+                                 ptr(self.a["walls_type"]), ptr(self.a["s_nx"]), ptr(self.a["s_ny"]),
+                                 ptr(self.a["s_nz"]), C.byref(self.counts))
+        f("params_from_control")(C.byref(self.control), fp_mode, C.byref(self.params), C.byref(self.derived))
+        f("inlet_profile")(C.byref(self.control), ptr(self.a["W_in"]))
+        f("init_fields")(C.byref(self.params), self.control.initial_fluid_distribution_option,
+                         self.derived.interface_z0, ptr(self.a["pdf"]), ptr(self.a["phi"]),
+                         ptr(self.a["f_convec_bc"]), ptr(self.a["g_convec_bc"]), ptr(self.a["phi_convec_bc"]))
+        self.color_gradient()
+        self.ntime = 1
+
+    def _f(self, name):
+        return getattr(self.lib, f"orc_{name}_{self.s}")
+
+    def color_gradient(self):
+        a = self.a
+        self._f("color_gradient")(C.byref(self.params), ptr(a["walls"]), ptr(a["walls_type"]), ptr(a["s_nx"]),
+                                  ptr(a["s_ny"]), ptr(a["s_nz"]), ptr(a["phi"]), ptr(a["cn_x"]), ptr(a["cn_y"]),
+                                  ptr(a["cn_z"]), ptr(a["c_norm"]), ptr(a["curv"]))
+
+    def run(self, nsteps):
+        a = self.a
+        self._f("run")(C.byref(self.params), self.ntime, nsteps, ptr(a["walls"]), ptr(a["walls_type"]),
+                       ptr(a["s_nx"]), ptr(a["s_ny"]), ptr(a["s_nz"]), ptr(a["pdf"]), ptr(a["phi"]),
+                       ptr(a["cn_x"]), ptr(a["cn_y"]), ptr(a["cn_z"]), ptr(a["c_norm"]), ptr(a["curv"]),
+                       ptr(a["W_in"]), ptr(a["f_convec_bc"]), ptr(a["g_convec_bc"]), ptr(a["phi_convec_bc"]))
+        self.ntime += nsteps
+
+    def macro(self):
+        """compute_macro_vars on a copy (rho, u, v, w and phi with solids zeroed)."""
+        a = self.a
+        out = {n: self.L.empty("s1", self.T) for n in ("rho", "u", "v", "w")}
+        phi = a["phi"].copy()
+        self._f("macro_vars")(C.byref(self.params), ptr(a["walls"]), ptr(a["pdf"]), ptr(phi), ptr(a["cn_x"]),
+                              ptr(a["cn_y"]), ptr(a["cn_z"]), ptr(a["c_norm"]), ptr(a["curv"]), ptr(out["rho"]),
+                              ptr(out["u"]), ptr(out["v"]), ptr(out["w"]))
+        out["phi"] = phi
+        return out
+
+    def monitor(self, nex_in=None, nex_out=None):
+        k = self.case.control_keys()
+        nex_in = int(k["n_exclude_inlet"]) if nex_in is None else nex_in
+        nex_out = int(k["n_exclude_outlet"]) if nex_out is None else nex_out
+        a = self.a
+        m = abi.Monitor()
+        self._f("monitor")(C.byref(self.params), ptr(a["walls"]), ptr(a["pdf"]), ptr(a["phi"]), ptr(a["cn_x"]),
+                           ptr(a["cn_y"]), ptr(a["cn_z"]), ptr(a["c_norm"]), ptr(a["curv"]), nex_in, nex_out,
+                           C.byref(m))
+        return m.as_dict()
+
+
+# ---------------------------------------------------------------------------
+# The reference compiled as host code.  Its state is global, so each case runs
+# in a fresh process (see run_reference_case).
+# ---------------------------------------------------------------------------
+def ref_lib(precision):
+    paths = obuild.build_ref()
+    if not paths:
+        return None
+    lib = C.CDLL(str(paths[suffix(precision)]))
+    lib.ref_init.argtypes = [C.c_char_p]
+    lib.ref_init.restype = C.c_int
+    lib.ref_step.argtypes = [C.c_int]
+    lib.ref_ptr.argtypes = [C.c_char_p]
+    lib.ref_ptr.restype = VP
+    lib.ref_scalar.argtypes = [C.c_char_p]
+    lib.ref_scalar.restype = C.c_double
+    return lib
+
+
+def ref_array(lib, L, name, T):
+    kind = abi.FIELD_KINDS[name]
+    dt = np.int32 if name in abi.INT_FIELDS else T
+    n = int(np.prod(L.shape(kind)))
+    p = lib.ref_ptr(name.encode())
+    if not p:
+        return None
+    buf = (C.c_char * (n * np.dtype(dt).itemsize)).from_address(p)
+    return np.frombuffer(buf, dtype=dt).reshape(L.shape(kind)).copy()
+
+
+def run_reference_case(case, precision, checkpoints, fields=STATE_FIELDS, workdir=None):
+    """Run `case` through oracle/_ref; returns {step: {field: array}} at each
+    checkpoint step (0 = after start-up) plus '_scalars'."""
+    lib = ref_lib(precision)
+    if lib is None:
+        raise RuntimeError("reference sources unavailable")
+    T = dtype_of(precision)
+    L = Layout(*case.shape)
+    tmp = workdir or tempfile.mkdtemp(prefix="mflbm_ref_")
+    write_case_dir(case, tmp)
+    devnull = os.open(os.devnull, os.O_WRONLY)
+    saved = os.dup(1)
+    os.dup2(devnull, 1)
+    try:
+        rc = lib.ref_init(tmp.encode())
+    finally:
+        os.dup2(saved, 1)
+        os.close(devnull)
+        os.close(saved)
+    if rc != 0:
+        raise RuntimeError(f"ref_init failed ({rc})")
+    out = {}
+    grab = lambda: {n: ref_array(lib, L, n, T) for n in fields}
+    scal = ["lbm_gamma", "force_z", "la_nui1", "la_nui2", "lbm_beta", "phi_inlet", "sa_inject", "uin_avg",
+            "relaxation", "cos_theta", "rho_in", "rho_out", "num_solid_boundary_global",
+            "num_fluid_boundary_global", "num_solid_boundary", "num_fluid_boundary", "pore_sum",
+            "interface_z0", "A_xy", "uin_avg_0", "flowrate"]
+    out["_scalars"] = {n: lib.ref_scalar(n.encode()) for n in scal}
+    out["_geometry"] = {n: ref_array(lib, L, n, T) for n in ("walls", "walls_type", "s_nx", "s_ny", "s_nz", "W_in")}
+    if 0 in checkpoints:
+        out[0] = grab()
+    nt = 1
+    for cp in sorted(c for c in checkpoints if c > 0):
+        while nt <= cp:
+            lib.ref_step(nt)
+            nt += 1
+        out[cp] = grab()
+    return out
