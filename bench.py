@@ -1,0 +1,332 @@
+"""Throughput benchmark of the MF-LBM hot path on GB300.
+
+Workload: two-phase drainage on a 256 x 256 x 256 lattice (flow along z,
+walls on x and y), seeded overlapping-sphere pack r ~ U[4, 10] at porosity
+0.45, tau 0.8/0.8, gamma 0.005, contact angle 30 deg, velocity inlet
+u = 5e-5, convective outlet; FP32 populations (the reference's default
+precision).  A step is one lattice-Boltzmann time step (collision+streaming,
+boundaries, colour gradient).  MLUPS counts all lattice nodes, solids
+included, as the reference does (src/main.cpp:194-197).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+N > 1 runs under torchrun as independent replicas (one lattice per GPU, no
+collective on the data path; the reference has no domain decomposition).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+PKG = REPO / "mf-lbm-cuda_gb300"
+for p in (str(PKG), str(REPO)):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+# Algorithmic bytes per fluid-node update (FP32 populations): 38 populations
+# read and written once (304 B); the phase field written by the collision and
+# read by the gradient step (8 B); plus one mask byte per lattice node.
+POP_BYTES = 4
+STEP_BYTES_PER_FLUID = 2 * 38 * POP_BYTES + 2 * 4
+# the collision kernel's share: populations in and out plus its phase-field write
+COLLIDE_BYTES_PER_FLUID = 2 * 38 * POP_BYTES + 4
+MASK_BYTES_PER_NODE = 1
+
+
+def peaks():
+    f = REPO / "MEASURED_PEAKS.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            parts = [x.strip() for x in l.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def read_traffic_profile():
+    """DRAM bytes per fluid node of the collision kernel from the committed ncu summary."""
+    f = REPO / "profiles" / "collide_stream_drainage.md"
+    if not f.exists():
+        return None, None
+    m = re.search(r"dram_bytes_per_fluid_node:\s*([0-9.]+)", f.read_text())
+    return (float(m.group(1)), f.name) if m else (None, None)
+
+
+def dist_setup(gpus):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        return rank, world, local, dist
+    return rank, world, local, None
+
+
+def max_over_ranks(dist, value):
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def cpu_reference_run(case, steps, warmup, budget_s=90.0):
+    """The oracle (CPU restatement of the reference's kernels, OpenMP) on the
+    same workload; the number of timed steps is capped to stay within budget."""
+    sys.path.insert(0, str(REPO / "tests"))
+    import oracle_harness as H
+    from mflbm import abi
+    geo = case.geometry_bytes()
+    t0 = time.perf_counter()
+    o = H.OracleState(case, abi.MFLBM_FP32, geometry=geo)
+    setup_s = time.perf_counter() - t0
+    threads = int(H.oracle_lib().orc_max_threads())
+    t0 = time.perf_counter()
+    o.run(max(1, warmup))
+    t_step = (time.perf_counter() - t0) / max(1, warmup)
+    n = int(max(2, min(steps, budget_s / max(t_step, 1e-6))))
+    t0 = time.perf_counter()
+    o.run(n)
+    dt = time.perf_counter() - t0
+    nx, ny, nz = case.shape
+    return {"mlups": nx * ny * nz * n / dt / 1e6, "steps": n, "seconds": dt, "threads": threads,
+            "setup_s": setup_s}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--size", type=int, default=256, help="lattice edge (default: the 256^3 workload)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    warmup = max(3, args.warmup)
+
+    from mflbm import abi, cases
+    case = cases.drainage_256x256x256()
+    if args.size != 256:
+        case.keys.update({"nxGlobal": args.size, "nyGlobal": args.size, "nzGlobal": args.size})
+        case.name = f"drainage_{args.size}x{args.size}x{args.size}"
+    nx, ny, nz = case.shape
+    n_all = nx * ny * nz
+    metric = f"MLUPS at {nx}^3 (all-node lattice updates per second, reference definition)"
+    data = ("synthetic: seeded overlapping-sphere pack, radii U[4,10], porosity 0.45, seed 1200, "
+            "2-layer inlet/outlet buffers (stands in for the reference's micro-CT inputs)")
+
+    rank, world, local, dist = dist_setup(args.gpus)
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        r = cpu_reference_run(case, args.steps, warmup)
+        line = {"impl": "reference", "metric": metric, "value": round(r["mlups"], 3), "unit": "MLUPS",
+                "n_gpus": args.gpus, "steps": r["steps"], "warmup": warmup,
+                "ms_per_step": r["seconds"] / r["steps"] * 1e3, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": data,
+                "config": {"workload": case.name, "lattice": [nx, ny, nz], "precision": "fp32"},
+                "cpu_baseline": {"value": round(r["mlups"], 3), "unit": "MLUPS", "cores": r["threads"],
+                                 "kind": "port",
+                                 "sample": f"{r['steps']} time steps of the full {nx}^3 workload after {warmup} "
+                                           f"warm-up steps (oracle: CPU restatement of the reference kernels, "
+                                           f"OpenMP, {r['threads']} threads); reference checkout absent on this host"},
+                "e2e": {"value": round(r["mlups"], 3), "unit": "MLUPS", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    from mflbm import lib
+    lib.load()
+    ctx, info = lib.setup_case(case, abi.MFLBM_FP32, abi.MFLBM_FAST)
+    n_fluid, _ = ctx.node_counts()
+    porosity = n_fluid / n_all
+
+    # launches per step (counted on eager steps)
+    c0 = lib.load().mflbm_kernel_launch_count()
+    ctx.step(1)
+    ctx.step(2)
+    ctx.sync()
+    launches_per_step = (lib.load().mflbm_kernel_launch_count() - c0) / 2
+    nt = 3
+    ctx.run(nt, warmup)
+    nt += warmup
+    ctx.sync()
+
+    # ---- timed region: K steps, state resident in HBM, graph-replayed ----
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(dist)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    ctx.run(nt, args.steps)
+    ev1.record(stream)
+    ctx.sync()
+    torch.cuda.synchronize()
+    barrier(dist)
+    clocks = sampler.stop()
+    elapsed_ms = ev0.elapsed_time(ev1)
+    nt += args.steps
+    t_max = max_over_ranks(dist, elapsed_ms)
+    value = world * n_all * args.steps / (t_max * 1e-3) / 1e6
+
+    # ---- per-kernel device time of the collision (events on the launching stream) ----
+    ktime_steps = min(args.steps, 200)
+    ctx.set_timing(True)
+    ctx.run(nt, ktime_steps)
+    nt += ktime_steps
+    tc, tg, ncoll = ctx.kernel_times()
+    ctx.set_timing(False)
+    collide_ms = tc / max(ncoll, 1)
+    gradient_ms = tg / max(ncoll, 1)
+    hbm, peak_kind = peaks()
+    coll_bytes = n_fluid * COLLIDE_BYTES_PER_FLUID + n_all * MASK_BYTES_PER_NODE
+    achieved = coll_bytes / (collide_ms * 1e-3) / 1e9
+    traffic_per_fluid, traffic_src = read_traffic_profile()
+    step_bytes = n_fluid * STEP_BYTES_PER_FLUID + n_all * MASK_BYTES_PER_NODE
+    step_ms = t_max / args.steps
+
+    # ---- end to end through the C ABI with pinned host buffers ----
+    e2e_steps = min(args.steps, 200)
+    L = ctx.L
+    host = {}
+    for n in ("pdf", "phi", "cn_x", "cn_y", "cn_z", "c_norm", "curv", "f_convec_bc", "g_convec_bc",
+              "phi_convec_bc", "W_in"):
+        shape = L.shape(abi.FIELD_KINDS[n])
+        host[n] = torch.empty(int(np.prod(shape)), dtype=torch.float32, pin_memory=True).numpy().reshape(shape)
+    d = ctx.download()
+    for n, a in d.items():
+        host[n][...] = a
+    host["W_in"][...] = info["W_in"]
+    h2d = sum(host[n].nbytes for n in host)
+    d2h = sum(host[n].nbytes for n in host if n != "W_in")
+    barrier(dist)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ctx.upload_fields(**host)
+    for s in range(e2e_steps):
+        ctx.step(nt + s)
+    out = ctx.download()
+    e2e_s = time.perf_counter() - t0
+    barrier(dist)
+    nt += e2e_steps
+    e2e_s = max_over_ranks(dist, e2e_s)
+    e2e_value = world * n_all * e2e_steps / e2e_s / 1e6
+    assert np.isfinite(out["phi"]).all()
+
+    mon = ctx.monitor(2, 2)
+
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        r = cpu_reference_run(case, 40, 3, budget_s=20.0)
+        cpu = {"value": round(r["mlups"], 3), "unit": "MLUPS", "cores": r["threads"], "kind": "port",
+               "sample": f"{r['steps']} time steps of the full {nx}^3 workload on the host cores "
+                         f"(oracle: CPU restatement of the reference kernels, OpenMP, FP32)"}
+    line = {
+        "metric": metric, "value": round(value, 2), "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
+        "warmup": warmup, "ms_per_step": round(step_ms, 5), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": data,
+        "config": {"workload": case.name, "lattice": [nx, ny, nz], "fluid_nodes": n_fluid,
+                   "porosity": round(porosity, 4), "precision": "fp32 populations, fp32 collision",
+                   "fp_mode": "fast", "l2": "inputs larger than L2 (populations 2.6 GB per replica), no flush",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "mflups": round(world * n_fluid * args.steps / (t_max * 1e-3) / 1e6, 2),
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                     "frac": round(achieved / hbm, 4), "peak_kind": peak_kind,
+                     "kernel": "collide_stream_kernel<float>", "kernel_ms": round(collide_ms, 5),
+                     "algorithmic_bytes_per_launch": coll_bytes,
+                     "traffic": (round(traffic_per_fluid * n_fluid) if traffic_per_fluid else None),
+                     "traffic_source": traffic_src},
+        "step_roofline": {"achieved": round(step_bytes / (step_ms * 1e-3) / 1e9, 1), "unit": "GB/s",
+                          "frac": round(step_bytes / (step_ms * 1e-3) / 1e9 / hbm, 4),
+                          "algorithmic_bytes_per_step": step_bytes, "gradient_ms": round(gradient_ms, 5)},
+        "e2e": {"value": round(e2e_value, 2), "unit": "MLUPS", "steps": e2e_steps,
+                "h2d_bytes_per_step": int(h2d / e2e_steps), "d2h_bytes_per_step": int(d2h / e2e_steps),
+                "how": "mflbm_upload_fields from pinned host buffers, mflbm_step per step, mflbm_download_fields"},
+        "gpu_launches": int(launches_per_step * args.steps),
+        "clocks": clocks,
+        "saturation": round(mon["saturation"], 6),
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line))
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()

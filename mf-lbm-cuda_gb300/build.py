@@ -1,0 +1,82 @@
+"""Build libmflbm.so (sm_103a) in-tree: mf-lbm-cuda_gb300/lib/libmflbm.so.
+
+Translation units compile in parallel:
+  step_fast.cu    step kernels with FMA contraction (production flavour)
+  step_strict.cu  the same kernels with -fmad=false (IEEE ops in reference order)
+  setup.cu        geometry preprocessing, start-up fields, FP64 reductions (-fmad=false)
+  capi.cu         the C ABI
+  host_setup.cpp  host parameter derivation and inlet profile (g++ -ffp-contract=off)
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+CSRC = PKG / "csrc"
+OUT = PKG / "lib"
+REPO = PKG.parent
+LIB = OUT / "libmflbm.so"
+
+NVCC = os.environ.get("NVCC", shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
+           "-Xcompiler", "-ffp-contract=off", *ARCH]
+UNITS = {
+    "step_fast.cu": [],
+    "step_strict.cu": ["-fmad=false"],
+    "setup.cu": ["-fmad=false"],
+    "capi.cu": [],
+}
+HEADERS = ["common.cuh", "context.cuh", "step_kernels.cuh", "setup.cuh"]
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"build step failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    return r.stdout + r.stderr
+
+
+def _stale(out: Path, deps) -> bool:
+    if not out.exists():
+        return True
+    t = out.stat().st_mtime
+    return any(Path(d).stat().st_mtime > t for d in deps)
+
+
+def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) -> Path:
+    OUT.mkdir(parents=True, exist_ok=True)
+    hdrs = [CSRC / h for h in HEADERS] + [REPO / "include" / "mflbm.h", Path(__file__)]
+    jobs, objs = [], []
+    for src, extra in UNITS.items():
+        obj = OUT / (Path(src).stem + ".o")
+        objs.append(obj)
+        if force or ptxas_info or _stale(obj, [CSRC / src, *hdrs]):
+            flags = list(NVFLAGS) + extra + (["-Xptxas", "-v"] if ptxas_info else [])
+            jobs.append([NVCC, *flags, "-c", str(CSRC / src), "-o", str(obj)])
+    host_obj = OUT / "host_setup.o"
+    objs.append(host_obj)
+    if force or _stale(host_obj, [CSRC / "host_setup.cpp", *hdrs]):
+        jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-c", str(CSRC / "host_setup.cpp"),
+                     "-o", str(host_obj)])
+    logs = []
+    if jobs:
+        with ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
+            logs = list(ex.map(_run, jobs))
+    if verbose or ptxas_info:
+        for l in logs:
+            sys.stdout.write(l)
+    if force or jobs or not LIB.exists():
+        tmp = LIB.with_suffix(".so.tmp")
+        _run([NVCC, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"])
+        os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True, ptxas_info="--ptxas" in sys.argv))

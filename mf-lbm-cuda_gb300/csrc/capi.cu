@@ -1,0 +1,436 @@
+// The C ABI of libmflbm (include/mflbm.h).
+#include <atomic>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "context.cuh"
+#include "setup.cuh"
+
+namespace mflbm {
+
+namespace {
+thread_local std::string g_last_error;
+std::atomic<unsigned long long> g_launches{0};
+
+struct TimingPool {
+    std::vector<cudaEvent_t> ev;  // 4 per timed step: collide start/end, gradient start/end
+    size_t used = 0;
+};
+TimingPool& timing_pool(mflbm_context* c);
+}  // namespace
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+namespace {
+
+size_t tsize(const mflbm_context* c) { return c->params.precision == MFLBM_FP32 ? 4 : 8; }
+
+int check_params(const mflbm_params* p) {
+    if (!p) return fail(MFLBM_E_ARG, "null params");
+    if (p->precision != MFLBM_FP32 && p->precision != MFLBM_FP64) return fail(MFLBM_E_ARG, "precision must be MFLBM_FP32 or MFLBM_FP64");
+    if (p->fp_mode != MFLBM_FAST && p->fp_mode != MFLBM_STRICT) return fail(MFLBM_E_ARG, "fp_mode must be MFLBM_FAST or MFLBM_STRICT");
+    if (p->nx < 3 || p->ny < 3 || p->nz < 4) return fail(MFLBM_E_ARG, "lattice must be at least 3 x 3 x 4");
+    if (p->nx + 8 >= 1024 || p->ny + 8 >= 2048 || p->nz + 8 >= 2048)
+        return fail(MFLBM_E_ARG, "lattice too large for packed node coordinates (nx <= 1015, ny, nz <= 2039)");
+    const ll n1 = (p->nx + 2) * (p->ny + 2) * (p->nz + 2);
+    if (n1 >= (1ll << 31)) return fail(MFLBM_E_ARG, "lattice too large: (nx+2)(ny+2)(nz+2) must be below 2^31");
+    if (p->inlet_BC < 0 || p->inlet_BC > 2 || p->outlet_BC < 0 || p->outlet_BC > 2) return fail(MFLBM_E_ARG, "inlet_BC/outlet_BC must be 0, 1 or 2");
+    if (p->porous_plate_cmd < 0 || p->porous_plate_cmd > 2) return fail(MFLBM_E_ARG, "porous_plate_cmd must be 0, 1 or 2");
+    return MFLBM_OK;
+}
+
+void free_all(mflbm_context* c) {
+    DeviceState& d = c->d;
+    void* ptrs[] = {d.pdf, d.phi, d.cn_x, d.cn_y, d.cn_z, d.c_norm, d.curv, d.W_in, d.f_cv, d.g_cv, d.phi_cv,
+                    d.walls, d.walls_type, d.s_nx, d.s_ny, d.s_nz, d.fluid_list, d.list_phi_ext, d.list_wet,
+                    d.list_cn_ext, d.red};
+    for (void* p : ptrs) if (p) cudaFree(p);
+    d = DeviceState{};
+    if (c->pair_graph) cudaGraphExecDestroy(c->pair_graph);
+    c->pair_graph = nullptr;
+}
+
+int alloc_zero(void** p, size_t bytes, cudaStream_t s) {
+    MFLBM_CUDA(cudaMalloc(p, bytes));
+    MFLBM_CUDA(cudaMemsetAsync(*p, 0, bytes, s));
+    return MFLBM_OK;
+}
+
+int upload_list(uint32_t** dptr, ll* n, const std::vector<uint32_t>& h) {
+    if (*dptr) cudaFree(*dptr);
+    *dptr = nullptr;
+    *n = (ll)h.size();
+    if (h.empty()) return MFLBM_OK;
+    MFLBM_CUDA(cudaMalloc(dptr, sizeof(uint32_t) * h.size()));
+    MFLBM_CUDA(cudaMemcpy(*dptr, h.data(), sizeof(uint32_t) * h.size(), cudaMemcpyHostToDevice));
+    return MFLBM_OK;
+}
+
+// Fluid-node and boundary-node lists from the device geometry (ascending
+// linear order, so consecutive threads touch consecutive x).
+int build_lists(mflbm_context* c) {
+    DeviceState& d = c->d;
+    const Grid g = d.g;
+    std::vector<int32_t> walls(g.n2()), wt(g.n4());
+    MFLBM_CUDA(cudaMemcpy(walls.data(), d.walls, sizeof(int32_t) * g.n2(), cudaMemcpyDeviceToHost));
+    MFLBM_CUDA(cudaMemcpy(wt.data(), d.walls_type, sizeof(int32_t) * g.n4(), cudaMemcpyDeviceToHost));
+    std::vector<uint32_t> fl, lphi, lwet, lcn;
+    for (int k = 1; k <= g.nz; ++k)
+        for (int j = 1; j <= g.ny; ++j)
+            for (int i = 1; i <= g.nx; ++i)
+                if (walls[g.s2(i, j, k)] == 0) fl.push_back(pack_xyz(i, j, k));
+    for (int k = -2; k <= g.nz + 3; ++k)
+        for (int j = -2; j <= g.ny + 3; ++j)
+            for (int i = -2; i <= g.nx + 3; ++i) {
+                const int v = wt[g.s4(i, j, k)];
+                const bool in1 = i >= -1 && i <= g.nx + 2 && j >= -1 && j <= g.ny + 2 && k >= -1 && k <= g.nz + 2;
+                const bool in0 = i >= 0 && i <= g.nx + 1 && j >= 0 && j <= g.ny + 1 && k >= 0 && k <= g.nz + 1;
+                if (v == 2) {
+                    lphi.push_back(pack_xyz(i, j, k));
+                    if (in0) lcn.push_back(pack_xyz(i, j, k));
+                }
+                if (v == -1 && in1) lwet.push_back(pack_xyz(i, j, k));
+            }
+    int rc;
+    if ((rc = upload_list(&d.fluid_list, &d.n_fluid, fl)) != MFLBM_OK) return rc;
+    if ((rc = upload_list(&d.list_phi_ext, &d.n_phi_ext, lphi)) != MFLBM_OK) return rc;
+    if ((rc = upload_list(&d.list_wet, &d.n_wet, lwet)) != MFLBM_OK) return rc;
+    if ((rc = upload_list(&d.list_cn_ext, &d.n_cn_ext, lcn)) != MFLBM_OK) return rc;
+    return MFLBM_OK;
+}
+
+int flavour_collide(mflbm_context* c, bool odd) {
+    return c->params.fp_mode == MFLBM_STRICT ? strict::collide(*c, odd) : fast::collide(*c, odd);
+}
+int flavour_boundaries(mflbm_context* c, bool odd) {
+    return c->params.fp_mode == MFLBM_STRICT ? strict::boundaries(*c, odd) : fast::boundaries(*c, odd);
+}
+int flavour_gradient(mflbm_context* c) {
+    return c->params.fp_mode == MFLBM_STRICT ? strict::gradient(*c) : fast::gradient(*c);
+}
+
+TimingPool& timing_pool(mflbm_context* c) {
+    static thread_local std::vector<std::pair<mflbm_context*, TimingPool*>> pools;
+    for (auto& p : pools) if (p.first == c) return *p.second;
+    pools.emplace_back(c, new TimingPool());
+    return *pools.back().second;
+}
+
+cudaEvent_t next_event(mflbm_context* c) {
+    TimingPool& tp = timing_pool(c);
+    if (tp.used == tp.ev.size()) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        tp.ev.push_back(e);
+    }
+    return tp.ev[tp.used++];
+}
+
+int one_step(mflbm_context* c, int ntime) {
+    const bool odd = (ntime % 2) != 0;
+    int rc;
+    if (c->timing) cudaEventRecord(next_event(c), c->stream);
+    if ((rc = flavour_collide(c, odd)) != MFLBM_OK) return rc;
+    if (c->timing) cudaEventRecord(next_event(c), c->stream);
+    if ((rc = flavour_boundaries(c, odd)) != MFLBM_OK) return rc;
+    if (c->timing) cudaEventRecord(next_event(c), c->stream);
+    if ((rc = flavour_gradient(c)) != MFLBM_OK) return rc;
+    if (c->timing) cudaEventRecord(next_event(c), c->stream);
+    return MFLBM_OK;
+}
+
+int require_ready(mflbm_context* c) {
+    if (!c) return fail(MFLBM_E_ARG, "null context");
+    if (!c->have_geometry) return fail(MFLBM_E_STATE, "geometry not set (mflbm_preprocess_geometry / mflbm_upload_geometry)");
+    if (!c->have_fields) return fail(MFLBM_E_STATE, "fields not set (mflbm_init_fields / mflbm_upload_fields)");
+    return MFLBM_OK;
+}
+
+int capture_pair(mflbm_context* c, int first_ntime) {
+    if (c->pair_graph) {
+        cudaGraphExecDestroy(c->pair_graph);
+        c->pair_graph = nullptr;
+    }
+    cudaGraph_t graph;
+    MFLBM_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = one_step(c, first_ntime);
+    if (rc == MFLBM_OK) rc = one_step(c, first_ntime + 1);
+    cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+    if (rc != MFLBM_OK) { if (e == cudaSuccess) cudaGraphDestroy(graph); return rc; }
+    if (e != cudaSuccess) return fail(MFLBM_E_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&c->pair_graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail(MFLBM_E_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    c->pair_graph_odd_first = first_ntime & 1;
+    return MFLBM_OK;
+}
+
+}  // namespace
+}  // namespace mflbm
+
+using namespace mflbm;
+
+extern "C" {
+
+int mflbm_abi_version(void) { return MFLBM_ABI_VERSION; }
+const char* mflbm_last_error(void) { return g_last_error.c_str(); }
+unsigned long long mflbm_kernel_launch_count(void) { return g_launches.load(); }
+
+int mflbm_create(const mflbm_params* params, mflbm_context** out) {
+    if (!out) return fail(MFLBM_E_ARG, "mflbm_create: null output pointer");
+    *out = nullptr;
+    int rc = check_params(params);
+    if (rc != MFLBM_OK) return rc;
+    mflbm_context* c = new mflbm_context();
+    c->params = *params;
+    DeviceState& d = c->d;
+    d.g = Grid{(int)params->nx, (int)params->ny, (int)params->nz};
+    d.precision = params->precision;
+    const Grid& g = d.g;
+    const size_t T = tsize(c);
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { delete c; return fail(MFLBM_E_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e)); }
+    struct { void** p; size_t bytes; } allocs[] = {
+        {&d.pdf, T * g.n1() * 38}, {&d.phi, T * g.n4()}, {&d.cn_x, T * g.n2()}, {&d.cn_y, T * g.n2()},
+        {&d.cn_z, T * g.n2()}, {&d.c_norm, T * g.n2()}, {&d.curv, T * g.n1()}, {&d.W_in, T * g.plane1()},
+        {&d.f_cv, T * g.plane1() * 19}, {&d.g_cv, T * g.plane1() * 19}, {&d.phi_cv, T * g.plane1()},
+        {(void**)&d.walls, sizeof(int32_t) * g.n2()}, {(void**)&d.walls_type, sizeof(int32_t) * g.n4()},
+        {&d.s_nx, T * g.n4()}, {&d.s_ny, T * g.n4()}, {&d.s_nz, T * g.n4()}};
+    for (auto& a : allocs) {
+        if ((rc = alloc_zero(a.p, a.bytes, c->stream)) != MFLBM_OK) {
+            free_all(c);
+            cudaStreamDestroy(c->stream);
+            delete c;
+            return rc == MFLBM_E_CUDA ? MFLBM_E_NOMEM : rc;
+        }
+    }
+    e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) { free_all(c); cudaStreamDestroy(c->stream); delete c; return fail(MFLBM_E_CUDA, cudaGetErrorString(e)); }
+    *out = c;
+    return MFLBM_OK;
+}
+
+int mflbm_destroy(mflbm_context* c) {
+    if (!c) return MFLBM_OK;
+    cudaStreamSynchronize(c->stream);
+    free_all(c);
+    TimingPool& tp = timing_pool(c);
+    for (auto e : tp.ev) cudaEventDestroy(e);
+    tp.ev.clear();
+    tp.used = 0;
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return MFLBM_OK;
+}
+
+int mflbm_set_params(mflbm_context* c, const mflbm_params* p) {
+    if (!c) return fail(MFLBM_E_ARG, "null context");
+    int rc = check_params(p);
+    if (rc != MFLBM_OK) return rc;
+    if (p->nx != c->params.nx || p->ny != c->params.ny || p->nz != c->params.nz || p->precision != c->params.precision)
+        return fail(MFLBM_E_ARG, "mflbm_set_params cannot change the lattice size or precision");
+    c->params = *p;
+    if (c->pair_graph) { cudaGraphExecDestroy(c->pair_graph); c->pair_graph = nullptr; }
+    return MFLBM_OK;
+}
+
+int mflbm_preprocess_geometry(mflbm_context* c, const int32_t* walls_global, int32_t* walls, int32_t* walls_type,
+                              void* s_nx, void* s_ny, void* s_nz, mflbm_geometry_counts* counts) {
+    if (!c || !walls_global) return fail(MFLBM_E_ARG, "mflbm_preprocess_geometry: null argument");
+    int rc = preprocess_geometry(*c, walls_global, 0);
+    if (rc != MFLBM_OK) return rc;
+    if ((rc = build_lists(c)) != MFLBM_OK) return rc;
+    c->have_geometry = true;
+    const Grid& g = c->d.g;
+    const size_t T = tsize(c);
+    if (walls) MFLBM_CUDA(cudaMemcpy(walls, c->d.walls, sizeof(int32_t) * g.n2(), cudaMemcpyDeviceToHost));
+    if (walls_type) MFLBM_CUDA(cudaMemcpy(walls_type, c->d.walls_type, sizeof(int32_t) * g.n4(), cudaMemcpyDeviceToHost));
+    if (s_nx) MFLBM_CUDA(cudaMemcpy(s_nx, c->d.s_nx, T * g.n4(), cudaMemcpyDeviceToHost));
+    if (s_ny) MFLBM_CUDA(cudaMemcpy(s_ny, c->d.s_ny, T * g.n4(), cudaMemcpyDeviceToHost));
+    if (s_nz) MFLBM_CUDA(cudaMemcpy(s_nz, c->d.s_nz, T * g.n4(), cudaMemcpyDeviceToHost));
+    if (counts) {
+        std::vector<int32_t> wt(g.n4()), w(g.n2());
+        MFLBM_CUDA(cudaMemcpy(wt.data(), c->d.walls_type, sizeof(int32_t) * g.n4(), cudaMemcpyDeviceToHost));
+        MFLBM_CUDA(cudaMemcpy(w.data(), c->d.walls, sizeof(int32_t) * g.n2(), cudaMemcpyDeviceToHost));
+        *counts = mflbm_geometry_counts{};
+        for (int k = -3; k <= g.nz + 4; ++k)
+            for (int j = -3; j <= g.ny + 4; ++j)
+                for (int i = -3; i <= g.nx + 4; ++i) {
+                    const int v = wt[g.s4(i, j, k)];
+                    const bool in3 = i >= -2 && i <= g.nx + 3 && j >= -2 && j <= g.ny + 3 && k >= -2 && k <= g.nz + 3;
+                    if (v == 2) { counts->num_solid_boundary_global++; if (in3) counts->num_solid_boundary++; }
+                    if (v == -1) { counts->num_fluid_boundary_global++; if (in3) counts->num_fluid_boundary++; }
+                }
+        counts->pore_sum = c->d.n_fluid;
+    }
+    return MFLBM_OK;
+}
+
+int mflbm_upload_geometry(mflbm_context* c, const int32_t* walls, const int32_t* walls_type, const void* s_nx,
+                          const void* s_ny, const void* s_nz) {
+    if (!c || !walls || !walls_type || !s_nx || !s_ny || !s_nz) return fail(MFLBM_E_ARG, "mflbm_upload_geometry: null argument");
+    const Grid& g = c->d.g;
+    const size_t T = tsize(c);
+    MFLBM_CUDA(cudaMemcpy(c->d.walls, walls, sizeof(int32_t) * g.n2(), cudaMemcpyHostToDevice));
+    MFLBM_CUDA(cudaMemcpy(c->d.walls_type, walls_type, sizeof(int32_t) * g.n4(), cudaMemcpyHostToDevice));
+    MFLBM_CUDA(cudaMemcpy(c->d.s_nx, s_nx, T * g.n4(), cudaMemcpyHostToDevice));
+    MFLBM_CUDA(cudaMemcpy(c->d.s_ny, s_ny, T * g.n4(), cudaMemcpyHostToDevice));
+    MFLBM_CUDA(cudaMemcpy(c->d.s_nz, s_nz, T * g.n4(), cudaMemcpyHostToDevice));
+    int rc = build_lists(c);
+    if (rc != MFLBM_OK) return rc;
+    c->have_geometry = true;
+    return MFLBM_OK;
+}
+
+int mflbm_init_fields(mflbm_context* c, int option, double interface_z0, const void* W_in) {
+    if (!c) return fail(MFLBM_E_ARG, "null context");
+    if (!c->have_geometry) return fail(MFLBM_E_STATE, "geometry must be set before mflbm_init_fields");
+    if (option < 1 || option > 5) return fail(MFLBM_E_ARG, "initial_fluid_distribution_option must be 1-5");
+    const Grid& g = c->d.g;
+    if (W_in) MFLBM_CUDA(cudaMemcpyAsync(c->d.W_in, W_in, tsize(c) * g.plane1(), cudaMemcpyHostToDevice, c->stream));
+    int rc = init_fields(*c, option, interface_z0);
+    if (rc != MFLBM_OK) return rc;
+    if ((rc = flavour_gradient(c)) != MFLBM_OK) return rc;
+    MFLBM_CUDA(cudaStreamSynchronize(c->stream));
+    c->have_fields = true;
+    return MFLBM_OK;
+}
+
+int mflbm_upload_fields(mflbm_context* c, const void* pdf, const void* phi, const void* cn_x, const void* cn_y,
+                        const void* cn_z, const void* c_norm, const void* curv, const void* W_in,
+                        const void* f_convec_bc, const void* g_convec_bc, const void* phi_convec_bc) {
+    if (!c || !pdf || !phi) return fail(MFLBM_E_ARG, "mflbm_upload_fields: pdf and phi are required");
+    if (!c->have_geometry) return fail(MFLBM_E_STATE, "geometry must be set before mflbm_upload_fields");
+    DeviceState& d = c->d;
+    const Grid& g = d.g;
+    const size_t T = tsize(c);
+    cudaStream_t s = c->stream;
+    MFLBM_CUDA(cudaMemcpyAsync(d.pdf, pdf, T * g.n1() * 38, cudaMemcpyHostToDevice, s));
+    MFLBM_CUDA(cudaMemcpyAsync(d.phi, phi, T * g.n4(), cudaMemcpyHostToDevice, s));
+    if (W_in) MFLBM_CUDA(cudaMemcpyAsync(d.W_in, W_in, T * g.plane1(), cudaMemcpyHostToDevice, s));
+    const bool have_grad = cn_x && cn_y && cn_z && c_norm && curv;
+    if (have_grad) {
+        MFLBM_CUDA(cudaMemcpyAsync(d.cn_x, cn_x, T * g.n2(), cudaMemcpyHostToDevice, s));
+        MFLBM_CUDA(cudaMemcpyAsync(d.cn_y, cn_y, T * g.n2(), cudaMemcpyHostToDevice, s));
+        MFLBM_CUDA(cudaMemcpyAsync(d.cn_z, cn_z, T * g.n2(), cudaMemcpyHostToDevice, s));
+        MFLBM_CUDA(cudaMemcpyAsync(d.c_norm, c_norm, T * g.n2(), cudaMemcpyHostToDevice, s));
+        MFLBM_CUDA(cudaMemcpyAsync(d.curv, curv, T * g.n1(), cudaMemcpyHostToDevice, s));
+    }
+    if (f_convec_bc) MFLBM_CUDA(cudaMemcpyAsync(d.f_cv, f_convec_bc, T * g.plane1() * 19, cudaMemcpyHostToDevice, s));
+    if (g_convec_bc) MFLBM_CUDA(cudaMemcpyAsync(d.g_cv, g_convec_bc, T * g.plane1() * 19, cudaMemcpyHostToDevice, s));
+    if (phi_convec_bc) MFLBM_CUDA(cudaMemcpyAsync(d.phi_cv, phi_convec_bc, T * g.plane1(), cudaMemcpyHostToDevice, s));
+    if (!have_grad) {
+        int rc = flavour_gradient(c);
+        if (rc != MFLBM_OK) return rc;
+    }
+    MFLBM_CUDA(cudaStreamSynchronize(s));
+    c->have_fields = true;
+    return MFLBM_OK;
+}
+
+int mflbm_download_fields(mflbm_context* c, void* pdf, void* phi, void* cn_x, void* cn_y, void* cn_z, void* c_norm,
+                          void* curv, void* f_convec_bc, void* g_convec_bc, void* phi_convec_bc) {
+    if (!c) return fail(MFLBM_E_ARG, "null context");
+    DeviceState& d = c->d;
+    const Grid& g = d.g;
+    const size_t T = tsize(c);
+    cudaStream_t s = c->stream;
+    struct { void* dst; const void* src; size_t n; } cp[] = {
+        {pdf, d.pdf, T * g.n1() * 38}, {phi, d.phi, T * g.n4()}, {cn_x, d.cn_x, T * g.n2()}, {cn_y, d.cn_y, T * g.n2()},
+        {cn_z, d.cn_z, T * g.n2()}, {c_norm, d.c_norm, T * g.n2()}, {curv, d.curv, T * g.n1()},
+        {f_convec_bc, d.f_cv, T * g.plane1() * 19}, {g_convec_bc, d.g_cv, T * g.plane1() * 19},
+        {phi_convec_bc, d.phi_cv, T * g.plane1()}};
+    for (auto& x : cp)
+        if (x.dst) MFLBM_CUDA(cudaMemcpyAsync(x.dst, x.src, x.n, cudaMemcpyDeviceToHost, s));
+    MFLBM_CUDA(cudaStreamSynchronize(s));
+    return MFLBM_OK;
+}
+
+int mflbm_step(mflbm_context* c, int ntime) {
+    int rc = require_ready(c);
+    if (rc != MFLBM_OK) return rc;
+    return one_step(c, ntime);
+}
+
+int mflbm_run(mflbm_context* c, int ntime_begin, int nsteps) {
+    int rc = require_ready(c);
+    if (rc != MFLBM_OK) return rc;
+    if (nsteps <= 0) return MFLBM_OK;
+    if (c->timing || nsteps < 4) {
+        for (int s = 0; s < nsteps; ++s)
+            if ((rc = one_step(c, ntime_begin + s)) != MFLBM_OK) return rc;
+        return MFLBM_OK;
+    }
+    int nt = ntime_begin, left = nsteps;
+    // the graph holds an (odd, even) pair
+    if ((nt & 1) == 0) {
+        if ((rc = one_step(c, nt)) != MFLBM_OK) return rc;
+        ++nt; --left;
+    }
+    if (!c->pair_graph || c->pair_graph_odd_first != 1)
+        if ((rc = capture_pair(c, nt)) != MFLBM_OK) return rc;
+    while (left >= 2) {
+        MFLBM_CUDA(cudaGraphLaunch(c->pair_graph, c->stream));
+        nt += 2; left -= 2;
+    }
+    if (left == 1 && (rc = one_step(c, nt)) != MFLBM_OK) return rc;
+    return MFLBM_OK;
+}
+
+int mflbm_synchronize(mflbm_context* c) {
+    if (!c) return fail(MFLBM_E_ARG, "null context");
+    MFLBM_CUDA(cudaStreamSynchronize(c->stream));
+    return MFLBM_OK;
+}
+
+int mflbm_monitor_reduce(mflbm_context* c, int n_exclude_inlet, int n_exclude_outlet, mflbm_monitor* out) {
+    int rc = require_ready(c);
+    if (rc != MFLBM_OK) return rc;
+    if (!out) return fail(MFLBM_E_ARG, "null output");
+    return monitor(*c, n_exclude_inlet, n_exclude_outlet, out);
+}
+
+int mflbm_node_counts(mflbm_context* c, long long counts[2]) {
+    if (!c || !counts) return fail(MFLBM_E_ARG, "null argument");
+    counts[0] = c->d.n_fluid;
+    counts[1] = c->d.g.n0();
+    return MFLBM_OK;
+}
+
+void* mflbm_stream(mflbm_context* c) { return c ? (void*)c->stream : nullptr; }
+
+int mflbm_set_kernel_timing(mflbm_context* c, int enable) {
+    if (!c) return fail(MFLBM_E_ARG, "null context");
+    MFLBM_CUDA(cudaStreamSynchronize(c->stream));
+    c->timing = enable != 0;
+    timing_pool(c).used = 0;
+    return MFLBM_OK;
+}
+
+int mflbm_kernel_times(mflbm_context* c, double* collide_ms_total, double* gradient_ms_total, int* n_collide,
+                       int* n_gradient) {
+    if (!c) return fail(MFLBM_E_ARG, "null context");
+    MFLBM_CUDA(cudaStreamSynchronize(c->stream));
+    TimingPool& tp = timing_pool(c);
+    double tc = 0, tg = 0;
+    int n = 0;
+    for (size_t b = 0; b + 4 <= tp.used; b += 4) {
+        float a = 0, g = 0;
+        MFLBM_CUDA(cudaEventElapsedTime(&a, tp.ev[b], tp.ev[b + 1]));
+        MFLBM_CUDA(cudaEventElapsedTime(&g, tp.ev[b + 2], tp.ev[b + 3]));
+        tc += a; tg += g; ++n;
+    }
+    if (collide_ms_total) *collide_ms_total = tc;
+    if (gradient_ms_total) *gradient_ms_total = tg;
+    if (n_collide) *n_collide = n;
+    if (n_gradient) *n_gradient = n;
+    return n;
+}
+
+}  // extern "C"

@@ -1,0 +1,161 @@
+// Internal definitions shared by every translation unit of libmflbm.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "../../include/mflbm.h"
+
+struct mflbm_context;
+
+namespace mflbm {
+
+// ---------------------------------------------------------------------------
+// D3Q19 (the reference's ex/ey/ez/opc tables, includes/Module.h:98-101).
+// ---------------------------------------------------------------------------
+__host__ __device__ constexpr int ex(int q) {
+    return (q == 1 || q == 7 || q == 9 || q == 11 || q == 13) ? 1
+         : (q == 2 || q == 8 || q == 10 || q == 12 || q == 14) ? -1 : 0;
+}
+__host__ __device__ constexpr int ey(int q) {
+    return (q == 3 || q == 7 || q == 8 || q == 15 || q == 17) ? 1
+         : (q == 4 || q == 9 || q == 10 || q == 16 || q == 18) ? -1 : 0;
+}
+__host__ __device__ constexpr int ez(int q) {
+    return (q == 5 || q == 11 || q == 12 || q == 15 || q == 16) ? 1
+         : (q == 6 || q == 13 || q == 14 || q == 17 || q == 18) ? -1 : 0;
+}
+__host__ __device__ constexpr int opp(int q) {
+    return q == 0 ? 0 : (q <= 6 ? ((q & 1) ? q + 1 : q - 1)
+                       : (q <= 10 ? 17 - q : (q <= 14 ? 25 - q : 33 - q)));
+}
+
+typedef long long ll;
+
+// ---------------------------------------------------------------------------
+// Padded, 1-based layouts of the reference (includes/Idx_gpu.cuh:54-70).
+// ---------------------------------------------------------------------------
+struct Grid {
+    int nx, ny, nz;
+    __host__ __device__ ll s0(ll x, ll y, ll z) const { return (x - 1) + (ll)nx * ((y - 1) + (ll)ny * (z - 1)); }
+    __host__ __device__ ll s1(ll x, ll y, ll z) const { return x + (ll)(nx + 2) * (y + (ll)(ny + 2) * z); }
+    __host__ __device__ ll s2(ll x, ll y, ll z) const { return (x + 1) + (ll)(nx + 4) * ((y + 1) + (ll)(ny + 4) * (z + 1)); }
+    __host__ __device__ ll s4(ll x, ll y, ll z) const { return (x + 3) + (ll)(nx + 8) * ((y + 3) + (ll)(ny + 8) * (z + 3)); }
+    __host__ __device__ ll f1(ll x, ll y, ll z, int e, int g) const { return s1(x, y, z) + n1() * (ll)(e + 19 * g); }
+    __host__ __device__ ll cnv(ll x, ll y, int e) const { return x + (ll)(nx + 2) * (y + (ll)(ny + 2) * e); }
+    __host__ __device__ ll n0() const { return (ll)nx * ny * nz; }
+    __host__ __device__ ll n1() const { return (ll)(nx + 2) * (ny + 2) * (nz + 2); }
+    __host__ __device__ ll n2() const { return (ll)(nx + 4) * (ny + 4) * (nz + 4); }
+    __host__ __device__ ll n4() const { return (ll)(nx + 8) * (ny + 8) * (nz + 8); }
+    __host__ __device__ ll plane1() const { return (ll)(nx + 2) * (ny + 2); }
+};
+
+// Packed node coordinates of the node lists: x in bits 0-9, y 10-20, z 21-31,
+// each stored with an offset of +4 so that ghost nodes down to -3 fit.
+constexpr int PACK_OFF = 4;
+__host__ __device__ inline uint32_t pack_xyz(int x, int y, int z) {
+    return (uint32_t)(x + PACK_OFF) | ((uint32_t)(y + PACK_OFF) << 10) | ((uint32_t)(z + PACK_OFF) << 21);
+}
+__host__ __device__ inline void unpack_xyz(uint32_t p, int& x, int& y, int& z) {
+    x = (int)(p & 1023u) - PACK_OFF;
+    y = (int)((p >> 10) & 2047u) - PACK_OFF;
+    z = (int)(p >> 21) - PACK_OFF;
+}
+
+// Model constants computed in T as the reference's host code computes them
+// (includes/Module.h:104-126, includes/Fluid_multiphase.h:31-35).
+template <class T> struct ModelConsts {
+    T w0, w1, w2, rk2, iso4a, iso4b;
+    T mrt_coef1, mrt_coef2, mrt_coef3, mrt_coef4, mrt_e2_coef1, mrt_e2_coef2, mrt_omega_xx;
+};
+
+// Physical parameters in the kernel precision.
+template <class T> struct Phys {
+    T gamma, force_z, nui1, nui2, beta, phi_inlet, sa_inject, uin_avg, relaxation, cos_theta, rho_in, rho_out;
+    ModelConsts<T> c;
+};
+
+// ---------------------------------------------------------------------------
+// Error handling.
+// ---------------------------------------------------------------------------
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+void count_launch();
+
+#define MFLBM_CUDA(call)                                                                     \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess)                                                               \
+            return ::mflbm::fail(MFLBM_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+// Count a launch and return its launch status as an MFLBM code.
+inline int after_launch(const char* what) {
+    count_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(MFLBM_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    return MFLBM_OK;
+}
+
+inline unsigned grid_for(ll n, int block) { return (unsigned)((n + block - 1) / block); }
+
+}  // namespace mflbm
+
+namespace mflbm {
+
+// Model constants and physical parameters in T, evaluated on the host with
+// the reference's T_P arithmetic (includes/Module.h:104-126,
+// includes/Fluid_multiphase.h:31-35).
+template <class T>
+inline ModelConsts<T> make_consts() {
+    ModelConsts<T> c;
+    c.w0 = T(1) / T(3);
+    c.w1 = T(1) / T(18);
+    c.w2 = T(1) / T(36);
+    c.rk2 = T(1) / (T)sqrt((T)2) / T(36);
+    c.iso4a = T(1) / T(6);
+    c.iso4b = T(1) / T(12);
+    c.mrt_coef1 = T(1) / T(19);
+    c.mrt_coef2 = T(1) / T(2394);
+    c.mrt_coef3 = T(1) / T(252);
+    c.mrt_coef4 = T(1) / T(72);
+    c.mrt_e2_coef1 = T(0);
+    c.mrt_e2_coef2 = T(-475) / T(63);
+    c.mrt_omega_xx = T(0);
+    return c;
+}
+
+template <class T>
+inline Phys<T> make_phys(const mflbm_params& p) {
+    Phys<T> h;
+    h.gamma = T(p.lbm_gamma);
+    h.force_z = T(p.force_z);
+    h.nui1 = T(p.la_nui1);
+    h.nui2 = T(p.la_nui2);
+    h.beta = T(p.lbm_beta);
+    h.phi_inlet = T(p.phi_inlet);
+    h.sa_inject = T(p.sa_inject);
+    h.uin_avg = T(p.uin_avg);
+    h.relaxation = T(p.relaxation);
+    h.cos_theta = T(p.cos_theta);
+    h.rho_in = T(p.rho_in);
+    h.rho_out = T(p.rho_out);
+    h.c = make_consts<T>();
+    return h;
+}
+
+// Flavour entry points (step_fast.cu / step_strict.cu).
+namespace fast {
+int collide(mflbm_context& c, bool odd);
+int boundaries(mflbm_context& c, bool odd);
+int gradient(mflbm_context& c);
+}
+namespace strict {
+int collide(mflbm_context& c, bool odd);
+int boundaries(mflbm_context& c, bool odd);
+int gradient(mflbm_context& c);
+}
+
+}  // namespace mflbm

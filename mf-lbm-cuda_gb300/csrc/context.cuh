@@ -1,0 +1,59 @@
+// The library context: device buffers in the reference layouts plus the
+// node lists, stream and captured graphs.
+#pragma once
+
+#include "common.cuh"
+
+namespace mflbm {
+
+struct DeviceState {
+    Grid g{};
+    int precision = MFLBM_FP32;
+    // populations and fields, reference layouts (f1 / s4 / s2 / s1)
+    void* pdf = nullptr;
+    void* phi = nullptr;
+    void* cn_x = nullptr;
+    void* cn_y = nullptr;
+    void* cn_z = nullptr;
+    void* c_norm = nullptr;
+    void* curv = nullptr;
+    void* W_in = nullptr;
+    void* f_cv = nullptr;
+    void* g_cv = nullptr;
+    void* phi_cv = nullptr;
+    // geometry
+    int32_t* walls = nullptr;       // s2
+    int32_t* walls_type = nullptr;  // s4
+    void* s_nx = nullptr;           // s4
+    void* s_ny = nullptr;
+    void* s_nz = nullptr;
+    // node lists (packed coordinates, ascending linear order)
+    uint32_t* fluid_list = nullptr;    // walls == 0 on [1, n]^3
+    ll n_fluid = 0;
+    uint32_t* list_phi_ext = nullptr;  // walls_type == 2 on [-2, n+3]^3
+    ll n_phi_ext = 0;
+    uint32_t* list_wet = nullptr;      // walls_type == -1 on [-1, n+2]^3
+    ll n_wet = 0;
+    uint32_t* list_cn_ext = nullptr;   // walls_type == 2 on [0, n+1]^3
+    ll n_cn_ext = 0;
+    double* red = nullptr;             // reduction scratch
+    ll red_len = 0;
+};
+
+}  // namespace mflbm
+
+struct mflbm_context {
+    mflbm_params params{};
+    mflbm::DeviceState d;
+    cudaStream_t stream = nullptr;
+    bool have_geometry = false;
+    bool have_fields = false;
+    // CUDA graph of one odd + even step pair (built lazily by mflbm_run)
+    cudaGraphExec_t pair_graph = nullptr;
+    int pair_graph_odd_first = -1;
+    // kernel timing
+    bool timing = false;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    double t_collide = 0, t_gradient = 0;
+    int n_collide = 0, n_gradient = 0;
+};

@@ -1,0 +1,440 @@
+// Device set-up: geometry preprocessing, start-up fields and the FP64
+// monitor reductions.  Built with -fmad=false: the geometry and start-up
+// arithmetic must be the reference's IEEE sequence so masks, solid normals
+// and initial populations are bit-identical to the reference's host code.
+#include <vector>
+
+#include "context.cuh"
+#include "setup.cuh"
+
+namespace mflbm {
+
+// ---------------------------------------------------------------------------
+// Geometry preprocessing (src/Geometry_preprocessing.cpp:29-403) on a copy of
+// the lattice padded by G = 10 layers: ghost fill, node classification
+// (1 solid, 2 solid boundary, 0 fluid, -1 fluid boundary), four 27-point
+// smoothing passes and the ISO8 solid normal at fluid boundary nodes.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int G = 10;
+
+struct Pad {
+    int nx, ny, nz;
+    __host__ __device__ int NX() const { return nx + 2 * G; }
+    __host__ __device__ int NY() const { return ny + 2 * G; }
+    __host__ __device__ int NZ() const { return nz + 2 * G; }
+    __host__ __device__ ll n() const { return (ll)NX() * NY() * NZ(); }
+    __host__ __device__ ll t(int x, int y, int z) const { return (x + G - 1) + (ll)NX() * ((y + G - 1) + (ll)NY() * (z + G - 1)); }
+};
+
+__global__ void pad_interior(Pad p, const int32_t* wg, int32_t* tmp) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z + 1;
+    if (i > p.nx) return;
+    tmp[p.t(i, j, k)] = wg[(i - 1) + (ll)p.nx * ((j - 1) + (ll)p.ny * (k - 1))];
+}
+
+// z ghosts for interior (i, j); then y ghosts for every z; then x ghosts for every (y, z)
+__global__ void pad_fill_z(Pad p, int per, int32_t* tmp) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, s = blockIdx.z;  // s in [0, 2G)
+    if (i > p.nx) return;
+    const int k = s < G ? 1 - G + s : p.nz + 1 + (s - G);
+    const int src = s < G ? (per ? p.nz + k : 1) : (per ? k - p.nz : p.nz);
+    tmp[p.t(i, j, k)] = tmp[p.t(i, j, src)];
+}
+__global__ void pad_fill_y(Pad p, int per, int32_t* tmp) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = (int)blockIdx.y + 1 - G, s = blockIdx.z;
+    if (i > p.nx) return;
+    const int j = s < G ? 1 - G + s : p.ny + 1 + (s - G);
+    const int src = s < G ? (per ? p.ny + j : 1) : (per ? j - p.ny : p.ny);
+    tmp[p.t(i, j, k)] = tmp[p.t(i, src, k)];
+}
+__global__ void pad_fill_x(Pad p, int per, int32_t* tmp) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;  // [0, 2G)
+    const int j = (int)blockIdx.y + 1 - G, k = (int)blockIdx.z + 1 - G;
+    if (s >= 2 * G) return;
+    const int i = s < G ? 1 - G + s : p.nx + 1 + (s - G);
+    const int src = s < G ? (per ? p.nx + i : 1) : (per ? i - p.nx : p.nx);
+    tmp[p.t(i, j, k)] = tmp[p.t(src, j, k)];
+}
+
+// classification on [2-G, n+G-1]: solid next to fluid -> 2, fluid next to solid -> -1
+__global__ void classify(Pad p, const int32_t* tmp, int32_t* typ) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 2 - G;
+    const int j = (int)blockIdx.y + 2 - G, k = (int)blockIdx.z + 2 - G;
+    if (i > p.nx + G - 1) return;
+    int v = tmp[p.t(i, j, k)];
+    if (v == 1) {
+        for (int q = 1; q <= 18; ++q)
+            if (tmp[p.t(i + ex(q), j + ey(q), k + ez(q))] <= 0) { v = 2; break; }
+    } else if (v == 0) {
+        for (int q = 1; q <= 18; ++q)
+            if (tmp[p.t(i + ex(q), j + ey(q), k + ez(q))] >= 1) { v = -1; break; }
+    }
+    typ[p.t(i, j, k)] = v;
+}
+
+template <class T>
+__global__ void to_real(ll n, const int32_t* a, T* b, T* c) {
+    const ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) { b[t] = T(a[t]); c[t] = T(a[t]); }
+}
+
+// the 27-point neighbourhood in the reference's order (src/Geometry_preprocessing.cpp:31-33)
+__device__ __constant__ const int kSx[27] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1};
+__device__ __constant__ const int kSy[27] = {0, 0, 0, 1, -1, 0, 0, 1, 1, -1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, -1, 1, -1, 1};
+__device__ __constant__ const int kSz[27] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 1, 1, -1, -1, -1, 1, 1, -1, -1, 1, 1, -1};
+
+template <class T>
+__global__ void smooth(Pad p, const T* in, T* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 2 - G;
+    const int j = (int)blockIdx.y + 2 - G, k = (int)blockIdx.z + 2 - G;
+    if (i > p.nx + G - 1) return;
+    const T we[4] = {T(8) / T(27), T(2) / T(27), T(1) / T(54), T(1) / T(216)};
+    T s = T(0);
+#pragma unroll
+    for (int q = 0; q < 27; ++q) {
+        const int m = kSx[q] * kSx[q] + kSy[q] * kSy[q] + kSz[q] * kSz[q];
+        s += in[p.t(i + kSx[q], j + kSy[q], k + kSz[q])] * we[m];
+    }
+    out[p.t(i, j, k)] = s;
+}
+
+// ISO8 gradient of the smoothed wall field at fluid boundary nodes
+// (src/Geometry_preprocessing.cpp:226-386), in the reference's term order.
+template <class T>
+__global__ void solid_normals(Pad p, Grid g, const int32_t* typ, const T* S_, T* snx, T* sny, T* snz) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x - 3;
+    const int j = (int)blockIdx.y - 3, k = (int)blockIdx.z - 3;
+    if (i > g.nx + 4) return;
+    if (typ[p.t(i, j, k)] != -1) return;
+    auto S = [&](int a, int b, int c) { return S_[p.t(a, b, c)]; };
+    const T W[7] = {T(4) / T(45), T(1) / T(21), T(2) / T(105), T(5) / T(504), T(1) / T(315), T(1) / T(630), T(1) / T(5040)};
+    const T nwx = W[0] * (S(i + 1, j, k) - S(i - 1, j, k)) +
+        W[1] * (S(i + 1, j + 1, k) - S(i - 1, j - 1, k) + S(i + 1, j - 1, k) - S(i - 1, j + 1, k) + S(i + 1, j, k + 1) - S(i - 1, j, k - 1) + S(i + 1, j, k - 1) - S(i - 1, j, k + 1)) +
+        W[2] * (S(i + 1, j + 1, k + 1) - S(i - 1, j - 1, k - 1) + S(i + 1, j + 1, k - 1) - S(i - 1, j - 1, k + 1) + S(i + 1, j - 1, k + 1) - S(i - 1, j + 1, k - 1) + S(i + 1, j - 1, k - 1) - S(i - 1, j + 1, k + 1)) +
+        W[3] * (S(i + 2, j, k) - S(i - 2, j, k)) +
+        W[4] * (S(i + 2, j + 1, k) - S(i - 2, j - 1, k) + S(i + 2, j - 1, k) - S(i - 2, j + 1, k) + S(i + 2, j, k + 1) - S(i - 2, j, k - 1) + S(i + 2, j, k - 1) - S(i - 2, j, k + 1) +
+                S(i + 1, j + 2, k) - S(i - 1, j - 2, k) + S(i + 1, j - 2, k) - S(i - 1, j + 2, k) + S(i + 1, j, k + 2) - S(i - 1, j, k - 2) + S(i + 1, j, k - 2) - S(i - 1, j, k + 2)) +
+        W[5] * (S(i + 2, j + 1, k + 1) - S(i - 2, j - 1, k - 1) + S(i + 2, j + 1, k - 1) - S(i - 2, j - 1, k + 1) + S(i + 2, j - 1, k + 1) - S(i - 2, j + 1, k - 1) + S(i + 2, j - 1, k - 1) - S(i - 2, j + 1, k + 1) +
+                S(i + 1, j + 2, k + 1) - S(i - 1, j - 2, k - 1) + S(i + 1, j + 2, k - 1) - S(i - 1, j - 2, k + 1) + S(i + 1, j - 2, k + 1) - S(i - 1, j + 2, k - 1) + S(i + 1, j - 2, k - 1) - S(i - 1, j + 2, k + 1) +
+                S(i + 1, j + 1, k + 2) - S(i - 1, j - 1, k - 2) + S(i + 1, j + 1, k - 2) - S(i - 1, j - 1, k + 2) + S(i + 1, j - 1, k + 2) - S(i - 1, j + 1, k - 2) + S(i + 1, j - 1, k - 2) - S(i - 1, j + 1, k + 2)) +
+        W[6] * (S(i + 2, j + 2, k) - S(i - 2, j - 2, k) + S(i + 2, j - 2, k) - S(i - 2, j + 2, k) + S(i + 2, j, k + 2) - S(i - 2, j, k - 2) + S(i + 2, j, k - 2) - S(i - 2, j, k + 2));
+    const T nwy = W[0] * (S(i, j + 1, k) - S(i, j - 1, k)) +
+        W[1] * (S(i + 1, j + 1, k) - S(i - 1, j - 1, k) + S(i - 1, j + 1, k) - S(i + 1, j - 1, k) + S(i, j + 1, k + 1) - S(i, j - 1, k - 1) + S(i, j + 1, k - 1) - S(i, j - 1, k + 1)) +
+        W[2] * (S(i + 1, j + 1, k + 1) - S(i - 1, j - 1, k - 1) + S(i + 1, j + 1, k - 1) - S(i - 1, j - 1, k + 1) + S(i - 1, j + 1, k - 1) - S(i + 1, j - 1, k + 1) + S(i - 1, j + 1, k + 1) - S(i + 1, j - 1, k - 1)) +
+        W[3] * (S(i, j + 2, k) - S(i, j - 2, k)) +
+        W[4] * (S(i + 2, j + 1, k) - S(i - 2, j - 1, k) + S(i - 2, j + 1, k) - S(i + 2, j - 1, k) + S(i, j + 2, k + 1) - S(i, j - 2, k - 1) + S(i, j + 2, k - 1) - S(i, j - 2, k + 1) +
+                S(i + 1, j + 2, k) - S(i - 1, j - 2, k) + S(i - 1, j + 2, k) - S(i + 1, j - 2, k) + S(i, j + 1, k + 2) - S(i, j - 1, k - 2) + S(i, j + 1, k - 2) - S(i, j - 1, k + 2)) +
+        W[5] * (S(i + 2, j + 1, k + 1) - S(i - 2, j - 1, k - 1) + S(i + 2, j + 1, k - 1) - S(i - 2, j - 1, k + 1) + S(i - 2, j + 1, k + 1) - S(i + 2, j - 1, k - 1) + S(i - 2, j + 1, k - 1) - S(i + 2, j - 1, k + 1) +
+                S(i + 1, j + 2, k + 1) - S(i - 1, j - 2, k - 1) + S(i + 1, j + 2, k - 1) - S(i - 1, j - 2, k + 1) + S(i - 1, j + 2, k + 1) - S(i + 1, j - 2, k - 1) + S(i - 1, j + 2, k - 1) - S(i + 1, j - 2, k + 1) +
+                S(i + 1, j + 1, k + 2) - S(i - 1, j - 1, k - 2) + S(i + 1, j + 1, k - 2) - S(i - 1, j - 1, k + 2) + S(i - 1, j + 1, k + 2) - S(i + 1, j - 1, k - 2) + S(i - 1, j + 1, k - 2) - S(i + 1, j - 1, k + 2)) +
+        W[6] * (S(i + 2, j + 2, k) - S(i - 2, j - 2, k) + S(i - 2, j + 2, k) - S(i + 2, j - 2, k) + S(i, j + 2, k + 2) - S(i, j - 2, k - 2) + S(i, j + 2, k - 2) - S(i, j - 2, k + 2));
+    const T nwz = W[0] * (S(i, j, k + 1) - S(i, j, k - 1)) +
+        W[1] * (S(i, j + 1, k + 1) - S(i, j - 1, k - 1) + S(i, j - 1, k + 1) - S(i, j + 1, k - 1) + S(i + 1, j, k + 1) - S(i - 1, j, k - 1) + S(i - 1, j, k + 1) - S(i + 1, j, k - 1)) +
+        W[2] * (S(i + 1, j + 1, k + 1) - S(i - 1, j - 1, k - 1) + S(i + 1, j - 1, k + 1) - S(i - 1, j + 1, k - 1) + S(i - 1, j + 1, k + 1) - S(i + 1, j - 1, k - 1) + S(i - 1, j - 1, k + 1) - S(i + 1, j + 1, k - 1)) +
+        W[3] * (S(i, j, k + 2) - S(i, j, k - 2)) +
+        W[4] * (S(i, j + 1, k + 2) - S(i, j - 1, k - 2) + S(i, j - 1, k + 2) - S(i, j + 1, k - 2) + S(i + 2, j, k + 1) - S(i - 2, j, k - 1) + S(i - 2, j, k + 1) - S(i + 2, j, k - 1) +
+                S(i, j + 2, k + 1) - S(i, j - 2, k - 1) + S(i, j - 2, k + 1) - S(i, j + 2, k - 1) + S(i + 1, j, k + 2) - S(i - 1, j, k - 2) + S(i - 1, j, k + 2) - S(i + 1, j, k - 2)) +
+        W[5] * (S(i + 2, j + 1, k + 1) - S(i - 2, j - 1, k - 1) + S(i + 2, j - 1, k + 1) - S(i - 2, j + 1, k - 1) + S(i - 2, j + 1, k + 1) - S(i + 2, j - 1, k - 1) + S(i - 2, j - 1, k + 1) - S(i + 2, j + 1, k - 1) +
+                S(i + 1, j + 2, k + 1) - S(i - 1, j - 2, k - 1) + S(i + 1, j - 2, k + 1) - S(i - 1, j + 2, k - 1) + S(i - 1, j + 2, k + 1) - S(i + 1, j - 2, k - 1) + S(i - 1, j - 2, k + 1) - S(i + 1, j + 2, k - 1) +
+                S(i + 1, j + 1, k + 2) - S(i - 1, j - 1, k - 2) + S(i + 1, j - 1, k + 2) - S(i - 1, j + 1, k - 2) + S(i - 1, j + 1, k + 2) - S(i + 1, j - 1, k - 2) + S(i - 1, j - 1, k + 2) - S(i + 1, j + 1, k - 2)) +
+        W[6] * (S(i, j + 2, k + 2) - S(i, j - 2, k - 2) + S(i, j - 2, k + 2) - S(i, j + 2, k - 2) + S(i + 2, j, k + 2) - S(i - 2, j, k - 2) + S(i - 2, j, k + 2) - S(i + 2, j, k - 2));
+    const T eps = T(1.1920928955078125e-07);  // numeric_limits<float>::epsilon() in both precisions
+    const T inv = T(1) / (sqrt(nwx * nwx + nwy * nwy + nwz * nwz) + eps);
+    const ll m = g.s4(i, j, k);
+    snx[m] = nwx * inv; sny[m] = nwy * inv; snz[m] = nwz * inv;
+}
+
+// copy the padded work arrays out to the reference layouts (walls s2, walls_type s4)
+__global__ void unpad(Pad p, Grid g, const int32_t* tmp, const int32_t* typ, int32_t* walls, int32_t* wt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x - 3;
+    const int j = (int)blockIdx.y - 3, k = (int)blockIdx.z - 3;
+    if (i > g.nx + 4) return;
+    wt[g.s4(i, j, k)] = typ[p.t(i, j, k)];
+    if (i >= -1 && i <= g.nx + 2 && j >= -1 && j <= g.ny + 2 && k >= -1 && k <= g.nz + 2)
+        walls[g.s2(i, j, k)] = tmp[p.t(i, j, k)];
+}
+
+template <class T>
+int preprocess_geometry_t(mflbm_context& c, const int32_t* walls_global_host, int iper) {
+    DeviceState& d = c.d;
+    const Grid g = d.g;
+    const Pad p{g.nx, g.ny, g.nz};
+    cudaStream_t s = c.stream;
+    int32_t *wg = nullptr, *tmp = nullptr, *typ = nullptr;
+    T *a = nullptr, *b = nullptr;
+    int rc = MFLBM_OK;
+    auto cleanup = [&]() { cudaFree(wg); cudaFree(tmp); cudaFree(typ); cudaFree(a); cudaFree(b); };
+#define GEO_CUDA(call)                                                                        \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess) { cleanup(); return fail(MFLBM_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); } \
+    } while (0)
+#define GEO_LAUNCH(name) do { if ((rc = after_launch(name)) != MFLBM_OK) { cleanup(); return rc; } } while (0)
+    GEO_CUDA(cudaMalloc(&wg, sizeof(int32_t) * g.n0()));
+    GEO_CUDA(cudaMalloc(&tmp, sizeof(int32_t) * p.n()));
+    GEO_CUDA(cudaMalloc(&typ, sizeof(int32_t) * p.n()));
+    GEO_CUDA(cudaMalloc(&a, sizeof(T) * p.n()));
+    GEO_CUDA(cudaMalloc(&b, sizeof(T) * p.n()));
+    GEO_CUDA(cudaMemcpyAsync(wg, walls_global_host, sizeof(int32_t) * g.n0(), cudaMemcpyHostToDevice, s));
+    GEO_CUDA(cudaMemsetAsync(tmp, 0, sizeof(int32_t) * p.n(), s));
+    const unsigned bx = grid_for(g.nx, 128);
+    pad_interior<<<dim3(bx, g.ny, g.nz), 128, 0, s>>>(p, wg, tmp);
+    GEO_LAUNCH("pad_interior");
+    pad_fill_z<<<dim3(bx, g.ny, 2 * G), 128, 0, s>>>(p, c.params.kper, tmp);
+    GEO_LAUNCH("pad_fill_z");
+    pad_fill_y<<<dim3(bx, g.nz + 2 * G, 2 * G), 128, 0, s>>>(p, c.params.jper, tmp);
+    GEO_LAUNCH("pad_fill_y");
+    pad_fill_x<<<dim3(1, g.ny + 2 * G, g.nz + 2 * G), 32, 0, s>>>(p, iper, tmp);
+    GEO_LAUNCH("pad_fill_x");
+    GEO_CUDA(cudaMemcpyAsync(typ, tmp, sizeof(int32_t) * p.n(), cudaMemcpyDeviceToDevice, s));
+    const dim3 gi(grid_for(g.nx + 2 * G - 2, 128), g.ny + 2 * G - 2, g.nz + 2 * G - 2);
+    classify<<<gi, 128, 0, s>>>(p, tmp, typ);
+    GEO_LAUNCH("classify");
+    to_real<T><<<grid_for(p.n(), 256), 256, 0, s>>>(p.n(), tmp, a, b);
+    GEO_LAUNCH("to_real");
+    for (int it = 0; it < 4; ++it) {
+        smooth<T><<<gi, 128, 0, s>>>(p, (it & 1) ? b : a, (it & 1) ? a : b);
+        GEO_LAUNCH("smooth");
+    }
+    // four passes: a -> b -> a -> b -> a; the final field is in `a`
+    const dim3 g4(grid_for(g.nx + 8, 128), g.ny + 8, g.nz + 8);
+    GEO_CUDA(cudaMemsetAsync(d.s_nx, 0, sizeof(T) * g.n4(), s));
+    GEO_CUDA(cudaMemsetAsync(d.s_ny, 0, sizeof(T) * g.n4(), s));
+    GEO_CUDA(cudaMemsetAsync(d.s_nz, 0, sizeof(T) * g.n4(), s));
+    solid_normals<T><<<g4, 128, 0, s>>>(p, g, typ, a, (T*)d.s_nx, (T*)d.s_ny, (T*)d.s_nz);
+    GEO_LAUNCH("solid_normals");
+    GEO_CUDA(cudaMemsetAsync(d.walls, 0, sizeof(int32_t) * g.n2(), s));
+    unpad<<<g4, 128, 0, s>>>(p, g, tmp, typ, d.walls, d.walls_type);
+    GEO_LAUNCH("unpad");
+    GEO_CUDA(cudaStreamSynchronize(s));
+    cleanup();
+#undef GEO_CUDA
+#undef GEO_LAUNCH
+    return MFLBM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Start-up fields: initialization_new_multi options 1-5 and the equilibrium
+// fill with u = v = w = 0, rho = 1 (src/Init_multiphase.cpp:299-496).
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void init_phi(Grid g, int option, T z0, int open_z, T phi_inlet, T* phi) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x - 3;
+    const int j = (int)blockIdx.y - 3, k = (int)blockIdx.z - 3;
+    if (i > g.nx + 4) return;
+    T v = T(0);
+    if (i >= 0 && i <= g.nx + 1 && j >= 0 && j <= g.ny + 1 && k >= 0 && k <= g.nz + 1) {
+        const T x = T(i), y = T(j), z = T(k);
+        auto sq = [](T a) { return a * a; };
+        switch (option) {
+        case 1: v = z <= z0 ? T(1) : T(-1); break;
+        case 2: v = z <= z0 ? T(-1) : T(1); break;
+        case 3: v = (sq(x - T(g.nx + 1) * T(0)) + sq(z - T(g.nz + 1) * T(0.5)) + sq(y - T(g.ny + 1) * T(0.5)) <= sq(z0)) ? T(1) : T(-1); break;
+        case 4: v = (sq(x - T(g.nx + 1) * T(0)) + sq(z - T(g.nz + 1) * T(0.5)) + sq(y - T(g.ny + 1) * T(0.5)) <= sq(z0)) ? T(-1) : T(1); break;
+        default: v = (sq(x - T(g.nx + 1) * T(0.5)) + sq(z - T(g.nz + 1) * T(0.5)) + sq(y - T(g.ny + 1) * T(0.5)) <= sq(z0)) ? T(1) : T(-1); break;
+        }
+    }
+    if (open_z && k <= 0) v = phi_inlet;
+    phi[g.s4(i, j, k)] = v;
+}
+
+template <class T>
+__global__ void init_pdf(Grid g, ModelConsts<T> c, const T* phi, T* pdf) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y, k = blockIdx.z;
+    if (i > g.nx + 1) return;
+    const T ph = phi[g.s4(i, j, k)];
+    const T r[2] = {T(1) * (T(1.0) + ph) * T(0.5), T(1) * (T(1.0) - ph) * T(0.5)};
+    const T usqrt = T(0) * T(0) + T(0) * T(0) + T(0) * T(0);
+    for (int gg = 0; gg < 2; ++gg) {
+        pdf[g.f1(i, j, k, 0, gg)] = r[gg] * c.w0 + r[gg] * c.w0 * (T(-1.5) * usqrt);
+        for (int q = 1; q < 19; ++q) {
+            const T wq = q < 7 ? c.w1 : c.w2;
+            const T cu = T(0);
+            pdf[g.f1(i, j, k, q, gg)] = r[gg] * wq + r[gg] * wq * (T(3.0) * cu + T(4.5) * cu * cu - T(1.5) * usqrt);
+        }
+    }
+}
+
+template <class T>
+__global__ void init_convective(Grid g, const T* pdf, const T* phi, T* f_cv, T* g_cv, T* phi_cv) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i > g.nx + 1) return;
+    for (int q = 0; q < 19; ++q) {
+        f_cv[g.cnv(i, j, q)] = pdf[g.f1(i, j, g.nz, q, 0)];
+        g_cv[g.cnv(i, j, q)] = pdf[g.f1(i, j, g.nz, q, 1)];
+    }
+    phi_cv[g.s1(i, j, 0)] = phi[g.s4(i, j, g.nz)];
+}
+
+template <class T>
+int init_fields_t(mflbm_context& c, int option, double z0) {
+    DeviceState& d = c.d;
+    const Grid g = d.g;
+    const mflbm_params& p = c.params;
+    cudaStream_t s = c.stream;
+    const int open_z = p.kper == 0 && p.domain_wall_status_z_min == 0 && p.domain_wall_status_z_max == 0;
+    int rc;
+    init_phi<T><<<dim3(grid_for(g.nx + 8, 128), g.ny + 8, g.nz + 8), 128, 0, s>>>(g, option, T(z0), open_z, T(p.phi_inlet), (T*)d.phi);
+    if ((rc = after_launch("init_phi")) != MFLBM_OK) return rc;
+    init_pdf<T><<<dim3(grid_for(g.nx + 2, 128), g.ny + 2, g.nz + 2), 128, 0, s>>>(g, make_consts<T>(), (const T*)d.phi, (T*)d.pdf);
+    if ((rc = after_launch("init_pdf")) != MFLBM_OK) return rc;
+    MFLBM_CUDA(cudaMemsetAsync(d.f_cv, 0, sizeof(T) * g.plane1() * 19, s));
+    MFLBM_CUDA(cudaMemsetAsync(d.g_cv, 0, sizeof(T) * g.plane1() * 19, s));
+    MFLBM_CUDA(cudaMemsetAsync(d.phi_cv, 0, sizeof(T) * g.plane1(), s));
+    if (p.outlet_BC == 1) {
+        init_convective<T><<<dim3(grid_for(g.nx + 2, 128), g.ny + 2), 128, 0, s>>>(g, (const T*)d.pdf, (const T*)d.phi, (T*)d.f_cv, (T*)d.g_cv, (T*)d.phi_cv);
+        if ((rc = after_launch("init_convective")) != MFLBM_OK) return rc;
+    }
+    return MFLBM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 monitor reductions (quantities of src/Monitor.cpp:17-140, 472-495)
+// over the fluid-node list, on post-even populations: per-block partials with
+// warp shuffles, then one block folds the partials in a fixed order.
+// ---------------------------------------------------------------------------
+constexpr int NRED = 9;  // vol1, vol2, mass1, mass2, flux1, flux2, vol1_full, vol2_full, umax2
+
+template <class T>
+__global__ void __launch_bounds__(256) monitor_partials(Grid g, const uint32_t* list, ll n, const T* pdf, const T* phi,
+                                                        const T* cnx, const T* cny, const T* cnz, const T* cnorm,
+                                                        const T* curv, double gamma, double force_z, int k_lo, int k_hi,
+                                                        double* partial) {
+    double acc[NRED] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (ll)gridDim.x * blockDim.x) {
+        int i, j, k;
+        unpack_xyz(list[t], i, j, k);
+        double f[19];
+        const ll n1 = g.s1(i, j, k);
+#pragma unroll
+        for (int q = 0; q < 19; ++q) f[q] = (double)pdf[n1 + g.n1() * q] + (double)pdf[n1 + g.n1() * (q + 19)];
+        double rho = 0;
+#pragma unroll
+        for (int q = 0; q < 19; ++q) rho += f[q];
+        const ll n2 = g.s2(i, j, k);
+        const double tmp = 0.5 * gamma * (double)curv[n1] * (double)cnorm[n2];
+        const double fx = tmp * cnx[n2], fy = tmp * cny[n2], fz = tmp * cnz[n2] + force_z;
+        const double u = f[1] - f[2] + f[7] - f[8] + f[9] - f[10] + f[11] - f[12] + f[13] - f[14] - 0.5 * fx;
+        const double v = f[3] - f[4] + f[7] + f[8] - f[9] - f[10] + f[15] - f[16] + f[17] - f[18] - 0.5 * fy;
+        const double w = f[5] - f[6] + f[11] + f[12] - f[13] - f[14] + f[15] + f[16] - f[17] - f[18] - 0.5 * fz;
+        const double ph = (double)phi[g.s4(i, j, k)];
+        const double a1 = 0.5 * (1.0 + ph), a2 = 0.5 * (1.0 - ph);
+        acc[6] += a1; acc[7] += a2;
+        acc[4] += w * a1; acc[5] += w * a2;
+        if (k >= k_lo && k <= k_hi) { acc[0] += a1; acc[1] += a2; acc[2] += rho * a1; acc[3] += rho * a2; }
+        acc[8] = fmax(acc[8], u * u + v * v + w * w);
+    }
+    __shared__ double sh[NRED][8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int r = 0; r < NRED; ++r) {
+        double x = acc[r];
+        for (int o = 16; o > 0; o >>= 1) {
+            const double y = __shfl_down_sync(0xffffffffu, x, o);
+            x = r == 8 ? fmax(x, y) : x + y;
+        }
+        if (lane == 0) sh[r][warp] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < NRED) {
+        const int r = threadIdx.x;
+        double x = sh[r][0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) x = r == 8 ? fmax(x, sh[r][w]) : x + sh[r][w];
+        partial[(ll)blockIdx.x * NRED + r] = x;
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) sum_all(ll n, const T* a, double* partial) {
+    double acc = 0;
+    for (ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (ll)gridDim.x * blockDim.x) acc += (double)a[t];
+    __shared__ double sh[8];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double x = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) x += sh[w];
+        partial[blockIdx.x] = x;
+    }
+}
+
+__global__ void fold_partials(int nblocks, int stride, const double* partial, double* out) {
+    // one warp per quantity, fixed order
+    const int r = blockIdx.x, lane = threadIdx.x;
+    const bool is_max = (stride == NRED && r == 8);
+    double x = is_max ? 0.0 : 0.0;
+    for (int b = lane; b < nblocks; b += 32) {
+        const double y = partial[(ll)b * stride + r];
+        x = is_max ? fmax(x, y) : x + y;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const double y = __shfl_down_sync(0xffffffffu, x, o);
+        x = is_max ? fmax(x, y) : x + y;
+    }
+    if (lane == 0) out[r] = x;
+}
+
+template <class T>
+int monitor_t(mflbm_context& c, int nex_in, int nex_out, mflbm_monitor* out) {
+    DeviceState& d = c.d;
+    const Grid g = d.g;
+    cudaStream_t s = c.stream;
+    const int blocks = 4 * 152;
+    // scratch: NRED*blocks partials, blocks partials, NRED+1 results
+    const ll need = (ll)NRED * blocks + blocks + NRED + 1;
+    if (d.red_len < need) {
+        cudaFree(d.red);
+        d.red = nullptr;
+        d.red_len = 0;
+        MFLBM_CUDA(cudaMalloc(&d.red, sizeof(double) * need));
+        d.red_len = need;
+    }
+    double* part = d.red;
+    double* part2 = d.red + (ll)NRED * blocks;
+    double* res = part2 + blocks;
+    int rc;
+    monitor_partials<T><<<blocks, 256, 0, s>>>(g, d.fluid_list, d.n_fluid, (const T*)d.pdf, (const T*)d.phi,
+                                               (const T*)d.cn_x, (const T*)d.cn_y, (const T*)d.cn_z,
+                                               (const T*)d.c_norm, (const T*)d.curv, (double)T(c.params.lbm_gamma),
+                                               (double)T(c.params.force_z), nex_in + 1, g.nz - nex_out, part);
+    if ((rc = after_launch("monitor_partials")) != MFLBM_OK) return rc;
+    fold_partials<<<NRED, 32, 0, s>>>(blocks, NRED, part, res);
+    if ((rc = after_launch("fold_partials")) != MFLBM_OK) return rc;
+    sum_all<T><<<blocks, 256, 0, s>>>(g.n1() * 38, (const T*)d.pdf, part2);
+    if ((rc = after_launch("sum_all")) != MFLBM_OK) return rc;
+    fold_partials<<<1, 32, 0, s>>>(blocks, 1, part2, res + NRED);
+    if ((rc = after_launch("fold_partials")) != MFLBM_OK) return rc;
+    double h[NRED + 1];
+    MFLBM_CUDA(cudaMemcpyAsync(h, res, sizeof h, cudaMemcpyDeviceToHost, s));
+    MFLBM_CUDA(cudaStreamSynchronize(s));
+    out->vol1_sum = h[0]; out->vol2_sum = h[1];
+    out->mass1_sum = h[2]; out->mass2_sum = h[3];
+    out->flux1_sum = h[4]; out->flux2_sum = h[5];
+    out->vol1_full = h[6]; out->vol2_full = h[7];
+    out->umax = sqrt(h[8]);
+    out->total_mass = h[9];
+    out->saturation = h[0] / (h[0] + h[1]);
+    return MFLBM_OK;
+}
+
+}  // namespace
+
+int preprocess_geometry(mflbm_context& c, const int32_t* walls_global, int iper) {
+    return c.params.precision == MFLBM_FP32 ? preprocess_geometry_t<float>(c, walls_global, iper)
+                                            : preprocess_geometry_t<double>(c, walls_global, iper);
+}
+
+int init_fields(mflbm_context& c, int option, double z0) {
+    return c.params.precision == MFLBM_FP32 ? init_fields_t<float>(c, option, z0) : init_fields_t<double>(c, option, z0);
+}
+
+int monitor(mflbm_context& c, int nex_in, int nex_out, mflbm_monitor* out) {
+    return c.params.precision == MFLBM_FP32 ? monitor_t<float>(c, nex_in, nex_out, out)
+                                            : monitor_t<double>(c, nex_in, nex_out, out);
+}
+
+}  // namespace mflbm

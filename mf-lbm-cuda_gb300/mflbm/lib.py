@@ -1,0 +1,210 @@
+"""ctypes binding of libmflbm.so (the C ABI of include/mflbm.h).
+
+The library is the only compute path: if it is missing or cannot be loaded,
+``load()`` raises; there is no fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+from . import abi
+from .abi import Layout, ptr
+
+PKG = Path(__file__).resolve().parent.parent
+DEFAULT_LIB = PKG / "lib" / "libmflbm.so"
+
+VP, I, LL, D = C.c_void_p, C.c_int, C.c_longlong, C.c_double
+
+# name -> (restype, argtypes); every entry point of include/mflbm.h
+SIGNATURES = {
+    "mflbm_abi_version": (I, []),
+    "mflbm_last_error": (C.c_char_p, []),
+    "mflbm_kernel_launch_count": (C.c_ulonglong, []),
+    "mflbm_params_from_control": (I, [VP, I, I, VP, VP]),
+    "mflbm_set_walls": (I, [VP, VP, VP]),
+    "mflbm_inlet_profile": (I, [VP, I, VP]),
+    "mflbm_create": (I, [VP, C.POINTER(VP)]),
+    "mflbm_destroy": (I, [VP]),
+    "mflbm_set_params": (I, [VP, VP]),
+    "mflbm_preprocess_geometry": (I, [VP, VP, VP, VP, VP, VP, VP, VP]),
+    "mflbm_upload_geometry": (I, [VP, VP, VP, VP, VP, VP]),
+    "mflbm_init_fields": (I, [VP, I, D, VP]),
+    "mflbm_upload_fields": (I, [VP] * 12),
+    "mflbm_download_fields": (I, [VP] * 11),
+    "mflbm_step": (I, [VP, I]),
+    "mflbm_run": (I, [VP, I, I]),
+    "mflbm_synchronize": (I, [VP]),
+    "mflbm_monitor_reduce": (I, [VP, I, I, VP]),
+    "mflbm_node_counts": (I, [VP, C.POINTER(LL)]),
+    "mflbm_stream": (VP, [VP]),
+    "mflbm_set_kernel_timing": (I, [VP, I]),
+    "mflbm_kernel_times": (I, [VP, C.POINTER(D), C.POINTER(D), C.POINTER(I), C.POINTER(I)]),
+}
+
+_LIB = None
+
+
+class MflbmError(RuntimeError):
+    pass
+
+
+def lib_path() -> Path:
+    return Path(os.environ.get("MFLBM_LIB", str(DEFAULT_LIB)))
+
+
+def load(path=None):
+    """Load libmflbm.so (raises if it is absent: there is no fallback path)."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    p = Path(path) if path else lib_path()
+    if not p.exists():
+        raise MflbmError(f"{p} not found: build it with mf-lbm-cuda_gb300/build.py (there is no CPU fallback)")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    if path is None:
+        _LIB = lib
+    return lib
+
+
+def check(rc, what=""):
+    if rc < 0:
+        msg = load().mflbm_last_error().decode(errors="replace")
+        raise MflbmError(f"{what}: error {rc}: {msg}")
+    return rc
+
+
+def params_from_control(control, precision, fp_mode):
+    p, d = abi.Params(), abi.Derived()
+    check(load().mflbm_params_from_control(C.byref(control), precision, fp_mode, C.byref(p), C.byref(d)),
+          "mflbm_params_from_control")
+    return p, d
+
+
+def set_walls(control, geometry):
+    L = Layout(control.nxGlobal, control.nyGlobal, control.nzGlobal)
+    wg = L.empty("s0", np.int32)
+    g = None if geometry is None else np.ascontiguousarray(geometry, dtype=np.uint8)
+    check(load().mflbm_set_walls(C.byref(control), ptr(g), ptr(wg)), "mflbm_set_walls")
+    return wg
+
+
+def inlet_profile(control, precision):
+    L = Layout(control.nxGlobal, control.nyGlobal, control.nzGlobal)
+    w = L.empty("plane1", np.float32 if precision == abi.MFLBM_FP32 else np.float64)
+    check(load().mflbm_inlet_profile(C.byref(control), precision, ptr(w)), "mflbm_inlet_profile")
+    return w
+
+
+class Context:
+    """One lattice on the current CUDA device."""
+
+    def __init__(self, params: abi.Params):
+        self.lib = load()
+        self.params = params
+        self.L = Layout(params.nx, params.ny, params.nz)
+        self.T = np.float32 if params.precision == abi.MFLBM_FP32 else np.float64
+        h = VP()
+        check(self.lib.mflbm_create(C.byref(params), C.byref(h)), "mflbm_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.mflbm_destroy(self.h)
+            self.h = VP()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def preprocess_geometry(self, walls_global, want_host=True):
+        L = self.L
+        out = {}
+        if want_host:
+            out = {"walls": L.empty("s2", np.int32), "walls_type": L.empty("s4", np.int32),
+                   "s_nx": L.empty("s4", self.T), "s_ny": L.empty("s4", self.T), "s_nz": L.empty("s4", self.T)}
+        cnt = abi.GeometryCounts()
+        check(self.lib.mflbm_preprocess_geometry(self.h, ptr(np.ascontiguousarray(walls_global, np.int32)),
+                                                 ptr(out.get("walls")), ptr(out.get("walls_type")),
+                                                 ptr(out.get("s_nx")), ptr(out.get("s_ny")), ptr(out.get("s_nz")),
+                                                 C.byref(cnt)), "mflbm_preprocess_geometry")
+        out["counts"] = abi.struct_dict(cnt)
+        return out
+
+    def upload_geometry(self, walls, walls_type, s_nx, s_ny, s_nz):
+        check(self.lib.mflbm_upload_geometry(self.h, ptr(walls), ptr(walls_type), ptr(s_nx), ptr(s_ny), ptr(s_nz)),
+              "mflbm_upload_geometry")
+
+    def init_fields(self, option, interface_z0, W_in=None):
+        check(self.lib.mflbm_init_fields(self.h, int(option), float(interface_z0), ptr(W_in)), "mflbm_init_fields")
+
+    def upload_fields(self, **a):
+        names = ["pdf", "phi", "cn_x", "cn_y", "cn_z", "c_norm", "curv", "W_in", "f_convec_bc", "g_convec_bc",
+                 "phi_convec_bc"]
+        check(self.lib.mflbm_upload_fields(self.h, *[ptr(a.get(n)) for n in names]), "mflbm_upload_fields")
+
+    def download(self, names=("pdf", "phi", "cn_x", "cn_y", "cn_z", "c_norm", "curv", "f_convec_bc",
+                              "g_convec_bc", "phi_convec_bc")):
+        order = ["pdf", "phi", "cn_x", "cn_y", "cn_z", "c_norm", "curv", "f_convec_bc", "g_convec_bc",
+                 "phi_convec_bc"]
+        out = {n: self.L.empty(abi.FIELD_KINDS[n], self.T) for n in names}
+        check(self.lib.mflbm_download_fields(self.h, *[ptr(out.get(n)) for n in order]), "mflbm_download_fields")
+        return out
+
+    def step(self, ntime):
+        check(self.lib.mflbm_step(self.h, int(ntime)), "mflbm_step")
+
+    def run(self, ntime_begin, nsteps):
+        check(self.lib.mflbm_run(self.h, int(ntime_begin), int(nsteps)), "mflbm_run")
+
+    def sync(self):
+        check(self.lib.mflbm_synchronize(self.h), "mflbm_synchronize")
+
+    def monitor(self, n_exclude_inlet, n_exclude_outlet):
+        m = abi.Monitor()
+        check(self.lib.mflbm_monitor_reduce(self.h, int(n_exclude_inlet), int(n_exclude_outlet), C.byref(m)),
+              "mflbm_monitor_reduce")
+        return m.as_dict()
+
+    def node_counts(self):
+        c = (LL * 2)()
+        check(self.lib.mflbm_node_counts(self.h, c), "mflbm_node_counts")
+        return int(c[0]), int(c[1])
+
+    def stream(self):
+        return self.lib.mflbm_stream(self.h)
+
+    def set_timing(self, enable):
+        check(self.lib.mflbm_set_kernel_timing(self.h, int(bool(enable))), "mflbm_set_kernel_timing")
+
+    def kernel_times(self):
+        tc, tg, nc, ng = D(), D(), I(), I()
+        check(self.lib.mflbm_kernel_times(self.h, C.byref(tc), C.byref(tg), C.byref(nc), C.byref(ng)),
+              "mflbm_kernel_times")
+        return tc.value, tg.value, nc.value
+
+
+def setup_case(case, precision=abi.MFLBM_FP32, fp_mode=abi.MFLBM_FAST, geometry=None, want_host_geometry=False):
+    """Build a ready-to-step Context for `case`: walls, device geometry
+    preprocessing, start-up fields and colour gradient (the reference's
+    start-up, src/main.cpp:71-99).  Returns (context, info)."""
+    control = case.control(precision)
+    params, derived = params_from_control(control, precision, fp_mode)
+    geo = case.geometry_bytes() if geometry is None else geometry
+    wg = set_walls(control, geo)
+    W_in = inlet_profile(control, precision)
+    ctx = Context(params)
+    g = ctx.preprocess_geometry(wg, want_host=want_host_geometry)
+    ctx.init_fields(control.initial_fluid_distribution_option, derived.interface_z0, W_in)
+    info = {"params": params, "derived": derived, "control": control, "geometry": g, "W_in": W_in,
+            "walls_global": wg}
+    return ctx, info

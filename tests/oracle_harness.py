@@ -165,7 +165,7 @@ def ref_array(lib, L, name, T):
     return np.frombuffer(buf, dtype=dt).reshape(L.shape(kind)).copy()
 
 
-def run_reference_case(case, precision, checkpoints, fields=STATE_FIELDS, workdir=None):
+def run_reference_case(case, precision, checkpoints, fields=STATE_FIELDS, workdir=None, geometry=None):
     """Run `case` through oracle/_ref; returns {step: {field: array}} at each
     checkpoint step (0 = after start-up) plus '_scalars'."""
     lib = ref_lib(precision)
@@ -174,7 +174,7 @@ def run_reference_case(case, precision, checkpoints, fields=STATE_FIELDS, workdi
     T = dtype_of(precision)
     L = Layout(*case.shape)
     tmp = workdir or tempfile.mkdtemp(prefix="mflbm_ref_")
-    write_case_dir(case, tmp)
+    write_case_dir(case, tmp, geometry=geometry)
     devnull = os.open(os.devnull, os.O_WRONLY)
     saved = os.dup(1)
     os.dup2(devnull, 1)

@@ -1,0 +1,145 @@
+"""CUDA path against the CPU oracle.
+
+Strict flavour (-fmad=false): every array bit-identical to the oracle (which
+is bit-identical to the reference's own code) after N steps — geometry,
+start-up fields, populations, phase field, normals, curvature and convective
+buffers, in FP32 and FP64, through the graph-replayed path and the eager
+path.  Fast flavour (FMA contraction): within the tolerances stated below.
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle_harness as H
+from mflbm import abi, cases
+from mflbm.geometry import read_dat
+
+pytestmark = pytest.mark.gpu
+GOLDEN = Path(__file__).resolve().parent / "golden"
+STATE = ["pdf", "phi", "cn_x", "cn_y", "cn_z", "c_norm", "curv", "f_convec_bc", "g_convec_bc", "phi_convec_bc"]
+PRECS = [abi.MFLBM_FP32, abi.MFLBM_FP64]
+
+# Fast-flavour tolerances (max abs difference against the oracle, populations
+# and phase field are O(1)): FMA contraction changes the last bits of each
+# operation; after 20 steps the drift stays within these bounds.
+FAST_TOL = {abi.MFLBM_FP32: 2e-5, abi.MFLBM_FP64: 1e-12}
+
+
+def _setup(kind, prec, mode):
+    from mflbm import lib
+    case = cases.small_case(kind)
+    geo = read_dat(GOLDEN / f"{case.name}.dat")
+    ctx, info = lib.setup_case(case, prec, mode, geometry=geo, want_host_geometry=True)
+    o = H.OracleState(case, prec, geometry=geo)
+    return case, ctx, info, o
+
+
+def _diff(a, b):
+    a64, b64 = a.astype(np.float64), b.astype(np.float64)
+    return float(np.max(np.abs(a64 - b64))) if a.size else 0.0
+
+
+@pytest.mark.parametrize("prec", PRECS, ids=["f32", "f64"])
+@pytest.mark.parametrize("kind", cases.SMALL_KINDS)
+def test_strict_is_bit_exact(mflbm_lib, kind, prec):
+    case, ctx, info, o = _setup(kind, prec, abi.MFLBM_STRICT)
+    g = info["geometry"]
+    for n in ("walls", "walls_type", "s_nx", "s_ny", "s_nz"):
+        assert g[n].tobytes() == o.a[n].tobytes(), f"geometry {n}"
+    for n in ("num_solid_boundary_global", "num_fluid_boundary_global", "num_solid_boundary", "num_fluid_boundary",
+              "pore_sum"):
+        assert g["counts"][n] == getattr(o.counts, n), n
+    done = 0
+    for cp in [0, 1, 2, 11, 20]:
+        if cp > done:
+            ctx.run(done + 1, cp - done)
+            o.run(cp - done)
+            done = cp
+        d = ctx.download()
+        for n in STATE:
+            assert d[n].tobytes() == o.a[n].tobytes(), f"{n} after {cp} steps (max diff {_diff(d[n], o.a[n])})"
+    ctx.close()
+
+
+@pytest.mark.parametrize("prec", PRECS, ids=["f32", "f64"])
+def test_strict_eager_steps_and_upload(mflbm_lib, prec):
+    """Per-step calls (mflbm_step) and a state uploaded from the host in the
+    reference layouts (the drop-in's MemAllocate_multi_GPU path)."""
+    from mflbm import lib
+    case, ctx, info, o = _setup("velocity_convective", prec, abi.MFLBM_STRICT)
+    o.run(5)
+    ctx2 = lib.Context(info["params"])
+    ctx2.upload_geometry(o.a["walls"], o.a["walls_type"], o.a["s_nx"], o.a["s_ny"], o.a["s_nz"])
+    ctx2.upload_fields(**{n: o.a[n] for n in STATE + ["W_in"]})
+    for nt in range(6, 13):
+        ctx2.step(nt)
+    o.run(7)
+    d = ctx2.download()
+    for n in STATE:
+        assert d[n].tobytes() == o.a[n].tobytes(), n
+    # upload without cn / c_norm / curv: recomputed on the device from phi
+    ctx3 = lib.Context(info["params"])
+    ctx3.upload_geometry(o.a["walls"], o.a["walls_type"], o.a["s_nx"], o.a["s_ny"], o.a["s_nz"])
+    ctx3.upload_fields(pdf=o.a["pdf"], phi=o.a["phi"], W_in=o.a["W_in"], f_convec_bc=o.a["f_convec_bc"],
+                       g_convec_bc=o.a["g_convec_bc"], phi_convec_bc=o.a["phi_convec_bc"])
+    d3 = ctx3.download()
+    for n in ("cn_x", "cn_y", "cn_z", "c_norm", "curv", "phi"):
+        assert d3[n].tobytes() == o.a[n].tobytes(), n
+    for c in (ctx, ctx2, ctx3):
+        c.close()
+
+
+@pytest.mark.parametrize("prec", PRECS, ids=["f32", "f64"])
+@pytest.mark.parametrize("kind", cases.SMALL_KINDS)
+def test_fast_within_tolerance(mflbm_lib, kind, prec):
+    case, ctx, info, o = _setup(kind, prec, abi.MFLBM_FAST)
+    ctx.run(1, 20)
+    o.run(20)
+    d = ctx.download()
+    for n in ("pdf", "phi", "cn_x", "cn_y", "cn_z", "c_norm"):
+        assert _diff(d[n], o.a[n]) <= FAST_TOL[prec], (n, _diff(d[n], o.a[n]))
+    # curvature is a second derivative of the normal: 10x looser
+    assert _diff(d["curv"], o.a["curv"]) <= 10 * FAST_TOL[prec]
+    ctx.close()
+
+
+@pytest.mark.parametrize("prec", PRECS, ids=["f32", "f64"])
+def test_monitor_reductions_match_oracle(mflbm_lib, prec):
+    case, ctx, info, o = _setup("pressure_pressure", prec, abi.MFLBM_STRICT)
+    ctx.run(1, 10)
+    o.run(10)
+    k = case.control_keys()
+    m = ctx.monitor(int(k["n_exclude_inlet"]), int(k["n_exclude_outlet"]))
+    mo = o.monitor()
+    for n, v in mo.items():
+        assert m[n] == pytest.approx(v, rel=1e-12, abs=1e-14), n
+    ctx.close()
+
+
+def test_drainage_48x48x64_fp64_2000_steps(mflbm_lib):
+    """The reference's FP64 parity workload: drainage in a 48 x 48 x 64 sphere
+    pack, 2000 steps.  Strict: bit-exact.  Fast: phase field within 1e-9,
+    populations within 1e-11, saturation within 1e-12 relative."""
+    from mflbm import lib
+    case = cases.drainage_48x48x64()
+    geo = case.geometry_bytes()
+    o = H.OracleState(case, abi.MFLBM_FP64, geometry=geo)
+    o.run(2000)
+    ms = o.macro()
+    mo = o.monitor()
+    for mode in (abi.MFLBM_STRICT, abi.MFLBM_FAST):
+        ctx, info = lib.setup_case(case, abi.MFLBM_FP64, mode, geometry=geo)
+        ctx.run(1, 2000)
+        d = ctx.download()
+        m = ctx.monitor(2, 2)
+        if mode == abi.MFLBM_STRICT:
+            for n in STATE:
+                assert d[n].tobytes() == o.a[n].tobytes(), n
+        else:
+            assert _diff(d["phi"], o.a["phi"]) < 1e-9
+            assert _diff(d["pdf"], o.a["pdf"]) < 1e-11
+            assert m["saturation"] == pytest.approx(mo["saturation"], rel=1e-12)
+        ctx.close()
+    assert 0.0 < mo["saturation"] < 1.0
+    assert np.isfinite(ms["w"]).all()
