@@ -75,7 +75,27 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
         tmp = LIB.with_suffix(".so.tmp")
         _run([NVCC, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"])
         os.replace(tmp, LIB)
+    build_refshim(force)
     return LIB
+
+
+def refshim_path(precision: str) -> Path:
+    return OUT / f"libmflbm_refshim_{precision}.a"
+
+
+def build_refshim(force: bool = False):
+    """Static archives with the reference's GPU entry points (include/mflbm_refshim.h)."""
+    src = CSRC / "refshim.cpp"
+    deps = [src, REPO / "include" / "mflbm.h", REPO / "include" / "mflbm_refshim.h"]
+    for prec, define in (("f32", []), ("f64", ["-DMFLBM_REF_DOUBLE"])):
+        out = refshim_path(prec)
+        if not force and not _stale(out, deps):
+            continue
+        obj = OUT / f"refshim_{prec}.o"
+        _run(["g++", "-O2", "-std=c++17", "-fPIC", *define, "-c", str(src), "-o", str(obj)])
+        if out.exists():
+            out.unlink()
+        _run(["ar", "rcs", str(out), str(obj)])
 
 
 if __name__ == "__main__":

@@ -80,6 +80,7 @@ class Geometry:
     buffer_layers: int = 2
     seed: int = 0
     empty: bool = False             # True: no spheres (open duct)
+    interpenetration: float = 0.0   # non-overlapping packs: allowed centre-distance deficit
 
 
 @dataclass
@@ -105,7 +106,7 @@ class Case:
         if g.empty:
             return np.zeros((nz, ny, nx), np.uint8)
         return sphere_pack((nx, ny, nz), g.radius, g.porosity, seed=g.seed, overlap=g.overlap,
-                           buffer_layers=g.buffer_layers,
+                           buffer_layers=g.buffer_layers, interpenetration=g.interpenetration,
                            periodic_y=bool(int(self.control_keys()["jper"])))
 
     def control(self, precision):
@@ -147,7 +148,9 @@ def write_case_dir(case: Case, root: str, geometry=None, job_status="new_simulat
 def drainage_48x48x64(seed=1100):
     """Two-phase drainage, 48 x 48 x 64, y periodic, velocity inlet u = 1e-4,
     convective outlet, tau 1.0 / 1.0, gamma 0.01, contact angle 45 deg,
-    non-overlapping r = 6 spheres at porosity ~0.6 with 2-layer buffers."""
+    r = 6 spheres with centres at least 11 lu apart (non-overlapping up to a
+    1 lu lens, which lets the pack reach porosity ~0.6 before jamming), with
+    2-layer buffers."""
     return Case("drainage_48x48x64", {
         "nxGlobal": 48, "nyGlobal": 48, "nzGlobal": 64,
         "jper": 1, "domain_wall_status_y_min": 0, "domain_wall_status_y_max": 0,
@@ -157,7 +160,7 @@ def drainage_48x48x64(seed=1100):
         "capillary_number": "1.6666666666666666e-3", "saturation_injection": "1.0",
         "initial_fluid_distribution_option": 1, "initial_interface_position": "2.0",
         "n_exclude_inlet": 2, "n_exclude_outlet": 2,
-    }, Geometry(radius=6.0, porosity=0.6, overlap=False, buffer_layers=2, seed=seed))
+    }, Geometry(radius=6.0, porosity=0.6, overlap=False, buffer_layers=2, seed=seed, interpenetration=1.0))
 
 
 def drainage_256x256x256(seed=1200):

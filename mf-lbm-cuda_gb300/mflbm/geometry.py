@@ -16,7 +16,27 @@ from __future__ import annotations
 
 import numpy as np
 
-__all__ = ["sphere_pack", "write_dat", "read_dat", "porosity"]
+__all__ = ["sphere_pack", "write_dat", "read_dat", "porosity", "SplitMix64"]
+
+
+class SplitMix64:
+    """SplitMix64 generator: a fixed, platform-independent stream, so a seed
+    produces the same pack under every numpy version and on every host."""
+
+    MASK = (1 << 64) - 1
+
+    def __init__(self, seed):
+        self.s = int(seed) & self.MASK
+
+    def next_u64(self):
+        self.s = (self.s + 0x9E3779B97F4A7C15) & self.MASK
+        z = self.s
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & self.MASK
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & self.MASK
+        return z ^ (z >> 31)
+
+    def uniform(self, lo=0.0, hi=1.0):
+        return lo + (hi - lo) * ((self.next_u64() >> 11) * (1.0 / (1 << 53)))
 
 
 def _paint(solid, c, r, periodic_y):
@@ -54,7 +74,8 @@ def _paint(solid, c, r, periodic_y):
 
 
 def sphere_pack(shape, radius, porosity_target, *, seed, overlap=True,
-                buffer_layers=2, periodic_y=False, max_attempts=2_000_000):
+                buffer_layers=2, periodic_y=False, max_attempts=200_000, tolerance=0.01,
+                interpenetration=0.0):
     """Random sphere pack with a target porosity.
 
     shape            (nx, ny, nz) lattice size, flow along z, nx == ny.
@@ -63,16 +84,22 @@ def sphere_pack(shape, radius, porosity_target, *, seed, overlap=True,
     porosity_target  spheres are added until the porosity of the core region
                      (z outside the inlet/outlet buffers) drops to this value.
     overlap          False rejects a sphere whose centre is closer than the
-                     sum of radii to an earlier one (non-overlapping pack).
+                     sum of radii to an earlier one (non-overlapping pack);
+                     centres may then lie up to one radius outside the x/y
+                     faces, so cut spheres fill the gaps next to the walls.
+    interpenetration with overlap=False, centres must be at least
+                     r1 + r2 - interpenetration apart.
     buffer_layers    empty (fluid) slabs kept at the inlet and the outlet.
     periodic_y       spheres wrap around the y faces.
+    max_attempts     a non-overlapping pack that jams before the target is
+                     accepted when within `tolerance` of it.
 
     Returns a uint8 array [nz, ny, nx] with 1 = solid.
     """
     nx, ny, nz = (int(s) for s in shape)
     if nx != ny:
         raise ValueError("MF-LBM geometry files are only unambiguous for nx == ny")
-    rng = np.random.default_rng(seed)
+    rng = SplitMix64(seed)
     solid = np.zeros((nz, ny, nx), dtype=bool)
     zc0, zc1 = buffer_layers, nz - buffer_layers
     core = solid[zc0:zc1]
@@ -84,15 +111,19 @@ def sphere_pack(shape, radius, porosity_target, *, seed, overlap=True,
     while n_solid < target_solid:
         attempts += 1
         if attempts > max_attempts:
-            raise RuntimeError(f"pack did not reach porosity {porosity_target} "
-                               f"(reached {1 - n_solid / n_core:.4f})")
-        r = float(radius) if np.isscalar(radius) else float(rng.uniform(radius[0], radius[1]))
-        c = (rng.uniform(0, zc1 - zc0), rng.uniform(0, ny), rng.uniform(0, nx))
+            reached = 1 - n_solid / n_core
+            if reached - porosity_target <= tolerance:
+                break
+            raise RuntimeError(f"pack did not reach porosity {porosity_target} (reached {reached:.4f})")
+        r = float(radius) if np.isscalar(radius) else rng.uniform(radius[0], radius[1])
+        ext = 0.0 if overlap else r
+        c = (rng.uniform(0, zc1 - zc0), rng.uniform(0, ny) if periodic_y else rng.uniform(-ext, ny + ext),
+             rng.uniform(-ext, nx + ext))
         if not overlap and centres:
             d = np.asarray(centres) - np.asarray(c)
             if periodic_y:
                 d[:, 1] -= ny * np.round(d[:, 1] / ny)
-            if np.any((d ** 2).sum(axis=1) < (np.asarray(radii) + r) ** 2):
+            if np.any((d ** 2).sum(axis=1) < (np.asarray(radii) + r - interpenetration) ** 2):
                 continue
         n_solid += _paint(core, c, r, periodic_y)
         centres.append(c)

@@ -28,6 +28,23 @@ STATE_FIELDS = ["pdf", "phi", "cn_x", "cn_y", "cn_z", "c_norm", "curv",
                 "f_convec_bc", "g_convec_bc", "phi_convec_bc"]
 
 
+def force_relevant_pairs(d, ref):
+    """(name, device, oracle) float64 arrays of the quantities the collision
+    consumes: populations, phase field, the colour gradient c_norm * n and the
+    surface-force factor c_norm * curv.  The unit normal alone is not compared
+    because its direction is rounding noise where |grad phi| is near the 1e-6
+    cut-off (those nodes carry no force)."""
+    f = lambda a: a.astype(np.float64)
+    out = [("pdf", f(d["pdf"]), f(ref["pdf"])), ("phi", f(d["phi"]), f(ref["phi"]))]
+    for c in ("cn_x", "cn_y", "cn_z"):
+        out.append((f"c_norm*{c}", f(d["c_norm"]) * f(d[c]), f(ref["c_norm"]) * f(ref[c])))
+    interior_s2 = (slice(2, -2),) * 3   # nodes [1, n] of an s2 array
+    interior_s1 = (slice(1, -1),) * 3   # nodes [1, n] of an s1 array
+    out.append(("c_norm*curv", f(d["c_norm"][interior_s2]) * f(d["curv"][interior_s1]),
+                f(ref["c_norm"][interior_s2]) * f(ref["curv"][interior_s1])))
+    return out
+
+
 def dtype_of(precision):
     return np.float32 if precision == abi.MFLBM_FP32 else np.float64
 
