@@ -1,4 +1,5 @@
 // The C ABI of libmflbm (include/mflbm.h).
+#include <algorithm>
 #include <atomic>
 #include <cstring>
 #include <string>
@@ -48,8 +49,8 @@ int check_params(const mflbm_params* p) {
 void free_all(mflbm_context* c) {
     DeviceState& d = c->d;
     void* ptrs[] = {d.pdf, d.phi, d.cn_x, d.cn_y, d.cn_z, d.c_norm, d.curv, d.W_in, d.f_cv, d.g_cv, d.phi_cv,
-                    d.walls, d.walls_type, d.s_nx, d.s_ny, d.s_nz, d.fluid_list, d.list_phi_ext, d.list_wet,
-                    d.list_cn_ext, d.red};
+                    d.walls, d.walls_type, d.s_nx, d.s_ny, d.s_nz, d.fluid_list, d.list_phi_ext,
+                    d.list_cn_ext, d.red, d.staging, d.aux, d.type8};
     for (void* p : ptrs) if (p) cudaFree(p);
     d = DeviceState{};
     if (c->pair_graph) cudaGraphExecDestroy(c->pair_graph);
@@ -62,46 +63,58 @@ int alloc_zero(void** p, size_t bytes, cudaStream_t s) {
     return MFLBM_OK;
 }
 
-int upload_list(uint32_t** dptr, ll* n, const std::vector<uint32_t>& h) {
+template <class V>
+int upload_list(V** dptr, ll* n, const std::vector<V>& h) {
     if (*dptr) cudaFree(*dptr);
     *dptr = nullptr;
     *n = (ll)h.size();
     if (h.empty()) return MFLBM_OK;
-    MFLBM_CUDA(cudaMalloc(dptr, sizeof(uint32_t) * h.size()));
-    MFLBM_CUDA(cudaMemcpy(*dptr, h.data(), sizeof(uint32_t) * h.size(), cudaMemcpyHostToDevice));
+    MFLBM_CUDA(cudaMalloc(dptr, sizeof(V) * h.size()));
+    MFLBM_CUDA(cudaMemcpy(*dptr, h.data(), sizeof(V) * h.size(), cudaMemcpyHostToDevice));
     return MFLBM_OK;
 }
 
-// Fluid-node and boundary-node lists from the device geometry (ascending
-// linear order, so consecutive threads touch consecutive x).
+// Node lists from the device geometry: the fluid nodes of [1, n]^3 in
+// brick-element order (consecutive threads touch consecutive elements), and
+// the solid boundary nodes with an 18-bit mask of their fluid neighbours
+// (bit q set when neighbour x + e_q has walls_type <= 0).
 int build_lists(mflbm_context* c) {
     DeviceState& d = c->d;
     const Grid g = d.g;
     std::vector<int32_t> walls(g.n2()), wt(g.n4());
     MFLBM_CUDA(cudaMemcpy(walls.data(), d.walls, sizeof(int32_t) * g.n2(), cudaMemcpyDeviceToHost));
     MFLBM_CUDA(cudaMemcpy(wt.data(), d.walls_type, sizeof(int32_t) * g.n4(), cudaMemcpyDeviceToHost));
-    std::vector<uint32_t> fl, lphi, lwet, lcn;
+    std::vector<std::pair<int, uint32_t>> fe;
     for (int k = 1; k <= g.nz; ++k)
         for (int j = 1; j <= g.ny; ++j)
             for (int i = 1; i <= g.nx; ++i)
-                if (walls[g.s2(i, j, k)] == 0) fl.push_back(pack_xyz(i, j, k));
+                if (walls[g.s2(i, j, k)] == 0) fe.emplace_back(d.b.elem(i, j, k), pack_xyz(i, j, k));
+    std::sort(fe.begin(), fe.end());
+    std::vector<uint32_t> fl(fe.size());
+    for (size_t n = 0; n < fe.size(); ++n) fl[n] = fe[n].second;
+    std::vector<uint2> lphi, lcn;
     for (int k = -2; k <= g.nz + 3; ++k)
         for (int j = -2; j <= g.ny + 3; ++j)
             for (int i = -2; i <= g.nx + 3; ++i) {
-                const int v = wt[g.s4(i, j, k)];
-                const bool in1 = i >= -1 && i <= g.nx + 2 && j >= -1 && j <= g.ny + 2 && k >= -1 && k <= g.nz + 2;
-                const bool in0 = i >= 0 && i <= g.nx + 1 && j >= 0 && j <= g.ny + 1 && k >= 0 && k <= g.nz + 1;
-                if (v == 2) {
-                    lphi.push_back(pack_xyz(i, j, k));
-                    if (in0) lcn.push_back(pack_xyz(i, j, k));
-                }
-                if (v == -1 && in1) lwet.push_back(pack_xyz(i, j, k));
+                if (wt[g.s4(i, j, k)] != 2) continue;
+                uint32_t mask = 0;
+                for (int q = 1; q < 19; ++q)
+                    if (wt[g.s4(i + ex(q), j + ey(q), k + ez(q))] <= 0) mask |= 1u << q;
+                const uint2 e = make_uint2(pack_xyz(i, j, k), mask);
+                lphi.push_back(e);
+                if (i >= 0 && i <= g.nx + 1 && j >= 0 && j <= g.ny + 1 && k >= 0 && k <= g.nz + 1) lcn.push_back(e);
             }
     int rc;
     if ((rc = upload_list(&d.fluid_list, &d.n_fluid, fl)) != MFLBM_OK) return rc;
     if ((rc = upload_list(&d.list_phi_ext, &d.n_phi_ext, lphi)) != MFLBM_OK) return rc;
-    if ((rc = upload_list(&d.list_wet, &d.n_wet, lwet)) != MFLBM_OK) return rc;
     if ((rc = upload_list(&d.list_cn_ext, &d.n_cn_ext, lcn)) != MFLBM_OK) return rc;
+    return MFLBM_OK;
+}
+
+int ensure_staging(mflbm_context* c) {
+    if (c->d.staging) return MFLBM_OK;
+    const size_t bytes = (c->params.precision == MFLBM_FP32 ? 4 : 8) * c->d.g.n1() * 38;
+    MFLBM_CUDA(cudaMalloc(&c->d.staging, bytes));
     return MFLBM_OK;
 }
 
@@ -191,13 +204,16 @@ int mflbm_create(const mflbm_params* params, mflbm_context** out) {
     c->params = *params;
     DeviceState& d = c->d;
     d.g = Grid{(int)params->nx, (int)params->ny, (int)params->nz};
+    d.b = make_bricks(d.g.nx, d.g.ny, d.g.nz);
     d.precision = params->precision;
     const Grid& g = d.g;
     const size_t T = tsize(c);
+    if (d.b.S >= (1ll << 31)) { delete c; return fail(MFLBM_E_ARG, "lattice too large for 32-bit brick indexing"); }
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { delete c; return fail(MFLBM_E_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e)); }
     struct { void** p; size_t bytes; } allocs[] = {
-        {&d.pdf, T * g.n1() * 38}, {&d.phi, T * g.n4()}, {&d.cn_x, T * g.n2()}, {&d.cn_y, T * g.n2()},
+        {&d.pdf, T * d.b.S * 38}, {&d.aux, T * 4 * d.b.S}, {(void**)&d.type8, (size_t)g.n4()},
+        {&d.phi, T * g.n4()}, {&d.cn_x, T * g.n2()}, {&d.cn_y, T * g.n2()},
         {&d.cn_z, T * g.n2()}, {&d.c_norm, T * g.n2()}, {&d.curv, T * g.n1()}, {&d.W_in, T * g.plane1()},
         {&d.f_cv, T * g.plane1() * 19}, {&d.g_cv, T * g.plane1() * 19}, {&d.phi_cv, T * g.plane1()},
         {(void**)&d.walls, sizeof(int32_t) * g.n2()}, {(void**)&d.walls_type, sizeof(int32_t) * g.n4()},
@@ -282,6 +298,9 @@ int mflbm_upload_geometry(mflbm_context* c, const int32_t* walls, const int32_t*
     MFLBM_CUDA(cudaMemcpy(c->d.s_nx, s_nx, T * g.n4(), cudaMemcpyHostToDevice));
     MFLBM_CUDA(cudaMemcpy(c->d.s_ny, s_ny, T * g.n4(), cudaMemcpyHostToDevice));
     MFLBM_CUDA(cudaMemcpy(c->d.s_nz, s_nz, T * g.n4(), cudaMemcpyHostToDevice));
+    std::vector<int8_t> t8(g.n4());
+    for (ll n = 0; n < g.n4(); ++n) t8[n] = (int8_t)walls_type[n];
+    MFLBM_CUDA(cudaMemcpy(c->d.type8, t8.data(), g.n4(), cudaMemcpyHostToDevice));
     int rc = build_lists(c);
     if (rc != MFLBM_OK) return rc;
     c->have_geometry = true;
@@ -311,24 +330,29 @@ int mflbm_upload_fields(mflbm_context* c, const void* pdf, const void* phi, cons
     const Grid& g = d.g;
     const size_t T = tsize(c);
     cudaStream_t s = c->stream;
-    MFLBM_CUDA(cudaMemcpyAsync(d.pdf, pdf, T * g.n1() * 38, cudaMemcpyHostToDevice, s));
+    int rc = ensure_staging(c);
+    if (rc != MFLBM_OK) return rc;
+    MFLBM_CUDA(cudaMemcpyAsync(d.staging, pdf, T * g.n1() * 38, cudaMemcpyHostToDevice, s));
+    if ((rc = convert_populations(*c, true)) != MFLBM_OK) return rc;
     MFLBM_CUDA(cudaMemcpyAsync(d.phi, phi, T * g.n4(), cudaMemcpyHostToDevice, s));
     if (W_in) MFLBM_CUDA(cudaMemcpyAsync(d.W_in, W_in, T * g.plane1(), cudaMemcpyHostToDevice, s));
     const bool have_grad = cn_x && cn_y && cn_z && c_norm && curv;
+    if (f_convec_bc) MFLBM_CUDA(cudaMemcpyAsync(d.f_cv, f_convec_bc, T * g.plane1() * 19, cudaMemcpyHostToDevice, s));
+    if (g_convec_bc) MFLBM_CUDA(cudaMemcpyAsync(d.g_cv, g_convec_bc, T * g.plane1() * 19, cudaMemcpyHostToDevice, s));
+    if (phi_convec_bc) MFLBM_CUDA(cudaMemcpyAsync(d.phi_cv, phi_convec_bc, T * g.plane1(), cudaMemcpyHostToDevice, s));
+    // the collision reads per-node records (n, 0.5*gamma*curv*c_norm): build
+    // them from the uploaded arrays, or run the gradient pass when they are absent
     if (have_grad) {
         MFLBM_CUDA(cudaMemcpyAsync(d.cn_x, cn_x, T * g.n2(), cudaMemcpyHostToDevice, s));
         MFLBM_CUDA(cudaMemcpyAsync(d.cn_y, cn_y, T * g.n2(), cudaMemcpyHostToDevice, s));
         MFLBM_CUDA(cudaMemcpyAsync(d.cn_z, cn_z, T * g.n2(), cudaMemcpyHostToDevice, s));
         MFLBM_CUDA(cudaMemcpyAsync(d.c_norm, c_norm, T * g.n2(), cudaMemcpyHostToDevice, s));
         MFLBM_CUDA(cudaMemcpyAsync(d.curv, curv, T * g.n1(), cudaMemcpyHostToDevice, s));
+        rc = c->params.fp_mode == MFLBM_STRICT ? strict::refresh_aux(*c) : fast::refresh_aux(*c);
+    } else {
+        rc = flavour_gradient(c);
     }
-    if (f_convec_bc) MFLBM_CUDA(cudaMemcpyAsync(d.f_cv, f_convec_bc, T * g.plane1() * 19, cudaMemcpyHostToDevice, s));
-    if (g_convec_bc) MFLBM_CUDA(cudaMemcpyAsync(d.g_cv, g_convec_bc, T * g.plane1() * 19, cudaMemcpyHostToDevice, s));
-    if (phi_convec_bc) MFLBM_CUDA(cudaMemcpyAsync(d.phi_cv, phi_convec_bc, T * g.plane1(), cudaMemcpyHostToDevice, s));
-    if (!have_grad) {
-        int rc = flavour_gradient(c);
-        if (rc != MFLBM_OK) return rc;
-    }
+    if (rc != MFLBM_OK) return rc;
     MFLBM_CUDA(cudaStreamSynchronize(s));
     c->have_fields = true;
     return MFLBM_OK;
@@ -341,8 +365,13 @@ int mflbm_download_fields(mflbm_context* c, void* pdf, void* phi, void* cn_x, vo
     const Grid& g = d.g;
     const size_t T = tsize(c);
     cudaStream_t s = c->stream;
+    if (pdf) {
+        int rc = ensure_staging(c);
+        if (rc != MFLBM_OK) return rc;
+        if ((rc = convert_populations(*c, false)) != MFLBM_OK) return rc;
+    }
     struct { void* dst; const void* src; size_t n; } cp[] = {
-        {pdf, d.pdf, T * g.n1() * 38}, {phi, d.phi, T * g.n4()}, {cn_x, d.cn_x, T * g.n2()}, {cn_y, d.cn_y, T * g.n2()},
+        {pdf, d.staging, T * g.n1() * 38}, {phi, d.phi, T * g.n4()}, {cn_x, d.cn_x, T * g.n2()}, {cn_y, d.cn_y, T * g.n2()},
         {cn_z, d.cn_z, T * g.n2()}, {c_norm, d.c_norm, T * g.n2()}, {curv, d.curv, T * g.n1()},
         {f_convec_bc, d.f_cv, T * g.plane1() * 19}, {g_convec_bc, d.g_cv, T * g.plane1() * 19},
         {phi_convec_bc, d.phi_cv, T * g.plane1()}};

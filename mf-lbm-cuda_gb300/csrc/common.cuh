@@ -52,6 +52,40 @@ struct Grid {
     __host__ __device__ ll plane1() const { return (ll)(nx + 2) * (ny + 2); }
 };
 
+// Internal population layout: the lattice [0, n+1]^3 is cut into 2x2x2
+// bricks stored x-fastest; the 8 nodes of a brick are consecutive
+// (bit 0 = x parity, bit 1 = y parity, bit 2 = z parity) and each slot holds
+// both components (g = 0, 1) side by side.  Population (node, e, g) is
+// element 2 * (e * S + elem(node)) + g of the population array.  A 64-byte
+// DRAM line then holds one brick of one direction, so partially fluid lines
+// waste far less than the reference's x-rows (one line = 16 nodes of a row).
+struct Bricks {
+    int nbx, nby, nbz;
+    ll S;  // elements (nodes incl. padding) per direction
+    __host__ __device__ int elem(int x, int y, int z) const {
+        return (((x >> 1) + nbx * ((y >> 1) + nby * (z >> 1))) << 3) | (x & 1) | ((y & 1) << 1) | ((z & 1) << 2);
+    }
+    __host__ __device__ ll at(int x, int y, int z, int e, int g) const {
+        return 2 * ((ll)e * S + elem(x, y, z)) + g;
+    }
+};
+inline Bricks make_bricks(int nx, int ny, int nz) {
+    Bricks b;
+    b.nbx = (nx + 3) / 2;  // covers x in [0, nx+1]
+    b.nby = (ny + 3) / 2;
+    b.nbz = (nz + 3) / 2;
+    b.S = (ll)b.nbx * b.nby * b.nbz * 8;
+    return b;
+}
+
+template <class T> struct Vec2;
+template <> struct Vec2<float> { typedef float2 type; };
+template <> struct Vec2<double> { typedef double2 type; };
+struct __align__(32) Double4 { double x, y, z, w; };
+template <class T> struct Vec4;
+template <> struct Vec4<float> { typedef float4 type; };
+template <> struct Vec4<double> { typedef Double4 type; };
+
 // Packed node coordinates of the node lists: x in bits 0-9, y 10-20, z 21-31,
 // each stored with an offset of +4 so that ghost nodes down to -3 fit.
 constexpr int PACK_OFF = 4;
@@ -148,11 +182,13 @@ inline Phys<T> make_phys(const mflbm_params& p) {
 
 // Flavour entry points (step_fast.cu / step_strict.cu).
 namespace fast {
+int refresh_aux(mflbm_context& c);
 int collide(mflbm_context& c, bool odd);
 int boundaries(mflbm_context& c, bool odd);
 int gradient(mflbm_context& c);
 }
 namespace strict {
+int refresh_aux(mflbm_context& c);
 int collide(mflbm_context& c, bool odd);
 int boundaries(mflbm_context& c, bool odd);
 int gradient(mflbm_context& c);

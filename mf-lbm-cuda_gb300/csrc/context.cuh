@@ -8,9 +8,13 @@ namespace mflbm {
 
 struct DeviceState {
     Grid g{};
+    Bricks b{};
     int precision = MFLBM_FP32;
-    // populations and fields, reference layouts (f1 / s4 / s2 / s1)
+    // populations in the brick layout (common.cuh); fields in the reference layouts (s4 / s2 / s1)
     void* pdf = nullptr;
+    void* staging = nullptr;        // reference-layout (f1) buffer for uploads / downloads
+    void* aux = nullptr;            // per brick element: (n_x, n_y, n_z, 0.5*gamma*curv*c_norm)
+    int8_t* type8 = nullptr;        // walls_type as int8 (s4)
     void* phi = nullptr;
     void* cn_x = nullptr;
     void* cn_y = nullptr;
@@ -27,14 +31,12 @@ struct DeviceState {
     void* s_nx = nullptr;           // s4
     void* s_ny = nullptr;
     void* s_nz = nullptr;
-    // node lists (packed coordinates, ascending linear order)
-    uint32_t* fluid_list = nullptr;    // walls == 0 on [1, n]^3
+    // node lists (packed coordinates)
+    uint32_t* fluid_list = nullptr;    // walls == 0 on [1, n]^3, in brick-element order
     ll n_fluid = 0;
-    uint32_t* list_phi_ext = nullptr;  // walls_type == 2 on [-2, n+3]^3
+    uint2* list_phi_ext = nullptr;     // walls_type == 2 on [-2, n+3]^3: (packed, fluid-neighbour mask)
     ll n_phi_ext = 0;
-    uint32_t* list_wet = nullptr;      // walls_type == -1 on [-1, n+2]^3
-    ll n_wet = 0;
-    uint32_t* list_cn_ext = nullptr;   // walls_type == 2 on [0, n+1]^3
+    uint2* list_cn_ext = nullptr;      // walls_type == 2 on [0, n+1]^3: (packed, fluid-neighbour mask)
     ll n_cn_ext = 0;
     double* red = nullptr;             // reduction scratch
     ll red_len = 0;

@@ -147,11 +147,14 @@ __global__ void solid_normals(Pad p, Grid g, const int32_t* typ, const T* S_, T*
 }
 
 // copy the padded work arrays out to the reference layouts (walls s2, walls_type s4)
-__global__ void unpad(Pad p, Grid g, const int32_t* tmp, const int32_t* typ, int32_t* walls, int32_t* wt) {
+__global__ void unpad(Pad p, Grid g, const int32_t* tmp, const int32_t* typ, int32_t* walls, int32_t* wt,
+                      int8_t* type8) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x - 3;
     const int j = (int)blockIdx.y - 3, k = (int)blockIdx.z - 3;
     if (i > g.nx + 4) return;
-    wt[g.s4(i, j, k)] = typ[p.t(i, j, k)];
+    const int v = typ[p.t(i, j, k)];
+    wt[g.s4(i, j, k)] = v;
+    type8[g.s4(i, j, k)] = (int8_t)v;
     if (i >= -1 && i <= g.nx + 2 && j >= -1 && j <= g.ny + 2 && k >= -1 && k <= g.nz + 2)
         walls[g.s2(i, j, k)] = tmp[p.t(i, j, k)];
 }
@@ -206,7 +209,7 @@ int preprocess_geometry_t(mflbm_context& c, const int32_t* walls_global_host, in
     solid_normals<T><<<g4, 128, 0, s>>>(p, g, typ, a, (T*)d.s_nx, (T*)d.s_ny, (T*)d.s_nz);
     GEO_LAUNCH("solid_normals");
     GEO_CUDA(cudaMemsetAsync(d.walls, 0, sizeof(int32_t) * g.n2(), s));
-    unpad<<<g4, 128, 0, s>>>(p, g, tmp, typ, d.walls, d.walls_type);
+    unpad<<<g4, 128, 0, s>>>(p, g, tmp, typ, d.walls, d.walls_type, d.type8);
     GEO_LAUNCH("unpad");
     GEO_CUDA(cudaStreamSynchronize(s));
     cleanup();
@@ -241,7 +244,7 @@ __global__ void init_phi(Grid g, int option, T z0, int open_z, T phi_inlet, T* p
 }
 
 template <class T>
-__global__ void init_pdf(Grid g, ModelConsts<T> c, const T* phi, T* pdf) {
+__global__ void init_pdf(Grid g, Bricks b, ModelConsts<T> c, const T* phi, T* pdf) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y, k = blockIdx.z;
     if (i > g.nx + 1) return;
@@ -249,22 +252,22 @@ __global__ void init_pdf(Grid g, ModelConsts<T> c, const T* phi, T* pdf) {
     const T r[2] = {T(1) * (T(1.0) + ph) * T(0.5), T(1) * (T(1.0) - ph) * T(0.5)};
     const T usqrt = T(0) * T(0) + T(0) * T(0) + T(0) * T(0);
     for (int gg = 0; gg < 2; ++gg) {
-        pdf[g.f1(i, j, k, 0, gg)] = r[gg] * c.w0 + r[gg] * c.w0 * (T(-1.5) * usqrt);
+        pdf[b.at(i, j, k, 0, gg)] = r[gg] * c.w0 + r[gg] * c.w0 * (T(-1.5) * usqrt);
         for (int q = 1; q < 19; ++q) {
             const T wq = q < 7 ? c.w1 : c.w2;
             const T cu = T(0);
-            pdf[g.f1(i, j, k, q, gg)] = r[gg] * wq + r[gg] * wq * (T(3.0) * cu + T(4.5) * cu * cu - T(1.5) * usqrt);
+            pdf[b.at(i, j, k, q, gg)] = r[gg] * wq + r[gg] * wq * (T(3.0) * cu + T(4.5) * cu * cu - T(1.5) * usqrt);
         }
     }
 }
 
 template <class T>
-__global__ void init_convective(Grid g, const T* pdf, const T* phi, T* f_cv, T* g_cv, T* phi_cv) {
+__global__ void init_convective(Grid g, Bricks b, const T* pdf, const T* phi, T* f_cv, T* g_cv, T* phi_cv) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
     if (i > g.nx + 1) return;
     for (int q = 0; q < 19; ++q) {
-        f_cv[g.cnv(i, j, q)] = pdf[g.f1(i, j, g.nz, q, 0)];
-        g_cv[g.cnv(i, j, q)] = pdf[g.f1(i, j, g.nz, q, 1)];
+        f_cv[g.cnv(i, j, q)] = pdf[b.at(i, j, g.nz, q, 0)];
+        g_cv[g.cnv(i, j, q)] = pdf[b.at(i, j, g.nz, q, 1)];
     }
     phi_cv[g.s1(i, j, 0)] = phi[g.s4(i, j, g.nz)];
 }
@@ -279,13 +282,13 @@ int init_fields_t(mflbm_context& c, int option, double z0) {
     int rc;
     init_phi<T><<<dim3(grid_for(g.nx + 8, 128), g.ny + 8, g.nz + 8), 128, 0, s>>>(g, option, T(z0), open_z, T(p.phi_inlet), (T*)d.phi);
     if ((rc = after_launch("init_phi")) != MFLBM_OK) return rc;
-    init_pdf<T><<<dim3(grid_for(g.nx + 2, 128), g.ny + 2, g.nz + 2), 128, 0, s>>>(g, make_consts<T>(), (const T*)d.phi, (T*)d.pdf);
+    init_pdf<T><<<dim3(grid_for(g.nx + 2, 128), g.ny + 2, g.nz + 2), 128, 0, s>>>(g, d.b, make_consts<T>(), (const T*)d.phi, (T*)d.pdf);
     if ((rc = after_launch("init_pdf")) != MFLBM_OK) return rc;
     MFLBM_CUDA(cudaMemsetAsync(d.f_cv, 0, sizeof(T) * g.plane1() * 19, s));
     MFLBM_CUDA(cudaMemsetAsync(d.g_cv, 0, sizeof(T) * g.plane1() * 19, s));
     MFLBM_CUDA(cudaMemsetAsync(d.phi_cv, 0, sizeof(T) * g.plane1(), s));
     if (p.outlet_BC == 1) {
-        init_convective<T><<<dim3(grid_for(g.nx + 2, 128), g.ny + 2), 128, 0, s>>>(g, (const T*)d.pdf, (const T*)d.phi, (T*)d.f_cv, (T*)d.g_cv, (T*)d.phi_cv);
+        init_convective<T><<<dim3(grid_for(g.nx + 2, 128), g.ny + 2), 128, 0, s>>>(g, d.b, (const T*)d.pdf, (const T*)d.phi, (T*)d.f_cv, (T*)d.g_cv, (T*)d.phi_cv);
         if ((rc = after_launch("init_convective")) != MFLBM_OK) return rc;
     }
     return MFLBM_OK;
@@ -299,7 +302,7 @@ int init_fields_t(mflbm_context& c, int option, double z0) {
 constexpr int NRED = 9;  // vol1, vol2, mass1, mass2, flux1, flux2, vol1_full, vol2_full, umax2
 
 template <class T>
-__global__ void __launch_bounds__(256) monitor_partials(Grid g, const uint32_t* list, ll n, const T* pdf, const T* phi,
+__global__ void __launch_bounds__(256) monitor_partials(Grid g, Bricks b, const uint32_t* list, ll n, const T* pdf, const T* phi,
                                                         const T* cnx, const T* cny, const T* cnz, const T* cnorm,
                                                         const T* curv, double gamma, double force_z, int k_lo, int k_hi,
                                                         double* partial) {
@@ -310,7 +313,7 @@ __global__ void __launch_bounds__(256) monitor_partials(Grid g, const uint32_t* 
         double f[19];
         const ll n1 = g.s1(i, j, k);
 #pragma unroll
-        for (int q = 0; q < 19; ++q) f[q] = (double)pdf[n1 + g.n1() * q] + (double)pdf[n1 + g.n1() * (q + 19)];
+        for (int q = 0; q < 19; ++q) f[q] = (double)pdf[b.at(i, j, k, q, 0)] + (double)pdf[b.at(i, j, k, q, 1)];
         double rho = 0;
 #pragma unroll
         for (int q = 0; q < 19; ++q) rho += f[q];
@@ -397,14 +400,15 @@ int monitor_t(mflbm_context& c, int nex_in, int nex_out, mflbm_monitor* out) {
     double* part2 = d.red + (ll)NRED * blocks;
     double* res = part2 + blocks;
     int rc;
-    monitor_partials<T><<<blocks, 256, 0, s>>>(g, d.fluid_list, d.n_fluid, (const T*)d.pdf, (const T*)d.phi,
+    monitor_partials<T><<<blocks, 256, 0, s>>>(g, d.b, d.fluid_list, d.n_fluid, (const T*)d.pdf, (const T*)d.phi,
                                                (const T*)d.cn_x, (const T*)d.cn_y, (const T*)d.cn_z,
                                                (const T*)d.c_norm, (const T*)d.curv, (double)T(c.params.lbm_gamma),
                                                (double)T(c.params.force_z), nex_in + 1, g.nz - nex_out, part);
     if ((rc = after_launch("monitor_partials")) != MFLBM_OK) return rc;
     fold_partials<<<NRED, 32, 0, s>>>(blocks, NRED, part, res);
     if ((rc = after_launch("fold_partials")) != MFLBM_OK) return rc;
-    sum_all<T><<<blocks, 256, 0, s>>>(g.n1() * 38, (const T*)d.pdf, part2);
+    // padding elements of the brick layout are zero and never written
+    sum_all<T><<<blocks, 256, 0, s>>>(d.b.S * 38, (const T*)d.pdf, part2);
     if ((rc = after_launch("sum_all")) != MFLBM_OK) return rc;
     fold_partials<<<1, 32, 0, s>>>(blocks, 1, part2, res + NRED);
     if ((rc = after_launch("fold_partials")) != MFLBM_OK) return rc;
@@ -421,7 +425,41 @@ int monitor_t(mflbm_context& c, int nex_in, int nex_out, mflbm_monitor* out) {
     return MFLBM_OK;
 }
 
+// Reference layout (f1) <-> brick layout, one thread per (node, direction).
+template <class T>
+__global__ void f1_to_bricks(Grid g, Bricks b, const T* f1, T* pdf) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, kq = blockIdx.z;
+    const int k = kq % (g.nz + 2), q = kq / (g.nz + 2);
+    if (i > g.nx + 1) return;
+    const ll s = g.s1(i, j, k);
+    pdf[b.at(i, j, k, q, 0)] = f1[s + g.n1() * q];
+    pdf[b.at(i, j, k, q, 1)] = f1[s + g.n1() * (q + 19)];
+}
+template <class T>
+__global__ void bricks_to_f1(Grid g, Bricks b, const T* pdf, T* f1) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, kq = blockIdx.z;
+    const int k = kq % (g.nz + 2), q = kq / (g.nz + 2);
+    if (i > g.nx + 1) return;
+    const ll s = g.s1(i, j, k);
+    f1[s + g.n1() * q] = pdf[b.at(i, j, k, q, 0)];
+    f1[s + g.n1() * (q + 19)] = pdf[b.at(i, j, k, q, 1)];
+}
+
+template <class T>
+int convert_t(mflbm_context& c, bool to_bricks) {
+    DeviceState& d = c.d;
+    const Grid g = d.g;
+    const dim3 grid(grid_for(g.nx + 2, 128), g.ny + 2, (g.nz + 2) * 19);
+    if (to_bricks) f1_to_bricks<T><<<grid, 128, 0, c.stream>>>(g, d.b, (const T*)d.staging, (T*)d.pdf);
+    else bricks_to_f1<T><<<grid, 128, 0, c.stream>>>(g, d.b, (const T*)d.pdf, (T*)d.staging);
+    return after_launch(to_bricks ? "f1_to_bricks" : "bricks_to_f1");
+}
+
 }  // namespace
+
+int convert_populations(mflbm_context& c, bool to_bricks) {
+    return c.params.precision == MFLBM_FP32 ? convert_t<float>(c, to_bricks) : convert_t<double>(c, to_bricks);
+}
 
 int preprocess_geometry(mflbm_context& c, const int32_t* walls_global, int iper) {
     return c.params.precision == MFLBM_FP32 ? preprocess_geometry_t<float>(c, walls_global, iper)

@@ -13,6 +13,10 @@ int boundaries(mflbm_context& c, bool odd) {
     return c.params.precision == MFLBM_FP32 ? launch_boundaries<float>(c, odd) : launch_boundaries<double>(c, odd);
 }
 
+int refresh_aux(mflbm_context& c) {
+    return c.params.precision == MFLBM_FP32 ? launch_refresh_aux<float>(c) : launch_refresh_aux<double>(c);
+}
+
 int gradient(mflbm_context& c) {
     return c.params.precision == MFLBM_FP32 ? launch_gradient<float>(c) : launch_gradient<double>(c);
 }

@@ -24,8 +24,7 @@ namespace MFLBM_NS {
 // post-collision, recoloured ones.  Returns the order parameter phi.
 // ===========================================================================
 template <class T>
-__device__ __forceinline__ T collide(const Phys<T>& P, T (&g1)[19], T (&g2)[19], T cnx, T cny, T cnz, T curv,
-                                     T cnorm) {
+__device__ __forceinline__ T collide(const Phys<T>& P, T (&g1)[19], T (&g2)[19], T cnx, T cny, T cnz, T force) {
     T f[19];
 #pragma unroll
     for (int q = 0; q < 19; ++q) f[q] = g1[q] + g2[q];
@@ -36,7 +35,7 @@ __device__ __forceinline__ T collide(const Phys<T>& P, T (&g1)[19], T (&g2)[19],
     for (int q = 1; q < 19; ++q) rho2 = rho2 + g2[q];
     const T phi = (rho1 - rho2) / (rho1 + rho2);
 
-    T tmp = T(0.5) * P.gamma * curv * cnorm;
+    T tmp = force;  // 0.5 * gamma * curv * c_norm (:147)
     const T fx = tmp * cnx, fy = tmp * cny, fz = tmp * cnz + P.force_z;
     const T omega = T(1) / (T(6) / ((T(1) + phi) * P.nui1 + (T(1) - phi) * P.nui2) + T(0.5));
     const T s_nu = omega;
@@ -169,139 +168,143 @@ __device__ __forceinline__ T collide(const Phys<T>& P, T (&g1)[19], T (&g2)[19],
 }
 
 // ===========================================================================
-// Collision + AA streaming over the fluid-node list.
+// Collision + AA streaming over the fluid-node list (brick layout).
 //   odd  step: populations pulled from slot q of node x - e_q, pushed to
 //              slot opp(q) of node x + e_q (src/main_iteration_GPU.cu:75-113, 348-384)
 //   even step: read from slot opp(q) of x, written to slot q of x (:414-452, 687-723)
-// pull[q + 19 g] / push[q + 19 g] are slot base pointers already offset by the
-// streaming displacement, so every access is base + n1.
+// In the brick layout the element offset of a neighbour depends only on the
+// parities of (x, y, z): each thread forms six deltas once and every access
+// is slot_base + element.
 // ===========================================================================
 template <class T> struct CollideArgs {
-    const T* pull[38];
-    T* push[38];
+    typedef typename Vec2<T>::type V2;
+    typedef typename Vec4<T>::type V4;
+    V2* slot[19];
     const uint32_t* list;
-    ll n;
-    int NX1, NY1, NX2, NY2, NX4, NY4;
+    int n;
+    int bx8, bxy8;  // element strides of one brick step in y and z
+    int nbx, nby;
+    int NX4, NY4;
     T* phi;
-    const T *cnx, *cny, *cnz, *cnorm, *curv;
+    const V4* aux;
     Phys<T> ph;
 };
 
 template <class T>
+__device__ __forceinline__ int brick_elem(const CollideArgs<T>& a, int x, int y, int z) {
+    return (((x >> 1) + a.nbx * ((y >> 1) + a.nby * (z >> 1))) << 3) | (x & 1) | ((y & 1) << 1) | ((z & 1) << 2);
+}
+
+template <class T, bool ODD>
 __global__ void __launch_bounds__(128) collide_stream_kernel(const CollideArgs<T> a) {
-    const ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+    typedef typename Vec2<T>::type V2;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= a.n) return;
     int x, y, z;
     unpack_xyz(a.list[t], x, y, z);
-    const int n1 = x + a.NX1 * (y + a.NY1 * z);
+    const int e0 = brick_elem(a, x, y, z);
+    // element deltas of the +1 / -1 neighbour along each axis
+    const int dxp = (x & 1) ? 7 : 1, dxm = (x & 1) ? -1 : -7;
+    const int dyp = (y & 1) ? a.bx8 - 2 : 2, dym = (y & 1) ? -2 : 2 - a.bx8;
+    const int dzp = (z & 1) ? a.bxy8 - 4 : 4, dzm = (z & 1) ? -4 : 4 - a.bxy8;
+    auto delta = [&](int q) {
+        return (ex(q) > 0 ? dxp : ex(q) < 0 ? dxm : 0) + (ey(q) > 0 ? dyp : ey(q) < 0 ? dym : 0) +
+               (ez(q) > 0 ? dzp : ez(q) < 0 ? dzm : 0);
+    };
     T g1[19], g2[19];
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
-        g1[q] = a.pull[q][n1];
-        g2[q] = a.pull[19 + q][n1];
+        const V2 v = ODD ? a.slot[q][e0 - delta(q)] : a.slot[opp(q)][e0];
+        g1[q] = v.x;
+        g2[q] = v.y;
     }
-    const ll n2 = (x + 1) + (ll)a.NX2 * ((y + 1) + (ll)a.NY2 * (z + 1));
-    const T cnx = a.cnx[n2], cny = a.cny[n2], cnz = a.cnz[n2], cnorm = a.cnorm[n2], curv = a.curv[n1];
-    const T phi = collide<T>(a.ph, g1, g2, cnx, cny, cnz, curv, cnorm);
-    a.phi[(x + 3) + (ll)a.NX4 * ((y + 3) + (ll)a.NY4 * (z + 3))] = phi;
+    const typename Vec4<T>::type av = a.aux[e0];
+    // aux.w = 0.5 * gamma * curv * c_norm, evaluated in that order by the gradient pass
+    const T phi = collide<T>(a.ph, g1, g2, av.x, av.y, av.z, av.w);
+    a.phi[(x + 3) + a.NX4 * ((y + 3) + a.NY4 * (z + 3))] = phi;
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
-        a.push[q][n1] = g1[q];
-        a.push[19 + q][n1] = g2[q];
+        V2 v;
+        v.x = g1[q];
+        v.y = g2[q];
+        if (ODD) a.slot[opp(q)][e0 + delta(q)] = v;
+        else a.slot[q][e0] = v;
     }
 }
 
 // ===========================================================================
-// Colour-gradient pipeline (src/main_iteration_GPU.cu:732-1003), ranges of the
-// reference launches (:2027-2054).  Solid / fluid boundary work runs over
-// precomputed node lists.
+// Colour-gradient pipeline (src/main_iteration_GPU.cu:732-1003), ranges of
+// the reference launches (:2027-2054):
+//   1. phi on solid boundary nodes (list, precomputed fluid-neighbour masks)
+//   2. interface normal + |grad phi| on [-1, n+2]^3, with the geometrical
+//      wetting applied in the same thread at fluid boundary nodes (the
+//      wetting only reads its own node's values, so fusing it is exact)
+//   3. normal on solid boundary nodes (list, masks)
+//   4. curvature on [1, n]^3, plus the per-node record the collision reads
 // ===========================================================================
 template <class T> struct GradArgs {
+    typedef typename Vec4<T>::type V4;
     Grid g;
-    const int32_t* walls;
-    const int32_t* wt;
+    Bricks b;
+    const int8_t* type8;
     const T *snx, *sny, *snz;
     T *phi, *cnx, *cny, *cnz, *cnorm, *curv;
-    const uint32_t *l_phi, *l_wet, *l_cn;
-    ll n_phi, n_wet, n_cn;
+    V4* aux;
+    const uint2 *l_phi, *l_cn;
+    int n_phi, n_cn;
     Phys<T> ph;
 };
 
-template <class T, class F>
-__device__ __forceinline__ T dx_iso4(const ModelConsts<T>& c, F f, int i, int j, int k) {
-    return c.iso4a * (f(i + 1, j, k) - f(i - 1, j, k)) +
-           c.iso4b * (f(i + 1, j + 1, k) - f(i - 1, j - 1, k) + f(i + 1, j - 1, k) - f(i - 1, j + 1, k) +
-                      f(i + 1, j, k + 1) - f(i - 1, j, k - 1) + f(i + 1, j, k - 1) - f(i - 1, j, k + 1));
+// ISO4 first derivatives along x, y, z of field F at flat index n of a padded
+// array with strides (1, sy, sz), in the reference's operand order.
+template <class T>
+__device__ __forceinline__ T iso4_dx(const ModelConsts<T>& c, const T* F, int n, int sy, int sz) {
+    return c.iso4a * (F[n + 1] - F[n - 1]) +
+           c.iso4b * (F[n + 1 + sy] - F[n - 1 - sy] + F[n + 1 - sy] - F[n - 1 + sy] +
+                      F[n + 1 + sz] - F[n - 1 - sz] + F[n + 1 - sz] - F[n - 1 + sz]);
 }
-template <class T, class F>
-__device__ __forceinline__ T dy_iso4(const ModelConsts<T>& c, F f, int i, int j, int k) {
-    return c.iso4a * (f(i, j + 1, k) - f(i, j - 1, k)) +
-           c.iso4b * (f(i + 1, j + 1, k) - f(i - 1, j - 1, k) + f(i - 1, j + 1, k) - f(i + 1, j - 1, k) +
-                      f(i, j + 1, k + 1) - f(i, j - 1, k - 1) + f(i, j + 1, k - 1) - f(i, j - 1, k + 1));
+template <class T>
+__device__ __forceinline__ T iso4_dy(const ModelConsts<T>& c, const T* F, int n, int sy, int sz) {
+    return c.iso4a * (F[n + sy] - F[n - sy]) +
+           c.iso4b * (F[n + 1 + sy] - F[n - 1 - sy] + F[n - 1 + sy] - F[n + 1 - sy] +
+                      F[n + sy + sz] - F[n - sy - sz] + F[n + sy - sz] - F[n - sy + sz]);
 }
-template <class T, class F>
-__device__ __forceinline__ T dz_iso4(const ModelConsts<T>& c, F f, int i, int j, int k) {
-    return c.iso4a * (f(i, j, k + 1) - f(i, j, k - 1)) +
-           c.iso4b * (f(i + 1, j, k + 1) - f(i - 1, j, k - 1) + f(i - 1, j, k + 1) - f(i + 1, j, k - 1) +
-                      f(i, j + 1, k + 1) - f(i, j - 1, k - 1) + f(i, j - 1, k + 1) - f(i, j + 1, k - 1));
+template <class T>
+__device__ __forceinline__ T iso4_dz(const ModelConsts<T>& c, const T* F, int n, int sy, int sz) {
+    return c.iso4a * (F[n + sz] - F[n - sz]) +
+           c.iso4b * (F[n + 1 + sz] - F[n - 1 - sz] + F[n - 1 + sz] - F[n + 1 - sz] +
+                      F[n + sy + sz] - F[n - sy - sz] + F[n - sy + sz] - F[n + sy - sz]);
 }
 
 template <class T> __device__ __forceinline__ T wq_of(const ModelConsts<T>& c, int q) { return q < 7 ? c.w1 : c.w2; }
 
 // phi on solid boundary nodes = weighted mean over fluid neighbours (:732-755)
 template <class T>
-__global__ void extrapolate_phi_kernel(const GradArgs<T> a) {
-    const ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(128) extrapolate_phi_kernel(const GradArgs<T> a) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= a.n_phi) return;
+    const uint2 e = a.l_phi[t];
     int i, j, k;
-    unpack_xyz(a.l_phi[t], i, j, k);
+    unpack_xyz(e.x, i, j, k);
+    const int sy = a.g.nx + 8, sz = (a.g.nx + 8) * (a.g.ny + 8);
+    const int n = (int)a.g.s4(i, j, k);
     T s = T(0), ws = T(0);
 #pragma unroll
     for (int q = 1; q < 19; ++q) {
-        const int u = i + ex(q), v = j + ey(q), w = k + ez(q);
-        if (a.wt[a.g.s4(u, v, w)] <= 0) {
-            s += a.phi[a.g.s4(u, v, w)] * wq_of(a.ph.c, q);
+        if (e.y & (1u << q)) {
+            s += a.phi[n + ex(q) + ey(q) * sy + ez(q) * sz] * wq_of(a.ph.c, q);
             ws += wq_of(a.ph.c, q);
         }
     }
-    a.phi[a.g.s4(i, j, k)] = s / ws;
+    a.phi[n] = s / ws;
 }
 
-// unit interface normal and |grad phi| on [-1, n+2]^3 (:757-807)
+// geometrical wetting: secant iteration turning the interface normal towards
+// the prescribed contact angle at a fluid boundary node (:809-878)
 template <class T>
-__global__ void __launch_bounds__(128) normals_kernel(const GradArgs<T> a) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
-    const int j = blockIdx.y - 1, k = blockIdx.z - 1;
-    if (i > a.g.nx + 2) return;
-    const Grid& g = a.g;
-    const T* phi = a.phi;
-    auto F = [&](int u, int v, int w) { return phi[g.s4(u, v, w)]; };
-    const T x = dx_iso4(a.ph.c, F, i, j, k);
-    const T y = dy_iso4(a.ph.c, F, i, j, k);
-    const T z = dz_iso4(a.ph.c, F, i, j, k);
-    const T nrm = sqrt(x * x + y * y + z * z);
-    const ll n = g.s2(i, j, k);
-    if (nrm < T(1e-6) || a.walls[n] == 1) {
-        a.cnx[n] = T(0); a.cny[n] = T(0); a.cnz[n] = T(0); a.cnorm[n] = T(0);
-    } else {
-        a.cnx[n] = x / nrm; a.cny[n] = y / nrm; a.cnz[n] = z / nrm; a.cnorm[n] = nrm;
-    }
-}
-
-// geometrical wetting at fluid boundary nodes: secant iteration that turns the
-// interface normal towards the prescribed contact angle (:809-878)
-template <class T>
-__global__ void wetting_kernel(const GradArgs<T> a) {
-    const ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= a.n_wet) return;
-    int i, j, k;
-    unpack_xyz(a.l_wet[t], i, j, k);
-    const ll n = a.g.s2(i, j, k), m = a.g.s4(i, j, k);
+__device__ __forceinline__ void wetting(T cs, T nwx, T nwy, T nwz, T& cx, T& cy, T& cz) {
     const T local_eps = T(1e-6), lambda = T(0.5);
-    if (!(a.cnorm[n] > local_eps)) return;
-    const T cs = a.ph.cos_theta;
-    const T nwx = a.snx[m], nwy = a.sny[m], nwz = a.snz[m];
-    T vcx0 = a.cnx[n], vcy0 = a.cny[n], vcz0 = a.cnz[n];
+    T vcx0 = cx, vcy0 = cy, vcz0 = cz;
     T vcx1 = vcx0 - lambda * (vcx0 + nwx);
     T vcy1 = vcy0 - lambda * (vcy0 + nwy);
     T vcz1 = vcz0 - lambda * (vcz0 + nwz);
@@ -331,53 +334,105 @@ __global__ void wetting_kernel(const GradArgs<T> a) {
         }
     }
     inv = T(1) / (T(1e-30) + sqrt(vcx2 * vcx2 + vcy2 * vcy2 + vcz2 * vcz2));
-    a.cnx[n] = vcx2 * inv; a.cny[n] = vcy2 * inv; a.cnz[n] = vcz2 * inv;
+    cx = vcx2 * inv; cy = vcy2 * inv; cz = vcz2 * inv;
+}
+
+// unit interface normal and |grad phi| on [-1, n+2]^3 (:757-807) + wetting (:809-878)
+template <class T>
+__global__ void __launch_bounds__(128) normals_kernel(const GradArgs<T> a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
+    const int j = (int)blockIdx.y - 1, k = (int)blockIdx.z - 1;
+    const Grid& g = a.g;
+    if (i > g.nx + 2) return;
+    const int sy4 = g.nx + 8, sz4 = (g.nx + 8) * (g.ny + 8);
+    const int n4 = (int)g.s4(i, j, k);
+    const T x = iso4_dx(a.ph.c, a.phi, n4, sy4, sz4);
+    const T y = iso4_dy(a.ph.c, a.phi, n4, sy4, sz4);
+    const T z = iso4_dz(a.ph.c, a.phi, n4, sy4, sz4);
+    const T nrm = sqrt(x * x + y * y + z * z);
+    const int type = a.type8[n4];
+    const int n2 = (int)g.s2(i, j, k);
+    if (nrm < T(1e-6) || type >= 1) {
+        a.cnx[n2] = T(0); a.cny[n2] = T(0); a.cnz[n2] = T(0); a.cnorm[n2] = T(0);
+        return;
+    }
+    T cx = x / nrm, cy = y / nrm, cz = z / nrm;
+    if (type == -1 && nrm > T(1e-6)) wetting(a.ph.cos_theta, a.snx[n4], a.sny[n4], a.snz[n4], cx, cy, cz);
+    a.cnx[n2] = cx; a.cny[n2] = cy; a.cnz[n2] = cz; a.cnorm[n2] = nrm;
 }
 
 // interface normal on solid boundary nodes = weighted mean over fluid neighbours (:880-906)
 template <class T>
-__global__ void extrapolate_normal_kernel(const GradArgs<T> a) {
-    const ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(128) extrapolate_normal_kernel(const GradArgs<T> a) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= a.n_cn) return;
+    const uint2 e = a.l_cn[t];
     int i, j, k;
-    unpack_xyz(a.l_cn[t], i, j, k);
-    T sx = T(0), sy = T(0), sz = T(0), ws = T(0);
+    unpack_xyz(e.x, i, j, k);
+    const int sy = a.g.nx + 4, sz = (a.g.nx + 4) * (a.g.ny + 4);
+    const int n = (int)a.g.s2(i, j, k);
+    T sx = T(0), syy = T(0), szz = T(0), ws = T(0);
 #pragma unroll
     for (int q = 1; q < 19; ++q) {
-        const int u = i + ex(q), v = j + ey(q), w = k + ez(q);
-        if (a.wt[a.g.s4(u, v, w)] <= 0) {
-            const ll m = a.g.s2(u, v, w);
+        if (e.y & (1u << q)) {
+            const int m = n + ex(q) + ey(q) * sy + ez(q) * sz;
             const T wq = wq_of(a.ph.c, q);
             sx += a.cnx[m] * wq;
-            sy += a.cny[m] * wq;
-            sz += a.cnz[m] * wq;
+            syy += a.cny[m] * wq;
+            szz += a.cnz[m] * wq;
             ws += wq;
         }
     }
-    const ll n = a.g.s2(i, j, k);
-    a.cnx[n] = sx / ws; a.cny[n] = sy / ws; a.cnz[n] = sz / ws;
+    a.cnx[n] = sx / ws; a.cny[n] = syy / ws; a.cnz[n] = szz / ws;
 }
 
-// interface curvature from the nine derivatives of the normal (:908-1003)
+// interface curvature from the nine derivatives of the normal (:908-1003);
+// one thread per node of [1, n]^3 mapped brick by brick so the per-node
+// record (n, 0.5*gamma*curv*c_norm) for the collision is written contiguously.
 template <class T>
 __global__ void __launch_bounds__(128) curvature_kernel(const GradArgs<T> a) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int j = blockIdx.y + 1, k = blockIdx.z + 1;
-    if (i > a.g.nx) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.b.S) return;
+    const int w = t & 7, brick = t >> 3;
+    const int bx = brick % a.b.nbx, byz = brick / a.b.nbx;
+    const int by = byz % a.b.nby, bz = byz / a.b.nby;
+    const int i = 2 * bx + (w & 1), j = 2 * by + ((w >> 1) & 1), k = 2 * bz + (w >> 2);
     const Grid& g = a.g;
-    const T *X = a.cnx, *Y = a.cny, *Z = a.cnz;
-    auto FX = [&](int u, int v, int w) { return X[g.s2(u, v, w)]; };
-    auto FY = [&](int u, int v, int w) { return Y[g.s2(u, v, w)]; };
-    auto FZ = [&](int u, int v, int w) { return Z[g.s2(u, v, w)]; };
+    if (i < 1 || i > g.nx || j < 1 || j > g.ny || k < 1 || k > g.nz) return;
+    const int sy = g.nx + 4, sz = (g.nx + 4) * (g.ny + 4);
+    const int n = (int)g.s2(i, j, k);
     const ModelConsts<T>& c = a.ph.c;
-    const T kxx = dx_iso4(c, FX, i, j, k), kyy = dy_iso4(c, FY, i, j, k), kzz = dz_iso4(c, FZ, i, j, k);
-    const T kxy = dy_iso4(c, FX, i, j, k), kxz = dz_iso4(c, FX, i, j, k);
-    const T kyx = dx_iso4(c, FY, i, j, k), kyz = dz_iso4(c, FY, i, j, k);
-    const T kzx = dx_iso4(c, FZ, i, j, k), kzy = dy_iso4(c, FZ, i, j, k);
-    const ll n = g.s2(i, j, k);
-    const T x = X[n], y = Y[n], z = Z[n];
-    a.curv[g.s1(i, j, k)] = (x * x - T(1)) * kxx + (y * y - T(1)) * kyy + (z * z - T(1)) * kzz +
-                            x * y * (kxy + kyx) + x * z * (kxz + kzx) + y * z * (kzy + kyz);
+    const T kxx = iso4_dx(c, a.cnx, n, sy, sz), kyy = iso4_dy(c, a.cny, n, sy, sz), kzz = iso4_dz(c, a.cnz, n, sy, sz);
+    const T kxy = iso4_dy(c, a.cnx, n, sy, sz), kxz = iso4_dz(c, a.cnx, n, sy, sz);
+    const T kyx = iso4_dx(c, a.cny, n, sy, sz), kyz = iso4_dz(c, a.cny, n, sy, sz);
+    const T kzx = iso4_dx(c, a.cnz, n, sy, sz), kzy = iso4_dy(c, a.cnz, n, sy, sz);
+    const T x = a.cnx[n], y = a.cny[n], z = a.cnz[n];
+    const T cv = (x * x - T(1)) * kxx + (y * y - T(1)) * kyy + (z * z - T(1)) * kzz +
+                 x * y * (kxy + kyx) + x * z * (kxz + kzx) + y * z * (kzy + kyz);
+    a.curv[g.s1(i, j, k)] = cv;
+    typename Vec4<T>::type r;
+    r.x = x; r.y = y; r.z = z;
+    r.w = T(0.5) * a.ph.gamma * cv * a.cnorm[n];
+    a.aux[t] = r;
+}
+
+// Per-node records (n, 0.5*gamma*curv*c_norm) from cn / c_norm / curv arrays
+// that were uploaded from the host (same mapping as curvature_kernel).
+template <class T>
+__global__ void __launch_bounds__(128) aux_kernel(const GradArgs<T> a) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.b.S) return;
+    const int w = t & 7, brick = t >> 3;
+    const int bx = brick % a.b.nbx, byz = brick / a.b.nbx;
+    const int by = byz % a.b.nby, bz = byz / a.b.nby;
+    const int i = 2 * bx + (w & 1), j = 2 * by + ((w >> 1) & 1), k = 2 * bz + (w >> 2);
+    const Grid& g = a.g;
+    if (i < 1 || i > g.nx || j < 1 || j > g.ny || k < 1 || k > g.nz) return;
+    const int n = (int)g.s2(i, j, k);
+    typename Vec4<T>::type r;
+    r.x = a.cnx[n]; r.y = a.cny[n]; r.z = a.cnz[n];
+    r.w = T(0.5) * a.ph.gamma * a.curv[g.s1(i, j, k)] * a.cnorm[n];
+    a.aux[t] = r;
 }
 
 // ===========================================================================
@@ -387,6 +442,7 @@ __global__ void __launch_bounds__(128) curvature_kernel(const GradArgs<T> a) {
 // ===========================================================================
 template <class T> struct BcArgs {
     Grid g;
+    Bricks b;
     const int32_t* walls;
     T *pdf, *phi, *W_in, *f_cv, *g_cv, *phi_cv;
     Phys<T> ph;
@@ -429,11 +485,11 @@ __global__ void inlet_velocity_kernel(const BcArgs<T> a) {
             const T wq = s == 0 ? a.ph.c.w1 : a.ph.c.w2;
             const int dx = kInlet[s][0], dy = kInlet[s][1], s0 = kInlet[s][2], s1 = kInlet[s][3];
             if (!AFTER_ODD) {
-                T& d = a.pdf[g.f1(i + dx, j + dy, 0, s0, gg)];
-                d = keep((a.pdf[g.f1(i, j, 1, s1, gg)] + T(6.0) * wq * inj), d, w);
+                T& d = a.pdf[a.b.at(i + dx, j + dy, 0, s0, gg)];
+                d = keep((a.pdf[a.b.at(i, j, 1, s1, gg)] + T(6.0) * wq * inj), d, w);
             } else {
-                T& d = a.pdf[g.f1(i, j, 1, s1, gg)];
-                d = keep((a.pdf[g.f1(i + dx, j + dy, 0, s0, gg)] + T(6.0) * wq * inj), d, w);
+                T& d = a.pdf[a.b.at(i, j, 1, s1, gg)];
+                d = keep((a.pdf[a.b.at(i + dx, j + dy, 0, s0, gg)] + T(6.0) * wq * inj), d, w);
             }
         }
     }
@@ -453,7 +509,7 @@ __global__ void inlet_pressure_kernel(const BcArgs<T> a) {
     const T c3 = T(0.333333333333333333), c6 = T(0.166666666666666667);
 #pragma unroll
     for (int gg = 0; gg < 2; ++gg) {
-        auto F = [&](int u, int v, int k, int e) -> T& { return a.pdf[g.f1(u, v, k, e, gg)]; };
+        auto F = [&](int u, int v, int k, int e) -> T& { return a.pdf[a.b.at(u, v, k, e, gg)]; };
         const T rc = gg == 0 ? r1 : r2;
         if (!AFTER_ODD) {
             const T t = (rc - (F(i, j, 1, 0) + F(i - 1, j, 1, 1) + F(i + 1, j, 1, 2) + F(i, j - 1, 1, 3) +
@@ -513,12 +569,12 @@ __global__ void outlet_convective_kernel(const BcArgs<T> a) {
             const int dx = kOutlet[s][0], dy = kOutlet[s][1], su = kOutlet[s][2], sd = kOutlet[s][3], sb = kOutlet[s][4];
             T& bv = buf[g.cnv(i, j, sb)];
             if (!AFTER_ODD) {
-                T& d = a.pdf[g.f1(i + dx, j + dy, nz + 1, su, gg)];
-                d = ((bv + u * a.pdf[g.f1(i + dx, j + dy, nz, su, gg)]) * temp) * T(1 - w) + d * T(w);
+                T& d = a.pdf[a.b.at(i + dx, j + dy, nz + 1, su, gg)];
+                d = ((bv + u * a.pdf[a.b.at(i + dx, j + dy, nz, su, gg)]) * temp) * T(1 - w) + d * T(w);
                 bv = d;
             } else {
-                T& d = a.pdf[g.f1(i, j, nz, sd, gg)];
-                d = ((bv + u * a.pdf[g.f1(i, j, nz - 1, sd, gg)]) * temp) * T(1 - w) + d * T(w);
+                T& d = a.pdf[a.b.at(i, j, nz, sd, gg)];
+                d = ((bv + u * a.pdf[a.b.at(i, j, nz - 1, sd, gg)]) * temp) * T(1 - w) + d * T(w);
                 bv = d;
             }
         }
@@ -538,7 +594,7 @@ __global__ void outlet_pressure_kernel(const BcArgs<T> a) {
     a.phi[g.s4(i, j, nz + 2)] = pz;
     a.phi[g.s4(i, j, nz + 3)] = pz;
     a.phi[g.s4(i, j, nz + 4)] = pz;
-    auto F = [&](int u, int v, int k, int e, int gg) -> T& { return a.pdf[g.f1(u, v, k, e, gg)]; };
+    auto F = [&](int u, int v, int k, int e, int gg) -> T& { return a.pdf[a.b.at(u, v, k, e, gg)]; };
     T t1;
     if (!AFTER_ODD) {
         t1 = (F(i, j, nz, 0, 0) + F(i - 1, j, nz, 1, 0) + F(i + 1, j, nz, 2, 0) + F(i, j - 1, nz, 3, 0) +
@@ -607,11 +663,11 @@ __global__ void periodic_z_kernel(const BcArgs<T> a) {
 #pragma unroll
         for (int s = 0; s < 5; ++s) {
             if (!ODD) {
-                a.pdf[g.f1(i, j, nz + 1, kZup[s], gg)] = a.pdf[g.f1(i, j, 1, kZup[s], gg)];
-                a.pdf[g.f1(i, j, 0, kZdn[s], gg)] = a.pdf[g.f1(i, j, nz, kZdn[s], gg)];
+                a.pdf[a.b.at(i, j, nz + 1, kZup[s], gg)] = a.pdf[a.b.at(i, j, 1, kZup[s], gg)];
+                a.pdf[a.b.at(i, j, 0, kZdn[s], gg)] = a.pdf[a.b.at(i, j, nz, kZdn[s], gg)];
             } else {
-                a.pdf[g.f1(i, j, 1, kZup[s], gg)] = a.pdf[g.f1(i, j, nz + 1, kZup[s], gg)];
-                a.pdf[g.f1(i, j, nz, kZdn[s], gg)] = a.pdf[g.f1(i, j, 0, kZdn[s], gg)];
+                a.pdf[a.b.at(i, j, 1, kZup[s], gg)] = a.pdf[a.b.at(i, j, nz + 1, kZup[s], gg)];
+                a.pdf[a.b.at(i, j, nz, kZdn[s], gg)] = a.pdf[a.b.at(i, j, 0, kZdn[s], gg)];
             }
         }
     for (int k = 1; k <= 4; ++k) {
@@ -631,11 +687,11 @@ __global__ void periodic_y_kernel(const BcArgs<T> a) {
 #pragma unroll
         for (int s = 0; s < 5; ++s) {
             if (!ODD) {
-                a.pdf[g.f1(i, ny + 1, k, kYup[s], gg)] = a.pdf[g.f1(i, 1, k, kYup[s], gg)];
-                a.pdf[g.f1(i, 0, k, kYdn[s], gg)] = a.pdf[g.f1(i, ny, k, kYdn[s], gg)];
+                a.pdf[a.b.at(i, ny + 1, k, kYup[s], gg)] = a.pdf[a.b.at(i, 1, k, kYup[s], gg)];
+                a.pdf[a.b.at(i, 0, k, kYdn[s], gg)] = a.pdf[a.b.at(i, ny, k, kYdn[s], gg)];
             } else {
-                a.pdf[g.f1(i, 1, k, kYup[s], gg)] = a.pdf[g.f1(i, ny + 1, k, kYup[s], gg)];
-                a.pdf[g.f1(i, ny, k, kYdn[s], gg)] = a.pdf[g.f1(i, 0, k, kYdn[s], gg)];
+                a.pdf[a.b.at(i, 1, k, kYup[s], gg)] = a.pdf[a.b.at(i, ny + 1, k, kYup[s], gg)];
+                a.pdf[a.b.at(i, ny, k, kYdn[s], gg)] = a.pdf[a.b.at(i, 0, k, kYdn[s], gg)];
             }
         }
     for (int j = 1; j <= 4; ++j) {
@@ -653,15 +709,15 @@ __global__ void periodic_zy_kernel(const BcArgs<T> a) {
 #pragma unroll
     for (int gg = 0; gg < 2; ++gg) {
         if (!ODD) {
-            a.pdf[g.f1(i, ny + 1, nz + 1, 18, gg)] = a.pdf[g.f1(i, 1, 1, 18, gg)];
-            a.pdf[g.f1(i, ny + 1, 0, 16, gg)] = a.pdf[g.f1(i, 1, nz, 16, gg)];
-            a.pdf[g.f1(i, 0, nz + 1, 17, gg)] = a.pdf[g.f1(i, ny, 1, 17, gg)];
-            a.pdf[g.f1(i, 0, 0, 15, gg)] = a.pdf[g.f1(i, ny, nz, 15, gg)];
+            a.pdf[a.b.at(i, ny + 1, nz + 1, 18, gg)] = a.pdf[a.b.at(i, 1, 1, 18, gg)];
+            a.pdf[a.b.at(i, ny + 1, 0, 16, gg)] = a.pdf[a.b.at(i, 1, nz, 16, gg)];
+            a.pdf[a.b.at(i, 0, nz + 1, 17, gg)] = a.pdf[a.b.at(i, ny, 1, 17, gg)];
+            a.pdf[a.b.at(i, 0, 0, 15, gg)] = a.pdf[a.b.at(i, ny, nz, 15, gg)];
         } else {
-            a.pdf[g.f1(i, 1, 1, 18, gg)] = a.pdf[g.f1(i, ny + 1, nz + 1, 18, gg)];
-            a.pdf[g.f1(i, 1, nz, 16, gg)] = a.pdf[g.f1(i, ny + 1, 0, 16, gg)];
-            a.pdf[g.f1(i, ny, 1, 17, gg)] = a.pdf[g.f1(i, 0, nz + 1, 17, gg)];
-            a.pdf[g.f1(i, ny, nz, 15, gg)] = a.pdf[g.f1(i, 0, 0, 15, gg)];
+            a.pdf[a.b.at(i, 1, 1, 18, gg)] = a.pdf[a.b.at(i, ny + 1, nz + 1, 18, gg)];
+            a.pdf[a.b.at(i, 1, nz, 16, gg)] = a.pdf[a.b.at(i, ny + 1, 0, 16, gg)];
+            a.pdf[a.b.at(i, ny, 1, 17, gg)] = a.pdf[a.b.at(i, 0, nz + 1, 17, gg)];
+            a.pdf[a.b.at(i, ny, nz, 15, gg)] = a.pdf[a.b.at(i, 0, 0, 15, gg)];
         }
     }
     for (int k = 1; k <= 4; ++k)
@@ -682,7 +738,7 @@ __global__ void porous_plate_kernel(const BcArgs<T> a) {
     const int zp = a.Zplate;
     if (!(zp >= 1 && zp <= g.nz) || (a.plate_cmd != 1 && a.plate_cmd != 2)) return;
     const int b = a.plate_cmd == 1 ? 0 : 1, o = 1 - b;
-    auto F = [&](int u, int v, int k, int e, int gg) -> T& { return a.pdf[g.f1(u, v, k, e, gg)]; };
+    auto F = [&](int u, int v, int k, int e, int gg) -> T& { return a.pdf[a.b.at(u, v, k, e, gg)]; };
     if (!AFTER_ODD) {
         F(i, j, zp, 6, b) = F(i, j, zp - 1, 5, b);
         F(i - 1, j, zp, 13, b) = F(i, j, zp - 1, 12, b);
@@ -736,20 +792,20 @@ GradArgs<T> grad_args(const mflbm_context& c) {
     const DeviceState& d = c.d;
     GradArgs<T> a;
     a.g = d.g;
-    a.walls = d.walls;
-    a.wt = d.walls_type;
+    a.b = d.b;
+    a.type8 = d.type8;
     a.snx = (const T*)d.s_nx; a.sny = (const T*)d.s_ny; a.snz = (const T*)d.s_nz;
     a.phi = (T*)d.phi; a.cnx = (T*)d.cn_x; a.cny = (T*)d.cn_y; a.cnz = (T*)d.cn_z;
     a.cnorm = (T*)d.c_norm; a.curv = (T*)d.curv;
-    a.l_phi = d.list_phi_ext; a.n_phi = d.n_phi_ext;
-    a.l_wet = d.list_wet; a.n_wet = d.n_wet;
-    a.l_cn = d.list_cn_ext; a.n_cn = d.n_cn_ext;
+    a.aux = (typename Vec4<T>::type*)d.aux;
+    a.l_phi = d.list_phi_ext; a.n_phi = (int)d.n_phi_ext;
+    a.l_cn = d.list_cn_ext; a.n_cn = (int)d.n_cn_ext;
     a.ph = make_phys<T>(c.params);
     return a;
 }
 
-// The five passes of the colour-gradient pipeline (also the start-up
-// colour_gradient, src/Phase_gradient.cpp:15-216, which is identical).
+// The colour-gradient pipeline (also the start-up colour_gradient,
+// src/Phase_gradient.cpp:15-216, which performs the same passes).
 template <class T>
 int launch_gradient(mflbm_context& c) {
     const GradArgs<T> a = grad_args<T>(c);
@@ -762,48 +818,41 @@ int launch_gradient(mflbm_context& c) {
     }
     normals_kernel<T><<<dim3(grid_for(g.nx + 4, 128), g.ny + 4, g.nz + 4), 128, 0, s>>>(a);
     if ((rc = after_launch("normals")) != MFLBM_OK) return rc;
-    if (a.n_wet) {
-        wetting_kernel<T><<<grid_for(a.n_wet, 128), 128, 0, s>>>(a);
-        if ((rc = after_launch("wetting")) != MFLBM_OK) return rc;
-    }
     if (a.n_cn) {
         extrapolate_normal_kernel<T><<<grid_for(a.n_cn, 128), 128, 0, s>>>(a);
         if ((rc = after_launch("extrapolate_normal")) != MFLBM_OK) return rc;
     }
-    curvature_kernel<T><<<dim3(grid_for(g.nx, 128), g.ny, g.nz), 128, 0, s>>>(a);
+    curvature_kernel<T><<<grid_for(c.d.b.S, 128), 128, 0, s>>>(a);
     return after_launch("curvature");
 }
 
 template <class T>
+int launch_refresh_aux(mflbm_context& c) {
+    const GradArgs<T> a = grad_args<T>(c);
+    aux_kernel<T><<<grid_for(c.d.b.S, 128), 128, 0, c.stream>>>(a);
+    return after_launch("aux");
+}
+
+template <class T>
 int launch_collide(mflbm_context& c, bool odd) {
+    typedef typename Vec2<T>::type V2;
     const DeviceState& d = c.d;
     const Grid& g = d.g;
     CollideArgs<T> a;
-    const ll S = g.n1();
-    const int NX1 = g.nx + 2, NY1 = g.ny + 2;
-    T* pdf = (T*)d.pdf;
-    for (int gg = 0; gg < 2; ++gg)
-        for (int q = 0; q < 19; ++q) {
-            const ll off = ex(q) + (ll)NX1 * (ey(q) + (ll)NY1 * ez(q));
-            if (odd) {
-                a.pull[q + 19 * gg] = pdf + S * (q + 19 * gg) - off;
-                a.push[q + 19 * gg] = pdf + S * (opp(q) + 19 * gg) + off;
-            } else {
-                a.pull[q + 19 * gg] = pdf + S * (opp(q) + 19 * gg);
-                a.push[q + 19 * gg] = pdf + S * (q + 19 * gg);
-            }
-        }
+    V2* pdf = (V2*)d.pdf;
+    for (int q = 0; q < 19; ++q) a.slot[q] = pdf + d.b.S * q;
     a.list = d.fluid_list;
-    a.n = d.n_fluid;
-    a.NX1 = NX1; a.NY1 = NY1;
-    a.NX2 = g.nx + 4; a.NY2 = g.ny + 4;
+    a.n = (int)d.n_fluid;
+    a.nbx = d.b.nbx; a.nby = d.b.nby;
+    a.bx8 = 8 * d.b.nbx;
+    a.bxy8 = 8 * d.b.nbx * d.b.nby;
     a.NX4 = g.nx + 8; a.NY4 = g.ny + 8;
     a.phi = (T*)d.phi;
-    a.cnx = (const T*)d.cn_x; a.cny = (const T*)d.cn_y; a.cnz = (const T*)d.cn_z;
-    a.cnorm = (const T*)d.c_norm; a.curv = (const T*)d.curv;
+    a.aux = (const typename Vec4<T>::type*)d.aux;
     a.ph = make_phys<T>(c.params);
     if (a.n == 0) return MFLBM_OK;
-    collide_stream_kernel<T><<<grid_for(a.n, 128), 128, 0, c.stream>>>(a);
+    if (odd) collide_stream_kernel<T, true><<<grid_for(a.n, 128), 128, 0, c.stream>>>(a);
+    else collide_stream_kernel<T, false><<<grid_for(a.n, 128), 128, 0, c.stream>>>(a);
     return after_launch("collide_stream");
 }
 
@@ -814,6 +863,7 @@ int launch_boundaries(mflbm_context& c, bool odd) {
     const mflbm_params& p = c.params;
     BcArgs<T> a;
     a.g = g;
+    a.b = d.b;
     a.walls = d.walls;
     a.pdf = (T*)d.pdf; a.phi = (T*)d.phi; a.W_in = (T*)d.W_in;
     a.f_cv = (T*)d.f_cv; a.g_cv = (T*)d.g_cv; a.phi_cv = (T*)d.phi_cv;
