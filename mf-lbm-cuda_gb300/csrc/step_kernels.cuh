@@ -211,10 +211,12 @@ __global__ void __launch_bounds__(128) collide_stream_kernel(const CollideArgs<T
         return (ex(q) > 0 ? dxp : ex(q) < 0 ? dxm : 0) + (ey(q) > 0 ? dyp : ey(q) < 0 ? dym : 0) +
                (ez(q) > 0 ? dzp : ez(q) < 0 ? dzm : 0);
     };
+    // delta(q) is the element offset of x + e_q; the offsets are not
+    // antisymmetric (they depend on parity), so x - e_q is at delta(opp(q))
     T g1[19], g2[19];
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
-        const V2 v = ODD ? a.slot[q][e0 - delta(q)] : a.slot[opp(q)][e0];
+        const V2 v = ODD ? a.slot[q][e0 + delta(opp(q))] : a.slot[opp(q)][e0];
         g1[q] = v.x;
         g2[q] = v.y;
     }
