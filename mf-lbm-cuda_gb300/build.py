@@ -32,7 +32,7 @@ UNITS = {
     "setup.cu": ["-fmad=false"],
     "capi.cu": [],
 }
-HEADERS = ["common.cuh", "context.cuh", "step_kernels.cuh", "setup.cuh"]
+HEADERS = ["common.cuh", "context.cuh", "step_kernels.cuh", "collide.cuh", "gradient.cuh", "boundary.cuh", "setup.cuh"]
 
 
 def _run(cmd):

@@ -50,7 +50,7 @@ void free_all(mflbm_context* c) {
     DeviceState& d = c->d;
     void* ptrs[] = {d.pdf, d.phi, d.cn_x, d.cn_y, d.cn_z, d.c_norm, d.curv, d.W_in, d.f_cv, d.g_cv, d.phi_cv,
                     d.walls, d.walls_type, d.s_nx, d.s_ny, d.s_nz, d.fluid_list, d.list_phi_ext,
-                    d.list_cn_ext, d.red, d.staging, d.aux, d.type8};
+                    d.list_cn_ext, d.red, d.staging, d.aux, d.type8, d.cnv4};
     for (void* p : ptrs) if (p) cudaFree(p);
     d = DeviceState{};
     if (c->pair_graph) cudaGraphExecDestroy(c->pair_graph);
@@ -125,7 +125,17 @@ int flavour_boundaries(mflbm_context* c, bool odd) {
     return c->params.fp_mode == MFLBM_STRICT ? strict::boundaries(*c, odd) : fast::boundaries(*c, odd);
 }
 int flavour_gradient(mflbm_context* c) {
+    c->d.arrays_stale = true;
     return c->params.fp_mode == MFLBM_STRICT ? strict::gradient(*c) : fast::gradient(*c);
+}
+
+// Materialise the reference-layout cn_x/y/z, c_norm and curv arrays from the
+// per-node records (only needed when the host reads them).
+int export_arrays(mflbm_context* c) {
+    if (!c->d.arrays_stale) return MFLBM_OK;
+    int rc = c->params.fp_mode == MFLBM_STRICT ? strict::export_arrays(*c) : fast::export_arrays(*c);
+    if (rc == MFLBM_OK) c->d.arrays_stale = false;
+    return rc;
 }
 
 TimingPool& timing_pool(mflbm_context* c) {
@@ -212,7 +222,8 @@ int mflbm_create(const mflbm_params* params, mflbm_context** out) {
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { delete c; return fail(MFLBM_E_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e)); }
     struct { void** p; size_t bytes; } allocs[] = {
-        {&d.pdf, T * d.b.S * 38}, {&d.aux, T * 4 * d.b.S}, {(void**)&d.type8, (size_t)g.n4()},
+        {&d.pdf, T * d.b.S * 38}, {&d.aux, T * 4 * g.n1()}, {&d.cnv4, T * 4 * g.n2()},
+        {(void**)&d.type8, (size_t)g.n4()},
         {&d.phi, T * g.n4()}, {&d.cn_x, T * g.n2()}, {&d.cn_y, T * g.n2()},
         {&d.cn_z, T * g.n2()}, {&d.c_norm, T * g.n2()}, {&d.curv, T * g.n1()}, {&d.W_in, T * g.plane1()},
         {&d.f_cv, T * g.plane1() * 19}, {&d.g_cv, T * g.plane1() * 19}, {&d.phi_cv, T * g.plane1()},
@@ -349,6 +360,7 @@ int mflbm_upload_fields(mflbm_context* c, const void* pdf, const void* phi, cons
         MFLBM_CUDA(cudaMemcpyAsync(d.c_norm, c_norm, T * g.n2(), cudaMemcpyHostToDevice, s));
         MFLBM_CUDA(cudaMemcpyAsync(d.curv, curv, T * g.n1(), cudaMemcpyHostToDevice, s));
         rc = c->params.fp_mode == MFLBM_STRICT ? strict::refresh_aux(*c) : fast::refresh_aux(*c);
+        c->d.arrays_stale = false;
     } else {
         rc = flavour_gradient(c);
     }
@@ -369,6 +381,10 @@ int mflbm_download_fields(mflbm_context* c, void* pdf, void* phi, void* cn_x, vo
         int rc = ensure_staging(c);
         if (rc != MFLBM_OK) return rc;
         if ((rc = convert_populations(*c, false)) != MFLBM_OK) return rc;
+    }
+    if (cn_x || cn_y || cn_z || c_norm || curv) {
+        int rc = export_arrays(c);
+        if (rc != MFLBM_OK) return rc;
     }
     struct { void* dst; const void* src; size_t n; } cp[] = {
         {pdf, d.staging, T * g.n1() * 38}, {phi, d.phi, T * g.n4()}, {cn_x, d.cn_x, T * g.n2()}, {cn_y, d.cn_y, T * g.n2()},
@@ -422,6 +438,7 @@ int mflbm_monitor_reduce(mflbm_context* c, int n_exclude_inlet, int n_exclude_ou
     int rc = require_ready(c);
     if (rc != MFLBM_OK) return rc;
     if (!out) return fail(MFLBM_E_ARG, "null output");
+    if ((rc = export_arrays(c)) != MFLBM_OK) return rc;
     return monitor(*c, n_exclude_inlet, n_exclude_outlet, out);
 }
 

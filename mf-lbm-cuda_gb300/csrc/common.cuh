@@ -183,12 +183,14 @@ inline Phys<T> make_phys(const mflbm_params& p) {
 // Flavour entry points (step_fast.cu / step_strict.cu).
 namespace fast {
 int refresh_aux(mflbm_context& c);
+int export_arrays(mflbm_context& c);
 int collide(mflbm_context& c, bool odd);
 int boundaries(mflbm_context& c, bool odd);
 int gradient(mflbm_context& c);
 }
 namespace strict {
 int refresh_aux(mflbm_context& c);
+int export_arrays(mflbm_context& c);
 int collide(mflbm_context& c, bool odd);
 int boundaries(mflbm_context& c, bool odd);
 int gradient(mflbm_context& c);

@@ -13,8 +13,10 @@ struct DeviceState {
     // populations in the brick layout (common.cuh); fields in the reference layouts (s4 / s2 / s1)
     void* pdf = nullptr;
     void* staging = nullptr;        // reference-layout (f1) buffer for uploads / downloads
-    void* aux = nullptr;            // per brick element: (n_x, n_y, n_z, 0.5*gamma*curv*c_norm)
+    void* cnv4 = nullptr;           // s2: (n_x, n_y, n_z, |grad phi|) per node
+    void* aux = nullptr;            // s1: (n_x, n_y, n_z, 0.5*gamma*curv*c_norm) per node
     int8_t* type8 = nullptr;        // walls_type as int8 (s4)
+    bool arrays_stale = false;      // cn_x/y/z, c_norm, curv behind the records
     void* phi = nullptr;
     void* cn_x = nullptr;
     void* cn_y = nullptr;

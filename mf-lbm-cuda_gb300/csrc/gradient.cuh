@@ -1,0 +1,316 @@
+// Colour-gradient pipeline of one time step (included by step_kernels.cuh):
+// src/main_iteration_GPU.cu:732-1003 with the ranges of the reference's
+// launches (:2027-2054).
+//
+//   1. phi on solid boundary nodes (list with precomputed fluid-neighbour masks)
+//   2. unit interface normal + |grad phi| on [-1, n+2]^3, with the geometrical
+//      wetting applied in the same thread at fluid boundary nodes (it only
+//      reads its own node's values, so fusing it is exact); stored as one
+//      record (n_x, n_y, n_z, |grad phi|) per node of the s2 layout
+//   3. normal on solid boundary nodes (list with masks)
+//   4. curvature on [1, n]^3 and the record the collision reads:
+//      (n_x, n_y, n_z, 0.5 * gamma * curv * c_norm) per node of the s1 layout
+//
+// The reference-layout arrays cn_x/y/z, c_norm and curv are produced from the
+// records only when the host asks for them (export), and records are rebuilt
+// from such arrays when the host uploads them (pack).
+#pragma once
+#include "context.cuh"
+
+namespace mflbm {
+namespace MFLBM_NS {
+
+template <class T> struct GradArgs {
+    typedef typename Vec4<T>::type V4;
+    Grid g;
+    const int8_t* type8;
+    const T *snx, *sny, *snz;
+    T* phi;
+    V4* cn;    // s2: (n_x, n_y, n_z, |grad phi|)
+    V4* aux;   // s1: (n_x, n_y, n_z, 0.5 * gamma * curv * c_norm)
+    T *cnx, *cny, *cnz, *cnorm, *curv;  // reference-layout arrays (export / pack)
+    const uint2 *l_phi, *l_cn;
+    int n_phi, n_cn;
+    Phys<T> ph;
+};
+
+template <class T> __device__ __forceinline__ T wq_of(const ModelConsts<T>& c, int q) { return q < 7 ? c.w1 : c.w2; }
+
+// phi on solid boundary nodes = weighted mean over fluid neighbours (:732-755)
+template <class T>
+__global__ void __launch_bounds__(128) extrapolate_phi_kernel(const GradArgs<T> a) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.n_phi) return;
+    const uint2 e = a.l_phi[t];
+    int i, j, k;
+    unpack_xyz(e.x, i, j, k);
+    const int sy = a.g.nx + 8, sz = (a.g.nx + 8) * (a.g.ny + 8);
+    const int n = (int)a.g.s4(i, j, k);
+    T s = T(0), ws = T(0);
+#pragma unroll
+    for (int q = 1; q < 19; ++q) {
+        if (e.y & (1u << q)) {
+            s += a.phi[n + ex(q) + ey(q) * sy + ez(q) * sz] * wq_of(a.ph.c, q);
+            ws += wq_of(a.ph.c, q);
+        }
+    }
+    a.phi[n] = s / ws;
+}
+
+// geometrical wetting: secant iteration turning the interface normal towards
+// the prescribed contact angle at a fluid boundary node (:809-878)
+template <class T>
+__device__ __forceinline__ void wetting(T cs, T nwx, T nwy, T nwz, T& cx, T& cy, T& cz) {
+    const T local_eps = T(1e-6), lambda = T(0.5);
+    T vcx0 = cx, vcy0 = cy, vcz0 = cz;
+    T vcx1 = vcx0 - lambda * (vcx0 + nwx);
+    T vcy1 = vcy0 - lambda * (vcy0 + nwy);
+    T vcz1 = vcz0 - lambda * (vcz0 + nwz);
+    T err0 = (nwx * vcx0 + nwy * vcy0 + nwz * vcz0) - cs;
+    if (!((fabs(vcx0 + nwx) + fabs(vcy0 + nwy) + fabs(vcz0 + nwz) > local_eps ||
+           fabs(vcx0 - nwx) + fabs(vcy0 - nwy) + fabs(vcz0 - nwz) > local_eps) &&
+          err0 > local_eps))
+        return;
+    T err1 = (nwx * vcx1 + nwy * vcy1 + nwz * vcz1) - sqrt(vcx1 * vcx1 + vcy1 * vcy1 + vcz1 * vcz1) * cs;
+    T inv = T(1) / (err1 - err0);
+    T vcx2 = inv * (vcx0 * err1 - vcx1 * err0);
+    T vcy2 = inv * (vcy0 * err1 - vcy1 * err0);
+    T vcz2 = inv * (vcz0 * err1 - vcz1 * err0);
+    T err2 = (nwx * vcx2 + nwy * vcy2 + nwz * vcz2) - sqrt(vcx2 * vcx2 + vcy2 * vcy2 + vcz2 * vcz2) * cs;
+    if (err2 > local_eps) {
+        for (int it = 2; it <= 4; ++it) {
+            vcx0 = vcx1; vcy0 = vcy1; vcz0 = vcz1;
+            vcx1 = vcx2; vcy1 = vcy2; vcz1 = vcz2;
+            err0 = (nwx * vcx0 + nwy * vcy0 + nwz * vcz0) - sqrt(vcx0 * vcx0 + vcy0 * vcy0 + vcz0 * vcz0) * cs;
+            err1 = (nwx * vcx1 + nwy * vcy1 + nwz * vcz1) - sqrt(vcx1 * vcx1 + vcy1 * vcy1 + vcz1 * vcz1) * cs;
+            inv = T(1) / (err1 - err0);
+            if (isinf(inv)) break;
+            vcx2 = inv * (vcx0 * err1 - vcx1 * err0);
+            vcy2 = inv * (vcy0 * err1 - vcy1 * err0);
+            vcz2 = inv * (vcz0 * err1 - vcz1 * err0);
+            err2 = (nwx * vcx2 + nwy * vcy2 + nwz * vcz2) - sqrt(vcx2 * vcx2 + vcy2 * vcy2 + vcz2 * vcz2) * cs;
+        }
+    }
+    inv = T(1) / (T(1e-30) + sqrt(vcx2 * vcx2 + vcy2 * vcy2 + vcz2 * vcz2));
+    cx = vcx2 * inv; cy = vcy2 * inv; cz = vcz2 * inv;
+}
+
+// ISO4 first derivatives of a scalar field at flat index n of an array with
+// strides (1, sy, sz), in the reference's operand order (:765-791).
+template <class T>
+__device__ __forceinline__ T iso4_dx(const ModelConsts<T>& c, const T* F, int n, int sy, int sz) {
+    return c.iso4a * (F[n + 1] - F[n - 1]) +
+           c.iso4b * (F[n + 1 + sy] - F[n - 1 - sy] + F[n + 1 - sy] - F[n - 1 + sy] +
+                      F[n + 1 + sz] - F[n - 1 - sz] + F[n + 1 - sz] - F[n - 1 + sz]);
+}
+template <class T>
+__device__ __forceinline__ T iso4_dy(const ModelConsts<T>& c, const T* F, int n, int sy, int sz) {
+    return c.iso4a * (F[n + sy] - F[n - sy]) +
+           c.iso4b * (F[n + 1 + sy] - F[n - 1 - sy] + F[n - 1 + sy] - F[n + 1 - sy] +
+                      F[n + sy + sz] - F[n - sy - sz] + F[n + sy - sz] - F[n - sy + sz]);
+}
+template <class T>
+__device__ __forceinline__ T iso4_dz(const ModelConsts<T>& c, const T* F, int n, int sy, int sz) {
+    return c.iso4a * (F[n + sz] - F[n - sz]) +
+           c.iso4b * (F[n + 1 + sz] - F[n - 1 - sz] + F[n - 1 + sz] - F[n + 1 - sz] +
+                      F[n + sy + sz] - F[n - sy - sz] + F[n - sy + sz] - F[n + sy - sz]);
+}
+
+// unit interface normal and |grad phi| on [-1, n+2]^3 (:757-807) + wetting (:809-878)
+template <class T>
+__global__ void __launch_bounds__(128) normals_kernel(const GradArgs<T> a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
+    const int j = (int)blockIdx.y - 1, k = (int)blockIdx.z - 1;
+    const Grid& g = a.g;
+    if (i > g.nx + 2) return;
+    const int sy4 = g.nx + 8, sz4 = (g.nx + 8) * (g.ny + 8);
+    const int n4 = (int)g.s4(i, j, k);
+    const T x = iso4_dx(a.ph.c, a.phi, n4, sy4, sz4);
+    const T y = iso4_dy(a.ph.c, a.phi, n4, sy4, sz4);
+    const T z = iso4_dz(a.ph.c, a.phi, n4, sy4, sz4);
+    const T nrm = sqrt(x * x + y * y + z * z);
+    const int type = a.type8[n4];
+    typename Vec4<T>::type r;
+    if (nrm < T(1e-6) || type >= 1) {
+        r.x = T(0); r.y = T(0); r.z = T(0); r.w = T(0);
+    } else {
+        T cx = x / nrm, cy = y / nrm, cz = z / nrm;
+        if (type == -1 && nrm > T(1e-6)) wetting(a.ph.cos_theta, a.snx[n4], a.sny[n4], a.snz[n4], cx, cy, cz);
+        r.x = cx; r.y = cy; r.z = cz; r.w = nrm;
+    }
+    a.cn[g.s2(i, j, k)] = r;
+}
+
+// interface normal on solid boundary nodes = weighted mean over fluid neighbours (:880-906)
+template <class T>
+__global__ void __launch_bounds__(128) extrapolate_normal_kernel(const GradArgs<T> a) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.n_cn) return;
+    const uint2 e = a.l_cn[t];
+    int i, j, k;
+    unpack_xyz(e.x, i, j, k);
+    const int sy = a.g.nx + 4, sz = (a.g.nx + 4) * (a.g.ny + 4);
+    const int n = (int)a.g.s2(i, j, k);
+    T sx = T(0), syy = T(0), szz = T(0), ws = T(0);
+#pragma unroll
+    for (int q = 1; q < 19; ++q) {
+        if (e.y & (1u << q)) {
+            const typename Vec4<T>::type v = a.cn[n + ex(q) + ey(q) * sy + ez(q) * sz];
+            const T wq = wq_of(a.ph.c, q);
+            sx += v.x * wq;
+            syy += v.y * wq;
+            szz += v.z * wq;
+            ws += wq;
+        }
+    }
+    typename Vec4<T>::type r = a.cn[n];
+    r.x = sx / ws; r.y = syy / ws; r.z = szz / ws;
+    a.cn[n] = r;
+}
+
+// curvature at node n (s2 index) from the nine ISO4 derivatives of the
+// normal (:916-1002); the 18 neighbour records are loaded once.
+template <class T>
+__device__ __forceinline__ T curvature_at(const ModelConsts<T>& c, const typename Vec4<T>::type* cn, int n, int sy,
+                                          int sz, typename Vec4<T>::type& ctr) {
+    typedef typename Vec4<T>::type V4;
+    ctr = cn[n];
+    const V4 xp = cn[n + 1], xm = cn[n - 1], yp = cn[n + sy], ym = cn[n - sy], zp = cn[n + sz], zm = cn[n - sz];
+    const V4 xpyp = cn[n + 1 + sy], xmym = cn[n - 1 - sy], xpym = cn[n + 1 - sy], xmyp = cn[n - 1 + sy];
+    const V4 xpzp = cn[n + 1 + sz], xmzm = cn[n - 1 - sz], xpzm = cn[n + 1 - sz], xmzp = cn[n - 1 + sz];
+    const V4 ypzp = cn[n + sy + sz], ymzm = cn[n - sy - sz], ypzm = cn[n + sy - sz], ymzp = cn[n - sy + sz];
+#define MFLBM_DX(C) (c.iso4a * (xp.C - xm.C) + c.iso4b * (xpyp.C - xmym.C + xpym.C - xmyp.C + xpzp.C - xmzm.C + xpzm.C - xmzp.C))
+#define MFLBM_DY(C) (c.iso4a * (yp.C - ym.C) + c.iso4b * (xpyp.C - xmym.C + xmyp.C - xpym.C + ypzp.C - ymzm.C + ypzm.C - ymzp.C))
+#define MFLBM_DZ(C) (c.iso4a * (zp.C - zm.C) + c.iso4b * (xpzp.C - xmzm.C + xmzp.C - xpzm.C + ypzp.C - ymzm.C + ymzp.C - ypzm.C))
+    const T kxx = MFLBM_DX(x), kyy = MFLBM_DY(y), kzz = MFLBM_DZ(z);
+    const T kxy = MFLBM_DY(x), kxz = MFLBM_DZ(x);
+    const T kyx = MFLBM_DX(y), kyz = MFLBM_DZ(y);
+    const T kzx = MFLBM_DX(z), kzy = MFLBM_DY(z);
+#undef MFLBM_DX
+#undef MFLBM_DY
+#undef MFLBM_DZ
+    const T x = ctr.x, y = ctr.y, z = ctr.z;
+    return (x * x - T(1)) * kxx + (y * y - T(1)) * kyy + (z * z - T(1)) * kzz +
+           x * y * (kxy + kyx) + x * z * (kxz + kzx) + y * z * (kzy + kyz);
+}
+
+// curvature on [1, n]^3: AUX writes the collision's record (s1 layout),
+// otherwise the reference-layout curv array.
+template <class T, bool AUX>
+__global__ void __launch_bounds__(128) curvature_kernel(const GradArgs<T> a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y + 1, k = blockIdx.z + 1;
+    const Grid& g = a.g;
+    if (i > g.nx) return;
+    const int sy = g.nx + 4, sz = (g.nx + 4) * (g.ny + 4);
+    typename Vec4<T>::type ctr;
+    const T cv = curvature_at<T>(a.ph.c, a.cn, (int)g.s2(i, j, k), sy, sz, ctr);
+    const int n1 = (int)g.s1(i, j, k);
+    if (AUX) {
+        typename Vec4<T>::type r;
+        r.x = ctr.x; r.y = ctr.y; r.z = ctr.z;
+        r.w = T(0.5) * a.ph.gamma * cv * ctr.w;
+        a.aux[n1] = r;
+    } else {
+        a.curv[n1] = cv;
+    }
+}
+
+// records -> reference arrays cn_x/y/z, c_norm on the s2 range
+template <class T>
+__global__ void __launch_bounds__(256) split_normals_kernel(const GradArgs<T> a, int n2) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n2) return;
+    const typename Vec4<T>::type v = a.cn[t];
+    a.cnx[t] = v.x; a.cny[t] = v.y; a.cnz[t] = v.z; a.cnorm[t] = v.w;
+}
+
+// reference arrays (uploaded by the host) -> records
+template <class T>
+__global__ void __launch_bounds__(256) pack_normals_kernel(const GradArgs<T> a, int n2) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n2) return;
+    typename Vec4<T>::type v;
+    v.x = a.cnx[t]; v.y = a.cny[t]; v.z = a.cnz[t]; v.w = a.cnorm[t];
+    a.cn[t] = v;
+}
+template <class T>
+__global__ void __launch_bounds__(128) aux_from_arrays_kernel(const GradArgs<T> a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y + 1, k = blockIdx.z + 1;
+    const Grid& g = a.g;
+    if (i > g.nx) return;
+    const int n2 = (int)g.s2(i, j, k), n1 = (int)g.s1(i, j, k);
+    typename Vec4<T>::type r;
+    r.x = a.cnx[n2]; r.y = a.cny[n2]; r.z = a.cnz[n2];
+    r.w = T(0.5) * a.ph.gamma * a.curv[n1] * a.cnorm[n2];
+    a.aux[n1] = r;
+}
+
+// ---------------------------------------------------------------------------
+template <class T>
+GradArgs<T> grad_args(const mflbm_context& c) {
+    const DeviceState& d = c.d;
+    GradArgs<T> a;
+    a.g = d.g;
+    a.type8 = d.type8;
+    a.snx = (const T*)d.s_nx; a.sny = (const T*)d.s_ny; a.snz = (const T*)d.s_nz;
+    a.phi = (T*)d.phi;
+    a.cn = (typename Vec4<T>::type*)d.cnv4;
+    a.aux = (typename Vec4<T>::type*)d.aux;
+    a.cnx = (T*)d.cn_x; a.cny = (T*)d.cn_y; a.cnz = (T*)d.cn_z;
+    a.cnorm = (T*)d.c_norm; a.curv = (T*)d.curv;
+    a.l_phi = d.list_phi_ext; a.n_phi = (int)d.n_phi_ext;
+    a.l_cn = d.list_cn_ext; a.n_cn = (int)d.n_cn_ext;
+    a.ph = make_phys<T>(c.params);
+    return a;
+}
+
+// The per-step pipeline (also the start-up colour_gradient,
+// src/Phase_gradient.cpp:15-216, which performs the same passes).
+template <class T>
+int launch_gradient(mflbm_context& c) {
+    const GradArgs<T> a = grad_args<T>(c);
+    const Grid& g = c.d.g;
+    cudaStream_t s = c.stream;
+    int rc;
+    if (a.n_phi) {
+        extrapolate_phi_kernel<T><<<grid_for(a.n_phi, 128), 128, 0, s>>>(a);
+        if ((rc = after_launch("extrapolate_phi")) != MFLBM_OK) return rc;
+    }
+    normals_kernel<T><<<dim3(grid_for(g.nx + 4, 128), g.ny + 4, g.nz + 4), 128, 0, s>>>(a);
+    if ((rc = after_launch("normals")) != MFLBM_OK) return rc;
+    if (a.n_cn) {
+        extrapolate_normal_kernel<T><<<grid_for(a.n_cn, 128), 128, 0, s>>>(a);
+        if ((rc = after_launch("extrapolate_normal")) != MFLBM_OK) return rc;
+    }
+    curvature_kernel<T, true><<<dim3(grid_for(g.nx, 128), g.ny, g.nz), 128, 0, s>>>(a);
+    return after_launch("curvature");
+}
+
+// Reference-layout cn_x/y/z, c_norm, curv from the records.
+template <class T>
+int launch_export(mflbm_context& c) {
+    const GradArgs<T> a = grad_args<T>(c);
+    const Grid& g = c.d.g;
+    split_normals_kernel<T><<<grid_for(g.n2(), 256), 256, 0, c.stream>>>(a, (int)g.n2());
+    int rc = after_launch("split_normals");
+    if (rc != MFLBM_OK) return rc;
+    curvature_kernel<T, false><<<dim3(grid_for(g.nx, 128), g.ny, g.nz), 128, 0, c.stream>>>(a);
+    return after_launch("curvature_export");
+}
+
+// Records from reference-layout arrays supplied by the host.
+template <class T>
+int launch_refresh_aux(mflbm_context& c) {
+    const GradArgs<T> a = grad_args<T>(c);
+    const Grid& g = c.d.g;
+    pack_normals_kernel<T><<<grid_for(g.n2(), 256), 256, 0, c.stream>>>(a, (int)g.n2());
+    int rc = after_launch("pack_normals");
+    if (rc != MFLBM_OK) return rc;
+    aux_from_arrays_kernel<T><<<dim3(grid_for(g.nx, 128), g.ny, g.nz), 128, 0, c.stream>>>(a);
+    return after_launch("aux_from_arrays");
+}
+
+}  // namespace MFLBM_NS
+}  // namespace mflbm

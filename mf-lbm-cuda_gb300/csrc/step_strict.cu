@@ -5,21 +5,14 @@
 namespace mflbm {
 namespace strict {
 
-int collide(mflbm_context& c, bool odd) {
-    return c.params.precision == MFLBM_FP32 ? launch_collide<float>(c, odd) : launch_collide<double>(c, odd);
-}
+#define MFLBM_DISPATCH(fn, ...) \
+    (c.params.precision == MFLBM_FP32 ? fn<float>(__VA_ARGS__) : fn<double>(__VA_ARGS__))
 
-int boundaries(mflbm_context& c, bool odd) {
-    return c.params.precision == MFLBM_FP32 ? launch_boundaries<float>(c, odd) : launch_boundaries<double>(c, odd);
-}
-
-int refresh_aux(mflbm_context& c) {
-    return c.params.precision == MFLBM_FP32 ? launch_refresh_aux<float>(c) : launch_refresh_aux<double>(c);
-}
-
-int gradient(mflbm_context& c) {
-    return c.params.precision == MFLBM_FP32 ? launch_gradient<float>(c) : launch_gradient<double>(c);
-}
+int collide(mflbm_context& c, bool odd) { return MFLBM_DISPATCH(launch_collide, c, odd); }
+int boundaries(mflbm_context& c, bool odd) { return MFLBM_DISPATCH(launch_boundaries, c, odd); }
+int gradient(mflbm_context& c) { return MFLBM_DISPATCH(launch_gradient, c); }
+int export_arrays(mflbm_context& c) { return MFLBM_DISPATCH(launch_export, c); }
+int refresh_aux(mflbm_context& c) { return MFLBM_DISPATCH(launch_refresh_aux, c); }
 
 }  // namespace strict
 }  // namespace mflbm
