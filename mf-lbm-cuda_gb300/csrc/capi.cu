@@ -50,7 +50,7 @@ void free_all(mflbm_context* c) {
     DeviceState& d = c->d;
     void* ptrs[] = {d.pdf, d.phi, d.cn_x, d.cn_y, d.cn_z, d.c_norm, d.curv, d.W_in, d.f_cv, d.g_cv, d.phi_cv,
                     d.walls, d.walls_type, d.s_nx, d.s_ny, d.s_nz, d.fluid_list, d.list_phi_ext,
-                    d.list_cn_ext, d.red, d.staging, d.aux, d.type8, d.cnv4};
+                    d.list_cn_ext, d.red, d.staging, d.aux, d.type8, d.cnv4, d.list_norm};
     for (void* p : ptrs) if (p) cudaFree(p);
     d = DeviceState{};
     if (c->pair_graph) cudaGraphExecDestroy(c->pair_graph);
@@ -92,6 +92,17 @@ int build_lists(mflbm_context* c) {
     std::sort(fe.begin(), fe.end());
     std::vector<uint32_t> fl(fe.size());
     for (size_t n = 0; n < fe.size(); ++n) fl[n] = fe[n].second;
+    // nodes whose normal the step needs: walls_type <= 0 on [-1, n+2]^3, in
+    // brick order of the grid shifted by one (so ghost layer -1 is included)
+    const Bricks bn = make_bricks(g.nx + 2, g.ny + 2, g.nz + 2);
+    std::vector<std::pair<ll, uint32_t>> ne;
+    for (int k = -1; k <= g.nz + 2; ++k)
+        for (int j = -1; j <= g.ny + 2; ++j)
+            for (int i = -1; i <= g.nx + 2; ++i)
+                if (wt[g.s4(i, j, k)] <= 0) ne.emplace_back((ll)bn.elem(i + 1, j + 1, k + 1), pack_xyz(i, j, k));
+    std::sort(ne.begin(), ne.end());
+    std::vector<uint32_t> ln(ne.size());
+    for (size_t n = 0; n < ne.size(); ++n) ln[n] = ne[n].second;
     std::vector<uint2> lphi, lcn;
     for (int k = -2; k <= g.nz + 3; ++k)
         for (int j = -2; j <= g.ny + 3; ++j)
@@ -108,6 +119,15 @@ int build_lists(mflbm_context* c) {
     if ((rc = upload_list(&d.fluid_list, &d.n_fluid, fl)) != MFLBM_OK) return rc;
     if ((rc = upload_list(&d.list_phi_ext, &d.n_phi_ext, lphi)) != MFLBM_OK) return rc;
     if ((rc = upload_list(&d.list_cn_ext, &d.n_cn_ext, lcn)) != MFLBM_OK) return rc;
+    if ((rc = upload_list(&d.list_norm, &d.n_norm, ln)) != MFLBM_OK) return rc;
+    if (d.aux) cudaFree(d.aux);
+    d.aux = nullptr;
+    const size_t rec = (c->params.precision == MFLBM_FP32 ? 4 : 8) * 4;
+    MFLBM_CUDA(cudaMalloc(&d.aux, rec * std::max<ll>(1, d.n_fluid)));
+    MFLBM_CUDA(cudaMemset(d.aux, 0, rec * std::max<ll>(1, d.n_fluid)));
+    // solid nodes keep a zero normal record (only fluid nodes are rewritten per step)
+    MFLBM_CUDA(cudaMemset(d.cnv4, 0, rec * g.n2()));
+    c->pair_graph_odd_first = -1;  // kernels are launched with the list sizes
     return MFLBM_OK;
 }
 
@@ -222,7 +242,7 @@ int mflbm_create(const mflbm_params* params, mflbm_context** out) {
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { delete c; return fail(MFLBM_E_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e)); }
     struct { void** p; size_t bytes; } allocs[] = {
-        {&d.pdf, T * d.b.S * 38}, {&d.aux, T * 4 * g.n1()}, {&d.cnv4, T * 4 * g.n2()},
+        {&d.pdf, T * d.b.S * 38}, {&d.cnv4, T * 4 * g.n2()},
         {(void**)&d.type8, (size_t)g.n4()},
         {&d.phi, T * g.n4()}, {&d.cn_x, T * g.n2()}, {&d.cn_y, T * g.n2()},
         {&d.cn_z, T * g.n2()}, {&d.c_norm, T * g.n2()}, {&d.curv, T * g.n1()}, {&d.W_in, T * g.plane1()},

@@ -175,9 +175,9 @@ template <class T> struct CollideArgs {
     int n;
     int bx8, bxy8;  // element strides of one brick step in y and z
     int nbx, nby;
-    int NX1, NY1, NX4, NY4;
+    int NX4, NY4;
     T* phi;
-    const V4* aux;  // per node of the s1 layout: (n_x, n_y, n_z, 0.5 * gamma * curv * c_norm)
+    const V4* aux;  // fluid-list order: (n_x, n_y, n_z, 0.5 * gamma * curv * c_norm)
     Phys<T> ph;
 };
 
@@ -205,7 +205,7 @@ __global__ void __launch_bounds__(128) collide_stream_kernel(const CollideArgs<T
         g1[q] = v.x;
         g2[q] = v.y;
     }
-    const typename Vec4<T>::type av = a.aux[x + a.NX1 * (y + a.NY1 * z)];
+    const typename Vec4<T>::type av = a.aux[t];
     const T phi = collide<T>(a.ph, g1, g2, av.x, av.y, av.z, av.w);
     a.phi[(x + 3) + a.NX4 * ((y + 3) + a.NY4 * (z + 3))] = phi;
 #pragma unroll
@@ -231,7 +231,6 @@ int launch_collide(mflbm_context& c, bool odd) {
     a.nbx = d.b.nbx; a.nby = d.b.nby;
     a.bx8 = 8 * d.b.nbx;
     a.bxy8 = 8 * d.b.nbx * d.b.nby;
-    a.NX1 = g.nx + 2; a.NY1 = g.ny + 2;
     a.NX4 = g.nx + 8; a.NY4 = g.ny + 8;
     a.phi = (T*)d.phi;
     a.aux = (const typename Vec4<T>::type*)d.aux;

@@ -14,7 +14,9 @@ struct DeviceState {
     void* pdf = nullptr;
     void* staging = nullptr;        // reference-layout (f1) buffer for uploads / downloads
     void* cnv4 = nullptr;           // s2: (n_x, n_y, n_z, |grad phi|) per node
-    void* aux = nullptr;            // s1: (n_x, n_y, n_z, 0.5*gamma*curv*c_norm) per node
+    void* aux = nullptr;            // per fluid node, fluid-list order: (n_x, n_y, n_z, 0.5*gamma*curv*c_norm)
+    uint32_t* list_norm = nullptr;  // walls_type <= 0 on [-1, n+2]^3, in brick order
+    ll n_norm = 0;
     int8_t* type8 = nullptr;        // walls_type as int8 (s4)
     bool arrays_stale = false;      // cn_x/y/z, c_norm, curv behind the records
     void* phi = nullptr;

@@ -3,17 +3,22 @@
 // launches (:2027-2054).
 //
 //   1. phi on solid boundary nodes (list with precomputed fluid-neighbour masks)
-//   2. unit interface normal + |grad phi| on [-1, n+2]^3, with the geometrical
-//      wetting applied in the same thread at fluid boundary nodes (it only
-//      reads its own node's values, so fusing it is exact); stored as one
-//      record (n_x, n_y, n_z, |grad phi|) per node of the s2 layout
+//   2. unit interface normal + |grad phi| at the fluid nodes of [-1, n+2]^3
+//      (list in brick order), with the geometrical wetting applied in the
+//      same thread at fluid boundary nodes (it only reads its own node's
+//      values, so fusing it is exact); stored as one record
+//      (n_x, n_y, n_z, |grad phi|) per node of the s2 layout.  Solid nodes
+//      keep the zero record the reference writes there every step (records
+//      are zeroed when the geometry is set and when arrays are packed).
 //   3. normal on solid boundary nodes (list with masks)
-//   4. curvature on [1, n]^3 and the record the collision reads:
-//      (n_x, n_y, n_z, 0.5 * gamma * curv * c_norm) per node of the s1 layout
+//   4. curvature at the fluid nodes of [1, n]^3 and the record the collision
+//      reads, (n_x, n_y, n_z, 0.5 * gamma * curv * c_norm), stored in
+//      fluid-list order so that both kernels access it contiguously
 //
-// The reference-layout arrays cn_x/y/z, c_norm and curv are produced from the
-// records only when the host asks for them (export), and records are rebuilt
-// from such arrays when the host uploads them (pack).
+// The reference-layout arrays cn_x/y/z, c_norm and curv (curvature on all of
+// [1, n]^3, solid nodes included) are produced from the records only when the
+// host asks for them (export), and records are rebuilt from such arrays when
+// the host uploads them (pack).
 #pragma once
 #include "context.cuh"
 
@@ -27,10 +32,11 @@ template <class T> struct GradArgs {
     const T *snx, *sny, *snz;
     T* phi;
     V4* cn;    // s2: (n_x, n_y, n_z, |grad phi|)
-    V4* aux;   // s1: (n_x, n_y, n_z, 0.5 * gamma * curv * c_norm)
+    V4* aux;   // fluid-list order: (n_x, n_y, n_z, 0.5 * gamma * curv * c_norm)
     T *cnx, *cny, *cnz, *cnorm, *curv;  // reference-layout arrays (export / pack)
     const uint2 *l_phi, *l_cn;
-    int n_phi, n_cn;
+    const uint32_t *l_fluid, *l_norm;
+    int n_phi, n_cn, n_fluid, n_norm;
     Phys<T> ph;
 };
 
@@ -116,13 +122,15 @@ __device__ __forceinline__ T iso4_dz(const ModelConsts<T>& c, const T* F, int n,
                       F[n + sy + sz] - F[n - sy - sz] + F[n - sy + sz] - F[n + sy - sz]);
 }
 
-// unit interface normal and |grad phi| on [-1, n+2]^3 (:757-807) + wetting (:809-878)
+// unit interface normal and |grad phi| at the fluid nodes of [-1, n+2]^3
+// (:757-807) + wetting (:809-878)
 template <class T>
 __global__ void __launch_bounds__(128) normals_kernel(const GradArgs<T> a) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
-    const int j = (int)blockIdx.y - 1, k = (int)blockIdx.z - 1;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.n_norm) return;
+    int i, j, k;
+    unpack_xyz(a.l_norm[t], i, j, k);
     const Grid& g = a.g;
-    if (i > g.nx + 2) return;
     const int sy4 = g.nx + 8, sz4 = (g.nx + 8) * (g.ny + 8);
     const int n4 = (int)g.s4(i, j, k);
     const T x = iso4_dx(a.ph.c, a.phi, n4, sy4, sz4);
@@ -194,26 +202,32 @@ __device__ __forceinline__ T curvature_at(const ModelConsts<T>& c, const typenam
            x * y * (kxy + kyx) + x * z * (kxz + kzx) + y * z * (kzy + kyz);
 }
 
-// curvature on [1, n]^3: AUX writes the collision's record (s1 layout),
-// otherwise the reference-layout curv array.
-template <class T, bool AUX>
+// curvature at the fluid nodes and the collision's record (fluid-list order)
+template <class T>
 __global__ void __launch_bounds__(128) curvature_kernel(const GradArgs<T> a) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.n_fluid) return;
+    int i, j, k;
+    unpack_xyz(a.l_fluid[t], i, j, k);
+    const Grid& g = a.g;
+    const int sy = g.nx + 4, sz = (g.nx + 4) * (g.ny + 4);
+    typename Vec4<T>::type ctr, r;
+    const T cv = curvature_at<T>(a.ph.c, a.cn, (int)g.s2(i, j, k), sy, sz, ctr);
+    r.x = ctr.x; r.y = ctr.y; r.z = ctr.z;
+    r.w = T(0.5) * a.ph.gamma * cv * ctr.w;
+    a.aux[t] = r;
+}
+
+// curvature on all of [1, n]^3 into the reference-layout curv array (export)
+template <class T>
+__global__ void __launch_bounds__(128) curvature_export_kernel(const GradArgs<T> a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y + 1, k = blockIdx.z + 1;
     const Grid& g = a.g;
     if (i > g.nx) return;
     const int sy = g.nx + 4, sz = (g.nx + 4) * (g.ny + 4);
     typename Vec4<T>::type ctr;
-    const T cv = curvature_at<T>(a.ph.c, a.cn, (int)g.s2(i, j, k), sy, sz, ctr);
-    const int n1 = (int)g.s1(i, j, k);
-    if (AUX) {
-        typename Vec4<T>::type r;
-        r.x = ctr.x; r.y = ctr.y; r.z = ctr.z;
-        r.w = T(0.5) * a.ph.gamma * cv * ctr.w;
-        a.aux[n1] = r;
-    } else {
-        a.curv[n1] = cv;
-    }
+    a.curv[g.s1(i, j, k)] = curvature_at<T>(a.ph.c, a.cn, (int)g.s2(i, j, k), sy, sz, ctr);
 }
 
 // records -> reference arrays cn_x/y/z, c_norm on the s2 range
@@ -225,26 +239,34 @@ __global__ void __launch_bounds__(256) split_normals_kernel(const GradArgs<T> a,
     a.cnx[t] = v.x; a.cny[t] = v.y; a.cnz[t] = v.z; a.cnorm[t] = v.w;
 }
 
-// reference arrays (uploaded by the host) -> records
+// reference arrays (uploaded by the host) -> records; solid nodes get the
+// zero record that the next gradient pass of the reference would leave there
 template <class T>
-__global__ void __launch_bounds__(256) pack_normals_kernel(const GradArgs<T> a, int n2) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n2) return;
+__global__ void __launch_bounds__(128) pack_normals_kernel(const GradArgs<T> a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
+    const int j = (int)blockIdx.y - 1, k = (int)blockIdx.z - 1;
+    const Grid& g = a.g;
+    if (i > g.nx + 2) return;
+    const ll n = g.s2(i, j, k);
     typename Vec4<T>::type v;
-    v.x = a.cnx[t]; v.y = a.cny[t]; v.z = a.cnz[t]; v.w = a.cnorm[t];
-    a.cn[t] = v;
+    if (a.type8[g.s4(i, j, k)] >= 1) {
+        v.x = T(0); v.y = T(0); v.z = T(0); v.w = T(0);
+    } else {
+        v.x = a.cnx[n]; v.y = a.cny[n]; v.z = a.cnz[n]; v.w = a.cnorm[n];
+    }
+    a.cn[n] = v;
 }
 template <class T>
 __global__ void __launch_bounds__(128) aux_from_arrays_kernel(const GradArgs<T> a) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int j = blockIdx.y + 1, k = blockIdx.z + 1;
-    const Grid& g = a.g;
-    if (i > g.nx) return;
-    const int n2 = (int)g.s2(i, j, k), n1 = (int)g.s1(i, j, k);
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.n_fluid) return;
+    int i, j, k;
+    unpack_xyz(a.l_fluid[t], i, j, k);
+    const ll n2 = a.g.s2(i, j, k);
     typename Vec4<T>::type r;
     r.x = a.cnx[n2]; r.y = a.cny[n2]; r.z = a.cnz[n2];
-    r.w = T(0.5) * a.ph.gamma * a.curv[n1] * a.cnorm[n2];
-    a.aux[n1] = r;
+    r.w = T(0.5) * a.ph.gamma * a.curv[a.g.s1(i, j, k)] * a.cnorm[n2];
+    a.aux[t] = r;
 }
 
 // ---------------------------------------------------------------------------
@@ -262,6 +284,8 @@ GradArgs<T> grad_args(const mflbm_context& c) {
     a.cnorm = (T*)d.c_norm; a.curv = (T*)d.curv;
     a.l_phi = d.list_phi_ext; a.n_phi = (int)d.n_phi_ext;
     a.l_cn = d.list_cn_ext; a.n_cn = (int)d.n_cn_ext;
+    a.l_fluid = d.fluid_list; a.n_fluid = (int)d.n_fluid;
+    a.l_norm = d.list_norm; a.n_norm = (int)d.n_norm;
     a.ph = make_phys<T>(c.params);
     return a;
 }
@@ -271,20 +295,22 @@ GradArgs<T> grad_args(const mflbm_context& c) {
 template <class T>
 int launch_gradient(mflbm_context& c) {
     const GradArgs<T> a = grad_args<T>(c);
-    const Grid& g = c.d.g;
     cudaStream_t s = c.stream;
     int rc;
     if (a.n_phi) {
         extrapolate_phi_kernel<T><<<grid_for(a.n_phi, 128), 128, 0, s>>>(a);
         if ((rc = after_launch("extrapolate_phi")) != MFLBM_OK) return rc;
     }
-    normals_kernel<T><<<dim3(grid_for(g.nx + 4, 128), g.ny + 4, g.nz + 4), 128, 0, s>>>(a);
-    if ((rc = after_launch("normals")) != MFLBM_OK) return rc;
+    if (a.n_norm) {
+        normals_kernel<T><<<grid_for(a.n_norm, 128), 128, 0, s>>>(a);
+        if ((rc = after_launch("normals")) != MFLBM_OK) return rc;
+    }
     if (a.n_cn) {
         extrapolate_normal_kernel<T><<<grid_for(a.n_cn, 128), 128, 0, s>>>(a);
         if ((rc = after_launch("extrapolate_normal")) != MFLBM_OK) return rc;
     }
-    curvature_kernel<T, true><<<dim3(grid_for(g.nx, 128), g.ny, g.nz), 128, 0, s>>>(a);
+    if (!a.n_fluid) return MFLBM_OK;
+    curvature_kernel<T><<<grid_for(a.n_fluid, 128), 128, 0, s>>>(a);
     return after_launch("curvature");
 }
 
@@ -296,7 +322,7 @@ int launch_export(mflbm_context& c) {
     split_normals_kernel<T><<<grid_for(g.n2(), 256), 256, 0, c.stream>>>(a, (int)g.n2());
     int rc = after_launch("split_normals");
     if (rc != MFLBM_OK) return rc;
-    curvature_kernel<T, false><<<dim3(grid_for(g.nx, 128), g.ny, g.nz), 128, 0, c.stream>>>(a);
+    curvature_export_kernel<T><<<dim3(grid_for(g.nx, 128), g.ny, g.nz), 128, 0, c.stream>>>(a);
     return after_launch("curvature_export");
 }
 
@@ -305,10 +331,10 @@ template <class T>
 int launch_refresh_aux(mflbm_context& c) {
     const GradArgs<T> a = grad_args<T>(c);
     const Grid& g = c.d.g;
-    pack_normals_kernel<T><<<grid_for(g.n2(), 256), 256, 0, c.stream>>>(a, (int)g.n2());
+    pack_normals_kernel<T><<<dim3(grid_for(g.nx + 4, 128), g.ny + 4, g.nz + 4), 128, 0, c.stream>>>(a);
     int rc = after_launch("pack_normals");
-    if (rc != MFLBM_OK) return rc;
-    aux_from_arrays_kernel<T><<<dim3(grid_for(g.nx, 128), g.ny, g.nz), 128, 0, c.stream>>>(a);
+    if (rc != MFLBM_OK || !a.n_fluid) return rc;
+    aux_from_arrays_kernel<T><<<grid_for(a.n_fluid, 128), 128, 0, c.stream>>>(a);
     return after_launch("aux_from_arrays");
 }
 
