@@ -219,6 +219,26 @@ int mflbm_synchronize(mflbm_context* ctx);
 int mflbm_monitor_reduce(mflbm_context* ctx, int n_exclude_inlet,
                          int n_exclude_outlet, mflbm_monitor* out);
 
+/* The same reductions without allocating device memory (no counterpart in
+ * the reference).  mflbm_monitor_reduce allocates its per-block partials on
+ * its first call; a caller whose lattice fills the GPU's memory, or that must
+ * not let cudaMalloc / cudaFree synchronise the device while other work runs
+ * on it, uses this entry point instead.  Its partials live in one fixed
+ * device array of the library (10,250 doubles: 4 partial blocks per SM, up to
+ * 256 SMs); a device with more SMs is rejected with MFLBM_E_ARG.
+ *   - The first call on each device looks up that array's address (which may
+ *     load the library's device code); make it before any stream capture.
+ *   - All contexts on one device share the array: calls that overlap in time
+ *     on the same device (two host threads, or contexts whose streams run
+ *     concurrently) race on it and must be serialised by the caller.  Calls
+ *     from one thread are serial, since each blocks until its result is on
+ *     the host.
+ *   - Nothing in the array needs clearing: each call writes every element it
+ *     reads.
+ * Same arguments, result and error behaviour as mflbm_monitor_reduce. */
+int mflbm_monitor_reduce_noalloc(mflbm_context* ctx, int n_exclude_inlet,
+                                 int n_exclude_outlet, mflbm_monitor* out);
+
 /* ---- introspection ---------------------------------------------------- */
 /* Counts of lattice nodes: [0] fluid nodes in [1,n]^3, [1] all nodes n^3. */
 int mflbm_node_counts(mflbm_context* ctx, long long counts[2]);

@@ -462,6 +462,14 @@ int mflbm_monitor_reduce(mflbm_context* c, int n_exclude_inlet, int n_exclude_ou
     return monitor(*c, n_exclude_inlet, n_exclude_outlet, out);
 }
 
+int mflbm_monitor_reduce_noalloc(mflbm_context* c, int n_exclude_inlet, int n_exclude_outlet, mflbm_monitor* out) {
+    int rc = require_ready(c);
+    if (rc != MFLBM_OK) return rc;
+    if (!out) return fail(MFLBM_E_ARG, "null output");
+    if ((rc = export_arrays(c)) != MFLBM_OK) return rc;
+    return monitor_noalloc(*c, n_exclude_inlet, n_exclude_outlet, out);
+}
+
 int mflbm_node_counts(mflbm_context* c, long long counts[2]) {
     if (!c || !counts) return fail(MFLBM_E_ARG, "null argument");
     counts[0] = c->d.n_fluid;

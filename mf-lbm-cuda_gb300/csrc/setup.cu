@@ -2,6 +2,8 @@
 // monitor reductions.  Built with -fmad=false: the geometry and start-up
 // arithmetic must be the reference's IEEE sequence so masks, solid normals
 // and initial populations are bit-identical to the reference's host code.
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "context.cuh"
@@ -425,6 +427,93 @@ int monitor_t(mflbm_context& c, int nex_in, int nex_out, mflbm_monitor* out) {
     return MFLBM_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Scratch of mflbm_monitor_reduce_noalloc: a fixed array in the library's
+// device image instead of the context's lazily allocated partials, for callers
+// that must not allocate device memory while the simulation runs (a lattice
+// sized to fill the GPU's memory leaves no room for a first-call cudaMalloc,
+// and cudaMalloc / cudaFree synchronise the whole device, stalling whatever
+// else runs on it).
+//
+// Capacity: 4 partial blocks per SM for up to 256 SMs, i.e. NRED * 1024 +
+// 1024 + NRED + 1 = 10,250 doubles (80 KiB).  A device with more SMs is
+// rejected with MFLBM_E_ARG.  One copy exists per device, shared by every
+// context on that device; nothing in it needs clearing, because each call
+// writes every element before it reads it.
+// ---------------------------------------------------------------------------
+constexpr int kNoallocBlocksMax = 4 * 256;
+constexpr ll kNoallocScratch = (ll)NRED * kNoallocBlocksMax + kNoallocBlocksMax + NRED + 1;
+static __device__ __align__(256) double g_monitor_scratch[kNoallocScratch];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mutex;
+double* g_scratch_ptr[kMaxDevices] = {};
+
+// Device address of g_monitor_scratch on the current device, looked up on the
+// first call for that device (which may load the library's device code).
+int noalloc_scratch(double** out, int* sms) {
+    int dev = 0;
+    MFLBM_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices)
+        return fail(MFLBM_E_ARG, "mflbm_monitor_reduce_noalloc: device ordinal " + std::to_string(dev) +
+                                     " beyond the supported " + std::to_string(kMaxDevices));
+    MFLBM_CUDA(cudaDeviceGetAttribute(sms, cudaDevAttrMultiProcessorCount, dev));
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    if (!g_scratch_ptr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_monitor_scratch);
+        if (e != cudaSuccess)
+            return fail(MFLBM_E_CUDA, std::string("mflbm_monitor_reduce_noalloc: cudaGetSymbolAddress: ") +
+                                          cudaGetErrorString(e));
+        g_scratch_ptr[dev] = (double*)p;
+    }
+    *out = g_scratch_ptr[dev];
+    return MFLBM_OK;
+}
+
+// The launches of monitor_t with the partials in g_monitor_scratch.
+template <class T>
+int monitor_noalloc_t(mflbm_context& c, int nex_in, int nex_out, mflbm_monitor* out) {
+    DeviceState& d = c.d;
+    const Grid g = d.g;
+    cudaStream_t s = c.stream;
+    double* scratch = nullptr;
+    int sms = 0;
+    int rc = noalloc_scratch(&scratch, &sms);
+    if (rc != MFLBM_OK) return rc;
+    const int blocks = 4 * sms;
+    const ll need = (ll)NRED * blocks + blocks + NRED + 1;
+    if (need > kNoallocScratch)
+        return fail(MFLBM_E_ARG, "mflbm_monitor_reduce_noalloc: " + std::to_string(sms) + " SMs need " +
+                                     std::to_string(need) + " doubles of scratch, the static array holds " +
+                                     std::to_string(kNoallocScratch) + " (at most 256 SMs)");
+    double* part = scratch;
+    double* part2 = scratch + (ll)NRED * blocks;
+    double* res = part2 + blocks;
+    monitor_partials<T><<<blocks, 256, 0, s>>>(g, d.b, d.fluid_list, d.n_fluid, (const T*)d.pdf, (const T*)d.phi,
+                                               (const T*)d.cn_x, (const T*)d.cn_y, (const T*)d.cn_z,
+                                               (const T*)d.c_norm, (const T*)d.curv, (double)T(c.params.lbm_gamma),
+                                               (double)T(c.params.force_z), nex_in + 1, g.nz - nex_out, part);
+    if ((rc = after_launch("monitor_partials")) != MFLBM_OK) return rc;
+    fold_partials<<<NRED, 32, 0, s>>>(blocks, NRED, part, res);
+    if ((rc = after_launch("fold_partials")) != MFLBM_OK) return rc;
+    sum_all<T><<<blocks, 256, 0, s>>>(d.b.S * 38, (const T*)d.pdf, part2);
+    if ((rc = after_launch("sum_all")) != MFLBM_OK) return rc;
+    fold_partials<<<1, 32, 0, s>>>(blocks, 1, part2, res + NRED);
+    if ((rc = after_launch("fold_partials")) != MFLBM_OK) return rc;
+    double h[NRED + 1];
+    MFLBM_CUDA(cudaMemcpyAsync(h, res, sizeof h, cudaMemcpyDeviceToHost, s));
+    MFLBM_CUDA(cudaStreamSynchronize(s));
+    out->vol1_sum = h[0]; out->vol2_sum = h[1];
+    out->mass1_sum = h[2]; out->mass2_sum = h[3];
+    out->flux1_sum = h[4]; out->flux2_sum = h[5];
+    out->vol1_full = h[6]; out->vol2_full = h[7];
+    out->umax = sqrt(h[8]);
+    out->total_mass = h[9];
+    out->saturation = h[0] / (h[0] + h[1]);
+    return MFLBM_OK;
+}
+
 // Reference layout (f1) <-> brick layout, one thread per (node, direction).
 template <class T>
 __global__ void f1_to_bricks(Grid g, Bricks b, const T* f1, T* pdf) {
@@ -473,6 +562,11 @@ int init_fields(mflbm_context& c, int option, double z0) {
 int monitor(mflbm_context& c, int nex_in, int nex_out, mflbm_monitor* out) {
     return c.params.precision == MFLBM_FP32 ? monitor_t<float>(c, nex_in, nex_out, out)
                                             : monitor_t<double>(c, nex_in, nex_out, out);
+}
+
+int monitor_noalloc(mflbm_context& c, int nex_in, int nex_out, mflbm_monitor* out) {
+    return c.params.precision == MFLBM_FP32 ? monitor_noalloc_t<float>(c, nex_in, nex_out, out)
+                                            : monitor_noalloc_t<double>(c, nex_in, nex_out, out);
 }
 
 }  // namespace mflbm

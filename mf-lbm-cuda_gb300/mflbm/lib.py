@@ -39,6 +39,7 @@ SIGNATURES = {
     "mflbm_run": (I, [VP, I, I]),
     "mflbm_synchronize": (I, [VP]),
     "mflbm_monitor_reduce": (I, [VP, I, I, VP]),
+    "mflbm_monitor_reduce_noalloc": (I, [VP, I, I, VP]),
     "mflbm_node_counts": (I, [VP, C.POINTER(LL)]),
     "mflbm_stream": (VP, [VP]),
     "mflbm_set_kernel_timing": (I, [VP, I]),
@@ -173,6 +174,14 @@ class Context:
         m = abi.Monitor()
         check(self.lib.mflbm_monitor_reduce(self.h, int(n_exclude_inlet), int(n_exclude_outlet), C.byref(m)),
               "mflbm_monitor_reduce")
+        return m.as_dict()
+
+    def monitor_noalloc(self, n_exclude_inlet, n_exclude_outlet):
+        """mflbm_monitor_reduce_noalloc: the same reductions with their
+        partials in the library's static device array (no allocation)."""
+        m = abi.Monitor()
+        check(self.lib.mflbm_monitor_reduce_noalloc(self.h, int(n_exclude_inlet), int(n_exclude_outlet),
+                                                    C.byref(m)), "mflbm_monitor_reduce_noalloc")
         return m.as_dict()
 
     def node_counts(self):
