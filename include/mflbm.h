@@ -127,6 +127,18 @@ typedef struct mflbm_monitor {
     double vol1_full, vol2_full;       /* cal_saturation sums over [1,n]^3 */
 } mflbm_monitor;
 
+/* Scalars of the monitors that need more than the sums above
+ * (src/Monitor.cpp:17-56 kinetic energy, :277-351 phase-field steady state,
+ * :355-441 capillary-pressure steady state, :447-466 breakthrough), FP64. */
+typedef struct mflbm_monitor_ext {
+    double umax2;                      /* max |u|^2 over fluid nodes */
+    double usq1, usq2;                 /* sum |u|^2 over fluid nodes with phi > 0.999 / phi < -0.999 */
+    double pre_w, pre_nw;              /* sum rho over fluid nodes with phi < -0.99 / phi > 0.99 */
+    long long n_w, n_nw;               /* their counts */
+    long long breakthrough;            /* fluid nodes of slice z = nz-1 with phi > 0 */
+    double dphi_max;                   /* max |phi - phi at the previous tracking call| over fluid nodes */
+} mflbm_monitor_ext;
+
 typedef struct mflbm_context mflbm_context;
 
 /* ---- library ---------------------------------------------------------- */
@@ -161,6 +173,9 @@ int mflbm_destroy(mflbm_context* ctx);
 /* Reference: copyConstantData (src/main_iteration_GPU.cu:14-47): replace the
  * physical parameters (same lattice size and precision). */
 int mflbm_set_params(mflbm_context* ctx, const mflbm_params* params);
+/* The context's current parameters (after mflbm_read_checkpoint they hold the
+ * checkpoint's force_z and rho_in). */
+int mflbm_get_params(mflbm_context* ctx, mflbm_params* out);
 
 /* Device geometry preprocessing, bit-exact with geometry_preprocessing_new
  * (src/Geometry_preprocessing.cpp:29-403).  walls_global: s0 int32 (host).
@@ -238,6 +253,53 @@ int mflbm_monitor_reduce(mflbm_context* ctx, int n_exclude_inlet,
  * Same arguments, result and error behaviour as mflbm_monitor_reduce. */
 int mflbm_monitor_reduce_noalloc(mflbm_context* ctx, int n_exclude_inlet,
                                  int n_exclude_outlet, mflbm_monitor* out);
+
+/* Per-slice monitor sums (the profiles of src/Monitor.cpp:58-104) in FP64
+ * on the current state (after an even step), deterministic: for slice
+ * k = 1..nz, slices[m * nz + k - 1] holds, over the fluid nodes of the slice,
+ * with a1 = (1 + phi)/2, a2 = (1 - phi)/2 and u, v, w the post-even velocity
+ * of compute_macro_vars:
+ *   m = 0: sum w a1   1: sum w a2   2: sum a1   3: sum a2
+ *       4: sum rho a1 5: sum rho a2 6: sum rho
+ * `ext` (may be NULL) receives the other monitor scalars; with track_phi != 0
+ * dphi_max is measured against the phi of the previous tracking call (zero
+ * before the first) and the current phi becomes the new reference.
+ * Blocks until the results are on the host. */
+int mflbm_monitor_profile(mflbm_context* ctx, double* slices, mflbm_monitor_ext* ext, int track_phi);
+
+/* ---- output files in the reference's formats -------------------------- */
+
+/* Reference: VTK_legacy_writer_3D (src/IO_multiphase.cpp:500-714) for the
+ * current state (after an even step).  vtk_type 1: phi (0 on solids),
+ * density and velocity (compute_macro_vars, src/Misc.cpp:222-274); 2: phi as
+ * float (0 on solids); 3: phi, c_norm and the interface normal, under the
+ * labels of type 1.  Types 1 and 3 name the data "float" when
+ * output_fieldData_precision_cmd is 0 and "double" otherwise, and hold values
+ * of the context's precision, as the reference does.  The body is assembled
+ * on the device; `path` is the file to create (the reference names them
+ * results/out3.field_data/{full_flow_field/full_flow_field_,
+ * phase_distribution/small_,full_flow_field/force_vector_}%010d.vtk).
+ * The device state is not modified. */
+int mflbm_write_vtk(mflbm_context* ctx, int vtk_type,
+                    int output_fieldData_precision_cmd, const char* path);
+/* Reference: VTK_walls_bin (src/IO_multiphase.cpp:800-841), the solid
+ * geometry as big-endian int (reference name: results/out3.field_data/
+ * walls_bin.vtk). */
+int mflbm_write_walls_vtk(mflbm_context* ctx, const char* path);
+/* Reference: save_checkpoint (src/IO_multiphase.cpp:252-305), file part:
+ * int ntime+1, force_z, rho_in, pdf (i_f1), phi (i_s4) and, with the
+ * convective outlet, the three convective buffers, in the context's
+ * precision and the host's byte order (reference name:
+ * results/out2.checkpoint/id0000).  job_status.txt is the caller's. */
+int mflbm_write_checkpoint(mflbm_context* ctx, int ntime, const char* path);
+/* Reference: initialization_old_multi (src/Init_multiphase.cpp:501-537) +
+ * the start-up colour gradient: loads a checkpoint written by the reference
+ * or by mflbm_write_checkpoint for the same lattice, precision and outlet_BC
+ * (anything else is rejected with MFLBM_E_ARG), sets force_z and rho_in from
+ * it, uploads the fields (and W_in, the inlet profile of
+ * mflbm_inlet_profile, unless NULL) and runs the gradient pass.  *ntime0
+ * receives the stored step - 1 (the reference's ntime0). */
+int mflbm_read_checkpoint(mflbm_context* ctx, const char* path, const void* W_in, int* ntime0);
 
 /* ---- introspection ---------------------------------------------------- */
 /* Counts of lattice nodes: [0] fluid nodes in [1,n]^3, [1] all nodes n^3. */

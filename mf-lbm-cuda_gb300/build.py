@@ -4,8 +4,10 @@ Translation units compile in parallel:
   step_fast.cu    step kernels with FMA contraction (production flavour)
   step_strict.cu  the same kernels with -fmad=false (IEEE ops in reference order)
   setup.cu        geometry preprocessing, start-up fields, FP64 reductions (-fmad=false)
+  output.cu       VTK and checkpoint files in the reference's formats (-fmad=false)
   capi.cu         the C ABI
   host_setup.cpp  host parameter derivation and inlet profile (g++ -ffp-contract=off)
+and the stand-alone program lib/mflbm_main (driver.cpp, g++, linked to the library).
 """
 from __future__ import annotations
 
@@ -30,6 +32,7 @@ UNITS = {
     "step_fast.cu": [],
     "step_strict.cu": ["-fmad=false"],
     "setup.cu": ["-fmad=false"],
+    "output.cu": ["-fmad=false"],
     "capi.cu": [],
 }
 HEADERS = ["common.cuh", "context.cuh", "step_kernels.cuh", "collide.cuh", "gradient.cuh", "boundary.cuh", "setup.cuh"]
@@ -76,7 +79,22 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
         _run([NVCC, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"])
         os.replace(tmp, LIB)
     build_refshim(force)
+    build_driver(force)
     return LIB
+
+
+DRIVER = OUT / "mflbm_main"
+
+
+def build_driver(force: bool = False):
+    """The stand-alone program (csrc/driver.cpp) on libmflbm.so."""
+    src = CSRC / "driver.cpp"
+    if not force and not _stale(DRIVER, [src, REPO / "include" / "mflbm.h", LIB]):
+        return DRIVER
+    tmp = DRIVER.with_name(DRIVER.name + ".tmp")
+    _run(["g++", "-O2", "-std=c++17", str(src), "-L", str(OUT), "-lmflbm", "-Wl,-rpath,$ORIGIN", "-o", str(tmp)])
+    os.replace(tmp, DRIVER)
+    return DRIVER
 
 
 def refshim_path(precision: str) -> Path:

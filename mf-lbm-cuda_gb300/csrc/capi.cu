@@ -50,7 +50,8 @@ void free_all(mflbm_context* c) {
     DeviceState& d = c->d;
     void* ptrs[] = {d.pdf, d.phi, d.cn_x, d.cn_y, d.cn_z, d.c_norm, d.curv, d.W_in, d.f_cv, d.g_cv, d.phi_cv,
                     d.walls, d.walls_type, d.s_nx, d.s_ny, d.s_nz, d.fluid_list, d.list_phi_ext,
-                    d.list_cn_ext, d.red, d.staging, d.aux, d.type8, d.cnv4, d.list_norm};
+                    d.list_cn_ext, d.red, d.staging, d.aux, d.type8, d.cnv4, d.list_norm, d.zpair_off,
+                    d.phi_prev, d.prof};
     for (void* p : ptrs) if (p) cudaFree(p);
     d = DeviceState{};
     if (c->pair_graph) cudaGraphExecDestroy(c->pair_graph);
@@ -92,6 +93,10 @@ int build_lists(mflbm_context* c) {
     std::sort(fe.begin(), fe.end());
     std::vector<uint32_t> fl(fe.size());
     for (size_t n = 0; n < fe.size(); ++n) fl[n] = fe[n].second;
+    // brick order is z-pair major: offsets of each pair of slices (2 kp, 2 kp + 1)
+    std::vector<int> zoff(d.b.nbz + 1, 0);
+    for (size_t n = 0; n < fe.size(); ++n) zoff[(fe[n].first >> 3) / (d.b.nbx * d.b.nby) + 1]++;
+    for (int kp = 0; kp < d.b.nbz; ++kp) zoff[kp + 1] += zoff[kp];
     // nodes whose normal the step needs: walls_type <= 0 on [-1, n+2]^3, in
     // brick order of the grid shifted by one (so ghost layer -1 is included)
     const Bricks bn = make_bricks(g.nx + 2, g.ny + 2, g.nz + 2);
@@ -120,6 +125,10 @@ int build_lists(mflbm_context* c) {
     if ((rc = upload_list(&d.list_phi_ext, &d.n_phi_ext, lphi)) != MFLBM_OK) return rc;
     if ((rc = upload_list(&d.list_cn_ext, &d.n_cn_ext, lcn)) != MFLBM_OK) return rc;
     if ((rc = upload_list(&d.list_norm, &d.n_norm, ln)) != MFLBM_OK) return rc;
+    ll nzo = 0;
+    if ((rc = upload_list(&d.zpair_off, &nzo, zoff)) != MFLBM_OK) return rc;
+    if (d.phi_prev) cudaFree(d.phi_prev);
+    d.phi_prev = nullptr;
     if (d.aux) cudaFree(d.aux);
     d.aux = nullptr;
     const size_t rec = (c->params.precision == MFLBM_FP32 ? 4 : 8) * 4;
@@ -284,6 +293,12 @@ int mflbm_set_params(mflbm_context* c, const mflbm_params* p) {
         return fail(MFLBM_E_ARG, "mflbm_set_params cannot change the lattice size or precision");
     c->params = *p;
     if (c->pair_graph) { cudaGraphExecDestroy(c->pair_graph); c->pair_graph = nullptr; }
+    return MFLBM_OK;
+}
+
+int mflbm_get_params(mflbm_context* c, mflbm_params* out) {
+    if (!c || !out) return fail(MFLBM_E_ARG, "mflbm_get_params: null argument");
+    *out = c->params;
     return MFLBM_OK;
 }
 
@@ -468,6 +483,79 @@ int mflbm_monitor_reduce_noalloc(mflbm_context* c, int n_exclude_inlet, int n_ex
     if (!out) return fail(MFLBM_E_ARG, "null output");
     if ((rc = export_arrays(c)) != MFLBM_OK) return rc;
     return monitor_noalloc(*c, n_exclude_inlet, n_exclude_outlet, out);
+}
+
+int mflbm_write_vtk(mflbm_context* c, int vtk_type, int output_fieldData_precision_cmd, const char* path) {
+    int rc = require_ready(c);
+    if (rc != MFLBM_OK) return rc;
+    if (!path) return fail(MFLBM_E_ARG, "mflbm_write_vtk: null path");
+    if (vtk_type < 1 || vtk_type > 3) return fail(MFLBM_E_ARG, "mflbm_write_vtk: vtk_type must be 1, 2 or 3");
+    if ((rc = ensure_staging(c)) != MFLBM_OK) return rc;
+    if (vtk_type != 2 && (rc = export_arrays(c)) != MFLBM_OK) return rc;
+    return write_vtk(*c, vtk_type, output_fieldData_precision_cmd, path);
+}
+
+int mflbm_write_walls_vtk(mflbm_context* c, const char* path) {
+    if (!c || !path) return fail(MFLBM_E_ARG, "mflbm_write_walls_vtk: null argument");
+    if (!c->have_geometry) return fail(MFLBM_E_STATE, "geometry not set (mflbm_preprocess_geometry / mflbm_upload_geometry)");
+    int rc = ensure_staging(c);
+    if (rc != MFLBM_OK) return rc;
+    return write_walls_vtk(*c, path);
+}
+
+int mflbm_write_checkpoint(mflbm_context* c, int ntime, const char* path) {
+    int rc = require_ready(c);
+    if (rc != MFLBM_OK) return rc;
+    if (!path) return fail(MFLBM_E_ARG, "mflbm_write_checkpoint: null path");
+    if ((rc = ensure_staging(c)) != MFLBM_OK) return rc;
+    return write_checkpoint(*c, ntime, path);
+}
+
+int mflbm_read_checkpoint(mflbm_context* c, const char* path, const void* W_in, int* ntime0) {
+    if (!c || !path) return fail(MFLBM_E_ARG, "mflbm_read_checkpoint: null argument");
+    if (!c->have_geometry) return fail(MFLBM_E_STATE, "geometry must be set before mflbm_read_checkpoint");
+    const Grid& g = c->d.g;
+    const size_t T = tsize(c), pl = (size_t)g.plane1();
+    const bool convec = c->params.outlet_BC == 1;
+    const size_t expect = sizeof(int) + 2 * T + T * ((size_t)g.n1() * 38 + (size_t)g.n4()) + (convec ? T * pl * 39 : 0);
+    FILE* f = fopen(path, "rb");
+    if (!f) return fail(MFLBM_E_ARG, std::string("checkpoint not found: ") + path);
+    std::vector<unsigned char> buf(expect + 1);
+    const size_t got = fread(buf.data(), 1, buf.size(), f);
+    fclose(f);
+    if (got != expect)
+        return fail(MFLBM_E_ARG, std::string("checkpoint ") + path + " has " + std::to_string(got) + " bytes, expected " +
+                                     std::to_string(expect) + " for this lattice, precision and outlet_BC");
+    int nt_next;
+    std::memcpy(&nt_next, buf.data(), sizeof(int));
+    const unsigned char* p = buf.data() + sizeof(int);
+    mflbm_params np = c->params;
+    if (T == 4) {
+        float fz, rin;
+        std::memcpy(&fz, p, 4); std::memcpy(&rin, p + 4, 4);
+        np.force_z = fz; np.rho_in = rin;
+    } else {
+        std::memcpy(&np.force_z, p, 8); std::memcpy(&np.rho_in, p + 8, 8);
+    }
+    p += 2 * T;
+    int rc = mflbm_set_params(c, &np);
+    if (rc != MFLBM_OK) return rc;
+    const unsigned char* pdf = p;
+    const unsigned char* phi = pdf + T * (size_t)g.n1() * 38;
+    const unsigned char* cv = phi + T * (size_t)g.n4();
+    rc = mflbm_upload_fields(c, pdf, phi, nullptr, nullptr, nullptr, nullptr, nullptr, W_in,
+                             convec ? cv : nullptr, convec ? cv + T * pl * 19 : nullptr,
+                             convec ? cv + T * pl * 38 : nullptr);
+    if (rc != MFLBM_OK) return rc;
+    if (ntime0) *ntime0 = nt_next - 1;
+    return MFLBM_OK;
+}
+
+int mflbm_monitor_profile(mflbm_context* c, double* slices, mflbm_monitor_ext* ext, int track_phi) {
+    int rc = require_ready(c);
+    if (rc != MFLBM_OK) return rc;
+    if (!slices) return fail(MFLBM_E_ARG, "mflbm_monitor_profile: null slices");
+    return monitor_profile(*c, slices, ext, track_phi != 0);
 }
 
 int mflbm_node_counts(mflbm_context* c, long long counts[2]) {

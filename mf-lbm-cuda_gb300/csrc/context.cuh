@@ -44,6 +44,9 @@ struct DeviceState {
     ll n_cn_ext = 0;
     double* red = nullptr;             // reduction scratch
     ll red_len = 0;
+    int* zpair_off = nullptr;          // fluid-list offset of each z pair (2 kp, 2 kp + 1), nbz + 1 entries
+    void* phi_prev = nullptr;          // phi at the previous tracking monitor call (s4)
+    double* prof = nullptr;            // per-slice and per-block monitor partials
 };
 
 }  // namespace mflbm

@@ -2,6 +2,7 @@
 // monitor reductions.  Built with -fmad=false: the geometry and start-up
 // arithmetic must be the reference's IEEE sequence so masks, solid normals
 // and initial populations are bit-identical to the reference's host code.
+#include <algorithm>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -514,6 +515,118 @@ int monitor_noalloc_t(mflbm_context& c, int nex_in, int nex_out, mflbm_monitor* 
     return MFLBM_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Per-slice monitor profiles and the other monitor scalars (FP64),
+// src/Monitor.cpp:17-104 (profiles, kinetic energy), :277-351 (phase-field
+// steady state), :355-441 (capillary-pressure steady state), :447-466
+// (breakthrough).  One block per z pair of the fluid list (brick order is
+// z-pair major): every sum is taken in a fixed order, so results repeat
+// exactly.  Thresholds compare phi in the solver precision, as the reference.
+// ---------------------------------------------------------------------------
+constexpr int kProfSums = 7, kProfExt = 9;  // ext: umax2 usq1 usq2 pre_w pre_nw n_w n_nw breakthrough dphi_max
+
+template <class T>
+__global__ void __launch_bounds__(256) monitor_profile_kernel(Grid g, Bricks b, const uint32_t* list, const int* zoff,
+                                                              const T* pdf, const T* phi, T* phi_prev,
+                                                              const typename Vec4<T>::type* aux, double force_z,
+                                                              int track, double* out) {
+    const int kp = blockIdx.x;
+    double acc[2 * kProfSums + kProfExt];
+#pragma unroll
+    for (int r = 0; r < 2 * kProfSums + kProfExt; ++r) acc[r] = 0.0;
+    double* ext = acc + 2 * kProfSums;
+    for (int t = zoff[kp] + threadIdx.x; t < zoff[kp + 1]; t += blockDim.x) {
+        int i, j, k;
+        unpack_xyz(list[t], i, j, k);
+        double f[19];
+#pragma unroll
+        for (int q = 0; q < 19; ++q) f[q] = (double)pdf[b.at(i, j, k, q, 0)] + (double)pdf[b.at(i, j, k, q, 1)];
+        double rho = 0;
+#pragma unroll
+        for (int q = 0; q < 19; ++q) rho += f[q];
+        const typename Vec4<T>::type a = aux[t];
+        const double tmp = (double)a.w;
+        const double fx = tmp * (double)a.x, fy = tmp * (double)a.y, fz = tmp * (double)a.z + force_z;
+        const double u = f[1] - f[2] + f[7] - f[8] + f[9] - f[10] + f[11] - f[12] + f[13] - f[14] - 0.5 * fx;
+        const double v = f[3] - f[4] + f[7] + f[8] - f[9] - f[10] + f[15] - f[16] + f[17] - f[18] - 0.5 * fy;
+        const double w = f[5] - f[6] + f[11] + f[12] - f[13] - f[14] + f[15] + f[16] - f[17] - f[18] - 0.5 * fz;
+        const ll n4 = g.s4(i, j, k);
+        const T ph = phi[n4];
+        const double pd = (double)ph, a1 = 0.5 * (1.0 + pd), a2 = 0.5 * (1.0 - pd);
+        double* sl = acc + (k & 1) * kProfSums;
+        sl[0] += w * a1; sl[1] += w * a2; sl[2] += a1; sl[3] += a2;
+        sl[4] += rho * a1; sl[5] += rho * a2; sl[6] += rho;
+        const double u2 = u * u + v * v + w * w;
+        ext[0] = fmax(ext[0], u2);
+        if (ph > T(0.999)) ext[1] += u2;
+        else if (ph < T(-0.999)) ext[2] += u2;
+        if (ph < T(-0.99)) { ext[3] += rho; ext[5] += 1.0; }
+        if (ph > T(0.99)) { ext[4] += rho; ext[6] += 1.0; }
+        if (k == g.nz - 1 && ph > T(0)) ext[7] += 1.0;
+        if (track) {
+            ext[8] = fmax(ext[8], fabs(pd - (double)phi_prev[n4]));
+            phi_prev[n4] = ph;
+        }
+    }
+    __shared__ double sh[2 * kProfSums + kProfExt][8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int r = 0; r < 2 * kProfSums + kProfExt; ++r) {
+        const bool is_max = r == 2 * kProfSums || r == 2 * kProfSums + 8;
+        double x = acc[r];
+        for (int o = 16; o > 0; o >>= 1) {
+            const double y = __shfl_down_sync(0xffffffffu, x, o);
+            x = is_max ? fmax(x, y) : x + y;
+        }
+        if (lane == 0) sh[r][warp] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < 2 * kProfSums + kProfExt) {
+        const int r = threadIdx.x;
+        const bool is_max = r == 2 * kProfSums || r == 2 * kProfSums + 8;
+        double x = sh[r][0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) x = is_max ? fmax(x, sh[r][w]) : x + sh[r][w];
+        out[(ll)kp * (2 * kProfSums + kProfExt) + r] = x;
+    }
+}
+
+template <class T>
+int monitor_profile_t(mflbm_context& c, double* slices, mflbm_monitor_ext* ext, bool track) {
+    DeviceState& d = c.d;
+    const Grid g = d.g;
+    const int nb = d.b.nbz, per = 2 * kProfSums + kProfExt;
+    if (!d.prof) MFLBM_CUDA(cudaMalloc(&d.prof, sizeof(double) * nb * per));
+    if (track && !d.phi_prev) {
+        MFLBM_CUDA(cudaMalloc(&d.phi_prev, sizeof(T) * g.n4()));
+        MFLBM_CUDA(cudaMemsetAsync(d.phi_prev, 0, sizeof(T) * g.n4(), c.stream));
+    }
+    monitor_profile_kernel<T><<<nb, 256, 0, c.stream>>>(g, d.b, d.fluid_list, d.zpair_off, (const T*)d.pdf,
+                                                        (const T*)d.phi, (T*)d.phi_prev,
+                                                        (const typename Vec4<T>::type*)d.aux,
+                                                        (double)T(c.params.force_z), track ? 1 : 0, d.prof);
+    int rc = after_launch("monitor_profile");
+    if (rc != MFLBM_OK) return rc;
+    std::vector<double> h((size_t)nb * per);
+    MFLBM_CUDA(cudaMemcpyAsync(h.data(), d.prof, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c.stream));
+    MFLBM_CUDA(cudaStreamSynchronize(c.stream));
+    for (int m = 0; m < kProfSums; ++m)
+        for (int k = 1; k <= g.nz; ++k) slices[(size_t)m * g.nz + k - 1] = h[(size_t)(k >> 1) * per + (k & 1) * kProfSums + m];
+    if (ext) {
+        double e[kProfExt] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        for (int kp = 0; kp < nb; ++kp)
+            for (int r = 0; r < kProfExt; ++r) {
+                const double x = h[(size_t)kp * per + 2 * kProfSums + r];
+                e[r] = (r == 0 || r == 8) ? std::max(e[r], x) : e[r] + x;
+            }
+        ext->umax2 = e[0]; ext->usq1 = e[1]; ext->usq2 = e[2];
+        ext->pre_w = e[3]; ext->pre_nw = e[4];
+        ext->n_w = (long long)e[5]; ext->n_nw = (long long)e[6];
+        ext->breakthrough = (long long)e[7];
+        ext->dphi_max = e[8];
+    }
+    return MFLBM_OK;
+}
+
 // Reference layout (f1) <-> brick layout, one thread per (node, direction).
 template <class T>
 __global__ void f1_to_bricks(Grid g, Bricks b, const T* f1, T* pdf) {
@@ -562,6 +675,11 @@ int init_fields(mflbm_context& c, int option, double z0) {
 int monitor(mflbm_context& c, int nex_in, int nex_out, mflbm_monitor* out) {
     return c.params.precision == MFLBM_FP32 ? monitor_t<float>(c, nex_in, nex_out, out)
                                             : monitor_t<double>(c, nex_in, nex_out, out);
+}
+
+int monitor_profile(mflbm_context& c, double* slices, mflbm_monitor_ext* ext, bool track_phi) {
+    return c.params.precision == MFLBM_FP32 ? monitor_profile_t<float>(c, slices, ext, track_phi)
+                                            : monitor_profile_t<double>(c, slices, ext, track_phi);
 }
 
 int monitor_noalloc(mflbm_context& c, int nex_in, int nex_out, mflbm_monitor* out) {

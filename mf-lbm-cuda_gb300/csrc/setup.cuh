@@ -6,8 +6,15 @@ namespace mflbm {
 int preprocess_geometry(mflbm_context& c, const int32_t* walls_global_host, int iper);
 int init_fields(mflbm_context& c, int option, double z0);
 int monitor(mflbm_context& c, int nex_in, int nex_out, mflbm_monitor* out);
+// per-slice monitor sums and the extra monitor scalars
+int monitor_profile(mflbm_context& c, double* slices, mflbm_monitor_ext* ext, bool track_phi);
 // monitor with its partials in a static device array (no allocation)
 int monitor_noalloc(mflbm_context& c, int nex_in, int nex_out, mflbm_monitor* out);
+// output files in the reference's formats (output.cu); d.staging must exist and,
+// for VTK types 1 and 3, the reference-layout gradient arrays must be current
+int write_vtk(mflbm_context& c, int vtk_type, int precision_cmd, const char* path);
+int write_walls_vtk(mflbm_context& c, const char* path);
+int write_checkpoint(mflbm_context& c, int ntime, const char* path);
 // copy populations between d.staging (reference f1 layout) and d.pdf (brick layout)
 int convert_populations(mflbm_context& c, bool to_bricks);
 }  // namespace mflbm

@@ -67,6 +67,19 @@ class Monitor(C.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
 
+class MonitorExt(C.Structure):
+    _fields_ = [("umax2", C.c_double), ("usq1", C.c_double), ("usq2", C.c_double), ("pre_w", C.c_double),
+                ("pre_nw", C.c_double), ("n_w", C.c_longlong), ("n_nw", C.c_longlong),
+                ("breakthrough", C.c_longlong), ("dphi_max", C.c_double)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+# rows of the per-slice monitor sums (mflbm_monitor_profile)
+PROFILE_ROWS = ["fl1", "fl2", "vol1", "vol2", "mass1", "mass2", "pre"]
+
+
 def struct_dict(s):
     return {n: getattr(s, n) for n, _ in s._fields_}
 

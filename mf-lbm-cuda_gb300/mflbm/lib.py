@@ -30,6 +30,7 @@ SIGNATURES = {
     "mflbm_create": (I, [VP, C.POINTER(VP)]),
     "mflbm_destroy": (I, [VP]),
     "mflbm_set_params": (I, [VP, VP]),
+    "mflbm_get_params": (I, [VP, VP]),
     "mflbm_preprocess_geometry": (I, [VP, VP, VP, VP, VP, VP, VP, VP]),
     "mflbm_upload_geometry": (I, [VP, VP, VP, VP, VP, VP]),
     "mflbm_init_fields": (I, [VP, I, D, VP]),
@@ -40,6 +41,11 @@ SIGNATURES = {
     "mflbm_synchronize": (I, [VP]),
     "mflbm_monitor_reduce": (I, [VP, I, I, VP]),
     "mflbm_monitor_reduce_noalloc": (I, [VP, I, I, VP]),
+    "mflbm_monitor_profile": (I, [VP, VP, VP, I]),
+    "mflbm_write_vtk": (I, [VP, I, I, C.c_char_p]),
+    "mflbm_write_walls_vtk": (I, [VP, C.c_char_p]),
+    "mflbm_write_checkpoint": (I, [VP, I, C.c_char_p]),
+    "mflbm_read_checkpoint": (I, [VP, C.c_char_p, VP, C.POINTER(I)]),
     "mflbm_node_counts": (I, [VP, C.POINTER(LL)]),
     "mflbm_stream": (VP, [VP]),
     "mflbm_set_kernel_timing": (I, [VP, I]),
@@ -183,6 +189,32 @@ class Context:
         check(self.lib.mflbm_monitor_reduce_noalloc(self.h, int(n_exclude_inlet), int(n_exclude_outlet),
                                                     C.byref(m)), "mflbm_monitor_reduce_noalloc")
         return m.as_dict()
+
+    def monitor_profile(self, track_phi=False):
+        """Per-slice sums {row: array(nz)} (rows of abi.PROFILE_ROWS) and the
+        extra monitor scalars (mflbm_monitor_profile)."""
+        nz = self.L.nz
+        sl = np.zeros((len(abi.PROFILE_ROWS), nz), dtype=np.float64)
+        e = abi.MonitorExt()
+        check(self.lib.mflbm_monitor_profile(self.h, ptr(sl), C.byref(e), int(bool(track_phi))),
+              "mflbm_monitor_profile")
+        return {n: sl[m] for m, n in enumerate(abi.PROFILE_ROWS)}, e.as_dict()
+
+    def write_vtk(self, vtk_type, path, precision_cmd=0):
+        check(self.lib.mflbm_write_vtk(self.h, int(vtk_type), int(precision_cmd), str(path).encode()), "mflbm_write_vtk")
+
+    def write_walls_vtk(self, path):
+        check(self.lib.mflbm_write_walls_vtk(self.h, str(path).encode()), "mflbm_write_walls_vtk")
+
+    def write_checkpoint(self, ntime, path):
+        check(self.lib.mflbm_write_checkpoint(self.h, int(ntime), str(path).encode()), "mflbm_write_checkpoint")
+
+    def read_checkpoint(self, path, W_in=None):
+        """Returns the reference's ntime0 (stored step - 1)."""
+        nt = I()
+        check(self.lib.mflbm_read_checkpoint(self.h, str(path).encode(), ptr(W_in), C.byref(nt)),
+              "mflbm_read_checkpoint")
+        return nt.value
 
     def node_counts(self):
         c = (LL * 2)()

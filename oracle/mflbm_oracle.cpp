@@ -26,6 +26,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <string>
 #include <vector>
 #include <limits>
 #ifdef _OPENMP
@@ -1212,6 +1213,102 @@ void monitor(const P<T>& p, const int32_t* walls, const T* pdf, const T* phi, co
     out->saturation = out->vol1_sum / (out->vol1_sum + out->vol2_sum);
 }
 
+/* Output files (src/IO_multiphase.cpp:252-305 save_checkpoint, :490-714
+ * SwapEnd + VTK_legacy_writer_3D, :800-841 VTK_walls_bin), restated from the
+ * host arrays of the reference layouts. */
+template <class V> void put_be(std::string& out, V v) {
+    unsigned char b[sizeof(V)];
+    std::memcpy(b, &v, sizeof(V));
+    for (int i = (int)sizeof(V) - 1; i >= 0; --i) out.push_back((char)b[i]);
+}
+
+inline std::string vtk_header(const Grid& g) {
+    char buf[512];
+    snprintf(buf, sizeof buf,
+             "# vtk DataFile Version 3.0\nvtk output\nBINARY\nDATASET STRUCTURED_POINTS\nDIMENSIONS %lld %lld %lld\n"
+             "ORIGIN 1 1 1\nSPACING 1 1 1\nPOINT_DATA %lld\n",
+             g.nx, g.ny, g.nz, g.nx * g.ny * g.nz);
+    return buf;
+}
+
+inline int save(const char* path, const std::string& bytes) {
+    FILE* f = fopen(path, "wb");
+    if (!f) return -1;
+    const size_t n = fwrite(bytes.data(), 1, bytes.size(), f);
+    return (fclose(f) == 0 && n == bytes.size()) ? 0 : -1;
+}
+
+template <class T>
+int write_vtk(const P<T>& p, const int32_t* walls, const T* pdf, const T* phi_in, const T* cnx, const T* cny,
+              const T* cnz, const T* cnorm, const T* curv, int type, int cmd, const char* path) {
+    const Grid& g = p.g;
+    std::vector<T> phi(phi_in, phi_in + g.n_s4());   /* the reference zeroes solids in its host copy */
+    std::vector<T> rho, u, v, w;
+    if (type == 1) {
+        rho.assign(g.n_s1(), T(0)); u = rho; v = rho; w = rho;
+        macro_vars<T>(p, walls, pdf, phi.data(), cnx, cny, cnz, cnorm, curv, rho.data(), u.data(), v.data(), w.data());
+    } else if (type == 2) {
+        for (ll k = 1; k <= g.nz; ++k)
+            for (ll j = 1; j <= g.ny; ++j)
+                for (ll i = 1; i <= g.nx; ++i) {
+                    const int wi = walls[g.s2(i, j, k)];
+                    phi[g.s4(i, j, k)] = T(0) * T(wi) + phi[g.s4(i, j, k)] * T(1 - wi);
+                }
+    }
+    std::string out = vtk_header(g);
+    const std::string fmt = type == 2 ? "float" : (cmd == 0 ? "float" : "double");
+    const char* names[5] = {"phi", "density", "velocity_X", "velocity_Y", "velocity_Z"};
+    const int nblk = type == 2 ? 1 : 5;
+    for (int b = 0; b < nblk; ++b) {
+        out += std::string("SCALARS ") + names[b] + " " + fmt + "\nLOOKUP_TABLE default\n";
+        for (ll k = 1; k <= g.nz; ++k)
+            for (ll j = 1; j <= g.ny; ++j)
+                for (ll i = 1; i <= g.nx; ++i) {
+                    const ll n1 = g.s1(i, j, k), n2 = g.s2(i, j, k), n4 = g.s4(i, j, k);
+                    if (type == 2) { put_be(out, (float)phi[n4]); continue; }
+                    T val;
+                    if (type == 1) {
+                        const T* src[5] = {nullptr, rho.data(), u.data(), v.data(), w.data()};
+                        val = b == 0 ? phi[n4] : src[b][n1];
+                    } else {
+                        const T* src[5] = {nullptr, cnorm, cnx, cny, cnz};
+                        val = b == 0 ? phi[n4] : src[b][n2];
+                    }
+                    put_be(out, val);
+                }
+    }
+    return save(path, out);
+}
+
+inline int write_walls_vtk(ll nx, ll ny, ll nz, const int32_t* walls, const char* path) {
+    const Grid g{nx, ny, nz};
+    std::string out = vtk_header(g) + "SCALARS walls int\nLOOKUP_TABLE default\n";
+    for (ll k = 1; k <= nz; ++k)
+        for (ll j = 1; j <= ny; ++j)
+            for (ll i = 1; i <= nx; ++i) put_be(out, (int32_t)walls[g.s2(i, j, k)]);
+    return save(path, out);
+}
+
+template <class T>
+int write_checkpoint(const P<T>& p, int ntime, const T* pdf, const T* phi, const T* f_cv, const T* g_cv,
+                     const T* phi_cv, const char* path) {
+    const Grid& g = p.g;
+    std::string out;
+    const int nt = ntime + 1;
+    out.append((const char*)&nt, sizeof nt);
+    out.append((const char*)&p.force_z, sizeof(T));
+    out.append((const char*)&p.rho_in, sizeof(T));
+    out.append((const char*)pdf, sizeof(T) * g.n_s1() * 38);
+    out.append((const char*)phi, sizeof(T) * g.n_s4());
+    if (p.outlet_BC == 1) {
+        const ll pl = (g.nx + 2) * (g.ny + 2);
+        out.append((const char*)f_cv, sizeof(T) * pl * 19);
+        out.append((const char*)g_cv, sizeof(T) * pl * 19);
+        out.append((const char*)phi_cv, sizeof(T) * pl);
+    }
+    return save(path, out);
+}
+
 } // namespace
 
 /* ---------------------------------------------------------------------------
@@ -1268,7 +1365,20 @@ void monitor(const P<T>& p, const int32_t* walls, const T* pdf, const T* phi, co
         monitor<T>(P<T>(prm), walls, pdf, phi, cnx, cny, cnz, cnorm, curv, nex_in, nex_out, out);                  \
     }
 
+#define ORC_TYPED_IO(T, SUF)                                                                                       \
+    ORC_EXPORT int orc_write_vtk_##SUF(const mflbm_params* prm, const int32_t* walls, const T* pdf, const T* phi,  \
+                                       const T* cnx, const T* cny, const T* cnz, const T* cnorm, const T* curv,    \
+                                       int type, int cmd, const char* path) {                                      \
+        return write_vtk<T>(P<T>(prm), walls, pdf, phi, cnx, cny, cnz, cnorm, curv, type, cmd, path);              \
+    }                                                                                                              \
+    ORC_EXPORT int orc_write_checkpoint_##SUF(const mflbm_params* prm, int ntime, const T* pdf, const T* phi,      \
+                                              const T* f_cv, const T* g_cv, const T* phi_cv, const char* path) {   \
+        return write_checkpoint<T>(P<T>(prm), ntime, pdf, phi, f_cv, g_cv, phi_cv, path);                          \
+    }
+
 ORC_TYPED(float, f32)
+ORC_TYPED_IO(float, f32)
+ORC_TYPED_IO(double, f64)
 ORC_TYPED(double, f64)
 
 ORC_EXPORT void orc_set_walls(const mflbm_control* ctl, const uint8_t* geo, int32_t* walls_global) {
@@ -1281,4 +1391,8 @@ ORC_EXPORT int orc_max_threads(void) {
 #else
     return 1;
 #endif
+}
+
+ORC_EXPORT int orc_write_walls_vtk(long long nx, long long ny, long long nz, const int32_t* walls, const char* path) {
+    return write_walls_vtk(nx, ny, nz, walls, path);
 }

@@ -17,7 +17,9 @@
  * initialization_new_multi / color_gradient in a working directory that holds
  * the reference's input files.
  */
+#include <sys/stat.h>
 #include <unistd.h>
+#include <cstdio>
 #include <cstring>
 #include <string>
 
@@ -32,6 +34,7 @@
 #include "Monitor.h"
 #include "Misc.h"
 #include "main_iteration_GPU.h"
+#include "IO_multiphase.h"
 
 thread_local shim_index3 threadIdx = {0, 0, 0}, blockIdx = {0, 0, 0}, blockDim = {1, 1, 1};
 
@@ -163,6 +166,39 @@ void ref_step(int nt) {
     launch3(nx + 4, ny + 4, nz + 4, [&] { alter_color_gradient_solid_surface_GPU(walls_type_d, cn_x_d, cn_y_d, cn_z_d, c_norm_d, s_nx_d, s_ny_d, s_nz_d); });
     launch3(nx + 2, ny + 2, nz + 2, [&] { extrapolateNormalToSolid(walls_type_d, cn_x_d, cn_y_d, cn_z_d, phi_d); });
     launch3(nx, ny, nz, [&] { CSF_Forces(cn_x_d, cn_y_d, cn_z_d, curv_d); });
+}
+
+/* The reference's own output writers on the current state, in `workdir`
+ * (src/IO_multiphase.cpp:252-305 save_checkpoint, :500-714
+ * VTK_legacy_writer_3D, :800-841 VTK_walls_bin).  Order: the checkpoint and
+ * the type-3 files first, because the type-1 and type-2 writers set phi to
+ * zero on solid nodes of the host array they share with the state. */
+int ref_write_outputs(const char* workdir, int nt) {
+    char cwd[4096];
+    if (!getcwd(cwd, sizeof cwd)) return -1;
+    if (chdir(workdir) != 0) return -2;
+    const char* dirs[] = {"results", "results/out2.checkpoint", "results/out3.field_data",
+                          "results/out3.field_data/full_flow_field", "results/out3.field_data/phase_distribution"};
+    for (const char* d : dirs) mkdir(d, 0755);
+    ntime = nt;
+    save_checkpoint(0);
+    output_fieldData_precision_cmd = 0;
+    VTK_legacy_writer_3D(nt, 3);
+    char name[256];
+    snprintf(name, sizeof name, "results/out3.field_data/full_flow_field/force_vector_%010d.vtk", nt);
+    rename(name, "vtk3_cmd0.tmp");
+    output_fieldData_precision_cmd = 1;
+    VTK_legacy_writer_3D(nt, 3);
+    VTK_walls_bin();
+    output_fieldData_precision_cmd = 0;
+    VTK_legacy_writer_3D(nt, 1);
+    snprintf(name, sizeof name, "results/out3.field_data/full_flow_field/full_flow_field_%010d.vtk", nt);
+    rename(name, "vtk1_cmd0.tmp");
+    output_fieldData_precision_cmd = 1;
+    VTK_legacy_writer_3D(nt, 1);
+    VTK_legacy_writer_3D(nt, 2);
+    if (chdir(cwd) != 0) return -3;
+    return 0;
 }
 
 /* Bind the "device" pointers of the kernels to the reference's host arrays

@@ -3,8 +3,9 @@
 For every small case of ``mflbm.cases.SMALL_KINDS`` and both precisions, the
 reference's own kernels and set-up (compiled as host code into oracle/_ref by
 oracle/build.py, from the reference checkout) run the case; the SHA-256 of
-every state array at a few steps, the derived scalars and the geometry arrays
-are written to ``<case>_<f32|f64>.json``; the geometry body used is written
+every state array at a few steps, the derived scalars, the geometry arrays
+and the reference's output files after the last step (VTK types 1-3, the
+geometry VTK, the checkpoint) are written to ``<case>_<f32|f64>.json``; the geometry body used is written
 to ``<case>.dat``.  The CPU tests compare the oracle against these files
 bit for bit.
 
@@ -41,7 +42,7 @@ def _job(args):
     from mflbm.geometry import read_dat
     case = cases.small_case(kind)
     geo = read_dat(HERE / f"{case.name}.dat")
-    out = H.run_reference_case(case, prec, CHECKPOINTS, geometry=geo)
+    out = H.run_reference_case(case, prec, CHECKPOINTS, geometry=geo, outputs=True)
     res = {"case": case.name, "kind": kind, "precision": "f32" if prec == 1 else "f64",
            "checkpoints": CHECKPOINTS, "scalars": out["_scalars"],
            "geometry": {n: digest(a) for n, a in out["_geometry"].items()},
@@ -49,7 +50,8 @@ def _job(args):
            "summary": {str(cp): {"phi_sum": float(np.sum(out[cp]["phi"].astype(np.float64))),
                                  "pdf_sum": float(np.sum(out[cp]["pdf"].astype(np.float64)))}
                        for cp in CHECKPOINTS},
-           "geometry_dat_sha256": digest(geo)}
+           "geometry_dat_sha256": digest(geo),
+           "outputs": {"step": CHECKPOINTS[-1], "sha256": out["_outputs"]}}
     return res
 
 

@@ -71,6 +71,9 @@ def oracle_lib():
             getattr(lib, f"orc_collide_{s}").argtypes = [VP, C.c_int] + [VP] * 8
             getattr(lib, f"orc_macro_vars_{s}").argtypes = [VP] * 13
             getattr(lib, f"orc_monitor_{s}").argtypes = [VP] * 9 + [C.c_int, C.c_int, VP]
+            getattr(lib, f"orc_write_vtk_{s}").argtypes = [VP] * 9 + [C.c_int, C.c_int, C.c_char_p]
+            getattr(lib, f"orc_write_checkpoint_{s}").argtypes = [VP, C.c_int] + [VP] * 5 + [C.c_char_p]
+        lib.orc_write_walls_vtk.argtypes = [C.c_longlong] * 3 + [VP, C.c_char_p]
         lib.orc_set_walls.argtypes = [VP, VP, VP]
         lib.orc_max_threads.restype = C.c_int
         _ORACLE = lib
@@ -140,6 +143,20 @@ class OracleState:
         out["phi"] = phi
         return out
 
+    def write_outputs(self, folder, ntime):
+        """The output files of OUTPUT_FILES for the current state (oracle writers)."""
+        a, folder = self.a, Path(folder)
+        for name, (vtk_type, cmd) in VTK_FILES.items():
+            rc = self._f("write_vtk")(C.byref(self.params), ptr(a["walls"]), ptr(a["pdf"]), ptr(a["phi"]),
+                                      ptr(a["cn_x"]), ptr(a["cn_y"]), ptr(a["cn_z"]), ptr(a["c_norm"]),
+                                      ptr(a["curv"]), vtk_type, cmd, str(folder / name).encode())
+            assert rc == 0, name
+        nx, ny, nz = self.case.shape
+        assert self.lib.orc_write_walls_vtk(nx, ny, nz, ptr(a["walls"]), str(folder / "walls_bin.vtk").encode()) == 0
+        assert self._f("write_checkpoint")(C.byref(self.params), ntime, ptr(a["pdf"]), ptr(a["phi"]),
+                                           ptr(a["f_convec_bc"]), ptr(a["g_convec_bc"]), ptr(a["phi_convec_bc"]),
+                                           str(folder / "checkpoint").encode()) == 0
+
     def monitor(self, nex_in=None, nex_out=None):
         k = self.case.control_keys()
         nex_in = int(k["n_exclude_inlet"]) if nex_in is None else nex_in
@@ -150,6 +167,43 @@ class OracleState:
                            ptr(a["cn_y"]), ptr(a["cn_z"]), ptr(a["c_norm"]), ptr(a["curv"]), nex_in, nex_out,
                            C.byref(m))
         return m.as_dict()
+
+
+# Output files compared with the reference's own writers: name -> (vtk_type,
+# output_fieldData_precision_cmd), plus walls_bin.vtk and the checkpoint.
+VTK_FILES = {"vtk1_cmd0.vtk": (1, 0), "vtk1_cmd1.vtk": (1, 1), "vtk2.vtk": (2, 0), "vtk3_cmd0.vtk": (3, 0),
+             "vtk3_cmd1.vtk": (3, 1)}
+OUTPUT_FILES = list(VTK_FILES) + ["walls_bin.vtk", "checkpoint"]
+
+
+def file_digest(path):
+    import hashlib
+    return hashlib.sha256(Path(path).read_bytes()).hexdigest()
+
+
+def reference_outputs(lib, workdir, ntime):
+    """Run the reference's writers (ref_write_outputs) in `workdir` and return
+    {name: sha256} keyed like OUTPUT_FILES."""
+    lib.ref_write_outputs.argtypes = [C.c_char_p, C.c_int]
+    devnull = os.open(os.devnull, os.O_WRONLY)
+    saved = os.dup(1)
+    os.dup2(devnull, 1)
+    try:
+        rc = lib.ref_write_outputs(str(workdir).encode(), ntime)
+    finally:
+        os.dup2(saved, 1)
+        os.close(devnull)
+        os.close(saved)
+    if rc != 0:
+        raise RuntimeError(f"ref_write_outputs failed ({rc})")
+    w = Path(workdir)
+    ff = w / "results" / "out3.field_data"
+    nt = f"{ntime:010d}"
+    files = {"vtk1_cmd0.vtk": w / "vtk1_cmd0.tmp", "vtk1_cmd1.vtk": ff / "full_flow_field" / f"full_flow_field_{nt}.vtk",
+             "vtk2.vtk": ff / "phase_distribution" / f"small_{nt}.vtk", "vtk3_cmd0.vtk": w / "vtk3_cmd0.tmp",
+             "vtk3_cmd1.vtk": ff / "full_flow_field" / f"force_vector_{nt}.vtk", "walls_bin.vtk": ff / "walls_bin.vtk",
+             "checkpoint": w / "results" / "out2.checkpoint" / "id0000"}
+    return {n: file_digest(f) for n, f in files.items()}
 
 
 # ---------------------------------------------------------------------------
@@ -182,9 +236,12 @@ def ref_array(lib, L, name, T):
     return np.frombuffer(buf, dtype=dt).reshape(L.shape(kind)).copy()
 
 
-def run_reference_case(case, precision, checkpoints, fields=STATE_FIELDS, workdir=None, geometry=None):
+def run_reference_case(case, precision, checkpoints, fields=STATE_FIELDS, workdir=None, geometry=None,
+                       outputs=False):
     """Run `case` through oracle/_ref; returns {step: {field: array}} at each
-    checkpoint step (0 = after start-up) plus '_scalars'."""
+    checkpoint step (0 = after start-up) plus '_scalars', and with `outputs`
+    the digests of the reference's output files after the last step
+    ('_outputs')."""
     lib = ref_lib(precision)
     if lib is None:
         raise RuntimeError("reference sources unavailable")
@@ -219,4 +276,6 @@ def run_reference_case(case, precision, checkpoints, fields=STATE_FIELDS, workdi
             lib.ref_step(nt)
             nt += 1
         out[cp] = grab()
+    if outputs:
+        out["_outputs"] = reference_outputs(lib, tmp, max(checkpoints))
     return out
