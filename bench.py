@@ -138,6 +138,12 @@ def barrier(dist):
         dist.barrier()
 
 
+def replica_mlups(world, nodes, steps, t_max_ms):
+    """Whole-job MLUPS of `world` independent replicas of `nodes` lattice nodes
+    each, `steps` steps, the slowest rank taking `t_max_ms`."""
+    return world * nodes * steps / (t_max_ms * 1e-3) / 1e6
+
+
 def cpu_reference_run(case, steps, warmup, budget_s=90.0):
     """The oracle (CPU restatement of the reference's kernels, OpenMP) on the
     same workload; the number of timed steps is capped to stay within budget."""
@@ -241,7 +247,7 @@ def main():
     elapsed_ms = ev0.elapsed_time(ev1)
     nt += args.steps
     t_max = max_over_ranks(dist, elapsed_ms)
-    value = world * n_all * args.steps / (t_max * 1e-3) / 1e6
+    value = replica_mlups(world, n_all, args.steps, t_max)
 
     # ---- per-kernel device time of the collision (events on the launching stream) ----
     ktime_steps = min(args.steps, 200)
