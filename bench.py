@@ -167,6 +167,78 @@ def cpu_reference_run(case, steps, warmup, budget_s=90.0):
             "setup_s": setup_s}
 
 
+def _timed_run(run, sync, stream):
+    import torch
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    run()
+    ev1.record(stream)
+    sync()
+    torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1)
+
+
+def storage_variants(case, geo, steps, nt):
+    """The same workload with 16-bit population storage (FP32 collision):
+    MLUPS, collision time and its algorithmic bandwidth (152 + 4 B per fluid
+    node for the populations and phi, + 1 B per node)."""
+    import torch
+    from mflbm import lib
+    out = {}
+    nx, ny, nz = case.shape
+    for name, st in (("f16", abi.MFLBM_STORE_F16), ("bf16", abi.MFLBM_STORE_BF16)):
+        c, _ = lib.setup_case(case, abi.MFLBM_FP32, abi.MFLBM_FAST, geometry=geo, storage=st)
+        n_fluid, n_all = c.node_counts()
+        c.run(1, 20)
+        stream = torch.cuda.ExternalStream(c.stream())
+        ms = _timed_run(lambda: c.run(21, steps), c.sync, stream)
+        c.set_timing(True)
+        c.run(21 + steps, 40)
+        tc, tg, n = c.kernel_times()
+        c.set_timing(False)
+        coll = tc / max(n, 1)
+        out[name] = {"value": round(n_all * steps / (ms * 1e-3) / 1e6, 2), "unit": "MLUPS",
+                     "ms_per_step": round(ms / steps, 5), "collide_ms": round(coll, 5),
+                     "gradient_ms": round(tg / max(n, 1), 5),
+                     "collide_gbs": round((n_fluid * 156 + n_all) / (coll * 1e-3) / 1e9, 1)}
+        c.close()
+    return out
+
+
+def batch_vs_sequential(steps):
+    """16 single-phase samples of 48^3 .. 96^3 (porosity 0.3 .. 0.7): one
+    graph launch per step pair for all of them (mflbm_batch) against each
+    context's own graph replays, one after the other."""
+    import torch
+    from mflbm import lib, permeability
+    samples = permeability.make_samples(16, 48, 96)
+    ctxs = [lib.setup_case(s, abi.MFLBM_FP32, abi.MFLBM_FAST)[0] for s in samples]
+    nodes = sum(int(np.prod(s.shape)) for s in samples)
+    steps += steps & 1
+    b = lib.Batch(ctxs)
+    b.run(1, 4)
+    for c in ctxs:
+        c.run(5, 4)
+        c.sync()
+    t0 = time.perf_counter()
+    b.run(9, steps)
+    t_batch = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for c in ctxs:
+        c.run(9 + steps, steps)
+    for c in ctxs:
+        c.sync()
+    t_seq = time.perf_counter() - t0
+    b.close()
+    for c in ctxs:
+        c.close()
+    return {"samples": len(samples), "sizes": [s.shape[0] for s in samples], "steps": steps,
+            "batched_mlups": round(nodes * steps / t_batch / 1e6, 1),
+            "sequential_mlups": round(nodes * steps / t_seq / 1e6, 1),
+            "how": "wall clock, mflbm_batch_run vs mflbm_run per context (each graph-replayed)"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -175,6 +247,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--size", type=int, default=256, help="lattice edge (default: the 256^3 workload)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the 16-bit storage and batch measurements")
     args = ap.parse_args()
     warmup = max(3, args.warmup)
 
@@ -214,7 +287,8 @@ def main():
     torch.cuda.set_device(local)
     from mflbm import lib
     lib.load()
-    ctx, info = lib.setup_case(case, abi.MFLBM_FP32, abi.MFLBM_FAST)
+    geo = case.geometry_bytes()
+    ctx, info = lib.setup_case(case, abi.MFLBM_FP32, abi.MFLBM_FAST, geometry=geo)
     n_fluid, _ = ctx.node_counts()
     porosity = n_fluid / n_all
 
@@ -294,6 +368,11 @@ def main():
     assert np.isfinite(out["phi"]).all()
 
     mon = ctx.monitor(2, 2)
+    extra = {}
+    if not args.no_extras:
+        ctx.close()
+        extra["storage"] = storage_variants(case, geo, min(args.steps, 200), nt)
+        extra["batch"] = batch_vs_sequential(min(args.steps, 200))
 
     if rank != 0:
         return
@@ -330,6 +409,7 @@ def main():
     }
     if cpu:
         line["cpu_baseline"] = cpu
+    line.update(extra)
     print(json.dumps(line))
     ctx.close()
 

@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define MFLBM_ABI_VERSION 1
+#define MFLBM_ABI_VERSION 2
 
 enum {
     MFLBM_OK = 0,
@@ -44,6 +44,12 @@ enum {
 
 enum { MFLBM_FP32 = 1, MFLBM_FP64 = 2 };         /* = reference SINGLE/DOUBLE_PRECISION */
 enum { MFLBM_FAST = 0, MFLBM_STRICT = 1 };       /* strict: IEEE ops in reference order, no FMA contraction */
+/* Storage of the populations (no counterpart in the reference): the solver
+ * precision itself, or, with MFLBM_FP32 only, 16-bit shifted deviations
+ * s = g / w_q - 1 from the lattice weight w_q of the direction (FP16 or BF16;
+ * the collision computes in FP32).  s is exact where a component is absent
+ * (g = 0, s = -1) and of order 1e-3 where it fills the node. */
+enum { MFLBM_STORE_NATIVE = 0, MFLBM_STORE_F16 = 1, MFLBM_STORE_BF16 = 2 };
 
 /*
  * Simulation parameters in the final form the reference host code hands to
@@ -74,6 +80,8 @@ typedef struct mflbm_params {
     double relaxation;                 /* inlet relaxation factor (1 in the reference) */
     double cos_theta;                  /* cos(180 deg - contact angle) */
     double rho_in, rho_out;            /* Zou-He inlet / outlet densities */
+    int storage;                       /* MFLBM_STORE_NATIVE (0, the reference's), _F16 or _BF16 */
+    int reserved;
 } mflbm_params;
 
 /*
@@ -300,6 +308,41 @@ int mflbm_write_checkpoint(mflbm_context* ctx, int ntime, const char* path);
  * mflbm_inlet_profile, unless NULL) and runs the gradient pass.  *ntime0
  * receives the stored step - 1 (the reference's ntime0). */
 int mflbm_read_checkpoint(mflbm_context* ctx, const char* path, const void* W_in, int* ntime0);
+
+/* ---- tuning and batches (no counterpart in the reference) -------------- */
+
+typedef struct mflbm_tuning {
+    int collide_block;                 /* threads per block of the collision */
+    int normals_block;                 /* ... of the interface-normal kernel */
+    int curvature_block;               /* ... of the curvature kernel */
+    int extrapolate_block;             /* ... of the two solid-boundary extrapolations */
+    double step_ms_before;             /* mean step time with the block sizes found on entry */
+    double step_ms_after;              /* ... with the chosen block sizes */
+} mflbm_tuning;
+
+/* Times the step kernels of this context with 64, 128 and 256 threads per
+ * block, one kernel family at a time, keeps the fastest combination and
+ * reports it.  reps: odd + even step pairs timed per candidate (>= 1).  The
+ * state is copied aside first (temporary device memory of one state) and
+ * restored afterwards, so the simulation's results are unchanged.  Not
+ * allowed while kernel timing is on. */
+int mflbm_autotune(mflbm_context* ctx, int reps, mflbm_tuning* out);
+/* Sets block sizes (64, 128 or 256; 0 keeps the current value), e.g. to reuse
+ * a tuning found on another context of the same size. */
+int mflbm_set_tuning(mflbm_context* ctx, const mflbm_tuning* t);
+
+/* A batch of independent contexts on the current device, advanced together:
+ * the odd + even step pairs of all of them are captured into one CUDA graph,
+ * one branch per context, so one graph launch steps every sample and small
+ * lattices run concurrently.  The contexts stay owned by the caller and must
+ * outlive the batch; a context whose parameters, geometry or tuning change
+ * is re-captured at the next run. */
+typedef struct mflbm_batch mflbm_batch;
+int mflbm_batch_create(mflbm_context* const* ctxs, int n, mflbm_batch** out);
+/* Steps ntime_begin .. ntime_begin + nsteps - 1 of every context of the
+ * batch; ntime_begin must be odd and nsteps even.  Blocks until done. */
+int mflbm_batch_run(mflbm_batch* b, int ntime_begin, int nsteps);
+int mflbm_batch_destroy(mflbm_batch* b);
 
 /* ---- introspection ---------------------------------------------------- */
 /* Counts of lattice nodes: [0] fluid nodes in [1,n]^3, [1] all nodes n^3. */

@@ -10,19 +10,19 @@ namespace MFLBM_NS {
 // (i, j) column (inlet / outlet / plate) or (i, k) row (periodic y).
 // keep(new, old, w) is the reference's  new*(1-w) + old*w  blend.
 // ===========================================================================
-template <class T> struct BcArgs {
+template <class T, class E> struct BcArgs {
     Grid g;
-    Bricks b;
+    PopView<T, E> P;  // populations
     const int32_t* walls;
-    T *pdf, *phi, *W_in, *f_cv, *g_cv, *phi_cv;
+    T *phi, *W_in, *f_cv, *g_cv, *phi_cv;
     Phys<T> ph;
     int plate_cmd, Zplate;
 };
 
 template <class T> __device__ __forceinline__ T keep(T v_new, T v_old, int w) { return v_new * T(1 - w) + v_old * T(w); }
 
-template <class T>
-__device__ __forceinline__ void inlet_phi(const BcArgs<T>& a, int i, int j, int w) {
+template <class T, class E>
+__device__ __forceinline__ void inlet_phi(const BcArgs<T, E>& a, int i, int j, int w) {
     const Grid& g = a.g;
     a.phi[g.s4(i, j, 0)] = a.ph.phi_inlet * T(1 - w) + a.phi[g.s4(i, j, 0)] * T(w);
     const T v = a.phi[g.s4(i, j, 0)];
@@ -37,8 +37,8 @@ __device__ __constant__ const int kInlet[5][4] = {{0, 0, 5, 6}, {-1, 0, 11, 14},
 __device__ __constant__ const int kOutlet[5][5] = {{0, 0, 6, 5, 6}, {-1, 0, 13, 12, 13}, {1, 0, 14, 11, 14}, {0, -1, 17, 16, 17}, {0, 1, 18, 15, 18}};
 
 // velocity inlet: bounce-back plus 6 w rho u injection, split by sa_inject (:1009-1077)
-template <class T, bool AFTER_ODD>
-__global__ void inlet_velocity_kernel(const BcArgs<T> a) {
+template <class T, class E, bool AFTER_ODD>
+__global__ void inlet_velocity_kernel(const BcArgs<T, E> a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1;
     if (i > a.g.nx) return;
     const Grid& g = a.g;
@@ -55,19 +55,19 @@ __global__ void inlet_velocity_kernel(const BcArgs<T> a) {
             const T wq = s == 0 ? a.ph.c.w1 : a.ph.c.w2;
             const int dx = kInlet[s][0], dy = kInlet[s][1], s0 = kInlet[s][2], s1 = kInlet[s][3];
             if (!AFTER_ODD) {
-                T& d = a.pdf[a.b.at(i + dx, j + dy, 0, s0, gg)];
-                d = keep((a.pdf[a.b.at(i, j, 1, s1, gg)] + T(6.0) * wq * inj), d, w);
+                const T d = a.P.get(i + dx, j + dy, 0, s0, gg);
+                a.P.set(i + dx, j + dy, 0, s0, gg, keep((a.P.get(i, j, 1, s1, gg) + T(6.0) * wq * inj), d, w));
             } else {
-                T& d = a.pdf[a.b.at(i, j, 1, s1, gg)];
-                d = keep((a.pdf[a.b.at(i + dx, j + dy, 0, s0, gg)] + T(6.0) * wq * inj), d, w);
+                const T d = a.P.get(i, j, 1, s1, gg);
+                a.P.set(i, j, 1, s1, gg, keep((a.P.get(i + dx, j + dy, 0, s0, gg) + T(6.0) * wq * inj), d, w));
             }
         }
     }
 }
 
 // Zou-He pressure inlet per component (:1085-1241)
-template <class T, bool AFTER_ODD>
-__global__ void inlet_pressure_kernel(const BcArgs<T> a) {
+template <class T, class E, bool AFTER_ODD>
+__global__ void inlet_pressure_kernel(const BcArgs<T, E> a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1;
     if (i > a.g.nx) return;
     const Grid& g = a.g;
@@ -79,7 +79,8 @@ __global__ void inlet_pressure_kernel(const BcArgs<T> a) {
     const T c3 = T(0.333333333333333333), c6 = T(0.166666666666666667);
 #pragma unroll
     for (int gg = 0; gg < 2; ++gg) {
-        auto F = [&](int u, int v, int k, int e) -> T& { return a.pdf[a.b.at(u, v, k, e, gg)]; };
+        auto F = [&](int u, int v, int k, int e) { return a.P.get(u, v, k, e, gg); };
+        auto S = [&](int u, int v, int k, int e, T x) { a.P.set(u, v, k, e, gg, x); };
         const T rc = gg == 0 ? r1 : r2;
         if (!AFTER_ODD) {
             const T t = (rc - (F(i, j, 1, 0) + F(i - 1, j, 1, 1) + F(i + 1, j, 1, 2) + F(i, j - 1, 1, 3) +
@@ -91,11 +92,11 @@ __global__ void inlet_pressure_kernel(const BcArgs<T> a) {
                                     (F(i + 1, j, 1, 2) + F(i + 1, j - 1, 1, 8) + F(i + 1, j + 1, 1, 10)));
             const T tny = T(0.5) * (F(i, j - 1, 1, 3) + F(i - 1, j - 1, 1, 7) + F(i + 1, j - 1, 1, 8) -
                                     (F(i, j + 1, 1, 4) + F(i + 1, j + 1, 1, 10) + F(i - 1, j + 1, 1, 9)));
-            F(i, j, 0, 5) = keep((F(i, j, 2, 6) + c3 * t), F(i, j, 0, 5), w);
-            F(i - 1, j, 0, 11) = keep((F(i + 1, j, 2, 14) + c6 * t - tnx), F(i - 1, j, 0, 11), w);
-            F(i + 1, j, 0, 12) = keep((F(i - 1, j, 2, 13) + c6 * t + tnx), F(i + 1, j, 0, 12), w);
-            F(i, j - 1, 0, 15) = keep((F(i, j + 1, 2, 18) + c6 * t - tny), F(i, j - 1, 0, 15), w);
-            F(i, j + 1, 0, 16) = keep((F(i, j - 1, 2, 17) + c6 * t + tny), F(i, j + 1, 0, 16), w);
+            S(i, j, 0, 5, keep((F(i, j, 2, 6) + c3 * t), F(i, j, 0, 5), w));
+            S(i - 1, j, 0, 11, keep((F(i + 1, j, 2, 14) + c6 * t - tnx), F(i - 1, j, 0, 11), w));
+            S(i + 1, j, 0, 12, keep((F(i - 1, j, 2, 13) + c6 * t + tnx), F(i + 1, j, 0, 12), w));
+            S(i, j - 1, 0, 15, keep((F(i, j + 1, 2, 18) + c6 * t - tny), F(i, j - 1, 0, 15), w));
+            S(i, j + 1, 0, 16, keep((F(i, j - 1, 2, 17) + c6 * t + tny), F(i, j + 1, 0, 16), w));
         } else {
             const T t = (rc - (F(i, j, 1, 0) + F(i, j, 1, 2) + F(i, j, 1, 1) + F(i, j, 1, 4) + F(i, j, 1, 3) +
                                F(i, j, 1, 8) + F(i, j, 1, 7) + F(i, j, 1, 10) + F(i, j, 1, 9) +
@@ -105,18 +106,18 @@ __global__ void inlet_pressure_kernel(const BcArgs<T> a) {
                                     (F(i, j, 1, 1) + F(i, j, 1, 7) + F(i, j, 1, 9)));
             const T tny = T(0.5) * (F(i, j, 1, 4) + F(i, j, 1, 9) + F(i, j, 1, 10) -
                                     (F(i, j, 1, 3) + F(i, j, 1, 8) + F(i, j, 1, 7)));
-            F(i, j, 1, 6) = keep((F(i, j, 1, 5) + c3 * t), F(i, j, 1, 6), w);
-            F(i, j, 1, 13) = keep((F(i, j, 1, 12) + c6 * t + tnx), F(i, j, 1, 13), w);
-            F(i, j, 1, 14) = keep((F(i, j, 1, 11) + c6 * t - tnx), F(i, j, 1, 14), w);
-            F(i, j, 1, 17) = keep((F(i, j, 1, 16) + c6 * t + tny), F(i, j, 1, 17), w);
-            F(i, j, 1, 18) = keep((F(i, j, 1, 15) + c6 * t - tny), F(i, j, 1, 18), w);
+            S(i, j, 1, 6, keep((F(i, j, 1, 5) + c3 * t), F(i, j, 1, 6), w));
+            S(i, j, 1, 13, keep((F(i, j, 1, 12) + c6 * t + tnx), F(i, j, 1, 13), w));
+            S(i, j, 1, 14, keep((F(i, j, 1, 11) + c6 * t - tnx), F(i, j, 1, 14), w));
+            S(i, j, 1, 17, keep((F(i, j, 1, 16) + c6 * t + tny), F(i, j, 1, 17), w));
+            S(i, j, 1, 18, keep((F(i, j, 1, 15) + c6 * t - tny), F(i, j, 1, 18), w));
         }
     }
 }
 
 // convective outflow with the previous-step buffers (:1246-1357)
-template <class T, bool AFTER_ODD>
-__global__ void outlet_convective_kernel(const BcArgs<T> a) {
+template <class T, class E, bool AFTER_ODD>
+__global__ void outlet_convective_kernel(const BcArgs<T, E> a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1;
     if (i > a.g.nx) return;
     const Grid& g = a.g;
@@ -139,12 +140,13 @@ __global__ void outlet_convective_kernel(const BcArgs<T> a) {
             const int dx = kOutlet[s][0], dy = kOutlet[s][1], su = kOutlet[s][2], sd = kOutlet[s][3], sb = kOutlet[s][4];
             T& bv = buf[g.cnv(i, j, sb)];
             if (!AFTER_ODD) {
-                T& d = a.pdf[a.b.at(i + dx, j + dy, nz + 1, su, gg)];
-                d = ((bv + u * a.pdf[a.b.at(i + dx, j + dy, nz, su, gg)]) * temp) * T(1 - w) + d * T(w);
+                const T d = ((bv + u * a.P.get(i + dx, j + dy, nz, su, gg)) * temp) * T(1 - w) +
+                            a.P.get(i + dx, j + dy, nz + 1, su, gg) * T(w);
+                a.P.set(i + dx, j + dy, nz + 1, su, gg, d);
                 bv = d;
             } else {
-                T& d = a.pdf[a.b.at(i, j, nz, sd, gg)];
-                d = ((bv + u * a.pdf[a.b.at(i, j, nz - 1, sd, gg)]) * temp) * T(1 - w) + d * T(w);
+                const T d = ((bv + u * a.P.get(i, j, nz - 1, sd, gg)) * temp) * T(1 - w) + a.P.get(i, j, nz, sd, gg) * T(w);
+                a.P.set(i, j, nz, sd, gg, d);
                 bv = d;
             }
         }
@@ -152,8 +154,8 @@ __global__ void outlet_convective_kernel(const BcArgs<T> a) {
 }
 
 // Zou-He pressure outlet on the total density, flux split by phi (:1363-1524)
-template <class T, bool AFTER_ODD>
-__global__ void outlet_pressure_kernel(const BcArgs<T> a) {
+template <class T, class E, bool AFTER_ODD>
+__global__ void outlet_pressure_kernel(const BcArgs<T, E> a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1;
     if (i > a.g.nx) return;
     const Grid& g = a.g;
@@ -164,7 +166,8 @@ __global__ void outlet_pressure_kernel(const BcArgs<T> a) {
     a.phi[g.s4(i, j, nz + 2)] = pz;
     a.phi[g.s4(i, j, nz + 3)] = pz;
     a.phi[g.s4(i, j, nz + 4)] = pz;
-    auto F = [&](int u, int v, int k, int e, int gg) -> T& { return a.pdf[a.b.at(u, v, k, e, gg)]; };
+    auto F = [&](int u, int v, int k, int e, int gg) { return a.P.get(u, v, k, e, gg); };
+    auto S = [&](int u, int v, int k, int e, int gg, T x) { a.P.set(u, v, k, e, gg, x); };
     T t1;
     if (!AFTER_ODD) {
         t1 = (F(i, j, nz, 0, 0) + F(i - 1, j, nz, 1, 0) + F(i + 1, j, nz, 2, 0) + F(i, j - 1, nz, 3, 0) +
@@ -198,21 +201,21 @@ __global__ void outlet_pressure_kernel(const BcArgs<T> a) {
                                     (F(i + 1, j, nz, 2, gg) + F(i + 1, j - 1, nz, 8, gg) + F(i + 1, j + 1, nz, 10, gg)));
             const T tny = T(0.5) * (F(i, j - 1, nz, 3, gg) + F(i - 1, j - 1, nz, 7, gg) + F(i + 1, j - 1, nz, 8, gg) -
                                     (F(i, j + 1, nz, 4, gg) + F(i + 1, j + 1, nz, 10, gg) + F(i - 1, j + 1, nz, 9, gg)));
-            F(i, j, nz + 1, 6, gg) = keep((F(i, j, nz - 1, 5, gg) - c3 * t), F(i, j, nz + 1, 6, gg), w);
-            F(i - 1, j, nz + 1, 13, gg) = keep((F(i + 1, j, nz - 1, 12, gg) - c6 * t - tnx), F(i - 1, j, nz + 1, 13, gg), w);
-            F(i + 1, j, nz + 1, 14, gg) = keep((F(i - 1, j, nz - 1, 11, gg) - c6 * t + tnx), F(i + 1, j, nz + 1, 14, gg), w);
-            F(i, j - 1, nz + 1, 17, gg) = keep((F(i, j + 1, nz - 1, 16, gg) - c6 * t - tny), F(i, j - 1, nz + 1, 17, gg), w);
-            F(i, j + 1, nz + 1, 18, gg) = keep((F(i, j - 1, nz - 1, 15, gg) - c6 * t + tny), F(i, j + 1, nz + 1, 18, gg), w);
+            S(i, j, nz + 1, 6, gg, keep((F(i, j, nz - 1, 5, gg) - c3 * t), F(i, j, nz + 1, 6, gg), w));
+            S(i - 1, j, nz + 1, 13, gg, keep((F(i + 1, j, nz - 1, 12, gg) - c6 * t - tnx), F(i - 1, j, nz + 1, 13, gg), w));
+            S(i + 1, j, nz + 1, 14, gg, keep((F(i - 1, j, nz - 1, 11, gg) - c6 * t + tnx), F(i + 1, j, nz + 1, 14, gg), w));
+            S(i, j - 1, nz + 1, 17, gg, keep((F(i, j + 1, nz - 1, 16, gg) - c6 * t - tny), F(i, j - 1, nz + 1, 17, gg), w));
+            S(i, j + 1, nz + 1, 18, gg, keep((F(i, j - 1, nz - 1, 15, gg) - c6 * t + tny), F(i, j + 1, nz + 1, 18, gg), w));
         } else {
             const T tnx = T(0.5) * (F(i, j, nz, 2, gg) + F(i, j, nz, 8, gg) + F(i, j, nz, 10, gg) -
                                     (F(i, j, nz, 1, gg) + F(i, j, nz, 7, gg) + F(i, j, nz, 9, gg)));
             const T tny = T(0.5) * (F(i, j, nz, 4, gg) + F(i, j, nz, 10, gg) + F(i, j, nz, 9, gg) -
                                     (F(i, j, nz, 3, gg) + F(i, j, nz, 7, gg) + F(i, j, nz, 8, gg)));
-            F(i, j, nz, 5, gg) = keep((F(i, j, nz, 6, gg) - c3 * t), F(i, j, nz, 5, gg), w);
-            F(i, j, nz, 11, gg) = keep((F(i, j, nz, 14, gg) - c6 * t + tnx), F(i, j, nz, 11, gg), w);
-            F(i, j, nz, 12, gg) = keep((F(i, j, nz, 13, gg) - c6 * t - tnx), F(i, j, nz, 12, gg), w);
-            F(i, j, nz, 15, gg) = keep((F(i, j, nz, 18, gg) - c6 * t + tny), F(i, j, nz, 15, gg), w);
-            F(i, j, nz, 16, gg) = keep((F(i, j, nz, 17, gg) - c6 * t - tny), F(i, j, nz, 16, gg), w);
+            S(i, j, nz, 5, gg, keep((F(i, j, nz, 6, gg) - c3 * t), F(i, j, nz, 5, gg), w));
+            S(i, j, nz, 11, gg, keep((F(i, j, nz, 14, gg) - c6 * t + tnx), F(i, j, nz, 11, gg), w));
+            S(i, j, nz, 12, gg, keep((F(i, j, nz, 13, gg) - c6 * t - tnx), F(i, j, nz, 12, gg), w));
+            S(i, j, nz, 15, gg, keep((F(i, j, nz, 18, gg) - c6 * t + tny), F(i, j, nz, 15, gg), w));
+            S(i, j, nz, 16, gg, keep((F(i, j, nz, 17, gg) - c6 * t - tny), F(i, j, nz, 16, gg), w));
         }
     }
 }
@@ -222,8 +225,8 @@ __global__ void outlet_pressure_kernel(const BcArgs<T> a) {
 __device__ __constant__ const int kZup[5] = {6, 14, 13, 18, 17}, kZdn[5] = {5, 11, 12, 15, 16};
 __device__ __constant__ const int kYup[5] = {4, 10, 9, 16, 18}, kYdn[5] = {3, 7, 8, 15, 17};
 
-template <class T, bool ODD>
-__global__ void periodic_z_kernel(const BcArgs<T> a) {
+template <class T, class E, bool ODD>
+__global__ void periodic_z_kernel(const BcArgs<T, E> a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1;
     if (i > a.g.nx) return;
     const Grid& g = a.g;
@@ -233,11 +236,11 @@ __global__ void periodic_z_kernel(const BcArgs<T> a) {
 #pragma unroll
         for (int s = 0; s < 5; ++s) {
             if (!ODD) {
-                a.pdf[a.b.at(i, j, nz + 1, kZup[s], gg)] = a.pdf[a.b.at(i, j, 1, kZup[s], gg)];
-                a.pdf[a.b.at(i, j, 0, kZdn[s], gg)] = a.pdf[a.b.at(i, j, nz, kZdn[s], gg)];
+                a.P.copy(i, j, nz + 1, kZup[s], gg, i, j, 1, kZup[s]);
+                a.P.copy(i, j, 0, kZdn[s], gg, i, j, nz, kZdn[s]);
             } else {
-                a.pdf[a.b.at(i, j, 1, kZup[s], gg)] = a.pdf[a.b.at(i, j, nz + 1, kZup[s], gg)];
-                a.pdf[a.b.at(i, j, nz, kZdn[s], gg)] = a.pdf[a.b.at(i, j, 0, kZdn[s], gg)];
+                a.P.copy(i, j, 1, kZup[s], gg, i, j, nz + 1, kZup[s]);
+                a.P.copy(i, j, nz, kZdn[s], gg, i, j, 0, kZdn[s]);
             }
         }
     for (int k = 1; k <= 4; ++k) {
@@ -246,8 +249,8 @@ __global__ void periodic_z_kernel(const BcArgs<T> a) {
     }
 }
 
-template <class T, bool ODD>
-__global__ void periodic_y_kernel(const BcArgs<T> a) {
+template <class T, class E, bool ODD>
+__global__ void periodic_y_kernel(const BcArgs<T, E> a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y + 1;
     if (i > a.g.nx) return;
     const Grid& g = a.g;
@@ -257,11 +260,11 @@ __global__ void periodic_y_kernel(const BcArgs<T> a) {
 #pragma unroll
         for (int s = 0; s < 5; ++s) {
             if (!ODD) {
-                a.pdf[a.b.at(i, ny + 1, k, kYup[s], gg)] = a.pdf[a.b.at(i, 1, k, kYup[s], gg)];
-                a.pdf[a.b.at(i, 0, k, kYdn[s], gg)] = a.pdf[a.b.at(i, ny, k, kYdn[s], gg)];
+                a.P.copy(i, ny + 1, k, kYup[s], gg, i, 1, k, kYup[s]);
+                a.P.copy(i, 0, k, kYdn[s], gg, i, ny, k, kYdn[s]);
             } else {
-                a.pdf[a.b.at(i, 1, k, kYup[s], gg)] = a.pdf[a.b.at(i, ny + 1, k, kYup[s], gg)];
-                a.pdf[a.b.at(i, ny, k, kYdn[s], gg)] = a.pdf[a.b.at(i, 0, k, kYdn[s], gg)];
+                a.P.copy(i, 1, k, kYup[s], gg, i, ny + 1, k, kYup[s]);
+                a.P.copy(i, ny, k, kYdn[s], gg, i, 0, k, kYdn[s]);
             }
         }
     for (int j = 1; j <= 4; ++j) {
@@ -270,8 +273,8 @@ __global__ void periodic_y_kernel(const BcArgs<T> a) {
     }
 }
 
-template <class T, bool ODD>
-__global__ void periodic_zy_kernel(const BcArgs<T> a) {
+template <class T, class E, bool ODD>
+__global__ void periodic_zy_kernel(const BcArgs<T, E> a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     if (i > a.g.nx) return;
     const Grid& g = a.g;
@@ -279,15 +282,15 @@ __global__ void periodic_zy_kernel(const BcArgs<T> a) {
 #pragma unroll
     for (int gg = 0; gg < 2; ++gg) {
         if (!ODD) {
-            a.pdf[a.b.at(i, ny + 1, nz + 1, 18, gg)] = a.pdf[a.b.at(i, 1, 1, 18, gg)];
-            a.pdf[a.b.at(i, ny + 1, 0, 16, gg)] = a.pdf[a.b.at(i, 1, nz, 16, gg)];
-            a.pdf[a.b.at(i, 0, nz + 1, 17, gg)] = a.pdf[a.b.at(i, ny, 1, 17, gg)];
-            a.pdf[a.b.at(i, 0, 0, 15, gg)] = a.pdf[a.b.at(i, ny, nz, 15, gg)];
+            a.P.copy(i, ny + 1, nz + 1, 18, gg, i, 1, 1, 18);
+            a.P.copy(i, ny + 1, 0, 16, gg, i, 1, nz, 16);
+            a.P.copy(i, 0, nz + 1, 17, gg, i, ny, 1, 17);
+            a.P.copy(i, 0, 0, 15, gg, i, ny, nz, 15);
         } else {
-            a.pdf[a.b.at(i, 1, 1, 18, gg)] = a.pdf[a.b.at(i, ny + 1, nz + 1, 18, gg)];
-            a.pdf[a.b.at(i, 1, nz, 16, gg)] = a.pdf[a.b.at(i, ny + 1, 0, 16, gg)];
-            a.pdf[a.b.at(i, ny, 1, 17, gg)] = a.pdf[a.b.at(i, 0, nz + 1, 17, gg)];
-            a.pdf[a.b.at(i, ny, nz, 15, gg)] = a.pdf[a.b.at(i, 0, 0, 15, gg)];
+            a.P.copy(i, 1, 1, 18, gg, i, ny + 1, nz + 1, 18);
+            a.P.copy(i, 1, nz, 16, gg, i, ny + 1, 0, 16);
+            a.P.copy(i, ny, 1, 17, gg, i, 0, nz + 1, 17);
+            a.P.copy(i, ny, nz, 15, gg, i, 0, 0, 15);
         }
     }
     for (int k = 1; k <= 4; ++k)
@@ -300,71 +303,74 @@ __global__ void periodic_zy_kernel(const BcArgs<T> a) {
 }
 
 // porous plate blocking one component at z = Zplate (:1744-1882); b = blocked component
-template <class T, bool AFTER_ODD>
-__global__ void porous_plate_kernel(const BcArgs<T> a) {
+template <class T, class E, bool AFTER_ODD>
+__global__ void porous_plate_kernel(const BcArgs<T, E> a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1;
     if (i > a.g.nx) return;
     const Grid& g = a.g;
     const int zp = a.Zplate;
     if (!(zp >= 1 && zp <= g.nz) || (a.plate_cmd != 1 && a.plate_cmd != 2)) return;
     const int b = a.plate_cmd == 1 ? 0 : 1, o = 1 - b;
-    auto F = [&](int u, int v, int k, int e, int gg) -> T& { return a.pdf[a.b.at(u, v, k, e, gg)]; };
+    auto F = [&](int u, int v, int k, int e, int gg, int us, int vs, int ks, int es) {
+        a.P.copy(u, v, k, e, gg, us, vs, ks, es);
+    };
     if (!AFTER_ODD) {
-        F(i, j, zp, 6, b) = F(i, j, zp - 1, 5, b);
-        F(i - 1, j, zp, 13, b) = F(i, j, zp - 1, 12, b);
-        F(i + 1, j, zp, 14, b) = F(i, j, zp - 1, 11, b);
-        F(i, j - 1, zp, 17, b) = F(i, j, zp - 1, 16, b);
-        F(i, j + 1, zp, 18, b) = F(i, j, zp - 1, 15, b);
-        F(i, j, zp, 5, b) = F(i, j, zp + 1, 6, b);
-        F(i + 1, j, zp, 12, b) = F(i, j, zp + 1, 13, b);
-        F(i - 1, j, zp, 11, b) = F(i, j, zp + 1, 14, b);
-        F(i, j + 1, zp, 16, b) = F(i, j, zp + 1, 17, b);
-        F(i, j - 1, zp, 15, b) = F(i, j, zp + 1, 18, b);
-        F(i, j, zp, 6, o) = F(i, j, zp + 1, 6, o);
-        F(i, j, zp, 13, o) = F(i, j, zp + 1, 13, o);
-        F(i, j, zp, 14, o) = F(i, j, zp + 1, 14, o);
-        F(i, j, zp, 17, o) = F(i, j, zp + 1, 17, o);
-        F(i, j, zp, 18, o) = F(i, j, zp + 1, 18, o);
-        F(i, j, zp, 5, o) = F(i, j, zp - 1, 5, o);
-        F(i, j, zp, 12, o) = F(i, j, zp - 1, 12, o);
-        F(i, j, zp, 11, o) = F(i, j, zp - 1, 11, o);
-        F(i, j, zp, 16, o) = F(i, j, zp - 1, 16, o);
-        F(i, j, zp, 15, o) = F(i, j, zp - 1, 15, o);
+        F(i, j, zp, 6, b, i, j, zp - 1, 5);
+        F(i - 1, j, zp, 13, b, i, j, zp - 1, 12);
+        F(i + 1, j, zp, 14, b, i, j, zp - 1, 11);
+        F(i, j - 1, zp, 17, b, i, j, zp - 1, 16);
+        F(i, j + 1, zp, 18, b, i, j, zp - 1, 15);
+        F(i, j, zp, 5, b, i, j, zp + 1, 6);
+        F(i + 1, j, zp, 12, b, i, j, zp + 1, 13);
+        F(i - 1, j, zp, 11, b, i, j, zp + 1, 14);
+        F(i, j + 1, zp, 16, b, i, j, zp + 1, 17);
+        F(i, j - 1, zp, 15, b, i, j, zp + 1, 18);
+        F(i, j, zp, 6, o, i, j, zp + 1, 6);
+        F(i, j, zp, 13, o, i, j, zp + 1, 13);
+        F(i, j, zp, 14, o, i, j, zp + 1, 14);
+        F(i, j, zp, 17, o, i, j, zp + 1, 17);
+        F(i, j, zp, 18, o, i, j, zp + 1, 18);
+        F(i, j, zp, 5, o, i, j, zp - 1, 5);
+        F(i, j, zp, 12, o, i, j, zp - 1, 12);
+        F(i, j, zp, 11, o, i, j, zp - 1, 11);
+        F(i, j, zp, 16, o, i, j, zp - 1, 16);
+        F(i, j, zp, 15, o, i, j, zp - 1, 15);
     } else {
-        F(i, j, zp - 1, 5, b) = F(i, j, zp, 6, b);
-        F(i, j, zp - 1, 12, b) = F(i - 1, j, zp, 13, b);
-        F(i, j, zp - 1, 11, b) = F(i + 1, j, zp, 14, b);
-        F(i, j, zp - 1, 16, b) = F(i, j - 1, zp, 17, b);
-        F(i, j, zp - 1, 15, b) = F(i, j + 1, zp, 18, b);
-        F(i, j, zp + 1, 6, b) = F(i, j, zp, 5, b);
-        F(i, j, zp + 1, 13, b) = F(i + 1, j, zp, 12, b);
-        F(i, j, zp + 1, 14, b) = F(i - 1, j, zp, 11, b);
-        F(i, j, zp + 1, 17, b) = F(i, j + 1, zp, 16, b);
-        F(i, j, zp + 1, 18, b) = F(i, j - 1, zp, 15, b);
-        F(i, j, zp - 1, 5, o) = F(i, j, zp, 5, o);
-        F(i, j, zp - 1, 12, o) = F(i, j, zp, 12, o);
-        F(i, j, zp - 1, 11, o) = F(i, j, zp, 11, o);
-        F(i, j, zp - 1, 16, o) = F(i, j, zp, 16, o);
-        F(i, j, zp - 1, 15, o) = F(i, j, zp, 15, o);
-        F(i, j, zp + 1, 6, o) = F(i, j, zp, 6, o);
-        F(i, j, zp + 1, 13, o) = F(i, j, zp, 13, o);
-        F(i, j, zp + 1, 14, o) = F(i, j, zp, 14, o);
-        F(i, j, zp + 1, 17, o) = F(i, j, zp, 17, o);
-        F(i, j, zp + 1, 18, o) = F(i, j, zp, 18, o);
+        F(i, j, zp - 1, 5, b, i, j, zp, 6);
+        F(i, j, zp - 1, 12, b, i - 1, j, zp, 13);
+        F(i, j, zp - 1, 11, b, i + 1, j, zp, 14);
+        F(i, j, zp - 1, 16, b, i, j - 1, zp, 17);
+        F(i, j, zp - 1, 15, b, i, j + 1, zp, 18);
+        F(i, j, zp + 1, 6, b, i, j, zp, 5);
+        F(i, j, zp + 1, 13, b, i + 1, j, zp, 12);
+        F(i, j, zp + 1, 14, b, i - 1, j, zp, 11);
+        F(i, j, zp + 1, 17, b, i, j + 1, zp, 16);
+        F(i, j, zp + 1, 18, b, i, j - 1, zp, 15);
+        F(i, j, zp - 1, 5, o, i, j, zp, 5);
+        F(i, j, zp - 1, 12, o, i, j, zp, 12);
+        F(i, j, zp - 1, 11, o, i, j, zp, 11);
+        F(i, j, zp - 1, 16, o, i, j, zp, 16);
+        F(i, j, zp - 1, 15, o, i, j, zp, 15);
+        F(i, j, zp + 1, 6, o, i, j, zp, 6);
+        F(i, j, zp + 1, 13, o, i, j, zp, 13);
+        F(i, j, zp + 1, 14, o, i, j, zp, 14);
+        F(i, j, zp + 1, 17, o, i, j, zp, 17);
+        F(i, j, zp + 1, 18, o, i, j, zp, 18);
     }
 }
 
 
-template <class T>
+template <class T, class E>
 int launch_boundaries(mflbm_context& c, bool odd) {
     const DeviceState& d = c.d;
     const Grid& g = d.g;
     const mflbm_params& p = c.params;
-    BcArgs<T> a;
+    BcArgs<T, E> a;
     a.g = g;
-    a.b = d.b;
+    a.P.p = (E*)d.pdf;
+    a.P.b = d.b;
     a.walls = d.walls;
-    a.pdf = (T*)d.pdf; a.phi = (T*)d.phi; a.W_in = (T*)d.W_in;
+    a.phi = (T*)d.phi; a.W_in = (T*)d.W_in;
     a.f_cv = (T*)d.f_cv; a.g_cv = (T*)d.g_cv; a.phi_cv = (T*)d.phi_cv;
     a.ph = make_phys<T>(p);
     a.plate_cmd = p.porous_plate_cmd; a.Zplate = p.Z_porous_plate;
@@ -373,8 +379,8 @@ int launch_boundaries(mflbm_context& c, bool odd) {
     int rc;
 #define MFLBM_BC(kernel, gridv, name)                                             \
     do {                                                                          \
-        if (odd) kernel<T, true><<<gridv, 128, 0, s>>>(a);                        \
-        else kernel<T, false><<<gridv, 128, 0, s>>>(a);                           \
+        if (odd) kernel<T, E, true><<<gridv, 128, 0, s>>>(a);                     \
+        else kernel<T, E, false><<<gridv, 128, 0, s>>>(a);                        \
         if ((rc = after_launch(name)) != MFLBM_OK) return rc;                     \
     } while (0)
     if (p.kper) MFLBM_BC(periodic_z_kernel, dim3(bx, g.ny), "periodic_z");

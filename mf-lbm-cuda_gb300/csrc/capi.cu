@@ -43,6 +43,10 @@ int check_params(const mflbm_params* p) {
     if (n1 >= (1ll << 31)) return fail(MFLBM_E_ARG, "lattice too large: (nx+2)(ny+2)(nz+2) must be below 2^31");
     if (p->inlet_BC < 0 || p->inlet_BC > 2 || p->outlet_BC < 0 || p->outlet_BC > 2) return fail(MFLBM_E_ARG, "inlet_BC/outlet_BC must be 0, 1 or 2");
     if (p->porous_plate_cmd < 0 || p->porous_plate_cmd > 2) return fail(MFLBM_E_ARG, "porous_plate_cmd must be 0, 1 or 2");
+    if (p->storage < MFLBM_STORE_NATIVE || p->storage > MFLBM_STORE_BF16)
+        return fail(MFLBM_E_ARG, "storage must be MFLBM_STORE_NATIVE, MFLBM_STORE_F16 or MFLBM_STORE_BF16");
+    if (p->storage != MFLBM_STORE_NATIVE && p->precision != MFLBM_FP32)
+        return fail(MFLBM_E_ARG, "16-bit population storage needs MFLBM_FP32 (the collision computes in FP32)");
     return MFLBM_OK;
 }
 
@@ -137,6 +141,7 @@ int build_lists(mflbm_context* c) {
     // solid nodes keep a zero normal record (only fluid nodes are rewritten per step)
     MFLBM_CUDA(cudaMemset(d.cnv4, 0, rec * g.n2()));
     c->pair_graph_odd_first = -1;  // kernels are launched with the list sizes
+    c->generation++;
     return MFLBM_OK;
 }
 
@@ -228,6 +233,51 @@ int capture_pair(mflbm_context* c, int first_ntime) {
 
 using namespace mflbm;
 
+struct mflbm_batch {
+    std::vector<mflbm_context*> ctx;
+    std::vector<unsigned long long> gen;  // generations at capture
+    cudaStream_t origin = nullptr;
+    cudaEvent_t fork = nullptr;
+    std::vector<cudaEvent_t> join;
+    cudaGraphExec_t exec = nullptr;
+};
+
+namespace mflbm {
+namespace {
+
+// One graph: fork from the batch stream to every context's stream, an odd and
+// an even step on each, join back.
+int capture_batch(mflbm_batch* b) {
+    if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
+    cudaGraph_t graph;
+    MFLBM_CUDA(cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeThreadLocal));
+    int rc = MFLBM_OK;
+    cudaError_t e = cudaEventRecord(b->fork, b->origin);
+    for (size_t i = 0; i < b->ctx.size() && rc == MFLBM_OK && e == cudaSuccess; ++i) {
+        mflbm_context* c = b->ctx[i];
+        e = cudaStreamWaitEvent(c->stream, b->fork, 0);
+        if (e != cudaSuccess) break;
+        if ((rc = one_step(c, 1)) != MFLBM_OK) break;
+        if ((rc = one_step(c, 2)) != MFLBM_OK) break;
+        if ((e = cudaEventRecord(b->join[i], c->stream)) != cudaSuccess) break;
+        e = cudaStreamWaitEvent(b->origin, b->join[i], 0);
+    }
+    const cudaError_t e2 = cudaStreamEndCapture(b->origin, &graph);
+    if (rc != MFLBM_OK) { if (e2 == cudaSuccess) cudaGraphDestroy(graph); return rc; }
+    if (e != cudaSuccess) { if (e2 == cudaSuccess) cudaGraphDestroy(graph); return fail(MFLBM_E_CUDA, std::string("batch capture: ") + cudaGetErrorString(e)); }
+    if (e2 != cudaSuccess) return fail(MFLBM_E_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e2));
+    e = cudaGraphInstantiate(&b->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail(MFLBM_E_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    for (size_t i = 0; i < b->ctx.size(); ++i) b->gen[i] = b->ctx[i]->generation;
+    return MFLBM_OK;
+}
+
+int check_block(int v) { return v == 0 || v == 64 || v == 128 || v == 256; }
+
+}  // namespace
+}  // namespace mflbm
+
 extern "C" {
 
 int mflbm_abi_version(void) { return MFLBM_ABI_VERSION; }
@@ -251,7 +301,7 @@ int mflbm_create(const mflbm_params* params, mflbm_context** out) {
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { delete c; return fail(MFLBM_E_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e)); }
     struct { void** p; size_t bytes; } allocs[] = {
-        {&d.pdf, T * d.b.S * 38}, {&d.cnv4, T * 4 * g.n2()},
+        {&d.pdf, (params->storage == MFLBM_STORE_NATIVE ? T : 2) * d.b.S * 38}, {&d.cnv4, T * 4 * g.n2()},
         {(void**)&d.type8, (size_t)g.n4()},
         {&d.phi, T * g.n4()}, {&d.cn_x, T * g.n2()}, {&d.cn_y, T * g.n2()},
         {&d.cn_z, T * g.n2()}, {&d.c_norm, T * g.n2()}, {&d.curv, T * g.n1()}, {&d.W_in, T * g.plane1()},
@@ -289,10 +339,12 @@ int mflbm_set_params(mflbm_context* c, const mflbm_params* p) {
     if (!c) return fail(MFLBM_E_ARG, "null context");
     int rc = check_params(p);
     if (rc != MFLBM_OK) return rc;
-    if (p->nx != c->params.nx || p->ny != c->params.ny || p->nz != c->params.nz || p->precision != c->params.precision)
-        return fail(MFLBM_E_ARG, "mflbm_set_params cannot change the lattice size or precision");
+    if (p->nx != c->params.nx || p->ny != c->params.ny || p->nz != c->params.nz || p->precision != c->params.precision ||
+        p->storage != c->params.storage)
+        return fail(MFLBM_E_ARG, "mflbm_set_params cannot change the lattice size, precision or storage");
     c->params = *p;
     if (c->pair_graph) { cudaGraphExecDestroy(c->pair_graph); c->pair_graph = nullptr; }
+    c->generation++;
     return MFLBM_OK;
 }
 
@@ -448,6 +500,7 @@ int mflbm_run(mflbm_context* c, int ntime_begin, int nsteps) {
         return MFLBM_OK;
     }
     int nt = ntime_begin, left = nsteps;
+    c->d.arrays_stale = true;  // graph replays do not pass through the host-side gradient launch
     // the graph holds an (odd, even) pair
     if ((nt & 1) == 0) {
         if ((rc = one_step(c, nt)) != MFLBM_OK) return rc;
@@ -556,6 +609,152 @@ int mflbm_monitor_profile(mflbm_context* c, double* slices, mflbm_monitor_ext* e
     if (rc != MFLBM_OK) return rc;
     if (!slices) return fail(MFLBM_E_ARG, "mflbm_monitor_profile: null slices");
     return monitor_profile(*c, slices, ext, track_phi != 0);
+}
+
+int mflbm_set_tuning(mflbm_context* c, const mflbm_tuning* t) {
+    if (!c || !t) return fail(MFLBM_E_ARG, "mflbm_set_tuning: null argument");
+    if (!check_block(t->collide_block) || !check_block(t->normals_block) || !check_block(t->curvature_block) ||
+        !check_block(t->extrapolate_block))
+        return fail(MFLBM_E_ARG, "mflbm_set_tuning: block sizes must be 64, 128, 256 or 0");
+    Tuning& tn = c->d.tune;
+    if (t->collide_block) tn.collide = t->collide_block;
+    if (t->normals_block) tn.normals = t->normals_block;
+    if (t->curvature_block) tn.curvature = t->curvature_block;
+    if (t->extrapolate_block) tn.extrapolate = t->extrapolate_block;
+    if (c->pair_graph) { cudaGraphExecDestroy(c->pair_graph); c->pair_graph = nullptr; }
+    c->generation++;
+    return MFLBM_OK;
+}
+
+int mflbm_autotune(mflbm_context* c, int reps, mflbm_tuning* out) {
+    int rc = require_ready(c);
+    if (rc != MFLBM_OK) return rc;
+    if (c->timing) return fail(MFLBM_E_STATE, "mflbm_autotune: switch kernel timing off first");
+    if (reps < 1) reps = 1;
+    DeviceState& d = c->d;
+    const Grid& g = d.g;
+    const size_t T = tsize(c), pl = (size_t)g.plane1();
+    const size_t pop_e = c->params.storage == MFLBM_STORE_NATIVE ? T : 2;
+    // everything a step writes: populations, phi, records, convective buffers
+    struct { void* p; size_t n; } st[] = {{d.pdf, pop_e * d.b.S * 38}, {d.phi, T * g.n4()},
+                                          {d.aux, T * 4 * std::max<ll>(1, d.n_fluid)}, {d.cnv4, T * 4 * g.n2()},
+                                          {d.f_cv, T * pl * 19}, {d.g_cv, T * pl * 19}, {d.phi_cv, T * pl}};
+    size_t total = 0;
+    for (auto& x : st) total += (x.n + 255) / 256 * 256;
+    char* save = nullptr;
+    MFLBM_CUDA(cudaMalloc(&save, total));
+    size_t off = 0;
+    for (auto& x : st) {
+        MFLBM_CUDA(cudaMemcpyAsync(save + off, x.p, x.n, cudaMemcpyDeviceToDevice, c->stream));
+        off += (x.n + 255) / 256 * 256;
+    }
+    const bool stale = d.arrays_stale;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    auto measure = [&](const Tuning& t, double* ms) -> int {
+        d.tune = t;
+        int r;
+        if ((r = one_step(c, 1)) != MFLBM_OK || (r = one_step(c, 2)) != MFLBM_OK) return r;   // warm-up pair
+        MFLBM_CUDA(cudaEventRecord(e0, c->stream));
+        for (int k = 0; k < reps; ++k)
+            if ((r = one_step(c, 1)) != MFLBM_OK || (r = one_step(c, 2)) != MFLBM_OK) return r;
+        MFLBM_CUDA(cudaEventRecord(e1, c->stream));
+        MFLBM_CUDA(cudaEventSynchronize(e1));
+        float f = 0;
+        MFLBM_CUDA(cudaEventElapsedTime(&f, e0, e1));
+        *ms = f / (2.0 * reps);
+        return MFLBM_OK;
+    };
+    Tuning best = d.tune;
+    double before = 0, best_ms = 0;
+    rc = measure(best, &before);
+    best_ms = before;
+    int* fields[4] = {&best.collide, &best.normals, &best.curvature, &best.extrapolate};
+    for (int f = 0; f < 4 && rc == MFLBM_OK; ++f)
+        for (int bs : {64, 128, 256}) {
+            Tuning t = best;
+            int* tf[4] = {&t.collide, &t.normals, &t.curvature, &t.extrapolate};
+            if (*tf[f] == bs) continue;
+            *tf[f] = bs;
+            double ms = 0;
+            if ((rc = measure(t, &ms)) != MFLBM_OK) break;
+            if (ms < best_ms) { best_ms = ms; best = t; }
+        }
+    (void)fields;
+    d.tune = best;
+    off = 0;
+    for (auto& x : st) {
+        cudaMemcpyAsync(x.p, save + off, x.n, cudaMemcpyDeviceToDevice, c->stream);
+        off += (x.n + 255) / 256 * 256;
+    }
+    cudaStreamSynchronize(c->stream);
+    cudaFree(save);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    d.arrays_stale = stale;
+    if (c->pair_graph) { cudaGraphExecDestroy(c->pair_graph); c->pair_graph = nullptr; }
+    c->generation++;
+    if (rc != MFLBM_OK) return rc;
+    if (out) {
+        out->collide_block = best.collide; out->normals_block = best.normals;
+        out->curvature_block = best.curvature; out->extrapolate_block = best.extrapolate;
+        out->step_ms_before = before; out->step_ms_after = best_ms;
+    }
+    return MFLBM_OK;
+}
+
+int mflbm_batch_create(mflbm_context* const* ctxs, int n, mflbm_batch** out) {
+    if (!ctxs || n < 1 || !out) return fail(MFLBM_E_ARG, "mflbm_batch_create: need n >= 1 contexts and an output pointer");
+    *out = nullptr;
+    for (int i = 0; i < n; ++i) {
+        int rc = require_ready(ctxs[i]);
+        if (rc != MFLBM_OK) return rc;
+        if (ctxs[i]->timing) return fail(MFLBM_E_STATE, "mflbm_batch_create: kernel timing is on for a context");
+        for (int j = 0; j < i; ++j)
+            if (ctxs[j] == ctxs[i]) return fail(MFLBM_E_ARG, "mflbm_batch_create: a context appears twice");
+    }
+    mflbm_batch* b = new mflbm_batch();
+    b->ctx.assign(ctxs, ctxs + n);
+    b->gen.assign(n, ~0ull);
+    b->join.assign(n, nullptr);
+    cudaError_t e = cudaStreamCreateWithFlags(&b->origin, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+    for (int i = 0; i < n && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&b->join[i], cudaEventDisableTiming);
+    if (e != cudaSuccess) { mflbm_batch_destroy(b); return fail(MFLBM_E_CUDA, std::string("mflbm_batch_create: ") + cudaGetErrorString(e)); }
+    *out = b;
+    return MFLBM_OK;
+}
+
+int mflbm_batch_run(mflbm_batch* b, int ntime_begin, int nsteps) {
+    if (!b) return fail(MFLBM_E_ARG, "null batch");
+    if ((ntime_begin & 1) == 0 || (nsteps & 1) != 0 || nsteps < 0)
+        return fail(MFLBM_E_ARG, "mflbm_batch_run: ntime_begin must be odd and nsteps even");
+    if (nsteps == 0) return MFLBM_OK;
+    bool stale = !b->exec;
+    for (size_t i = 0; i < b->ctx.size(); ++i) {
+        mflbm_context* c = b->ctx[i];
+        if (c->timing) return fail(MFLBM_E_STATE, "mflbm_batch_run: kernel timing is on for a context");
+        MFLBM_CUDA(cudaStreamSynchronize(c->stream));
+        stale = stale || b->gen[i] != c->generation;
+        c->d.arrays_stale = true;
+    }
+    int rc;
+    if (stale && (rc = capture_batch(b)) != MFLBM_OK) return rc;
+    for (int s = 0; s < nsteps; s += 2) MFLBM_CUDA(cudaGraphLaunch(b->exec, b->origin));
+    MFLBM_CUDA(cudaStreamSynchronize(b->origin));
+    return MFLBM_OK;
+}
+
+int mflbm_batch_destroy(mflbm_batch* b) {
+    if (!b) return MFLBM_OK;
+    if (b->origin) cudaStreamSynchronize(b->origin);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->fork) cudaEventDestroy(b->fork);
+    for (auto e : b->join) if (e) cudaEventDestroy(e);
+    if (b->origin) cudaStreamDestroy(b->origin);
+    delete b;
+    return MFLBM_OK;
 }
 
 int mflbm_node_counts(mflbm_context* c, long long counts[2]) {

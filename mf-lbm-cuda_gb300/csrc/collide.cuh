@@ -1,5 +1,7 @@
 // Collision + AA streaming of one time step (included by step_kernels.cuh).
 #pragma once
+#include <type_traits>
+
 #include "context.cuh"
 
 namespace mflbm {
@@ -167,10 +169,10 @@ __device__ __forceinline__ T collide(const Phys<T>& P, T (&g1)[19], T (&g2)[19],
 // parities of (x, y, z): each thread forms six deltas once and every access
 // is slot_base + element.
 // ===========================================================================
-template <class T> struct CollideArgs {
-    typedef typename Vec2<T>::type V2;
+template <class T, class E> struct CollideArgs {
+    typedef typename Pop2<E>::type P2;
     typedef typename Vec4<T>::type V4;
-    V2* slot[19];
+    P2* slot[19];
     const uint32_t* list;
     int n;
     int bx8, bxy8;  // element strides of one brick step in y and z
@@ -181,9 +183,10 @@ template <class T> struct CollideArgs {
     Phys<T> ph;
 };
 
-template <class T, bool ODD>
-__global__ void __launch_bounds__(128) collide_stream_kernel(const CollideArgs<T> a) {
-    typedef typename Vec2<T>::type V2;
+template <class T, class E, bool ODD>
+__global__ void __launch_bounds__(256) collide_stream_kernel(const CollideArgs<T, E> a) {
+    typedef typename Pop2<E>::type P2;
+    typedef PopCodec<T, E> Codec;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= a.n) return;
     int x, y, z;
@@ -201,30 +204,40 @@ __global__ void __launch_bounds__(128) collide_stream_kernel(const CollideArgs<T
     T g1[19], g2[19];
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
-        const V2 v = ODD ? a.slot[q][e0 + delta(opp(q))] : a.slot[opp(q)][e0];
-        g1[q] = v.x;
-        g2[q] = v.y;
+        const P2 v = ODD ? a.slot[q][e0 + delta(opp(q))] : a.slot[opp(q)][e0];
+        g1[q] = Codec::dec(v.x, lat_w<T>(q), lat_winv<T>(q));
+        g2[q] = Codec::dec(v.y, lat_w<T>(q), lat_winv<T>(q));
     }
     const typename Vec4<T>::type av = a.aux[t];
+    // dither seed of 16-bit storage: the node and its incoming populations
+    // (deterministic, and different at every step of an evolving flow)
+    uint32_t seed = 0;
+    if (!std::is_same<T, E>::value) seed = mix32((uint32_t)e0 ^ mix32(__float_as_uint((float)g1[1]) ^ __float_as_uint((float)g2[2])));
     const T phi = collide<T>(a.ph, g1, g2, av.x, av.y, av.z, av.w);
     a.phi[(x + 3) + a.NX4 * ((y + 3) + a.NY4 * (z + 3))] = phi;
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
-        V2 v;
-        v.x = g1[q];
-        v.y = g2[q];
+        P2 v;
+        if (std::is_same<T, E>::value) {
+            v.x = Codec::enc(g1[q], lat_w<T>(q), lat_winv<T>(q));
+            v.y = Codec::enc(g2[q], lat_w<T>(q), lat_winv<T>(q));
+        } else {
+            const uint32_t r = mix32(seed + (uint32_t)q);
+            v.x = Codec::enc_dither(g1[q], lat_w<T>(q), lat_winv<T>(q), r & 0xffffu);
+            v.y = Codec::enc_dither(g2[q], lat_w<T>(q), lat_winv<T>(q), r >> 16);
+        }
         if (ODD) a.slot[opp(q)][e0 + delta(q)] = v;
         else a.slot[q][e0] = v;
     }
 }
 
-template <class T>
+template <class T, class E>
 int launch_collide(mflbm_context& c, bool odd) {
-    typedef typename Vec2<T>::type V2;
+    typedef typename Pop2<E>::type P2;
     const DeviceState& d = c.d;
     const Grid& g = d.g;
-    CollideArgs<T> a;
-    V2* pdf = (V2*)d.pdf;
+    CollideArgs<T, E> a;
+    P2* pdf = (P2*)d.pdf;
     for (int q = 0; q < 19; ++q) a.slot[q] = pdf + d.b.S * q;
     a.list = d.fluid_list;
     a.n = (int)d.n_fluid;
@@ -236,8 +249,9 @@ int launch_collide(mflbm_context& c, bool odd) {
     a.aux = (const typename Vec4<T>::type*)d.aux;
     a.ph = make_phys<T>(c.params);
     if (a.n == 0) return MFLBM_OK;
-    if (odd) collide_stream_kernel<T, true><<<grid_for(a.n, 128), 128, 0, c.stream>>>(a);
-    else collide_stream_kernel<T, false><<<grid_for(a.n, 128), 128, 0, c.stream>>>(a);
+    const int bs = d.tune.collide;
+    if (odd) collide_stream_kernel<T, E, true><<<grid_for(a.n, bs), bs, 0, c.stream>>>(a);
+    else collide_stream_kernel<T, E, false><<<grid_for(a.n, bs), bs, 0, c.stream>>>(a);
     return after_launch("collide_stream");
 }
 

@@ -2,6 +2,8 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <cuda_bf16.h>
 #include <cstdint>
 #include <cstdio>
 #include <string>
@@ -85,6 +87,78 @@ struct __align__(32) Double4 { double x, y, z, w; };
 template <class T> struct Vec4;
 template <> struct Vec4<float> { typedef float4 type; };
 template <> struct Vec4<double> { typedef Double4 type; };
+
+// ---------------------------------------------------------------------------
+// Population storage (mflbm_params.storage).  E is the stored element type:
+// T itself, or __half / __nv_bfloat16 holding the shifted deviation
+// s = g / w_q - 1 of the population g from its lattice weight w_q (decoded in
+// T = float).  Pop2<E> is the pair (component 1, component 2) of one slot.
+// ---------------------------------------------------------------------------
+template <class E> struct Pop2;
+template <> struct Pop2<float> { typedef float2 type; };
+template <> struct Pop2<double> { typedef double2 type; };
+template <> struct Pop2<__half> { typedef __half2 type; };
+template <> struct Pop2<__nv_bfloat16> { typedef __nv_bfloat162 type; };
+
+// enc rounds to nearest.  enc_dither rounds stochastically: to the upper of
+// the two neighbouring 16-bit values with probability (x - lo) / (hi - lo),
+// using r16 / 65536 as the uniform variate, so the stored value is unbiased
+// (round-to-nearest would flush the small populations of a component near an
+// interface to exactly zero, a systematic mass loss).  Exactly representable
+// values, among them s = -1 of an absent component, are stored exactly.
+template <class T, class E> struct PopCodec {  // native storage: identity
+    __device__ __forceinline__ static T dec(E e, T, T) { return e; }
+    __device__ __forceinline__ static E enc(T v, T, T) { return v; }
+    __device__ __forceinline__ static E enc_dither(T v, T, T, uint32_t) { return v; }
+};
+template <> struct PopCodec<float, __half> {
+    __device__ __forceinline__ static float dec(__half e, float w, float) { return w + w * __half2float(e); }
+    __device__ __forceinline__ static __half enc(float v, float, float winv) { return __float2half_rn(v * winv - 1.0f); }
+    __device__ __forceinline__ static __half enc_dither(float v, float, float winv, uint32_t r16) {
+        const float x = v * winv - 1.0f;
+        const __half lo = __float2half_rd(x), hi = __float2half_ru(x);
+        const float flo = __half2float(lo), fhi = __half2float(hi);
+        if (!(fhi > flo)) return lo;
+        return (float)r16 * (1.0f / 65536.0f) * (fhi - flo) < x - flo ? hi : lo;
+    }
+};
+template <> struct PopCodec<float, __nv_bfloat16> {
+    __device__ __forceinline__ static float dec(__nv_bfloat16 e, float w, float) { return w + w * __bfloat162float(e); }
+    __device__ __forceinline__ static __nv_bfloat16 enc(float v, float, float winv) {
+        return __float2bfloat16_rn(v * winv - 1.0f);
+    }
+    __device__ __forceinline__ static __nv_bfloat16 enc_dither(float v, float, float winv, uint32_t r16) {
+        const float x = v * winv - 1.0f;
+        const __nv_bfloat16 lo = __float2bfloat16_rd(x), hi = __float2bfloat16_ru(x);
+        const float flo = __bfloat162float(lo), fhi = __bfloat162float(hi);
+        if (!(fhi > flo)) return lo;
+        return (float)r16 * (1.0f / 65536.0f) * (fhi - flo) < x - flo ? hi : lo;
+    }
+};
+// integer hash for the dither (a 32-bit avalanche mixer)
+__device__ __forceinline__ uint32_t mix32(uint32_t x) {
+    x ^= x >> 16; x *= 0x7feb352du; x ^= x >> 15; x *= 0x846ca68bu; x ^= x >> 16;
+    return x;
+}
+// lattice weight of direction q and its inverse, in T
+template <class T> __device__ __forceinline__ T lat_w(int q) { return q == 0 ? T(1) / T(3) : (q < 7 ? T(1) / T(18) : T(1) / T(36)); }
+template <class T> __device__ __forceinline__ T lat_winv(int q) { return q == 0 ? T(3) : (q < 7 ? T(18) : T(36)); }
+
+// Element-wise access to the populations in the brick layout.
+template <class T, class E> struct PopView {
+    E* p;
+    Bricks b;
+    __device__ __forceinline__ T get(int x, int y, int z, int q, int g) const {
+        return PopCodec<T, E>::dec(p[b.at(x, y, z, q, g)], lat_w<T>(q), lat_winv<T>(q));
+    }
+    __device__ __forceinline__ void set(int x, int y, int z, int q, int g, T v) const {
+        p[b.at(x, y, z, q, g)] = PopCodec<T, E>::enc(v, lat_w<T>(q), lat_winv<T>(q));
+    }
+    // copy of a stored population between slots of equal weight (no decode / encode)
+    __device__ __forceinline__ void copy(int x, int y, int z, int q, int g, int xs, int ys, int zs, int qs) const {
+        p[b.at(x, y, z, q, g)] = p[b.at(xs, ys, zs, qs, g)];
+    }
+};
 
 // Packed node coordinates of the node lists: x in bits 0-9, y 10-20, z 21-31,
 // each stored with an offset of +4 so that ghost nodes down to -3 fit.

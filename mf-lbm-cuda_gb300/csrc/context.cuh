@@ -6,7 +6,13 @@
 
 namespace mflbm {
 
+// Threads per block of the step kernels (chosen by mflbm_autotune).
+struct Tuning {
+    int collide = 128, normals = 128, curvature = 128, extrapolate = 128;
+};
+
 struct DeviceState {
+    Tuning tune;
     Grid g{};
     Bricks b{};
     int precision = MFLBM_FP32;
@@ -57,6 +63,7 @@ struct mflbm_context {
     cudaStream_t stream = nullptr;
     bool have_geometry = false;
     bool have_fields = false;
+    unsigned long long generation = 0;  // bumped whenever captured launches would change
     // CUDA graph of one odd + even step pair (built lazily by mflbm_run)
     cudaGraphExec_t pair_graph = nullptr;
     int pair_graph_odd_first = -1;

@@ -44,7 +44,7 @@ template <class T> __device__ __forceinline__ T wq_of(const ModelConsts<T>& c, i
 
 // phi on solid boundary nodes = weighted mean over fluid neighbours (:732-755)
 template <class T>
-__global__ void __launch_bounds__(128) extrapolate_phi_kernel(const GradArgs<T> a) {
+__global__ void __launch_bounds__(256) extrapolate_phi_kernel(const GradArgs<T> a) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= a.n_phi) return;
     const uint2 e = a.l_phi[t];
@@ -125,7 +125,7 @@ __device__ __forceinline__ T iso4_dz(const ModelConsts<T>& c, const T* F, int n,
 // unit interface normal and |grad phi| at the fluid nodes of [-1, n+2]^3
 // (:757-807) + wetting (:809-878)
 template <class T>
-__global__ void __launch_bounds__(128) normals_kernel(const GradArgs<T> a) {
+__global__ void __launch_bounds__(256) normals_kernel(const GradArgs<T> a) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= a.n_norm) return;
     int i, j, k;
@@ -151,7 +151,7 @@ __global__ void __launch_bounds__(128) normals_kernel(const GradArgs<T> a) {
 
 // interface normal on solid boundary nodes = weighted mean over fluid neighbours (:880-906)
 template <class T>
-__global__ void __launch_bounds__(128) extrapolate_normal_kernel(const GradArgs<T> a) {
+__global__ void __launch_bounds__(256) extrapolate_normal_kernel(const GradArgs<T> a) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= a.n_cn) return;
     const uint2 e = a.l_cn[t];
@@ -204,7 +204,7 @@ __device__ __forceinline__ T curvature_at(const ModelConsts<T>& c, const typenam
 
 // curvature at the fluid nodes and the collision's record (fluid-list order)
 template <class T>
-__global__ void __launch_bounds__(128) curvature_kernel(const GradArgs<T> a) {
+__global__ void __launch_bounds__(256) curvature_kernel(const GradArgs<T> a) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= a.n_fluid) return;
     int i, j, k;
@@ -295,22 +295,23 @@ GradArgs<T> grad_args(const mflbm_context& c) {
 template <class T>
 int launch_gradient(mflbm_context& c) {
     const GradArgs<T> a = grad_args<T>(c);
+    const Tuning& tn = c.d.tune;
     cudaStream_t s = c.stream;
     int rc;
     if (a.n_phi) {
-        extrapolate_phi_kernel<T><<<grid_for(a.n_phi, 128), 128, 0, s>>>(a);
+        extrapolate_phi_kernel<T><<<grid_for(a.n_phi, tn.extrapolate), tn.extrapolate, 0, s>>>(a);
         if ((rc = after_launch("extrapolate_phi")) != MFLBM_OK) return rc;
     }
     if (a.n_norm) {
-        normals_kernel<T><<<grid_for(a.n_norm, 128), 128, 0, s>>>(a);
+        normals_kernel<T><<<grid_for(a.n_norm, tn.normals), tn.normals, 0, s>>>(a);
         if ((rc = after_launch("normals")) != MFLBM_OK) return rc;
     }
     if (a.n_cn) {
-        extrapolate_normal_kernel<T><<<grid_for(a.n_cn, 128), 128, 0, s>>>(a);
+        extrapolate_normal_kernel<T><<<grid_for(a.n_cn, tn.extrapolate), tn.extrapolate, 0, s>>>(a);
         if ((rc = after_launch("extrapolate_normal")) != MFLBM_OK) return rc;
     }
     if (!a.n_fluid) return MFLBM_OK;
-    curvature_kernel<T><<<grid_for(a.n_fluid, 128), 128, 0, s>>>(a);
+    curvature_kernel<T><<<grid_for(a.n_fluid, tn.curvature), tn.curvature, 0, s>>>(a);
     return after_launch("curvature");
 }
 

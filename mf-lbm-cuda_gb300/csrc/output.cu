@@ -32,10 +32,10 @@ __device__ __forceinline__ void store_be(unsigned char* p, double v) {
 }
 __device__ __forceinline__ void store_be(unsigned char* p, int v) { store_be(p, __int_as_float(v)); }
 
-struct VtkArgs {
+template <class T, class E> struct VtkArgs {
     Grid g;
-    Bricks b;
-    const void *pdf, *phi, *cnx, *cny, *cnz, *cnorm, *curv;
+    PopView<T, E> P;
+    const void *phi, *cnx, *cny, *cnz, *cnorm, *curv;
     const int32_t* walls;
     double gamma, force_z;  // exact T values
     unsigned char* out;
@@ -45,8 +45,8 @@ struct VtkArgs {
 // populations (compute_macro_vars); vtk_type 3: phi, c_norm, cn_x/y/z;
 // vtk_type 2: phi (0 on solids) as float.  Five (or one) blocks of n0 values,
 // node (i, j, k) at (i-1) + nx ((j-1) + ny (k-1)).
-template <class T, int TYPE>
-__global__ void vtk_body_kernel(VtkArgs a) {
+template <class T, class E, int TYPE>
+__global__ void vtk_body_kernel(VtkArgs<T, E> a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y + 1, k = blockIdx.z + 1;
     const Grid& g = a.g;
@@ -72,10 +72,9 @@ __global__ void vtk_body_kernel(VtkArgs a) {
         store_be(o + 4 * blk, ((const T*)a.cnz)[n2]);
         return;
     }
-    const T* pdf = (const T*)a.pdf;
     T f[19];
 #pragma unroll
-    for (int q = 0; q < 19; ++q) f[q] = pdf[a.b.at(i, j, k, q, 0)] + pdf[a.b.at(i, j, k, q, 1)];
+    for (int q = 0; q < 19; ++q) f[q] = a.P.get(i, j, k, q, 0) + a.P.get(i, j, k, q, 1);
     const T keep = T(1 - wall);
     T s = f[0];
 #pragma unroll
@@ -127,7 +126,7 @@ int write_file(const char* path, const std::vector<std::pair<std::string, std::p
     return ok ? MFLBM_OK : fail(MFLBM_E_ARG, std::string("write failed: ") + path);
 }
 
-template <class T>
+template <class T, class E>
 int write_vtk_t(mflbm_context& c, int vtk_type, int precision_cmd, const char* path) {
     DeviceState& d = c.d;
     const Grid g = d.g;
@@ -136,17 +135,19 @@ int write_vtk_t(mflbm_context& c, int vtk_type, int precision_cmd, const char* p
     const size_t vsize = vtk_type == 2 ? 4 : sizeof(T);
     const size_t bytes = (size_t)nblk * n0 * vsize;
     unsigned char* dout = (unsigned char*)d.staging;  // the population staging buffer holds 38 n1 values
-    VtkArgs a;
-    a.g = g; a.b = d.b;
-    a.pdf = d.pdf; a.phi = d.phi; a.cnx = d.cn_x; a.cny = d.cn_y; a.cnz = d.cn_z; a.cnorm = d.c_norm; a.curv = d.curv;
+    VtkArgs<T, E> a;
+    a.g = g;
+    a.P.p = (E*)d.pdf;
+    a.P.b = d.b;
+    a.phi = d.phi; a.cnx = d.cn_x; a.cny = d.cn_y; a.cnz = d.cn_z; a.cnorm = d.c_norm; a.curv = d.curv;
     a.walls = d.walls;
     a.gamma = (double)T(c.params.lbm_gamma);
     a.force_z = (double)T(c.params.force_z);
     a.out = dout;
     const dim3 grid(grid_for(g.nx, 128), g.ny, g.nz);
-    if (vtk_type == 1) vtk_body_kernel<T, 1><<<grid, 128, 0, c.stream>>>(a);
-    else if (vtk_type == 2) vtk_body_kernel<T, 2><<<grid, 128, 0, c.stream>>>(a);
-    else vtk_body_kernel<T, 3><<<grid, 128, 0, c.stream>>>(a);
+    if (vtk_type == 1) vtk_body_kernel<T, E, 1><<<grid, 128, 0, c.stream>>>(a);
+    else if (vtk_type == 2) vtk_body_kernel<T, E, 2><<<grid, 128, 0, c.stream>>>(a);
+    else vtk_body_kernel<T, E, 3><<<grid, 128, 0, c.stream>>>(a);
     int rc = after_launch("vtk_body");
     if (rc != MFLBM_OK) return rc;
     std::vector<unsigned char> host(bytes);
@@ -199,8 +200,10 @@ int write_checkpoint_t(mflbm_context& c, int ntime, const char* path) {
 }  // namespace
 
 int write_vtk(mflbm_context& c, int vtk_type, int precision_cmd, const char* path) {
-    return c.params.precision == MFLBM_FP32 ? write_vtk_t<float>(c, vtk_type, precision_cmd, path)
-                                            : write_vtk_t<double>(c, vtk_type, precision_cmd, path);
+    if (c.params.precision == MFLBM_FP64) return write_vtk_t<double, double>(c, vtk_type, precision_cmd, path);
+    if (c.params.storage == MFLBM_STORE_F16) return write_vtk_t<float, __half>(c, vtk_type, precision_cmd, path);
+    if (c.params.storage == MFLBM_STORE_BF16) return write_vtk_t<float, __nv_bfloat16>(c, vtk_type, precision_cmd, path);
+    return write_vtk_t<float, float>(c, vtk_type, precision_cmd, path);
 }
 
 int write_walls_vtk(mflbm_context& c, const char* path) {

@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "context.cuh"
@@ -246,8 +247,8 @@ __global__ void init_phi(Grid g, int option, T z0, int open_z, T phi_inlet, T* p
     phi[g.s4(i, j, k)] = v;
 }
 
-template <class T>
-__global__ void init_pdf(Grid g, Bricks b, ModelConsts<T> c, const T* phi, T* pdf) {
+template <class T, class E>
+__global__ void init_pdf(Grid g, PopView<T, E> P, ModelConsts<T> c, const T* phi) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y, k = blockIdx.z;
     if (i > g.nx + 1) return;
@@ -255,27 +256,35 @@ __global__ void init_pdf(Grid g, Bricks b, ModelConsts<T> c, const T* phi, T* pd
     const T r[2] = {T(1) * (T(1.0) + ph) * T(0.5), T(1) * (T(1.0) - ph) * T(0.5)};
     const T usqrt = T(0) * T(0) + T(0) * T(0) + T(0) * T(0);
     for (int gg = 0; gg < 2; ++gg) {
-        pdf[b.at(i, j, k, 0, gg)] = r[gg] * c.w0 + r[gg] * c.w0 * (T(-1.5) * usqrt);
+        P.set(i, j, k, 0, gg, r[gg] * c.w0 + r[gg] * c.w0 * (T(-1.5) * usqrt));
         for (int q = 1; q < 19; ++q) {
             const T wq = q < 7 ? c.w1 : c.w2;
             const T cu = T(0);
-            pdf[b.at(i, j, k, q, gg)] = r[gg] * wq + r[gg] * wq * (T(3.0) * cu + T(4.5) * cu * cu - T(1.5) * usqrt);
+            P.set(i, j, k, q, gg, r[gg] * wq + r[gg] * wq * (T(3.0) * cu + T(4.5) * cu * cu - T(1.5) * usqrt));
         }
     }
 }
 
-template <class T>
-__global__ void init_convective(Grid g, Bricks b, const T* pdf, const T* phi, T* f_cv, T* g_cv, T* phi_cv) {
+template <class T, class E>
+__global__ void init_convective(Grid g, PopView<T, E> P, const T* phi, T* f_cv, T* g_cv, T* phi_cv) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
     if (i > g.nx + 1) return;
     for (int q = 0; q < 19; ++q) {
-        f_cv[g.cnv(i, j, q)] = pdf[b.at(i, j, g.nz, q, 0)];
-        g_cv[g.cnv(i, j, q)] = pdf[b.at(i, j, g.nz, q, 1)];
+        f_cv[g.cnv(i, j, q)] = P.get(i, j, g.nz, q, 0);
+        g_cv[g.cnv(i, j, q)] = P.get(i, j, g.nz, q, 1);
     }
     phi_cv[g.s1(i, j, 0)] = phi[g.s4(i, j, g.nz)];
 }
 
-template <class T>
+template <class T, class E>
+PopView<T, E> pop_view(const DeviceState& d) {
+    PopView<T, E> P;
+    P.p = (E*)d.pdf;
+    P.b = d.b;
+    return P;
+}
+
+template <class T, class E>
 int init_fields_t(mflbm_context& c, int option, double z0) {
     DeviceState& d = c.d;
     const Grid g = d.g;
@@ -285,13 +294,13 @@ int init_fields_t(mflbm_context& c, int option, double z0) {
     int rc;
     init_phi<T><<<dim3(grid_for(g.nx + 8, 128), g.ny + 8, g.nz + 8), 128, 0, s>>>(g, option, T(z0), open_z, T(p.phi_inlet), (T*)d.phi);
     if ((rc = after_launch("init_phi")) != MFLBM_OK) return rc;
-    init_pdf<T><<<dim3(grid_for(g.nx + 2, 128), g.ny + 2, g.nz + 2), 128, 0, s>>>(g, d.b, make_consts<T>(), (const T*)d.phi, (T*)d.pdf);
+    init_pdf<T, E><<<dim3(grid_for(g.nx + 2, 128), g.ny + 2, g.nz + 2), 128, 0, s>>>(g, pop_view<T, E>(d), make_consts<T>(), (const T*)d.phi);
     if ((rc = after_launch("init_pdf")) != MFLBM_OK) return rc;
     MFLBM_CUDA(cudaMemsetAsync(d.f_cv, 0, sizeof(T) * g.plane1() * 19, s));
     MFLBM_CUDA(cudaMemsetAsync(d.g_cv, 0, sizeof(T) * g.plane1() * 19, s));
     MFLBM_CUDA(cudaMemsetAsync(d.phi_cv, 0, sizeof(T) * g.plane1(), s));
     if (p.outlet_BC == 1) {
-        init_convective<T><<<dim3(grid_for(g.nx + 2, 128), g.ny + 2), 128, 0, s>>>(g, d.b, (const T*)d.pdf, (const T*)d.phi, (T*)d.f_cv, (T*)d.g_cv, (T*)d.phi_cv);
+        init_convective<T, E><<<dim3(grid_for(g.nx + 2, 128), g.ny + 2), 128, 0, s>>>(g, pop_view<T, E>(d), (const T*)d.phi, (T*)d.f_cv, (T*)d.g_cv, (T*)d.phi_cv);
         if ((rc = after_launch("init_convective")) != MFLBM_OK) return rc;
     }
     return MFLBM_OK;
@@ -304,8 +313,8 @@ int init_fields_t(mflbm_context& c, int option, double z0) {
 // ---------------------------------------------------------------------------
 constexpr int NRED = 9;  // vol1, vol2, mass1, mass2, flux1, flux2, vol1_full, vol2_full, umax2
 
-template <class T>
-__global__ void __launch_bounds__(256) monitor_partials(Grid g, Bricks b, const uint32_t* list, ll n, const T* pdf, const T* phi,
+template <class T, class E>
+__global__ void __launch_bounds__(256) monitor_partials(Grid g, PopView<T, E> P, const uint32_t* list, ll n, const T* phi,
                                                         const T* cnx, const T* cny, const T* cnz, const T* cnorm,
                                                         const T* curv, double gamma, double force_z, int k_lo, int k_hi,
                                                         double* partial) {
@@ -316,7 +325,7 @@ __global__ void __launch_bounds__(256) monitor_partials(Grid g, Bricks b, const 
         double f[19];
         const ll n1 = g.s1(i, j, k);
 #pragma unroll
-        for (int q = 0; q < 19; ++q) f[q] = (double)pdf[b.at(i, j, k, q, 0)] + (double)pdf[b.at(i, j, k, q, 1)];
+        for (int q = 0; q < 19; ++q) f[q] = (double)P.get(i, j, k, q, 0) + (double)P.get(i, j, k, q, 1);
         double rho = 0;
 #pragma unroll
         for (int q = 0; q < 19; ++q) rho += f[q];
@@ -353,10 +362,27 @@ __global__ void __launch_bounds__(256) monitor_partials(Grid g, Bricks b, const 
     }
 }
 
-template <class T>
-__global__ void __launch_bounds__(256) sum_all(ll n, const T* a, double* partial) {
+// sum of every stored population of both components; with 16-bit storage the
+// elements are decoded and the brick padding beyond [0, n+1] is skipped
+// (its zero bits do not encode a zero population)
+template <class T, class E>
+__global__ void __launch_bounds__(256) sum_all(Grid g, PopView<T, E> P, double* partial) {
+    const ll n = P.b.S * 38;
     double acc = 0;
-    for (ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (ll)gridDim.x * blockDim.x) acc += (double)a[t];
+    for (ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (ll)gridDim.x * blockDim.x) {
+        if (std::is_same<T, E>::value) {
+            acc += (double)PopCodec<T, E>::dec(P.p[t], T(0), T(0));
+        } else {
+            const ll slot = t >> 1;
+            const int q = (int)(slot / P.b.S);
+            const ll el = slot - (ll)q * P.b.S, brick = el >> 3;
+            const int x = (int)(2 * (brick % P.b.nbx)) + (int)(el & 1);
+            const int y = (int)(2 * ((brick / P.b.nbx) % P.b.nby)) + (int)((el >> 1) & 1);
+            const int z = (int)(2 * (brick / ((ll)P.b.nbx * P.b.nby))) + (int)((el >> 2) & 1);
+            if (x <= g.nx + 1 && y <= g.ny + 1 && z <= g.nz + 1)
+                acc += (double)PopCodec<T, E>::dec(P.p[t], lat_w<T>(q), lat_winv<T>(q));
+        }
+    }
     __shared__ double sh[8];
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
     if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
@@ -384,7 +410,7 @@ __global__ void fold_partials(int nblocks, int stride, const double* partial, do
     if (lane == 0) out[r] = x;
 }
 
-template <class T>
+template <class T, class E>
 int monitor_t(mflbm_context& c, int nex_in, int nex_out, mflbm_monitor* out) {
     DeviceState& d = c.d;
     const Grid g = d.g;
@@ -403,7 +429,7 @@ int monitor_t(mflbm_context& c, int nex_in, int nex_out, mflbm_monitor* out) {
     double* part2 = d.red + (ll)NRED * blocks;
     double* res = part2 + blocks;
     int rc;
-    monitor_partials<T><<<blocks, 256, 0, s>>>(g, d.b, d.fluid_list, d.n_fluid, (const T*)d.pdf, (const T*)d.phi,
+    monitor_partials<T, E><<<blocks, 256, 0, s>>>(g, pop_view<T, E>(d), d.fluid_list, d.n_fluid, (const T*)d.phi,
                                                (const T*)d.cn_x, (const T*)d.cn_y, (const T*)d.cn_z,
                                                (const T*)d.c_norm, (const T*)d.curv, (double)T(c.params.lbm_gamma),
                                                (double)T(c.params.force_z), nex_in + 1, g.nz - nex_out, part);
@@ -411,7 +437,7 @@ int monitor_t(mflbm_context& c, int nex_in, int nex_out, mflbm_monitor* out) {
     fold_partials<<<NRED, 32, 0, s>>>(blocks, NRED, part, res);
     if ((rc = after_launch("fold_partials")) != MFLBM_OK) return rc;
     // padding elements of the brick layout are zero and never written
-    sum_all<T><<<blocks, 256, 0, s>>>(d.b.S * 38, (const T*)d.pdf, part2);
+    sum_all<T, E><<<blocks, 256, 0, s>>>(g, pop_view<T, E>(d), part2);
     if ((rc = after_launch("sum_all")) != MFLBM_OK) return rc;
     fold_partials<<<1, 32, 0, s>>>(blocks, 1, part2, res + NRED);
     if ((rc = after_launch("fold_partials")) != MFLBM_OK) return rc;
@@ -473,7 +499,7 @@ int noalloc_scratch(double** out, int* sms) {
 }
 
 // The launches of monitor_t with the partials in g_monitor_scratch.
-template <class T>
+template <class T, class E>
 int monitor_noalloc_t(mflbm_context& c, int nex_in, int nex_out, mflbm_monitor* out) {
     DeviceState& d = c.d;
     const Grid g = d.g;
@@ -491,14 +517,14 @@ int monitor_noalloc_t(mflbm_context& c, int nex_in, int nex_out, mflbm_monitor* 
     double* part = scratch;
     double* part2 = scratch + (ll)NRED * blocks;
     double* res = part2 + blocks;
-    monitor_partials<T><<<blocks, 256, 0, s>>>(g, d.b, d.fluid_list, d.n_fluid, (const T*)d.pdf, (const T*)d.phi,
+    monitor_partials<T, E><<<blocks, 256, 0, s>>>(g, pop_view<T, E>(d), d.fluid_list, d.n_fluid, (const T*)d.phi,
                                                (const T*)d.cn_x, (const T*)d.cn_y, (const T*)d.cn_z,
                                                (const T*)d.c_norm, (const T*)d.curv, (double)T(c.params.lbm_gamma),
                                                (double)T(c.params.force_z), nex_in + 1, g.nz - nex_out, part);
     if ((rc = after_launch("monitor_partials")) != MFLBM_OK) return rc;
     fold_partials<<<NRED, 32, 0, s>>>(blocks, NRED, part, res);
     if ((rc = after_launch("fold_partials")) != MFLBM_OK) return rc;
-    sum_all<T><<<blocks, 256, 0, s>>>(d.b.S * 38, (const T*)d.pdf, part2);
+    sum_all<T, E><<<blocks, 256, 0, s>>>(g, pop_view<T, E>(d), part2);
     if ((rc = after_launch("sum_all")) != MFLBM_OK) return rc;
     fold_partials<<<1, 32, 0, s>>>(blocks, 1, part2, res + NRED);
     if ((rc = after_launch("fold_partials")) != MFLBM_OK) return rc;
@@ -525,9 +551,9 @@ int monitor_noalloc_t(mflbm_context& c, int nex_in, int nex_out, mflbm_monitor* 
 // ---------------------------------------------------------------------------
 constexpr int kProfSums = 7, kProfExt = 9;  // ext: umax2 usq1 usq2 pre_w pre_nw n_w n_nw breakthrough dphi_max
 
-template <class T>
-__global__ void __launch_bounds__(256) monitor_profile_kernel(Grid g, Bricks b, const uint32_t* list, const int* zoff,
-                                                              const T* pdf, const T* phi, T* phi_prev,
+template <class T, class E>
+__global__ void __launch_bounds__(256) monitor_profile_kernel(Grid g, PopView<T, E> P, const uint32_t* list, const int* zoff,
+                                                              const T* phi, T* phi_prev,
                                                               const typename Vec4<T>::type* aux, double force_z,
                                                               int track, double* out) {
     const int kp = blockIdx.x;
@@ -540,7 +566,7 @@ __global__ void __launch_bounds__(256) monitor_profile_kernel(Grid g, Bricks b, 
         unpack_xyz(list[t], i, j, k);
         double f[19];
 #pragma unroll
-        for (int q = 0; q < 19; ++q) f[q] = (double)pdf[b.at(i, j, k, q, 0)] + (double)pdf[b.at(i, j, k, q, 1)];
+        for (int q = 0; q < 19; ++q) f[q] = (double)P.get(i, j, k, q, 0) + (double)P.get(i, j, k, q, 1);
         double rho = 0;
 #pragma unroll
         for (int q = 0; q < 19; ++q) rho += f[q];
@@ -590,7 +616,7 @@ __global__ void __launch_bounds__(256) monitor_profile_kernel(Grid g, Bricks b, 
     }
 }
 
-template <class T>
+template <class T, class E>
 int monitor_profile_t(mflbm_context& c, double* slices, mflbm_monitor_ext* ext, bool track) {
     DeviceState& d = c.d;
     const Grid g = d.g;
@@ -600,7 +626,7 @@ int monitor_profile_t(mflbm_context& c, double* slices, mflbm_monitor_ext* ext, 
         MFLBM_CUDA(cudaMalloc(&d.phi_prev, sizeof(T) * g.n4()));
         MFLBM_CUDA(cudaMemsetAsync(d.phi_prev, 0, sizeof(T) * g.n4(), c.stream));
     }
-    monitor_profile_kernel<T><<<nb, 256, 0, c.stream>>>(g, d.b, d.fluid_list, d.zpair_off, (const T*)d.pdf,
+    monitor_profile_kernel<T, E><<<nb, 256, 0, c.stream>>>(g, pop_view<T, E>(d), d.fluid_list, d.zpair_off,
                                                         (const T*)d.phi, (T*)d.phi_prev,
                                                         (const typename Vec4<T>::type*)d.aux,
                                                         (double)T(c.params.force_z), track ? 1 : 0, d.prof);
@@ -628,63 +654,63 @@ int monitor_profile_t(mflbm_context& c, double* slices, mflbm_monitor_ext* ext, 
 }
 
 // Reference layout (f1) <-> brick layout, one thread per (node, direction).
-template <class T>
-__global__ void f1_to_bricks(Grid g, Bricks b, const T* f1, T* pdf) {
+template <class T, class E>
+__global__ void f1_to_bricks(Grid g, PopView<T, E> P, const T* f1) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, kq = blockIdx.z;
     const int k = kq % (g.nz + 2), q = kq / (g.nz + 2);
     if (i > g.nx + 1) return;
     const ll s = g.s1(i, j, k);
-    pdf[b.at(i, j, k, q, 0)] = f1[s + g.n1() * q];
-    pdf[b.at(i, j, k, q, 1)] = f1[s + g.n1() * (q + 19)];
+    P.set(i, j, k, q, 0, f1[s + g.n1() * q]);
+    P.set(i, j, k, q, 1, f1[s + g.n1() * (q + 19)]);
 }
-template <class T>
-__global__ void bricks_to_f1(Grid g, Bricks b, const T* pdf, T* f1) {
+template <class T, class E>
+__global__ void bricks_to_f1(Grid g, PopView<T, E> P, T* f1) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, kq = blockIdx.z;
     const int k = kq % (g.nz + 2), q = kq / (g.nz + 2);
     if (i > g.nx + 1) return;
     const ll s = g.s1(i, j, k);
-    f1[s + g.n1() * q] = pdf[b.at(i, j, k, q, 0)];
-    f1[s + g.n1() * (q + 19)] = pdf[b.at(i, j, k, q, 1)];
+    f1[s + g.n1() * q] = P.get(i, j, k, q, 0);
+    f1[s + g.n1() * (q + 19)] = P.get(i, j, k, q, 1);
 }
 
-template <class T>
+template <class T, class E>
 int convert_t(mflbm_context& c, bool to_bricks) {
     DeviceState& d = c.d;
     const Grid g = d.g;
     const dim3 grid(grid_for(g.nx + 2, 128), g.ny + 2, (g.nz + 2) * 19);
-    if (to_bricks) f1_to_bricks<T><<<grid, 128, 0, c.stream>>>(g, d.b, (const T*)d.staging, (T*)d.pdf);
-    else bricks_to_f1<T><<<grid, 128, 0, c.stream>>>(g, d.b, (const T*)d.pdf, (T*)d.staging);
+    if (to_bricks) f1_to_bricks<T, E><<<grid, 128, 0, c.stream>>>(g, pop_view<T, E>(d), (const T*)d.staging);
+    else bricks_to_f1<T, E><<<grid, 128, 0, c.stream>>>(g, pop_view<T, E>(d), (T*)d.staging);
     return after_launch(to_bricks ? "f1_to_bricks" : "bricks_to_f1");
 }
 
 }  // namespace
 
-int convert_populations(mflbm_context& c, bool to_bricks) {
-    return c.params.precision == MFLBM_FP32 ? convert_t<float>(c, to_bricks) : convert_t<double>(c, to_bricks);
-}
+// the population storage selects the element type E of the kernels that touch them
+#define MFLBM_POP(fn, ...)                                                             \
+    (c.params.precision == MFLBM_FP64         ? fn<double, double>(__VA_ARGS__)         \
+     : c.params.storage == MFLBM_STORE_F16    ? fn<float, __half>(__VA_ARGS__)          \
+     : c.params.storage == MFLBM_STORE_BF16   ? fn<float, __nv_bfloat16>(__VA_ARGS__)   \
+                                              : fn<float, float>(__VA_ARGS__))
+
+int convert_populations(mflbm_context& c, bool to_bricks) { return MFLBM_POP(convert_t, c, to_bricks); }
 
 int preprocess_geometry(mflbm_context& c, const int32_t* walls_global, int iper) {
     return c.params.precision == MFLBM_FP32 ? preprocess_geometry_t<float>(c, walls_global, iper)
                                             : preprocess_geometry_t<double>(c, walls_global, iper);
 }
 
-int init_fields(mflbm_context& c, int option, double z0) {
-    return c.params.precision == MFLBM_FP32 ? init_fields_t<float>(c, option, z0) : init_fields_t<double>(c, option, z0);
-}
+int init_fields(mflbm_context& c, int option, double z0) { return MFLBM_POP(init_fields_t, c, option, z0); }
 
 int monitor(mflbm_context& c, int nex_in, int nex_out, mflbm_monitor* out) {
-    return c.params.precision == MFLBM_FP32 ? monitor_t<float>(c, nex_in, nex_out, out)
-                                            : monitor_t<double>(c, nex_in, nex_out, out);
+    return MFLBM_POP(monitor_t, c, nex_in, nex_out, out);
 }
 
 int monitor_profile(mflbm_context& c, double* slices, mflbm_monitor_ext* ext, bool track_phi) {
-    return c.params.precision == MFLBM_FP32 ? monitor_profile_t<float>(c, slices, ext, track_phi)
-                                            : monitor_profile_t<double>(c, slices, ext, track_phi);
+    return MFLBM_POP(monitor_profile_t, c, slices, ext, track_phi);
 }
 
 int monitor_noalloc(mflbm_context& c, int nex_in, int nex_out, mflbm_monitor* out) {
-    return c.params.precision == MFLBM_FP32 ? monitor_noalloc_t<float>(c, nex_in, nex_out, out)
-                                            : monitor_noalloc_t<double>(c, nex_in, nex_out, out);
+    return MFLBM_POP(monitor_noalloc_t, c, nex_in, nex_out, out);
 }
 
 }  // namespace mflbm

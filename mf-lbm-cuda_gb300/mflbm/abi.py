@@ -8,6 +8,7 @@ import numpy as np
 MFLBM_OK = 0
 MFLBM_FP32, MFLBM_FP64 = 1, 2
 MFLBM_FAST, MFLBM_STRICT = 0, 1
+MFLBM_STORE_NATIVE, MFLBM_STORE_F16, MFLBM_STORE_BF16 = 0, 1, 2
 
 
 class Params(C.Structure):
@@ -24,6 +25,7 @@ class Params(C.Structure):
         ("sa_inject", C.c_double), ("uin_avg", C.c_double),
         ("relaxation", C.c_double), ("cos_theta", C.c_double),
         ("rho_in", C.c_double), ("rho_out", C.c_double),
+        ("storage", C.c_int), ("reserved", C.c_int),
     ]
 
 
@@ -71,6 +73,14 @@ class MonitorExt(C.Structure):
     _fields_ = [("umax2", C.c_double), ("usq1", C.c_double), ("usq2", C.c_double), ("pre_w", C.c_double),
                 ("pre_nw", C.c_double), ("n_w", C.c_longlong), ("n_nw", C.c_longlong),
                 ("breakthrough", C.c_longlong), ("dphi_max", C.c_double)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class Tuning(C.Structure):
+    _fields_ = [("collide_block", C.c_int), ("normals_block", C.c_int), ("curvature_block", C.c_int),
+                ("extrapolate_block", C.c_int), ("step_ms_before", C.c_double), ("step_ms_after", C.c_double)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}

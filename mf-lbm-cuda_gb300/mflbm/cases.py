@@ -213,5 +213,23 @@ def small_case(kind: str, n=(20, 20, 28), seed=7):
     return Case(f"{kind}_{nx}x{ny}x{nz}", base, geo)
 
 
+def permeability_sample(n, porosity, seed, body_force=1e-6, radius=(3.0, 6.0)):
+    """Single-phase permeability sample (the multiphase path with phi = 1
+    everywhere): an n^3 grain pack of the given porosity, periodic in y and z,
+    walled in x, tau = 1 (nu = 1/6), driven by the body force along z.  The
+    reference has no single-phase kernel; phi = 1 (initial interface beyond
+    the domain) makes the second component vanish, so neither recolouring nor
+    surface force acts."""
+    keys = {"nxGlobal": n, "nyGlobal": n, "nzGlobal": n,
+            "jper": 1, "kper": 1, "domain_wall_status_y_min": 0, "domain_wall_status_y_max": 0,
+            "domain_wall_status_z_min": 0, "domain_wall_status_z_max": 0,
+            "initial_fluid_distribution_option": 1, "initial_interface_position": str(float(n + 10)),
+            "fluid1_viscosity": "0.16666666666666666", "fluid2_viscosity": "0.16666666666666666",
+            "body_force_0": repr(float(body_force)), "inlet_BC": 0, "outlet_BC": 0,
+            "n_exclude_inlet": 0, "n_exclude_outlet": 0}
+    geo = Geometry(radius=radius, porosity=porosity, overlap=True, buffer_layers=0, seed=seed)
+    return Case(f"permeability_{n}x{n}x{n}_s{seed}", keys, geo)
+
+
 SMALL_KINDS = ["velocity_convective", "pressure_pressure", "velocity_pressure",
                "periodic_drop", "closed_contact", "plate_drainage"]

@@ -42,6 +42,11 @@ SIGNATURES = {
     "mflbm_monitor_reduce": (I, [VP, I, I, VP]),
     "mflbm_monitor_reduce_noalloc": (I, [VP, I, I, VP]),
     "mflbm_monitor_profile": (I, [VP, VP, VP, I]),
+    "mflbm_autotune": (I, [VP, I, VP]),
+    "mflbm_set_tuning": (I, [VP, VP]),
+    "mflbm_batch_create": (I, [C.POINTER(VP), I, C.POINTER(VP)]),
+    "mflbm_batch_run": (I, [VP, I, I]),
+    "mflbm_batch_destroy": (I, [VP]),
     "mflbm_write_vtk": (I, [VP, I, I, C.c_char_p]),
     "mflbm_write_walls_vtk": (I, [VP, C.c_char_p]),
     "mflbm_write_checkpoint": (I, [VP, I, C.c_char_p]),
@@ -200,6 +205,16 @@ class Context:
               "mflbm_monitor_profile")
         return {n: sl[m] for m, n in enumerate(abi.PROFILE_ROWS)}, e.as_dict()
 
+    def autotune(self, reps=5):
+        """mflbm_autotune: block sizes of the step kernels; the state is unchanged."""
+        t = abi.Tuning()
+        check(self.lib.mflbm_autotune(self.h, int(reps), C.byref(t)), "mflbm_autotune")
+        return t.as_dict()
+
+    def set_tuning(self, collide=0, normals=0, curvature=0, extrapolate=0):
+        t = abi.Tuning(collide, normals, curvature, extrapolate, 0.0, 0.0)
+        check(self.lib.mflbm_set_tuning(self.h, C.byref(t)), "mflbm_set_tuning")
+
     def write_vtk(self, vtk_type, path, precision_cmd=0):
         check(self.lib.mflbm_write_vtk(self.h, int(vtk_type), int(precision_cmd), str(path).encode()), "mflbm_write_vtk")
 
@@ -234,12 +249,41 @@ class Context:
         return tc.value, tg.value, nc.value
 
 
-def setup_case(case, precision=abi.MFLBM_FP32, fp_mode=abi.MFLBM_FAST, geometry=None, want_host_geometry=False):
+class Batch:
+    """mflbm_batch: contexts advanced together by one CUDA graph launch per step pair."""
+
+    def __init__(self, contexts):
+        self.lib = load()
+        self.contexts = list(contexts)           # kept alive while the batch exists
+        arr = (VP * len(self.contexts))(*[c.h for c in self.contexts])
+        h = VP()
+        check(self.lib.mflbm_batch_create(arr, len(self.contexts), C.byref(h)), "mflbm_batch_create")
+        self.h = h
+
+    def run(self, ntime_begin, nsteps):
+        check(self.lib.mflbm_batch_run(self.h, int(ntime_begin), int(nsteps)), "mflbm_batch_run")
+
+    def close(self):
+        if self.h:
+            self.lib.mflbm_batch_destroy(self.h)
+            self.h = VP()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def setup_case(case, precision=abi.MFLBM_FP32, fp_mode=abi.MFLBM_FAST, geometry=None, want_host_geometry=False,
+               storage=abi.MFLBM_STORE_NATIVE):
     """Build a ready-to-step Context for `case`: walls, device geometry
     preprocessing, start-up fields and colour gradient (the reference's
-    start-up, src/main.cpp:71-99).  Returns (context, info)."""
+    start-up, src/main.cpp:71-99).  `storage` selects the population storage
+    (abi.MFLBM_STORE_*).  Returns (context, info)."""
     control = case.control(precision)
     params, derived = params_from_control(control, precision, fp_mode)
+    params.storage = storage
     geo = case.geometry_bytes() if geometry is None else geometry
     wg = set_walls(control, geo)
     W_in = inlet_profile(control, precision)

@@ -187,3 +187,17 @@ def test_drainage_48x48x64_fp64_2000_steps(mflbm_lib):
         ctx.close()
     assert 0.0 < mo["saturation"] < 1.0
     assert np.isfinite(ms["w"]).all()
+
+
+def test_graph_replays_refresh_exported_arrays(mflbm_lib):
+    """Steps that only replay the captured step-pair graph still refresh the
+    reference-layout gradient arrays a later download exports."""
+    case, ctx, info, o = _setup("velocity_convective", abi.MFLBM_FP32, abi.MFLBM_STRICT)
+    ctx.run(1, 4)        # captures the pair graph
+    ctx.download()       # exports the arrays
+    ctx.run(5, 4)        # graph replays only
+    o.run(8)
+    d = ctx.download()
+    for n in ("cn_x", "c_norm", "curv", "pdf", "phi"):
+        assert d[n].tobytes() == o.a[n].tobytes(), n
+    ctx.close()
