@@ -184,7 +184,7 @@ def storage_variants(case, geo, steps, nt):
     MLUPS, collision time and its algorithmic bandwidth (152 + 4 B per fluid
     node for the populations and phi, + 1 B per node)."""
     import torch
-    from mflbm import lib
+    from mflbm import abi, lib
     out = {}
     nx, ny, nz = case.shape
     for name, st in (("f16", abi.MFLBM_STORE_F16), ("bf16", abi.MFLBM_STORE_BF16)):
@@ -210,8 +210,7 @@ def batch_vs_sequential(steps):
     """16 single-phase samples of 48^3 .. 96^3 (porosity 0.3 .. 0.7): one
     graph launch per step pair for all of them (mflbm_batch) against each
     context's own graph replays, one after the other."""
-    import torch
-    from mflbm import lib, permeability
+    from mflbm import abi, lib, permeability
     samples = permeability.make_samples(16, 48, 96)
     ctxs = [lib.setup_case(s, abi.MFLBM_FP32, abi.MFLBM_FAST)[0] for s in samples]
     nodes = sum(int(np.prod(s.shape)) for s in samples)
