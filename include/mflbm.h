@@ -208,6 +208,15 @@ int mflbm_upload_geometry(mflbm_context* ctx, const int32_t* walls,
 int mflbm_init_fields(mflbm_context* ctx, int initial_fluid_distribution_option,
                       double interface_z0, const void* W_in);
 
+/* Warm-start entry: the equilibrium fill of initialization_new_multi_pdf
+ * (src/Init_multiphase.cpp:389-496) with given macroscopic fields over the
+ * phi already set, f_q = r w_q (1 + 3 c.u + 4.5 (c.u)^2 - 1.5 u.u), r = rho
+ * (1 +- phi) / 2.  rho, u, v, w: host arrays of (nx+2)(ny+2)(nz+2) values in
+ * the context's precision, index i + (nx+2)(j + (ny+2) k), each may be NULL
+ * (rho = 1, velocity 0).  Call after mflbm_init_fields / mflbm_upload_fields. */
+int mflbm_init_flow(mflbm_context* ctx, const void* rho, const void* u,
+                    const void* v, const void* w);
+
 /* Reference: MemAllocate_multi_GPU(1) (src/Init_multiphase_GPU.cu:73-104):
  * upload a full host state.  Any pointer except pdf and phi may be NULL
  * (cn/c_norm/curv are then recomputed from phi; convective buffers are taken
@@ -343,6 +352,42 @@ int mflbm_batch_create(mflbm_context* const* ctxs, int n, mflbm_batch** out);
  * batch; ntime_begin must be odd and nsteps even.  Blocks until done. */
 int mflbm_batch_run(mflbm_batch* b, int ntime_begin, int nsteps);
 int mflbm_batch_destroy(mflbm_batch* b);
+
+/* ---- learned warm start: 3-D U-Net --------------------------------------
+ * (no counterpart in the reference)  4 levels of 16/32/64/128 channels, two
+ * 3x3x3 convolutions + ReLU per level, 2x2x2 average pooling, nearest
+ * up-sampling with concatenated skips, a final 3x3x3 convolution to 4
+ * outputs.  BF16 weights and activations, FP32 accumulation on the tensor
+ * cores, FP32 master weights, Adam.  Inputs per voxel: 2 channels (solid
+ * mask, signed distance); outputs: 4 (u, v, w, p).  Host arrays are FP32,
+ * D x H x W x channels with the channel fastest; D, H, W multiples of 8. */
+typedef struct mflbm_unet mflbm_unet;
+int mflbm_unet_create(int D, int H, int W, unsigned long long seed, mflbm_unet** out);
+int mflbm_unet_destroy(mflbm_unet* net);
+int mflbm_unet_param_count(mflbm_unet* net, long long* count);
+/* x: D*H*W*2 inputs; y: D*H*W*4 outputs. */
+int mflbm_unet_forward(mflbm_unet* net, const float* x, float* y);
+/* One Adam step on the masked MSE of the 4 outputs against target
+ * (D*H*W*4) over the voxels where mask (D*H*W) is non-zero; loss: the MSE
+ * before the step (may be NULL). */
+int mflbm_unet_train_step(mflbm_unet* net, const float* x, const float* target,
+                          const float* mask, float lr, float* loss);
+/* The loss and its gradient with respect to every weight and bias (same
+ * layout as mflbm_unet_get_params), without an update. */
+int mflbm_unet_gradients(mflbm_unet* net, const float* x, const float* target,
+                         const float* mask, float* grads, float* loss);
+/* Weights and biases as one FP32 vector of mflbm_unet_param_count values
+ * (layer by layer: weights [cout][27][cin], then biases). */
+int mflbm_unet_get_params(mflbm_unet* net, float* params);
+int mflbm_unet_set_params(mflbm_unet* net, const float* params);
+/* One convolution layer and its gradients, for checks against a CPU
+ * restatement: x D*H*W*cin, w cout*27*cin (tap = 9 (dz+1) + 3 (dy+1) + dx+1),
+ * b cout, gy D*H*W*cout or NULL; cin, cout multiples of 16.  Inputs are
+ * rounded to BF16 on the device; y is the FP32 output before rounding, gx
+ * the BF16 data gradient widened to FP32, gw and gb FP32. */
+int mflbm_unet_conv_check(int D, int H, int W, int cin, int cout, const float* x,
+                          const float* w, const float* b, int relu, const float* gy,
+                          float* y, float* gx, float* gw, float* gb);
 
 /* ---- introspection ---------------------------------------------------- */
 /* Counts of lattice nodes: [0] fluid nodes in [1,n]^3, [1] all nodes n^3. */

@@ -6,6 +6,7 @@ Translation units compile in parallel:
   setup.cu        geometry preprocessing, start-up fields, FP64 reductions (-fmad=false)
   output.cu       VTK and checkpoint files in the reference's formats (-fmad=false)
   capi.cu         the C ABI
+  unet.cu         the 3-D U-Net warm start (BF16 tensor-core convolutions and their gradients)
   host_setup.cpp  host parameter derivation and inlet profile (g++ -ffp-contract=off)
 and the stand-alone program lib/mflbm_main (driver.cpp, g++, linked to the library).
 """
@@ -34,8 +35,10 @@ UNITS = {
     "setup.cu": ["-fmad=false"],
     "output.cu": ["-fmad=false"],
     "capi.cu": [],
+    "unet.cu": [],
 }
-HEADERS = ["common.cuh", "context.cuh", "step_kernels.cuh", "collide.cuh", "gradient.cuh", "boundary.cuh", "setup.cuh"]
+HEADERS = ["common.cuh", "context.cuh", "step_kernels.cuh", "collide.cuh", "gradient.cuh", "boundary.cuh", "setup.cuh",
+           "unet_kernels.cuh"]
 
 
 def _run(cmd):

@@ -55,7 +55,7 @@ void free_all(mflbm_context* c) {
     void* ptrs[] = {d.pdf, d.phi, d.cn_x, d.cn_y, d.cn_z, d.c_norm, d.curv, d.W_in, d.f_cv, d.g_cv, d.phi_cv,
                     d.walls, d.walls_type, d.s_nx, d.s_ny, d.s_nz, d.fluid_list, d.list_phi_ext,
                     d.list_cn_ext, d.red, d.staging, d.aux, d.type8, d.cnv4, d.list_norm, d.zpair_off,
-                    d.phi_prev, d.prof};
+                    d.phi_prev, d.prof, d.dither};
     for (void* p : ptrs) if (p) cudaFree(p);
     d = DeviceState{};
     if (c->pair_graph) cudaGraphExecDestroy(c->pair_graph);
@@ -307,7 +307,8 @@ int mflbm_create(const mflbm_params* params, mflbm_context** out) {
         {&d.cn_z, T * g.n2()}, {&d.c_norm, T * g.n2()}, {&d.curv, T * g.n1()}, {&d.W_in, T * g.plane1()},
         {&d.f_cv, T * g.plane1() * 19}, {&d.g_cv, T * g.plane1() * 19}, {&d.phi_cv, T * g.plane1()},
         {(void**)&d.walls, sizeof(int32_t) * g.n2()}, {(void**)&d.walls_type, sizeof(int32_t) * g.n4()},
-        {&d.s_nx, T * g.n4()}, {&d.s_ny, T * g.n4()}, {&d.s_nz, T * g.n4()}};
+        {&d.s_nx, T * g.n4()}, {&d.s_ny, T * g.n4()}, {&d.s_nz, T * g.n4()},
+        {(void**)&d.dither, 2 * sizeof(uint32_t)}};
     for (auto& a : allocs) {
         if ((rc = alloc_zero(a.p, a.bytes, c->stream)) != MFLBM_OK) {
             free_all(c);
@@ -416,6 +417,27 @@ int mflbm_init_fields(mflbm_context* c, int option, double interface_z0, const v
     if ((rc = flavour_gradient(c)) != MFLBM_OK) return rc;
     MFLBM_CUDA(cudaStreamSynchronize(c->stream));
     c->have_fields = true;
+    return MFLBM_OK;
+}
+
+int mflbm_init_flow(mflbm_context* c, const void* rho, const void* u, const void* v, const void* w) {
+    if (!c) return fail(MFLBM_E_ARG, "null context");
+    if (!c->have_fields) return fail(MFLBM_E_STATE, "mflbm_init_flow needs phi (mflbm_init_fields or mflbm_upload_fields first)");
+    const Grid& g = c->d.g;
+    const size_t T = tsize(c), n = T * g.n1();
+    int rc = ensure_staging(c);
+    if (rc != MFLBM_OK) return rc;
+    const void* host[4] = {rho, u, v, w};
+    const void* dev[4] = {nullptr, nullptr, nullptr, nullptr};
+    for (int a = 0; a < 4; ++a) {
+        if (!host[a]) continue;
+        void* dst = (char*)c->d.staging + a * n;
+        MFLBM_CUDA(cudaMemcpyAsync(dst, host[a], n, cudaMemcpyHostToDevice, c->stream));
+        dev[a] = dst;
+    }
+    if ((rc = init_flow(*c, dev[0], dev[1], dev[2], dev[3])) != MFLBM_OK) return rc;
+    MFLBM_CUDA(cudaStreamSynchronize(c->stream));
+    c->d.arrays_stale = true;
     return MFLBM_OK;
 }
 
@@ -638,7 +660,8 @@ int mflbm_autotune(mflbm_context* c, int reps, mflbm_tuning* out) {
     // everything a step writes: populations, phi, records, convective buffers
     struct { void* p; size_t n; } st[] = {{d.pdf, pop_e * d.b.S * 38}, {d.phi, T * g.n4()},
                                           {d.aux, T * 4 * std::max<ll>(1, d.n_fluid)}, {d.cnv4, T * 4 * g.n2()},
-                                          {d.f_cv, T * pl * 19}, {d.g_cv, T * pl * 19}, {d.phi_cv, T * pl}};
+                                          {d.f_cv, T * pl * 19}, {d.g_cv, T * pl * 19}, {d.phi_cv, T * pl},
+                                          {d.dither, 2 * sizeof(uint32_t)}};
     size_t total = 0;
     for (auto& x : st) total += (x.n + 255) / 256 * 256;
     char* save = nullptr;
@@ -670,7 +693,6 @@ int mflbm_autotune(mflbm_context* c, int reps, mflbm_tuning* out) {
     double before = 0, best_ms = 0;
     rc = measure(best, &before);
     best_ms = before;
-    int* fields[4] = {&best.collide, &best.normals, &best.curvature, &best.extrapolate};
     for (int f = 0; f < 4 && rc == MFLBM_OK; ++f)
         for (int bs : {64, 128, 256}) {
             Tuning t = best;
@@ -681,7 +703,6 @@ int mflbm_autotune(mflbm_context* c, int reps, mflbm_tuning* out) {
             if ((rc = measure(t, &ms)) != MFLBM_OK) break;
             if (ms < best_ms) { best_ms = ms; best = t; }
         }
-    (void)fields;
     d.tune = best;
     off = 0;
     for (auto& x : st) {

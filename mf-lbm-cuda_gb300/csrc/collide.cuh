@@ -180,6 +180,7 @@ template <class T, class E> struct CollideArgs {
     int NX4, NY4;
     T* phi;
     const V4* aux;  // fluid-list order: (n_x, n_y, n_z, 0.5 * gamma * curv * c_norm)
+    uint32_t* dither;  // step counter pair of stochastic rounding (16-bit storage)
     Phys<T> ph;
 };
 
@@ -209,10 +210,19 @@ __global__ void __launch_bounds__(256) collide_stream_kernel(const CollideArgs<T
         g2[q] = Codec::dec(v.y, lat_w<T>(q), lat_winv<T>(q));
     }
     const typename Vec4<T>::type av = a.aux[t];
-    // dither seed of 16-bit storage: the node and its incoming populations
-    // (deterministic, and different at every step of an evolving flow)
+    // dither seed of 16-bit storage: the node, the step counter and two
+    // incoming populations, so that rounding directions are drawn afresh at
+    // every step even in a steady flow (a state-only seed freezes them and
+    // biases the steady state).  The odd kernel reads counter [0] and writes
+    // [1] = [0] + 1, the even kernel the other way round: no word is read and
+    // written by the same launch.
     uint32_t seed = 0;
-    if (!std::is_same<T, E>::value) seed = mix32((uint32_t)e0 ^ mix32(__float_as_uint((float)g1[1]) ^ __float_as_uint((float)g2[2])));
+    if (!std::is_same<T, E>::value) {
+        const uint32_t step = a.dither[ODD ? 0 : 1];
+        if (t == 0) a.dither[ODD ? 1 : 0] = step + 1u;
+        seed = mix32((uint32_t)e0 ^ mix32(step * 0x9E3779B9u ^ __float_as_uint((float)g1[1]) ^
+                                          mix32(__float_as_uint((float)g2[2]))));
+    }
     const T phi = collide<T>(a.ph, g1, g2, av.x, av.y, av.z, av.w);
     a.phi[(x + 3) + a.NX4 * ((y + 3) + a.NY4 * (z + 3))] = phi;
 #pragma unroll
@@ -247,6 +257,7 @@ int launch_collide(mflbm_context& c, bool odd) {
     a.NX4 = g.nx + 8; a.NY4 = g.ny + 8;
     a.phi = (T*)d.phi;
     a.aux = (const typename Vec4<T>::type*)d.aux;
+    a.dither = d.dither;
     a.ph = make_phys<T>(c.params);
     if (a.n == 0) return MFLBM_OK;
     const int bs = d.tune.collide;

@@ -53,6 +53,7 @@ struct DeviceState {
     int* zpair_off = nullptr;          // fluid-list offset of each z pair (2 kp, 2 kp + 1), nbz + 1 entries
     void* phi_prev = nullptr;          // phi at the previous tracking monitor call (s4)
     double* prof = nullptr;            // per-slice and per-block monitor partials
+    uint32_t* dither = nullptr;        // step counter of 16-bit stochastic rounding: [0] read by odd, [1] by even steps
 };
 
 }  // namespace mflbm

@@ -247,19 +247,37 @@ __global__ void init_phi(Grid g, int option, T z0, int open_z, T phi_inlet, T* p
     phi[g.s4(i, j, k)] = v;
 }
 
+// Equilibrium fill of initialization_new_multi_pdf (src/Init_multiphase.cpp:389-496):
+// f_q = r w_q (1 + 3 c.u + 4.5 (c.u)^2 - 1.5 u.u) with r = rho (1 +- phi) / 2
+// per component; rho, u, v, w in the (nx+2)(ny+2)(nz+2) layout, NULL for
+// rho = 1 and u = v = w = 0 (the rest state of the cold start).
 template <class T, class E>
-__global__ void init_pdf(Grid g, PopView<T, E> P, ModelConsts<T> c, const T* phi) {
+__global__ void init_pdf(Grid g, PopView<T, E> P, ModelConsts<T> c, const T* phi, const T* rho, const T* u,
+                         const T* v, const T* w) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y, k = blockIdx.z;
     if (i > g.nx + 1) return;
+    const ll n1 = g.s1(i, j, k);
     const T ph = phi[g.s4(i, j, k)];
-    const T r[2] = {T(1) * (T(1.0) + ph) * T(0.5), T(1) * (T(1.0) - ph) * T(0.5)};
-    const T usqrt = T(0) * T(0) + T(0) * T(0) + T(0) * T(0);
+    const T rh = rho ? rho[n1] : T(1);
+    const T ux = u ? u[n1] : T(0), uy = v ? v[n1] : T(0), uz = w ? w[n1] : T(0);
+    const T r[2] = {rh * (T(1.0) + ph) * T(0.5), rh * (T(1.0) - ph) * T(0.5)};
+    const T usqrt = ux * ux + uy * uy + uz * uz;
     for (int gg = 0; gg < 2; ++gg) {
         P.set(i, j, k, 0, gg, r[gg] * c.w0 + r[gg] * c.w0 * (T(-1.5) * usqrt));
         for (int q = 1; q < 19; ++q) {
             const T wq = q < 7 ? c.w1 : c.w2;
-            const T cu = T(0);
+            // the reference's per-direction sums: only the non-zero components, left to right
+            T cu = T(0);
+            bool first = true;
+            const int e3[3] = {ex(q), ey(q), ez(q)};
+            const T u3[3] = {ux, uy, uz};
+            for (int a = 0; a < 3; ++a) {
+                if (e3[a] == 0) continue;
+                const T term = e3[a] > 0 ? u3[a] : -u3[a];
+                cu = first ? term : cu + term;
+                first = false;
+            }
             P.set(i, j, k, q, gg, r[gg] * wq + r[gg] * wq * (T(3.0) * cu + T(4.5) * cu * cu - T(1.5) * usqrt));
         }
     }
@@ -294,12 +312,32 @@ int init_fields_t(mflbm_context& c, int option, double z0) {
     int rc;
     init_phi<T><<<dim3(grid_for(g.nx + 8, 128), g.ny + 8, g.nz + 8), 128, 0, s>>>(g, option, T(z0), open_z, T(p.phi_inlet), (T*)d.phi);
     if ((rc = after_launch("init_phi")) != MFLBM_OK) return rc;
-    init_pdf<T, E><<<dim3(grid_for(g.nx + 2, 128), g.ny + 2, g.nz + 2), 128, 0, s>>>(g, pop_view<T, E>(d), make_consts<T>(), (const T*)d.phi);
+    init_pdf<T, E><<<dim3(grid_for(g.nx + 2, 128), g.ny + 2, g.nz + 2), 128, 0, s>>>(g, pop_view<T, E>(d), make_consts<T>(), (const T*)d.phi,
+                                                                                nullptr, nullptr, nullptr, nullptr);
     if ((rc = after_launch("init_pdf")) != MFLBM_OK) return rc;
     MFLBM_CUDA(cudaMemsetAsync(d.f_cv, 0, sizeof(T) * g.plane1() * 19, s));
     MFLBM_CUDA(cudaMemsetAsync(d.g_cv, 0, sizeof(T) * g.plane1() * 19, s));
     MFLBM_CUDA(cudaMemsetAsync(d.phi_cv, 0, sizeof(T) * g.plane1(), s));
     if (p.outlet_BC == 1) {
+        init_convective<T, E><<<dim3(grid_for(g.nx + 2, 128), g.ny + 2), 128, 0, s>>>(g, pop_view<T, E>(d), (const T*)d.phi, (T*)d.f_cv, (T*)d.g_cv, (T*)d.phi_cv);
+        if ((rc = after_launch("init_convective")) != MFLBM_OK) return rc;
+    }
+    return MFLBM_OK;
+}
+
+// Equilibrium fill from given macroscopic fields over the current phi (the
+// warm-start entry): rho, u, v, w are device arrays of (nx+2)(ny+2)(nz+2) T,
+// any of them NULL.  The convective outlet buffers follow the new populations.
+template <class T, class E>
+int init_flow_t(mflbm_context& c, const void* rho, const void* u, const void* v, const void* w) {
+    DeviceState& d = c.d;
+    const Grid g = d.g;
+    cudaStream_t s = c.stream;
+    int rc;
+    init_pdf<T, E><<<dim3(grid_for(g.nx + 2, 128), g.ny + 2, g.nz + 2), 128, 0, s>>>(
+        g, pop_view<T, E>(d), make_consts<T>(), (const T*)d.phi, (const T*)rho, (const T*)u, (const T*)v, (const T*)w);
+    if ((rc = after_launch("init_pdf")) != MFLBM_OK) return rc;
+    if (c.params.outlet_BC == 1) {
         init_convective<T, E><<<dim3(grid_for(g.nx + 2, 128), g.ny + 2), 128, 0, s>>>(g, pop_view<T, E>(d), (const T*)d.phi, (T*)d.f_cv, (T*)d.g_cv, (T*)d.phi_cv);
         if ((rc = after_launch("init_convective")) != MFLBM_OK) return rc;
     }
@@ -700,6 +738,9 @@ int preprocess_geometry(mflbm_context& c, const int32_t* walls_global, int iper)
 }
 
 int init_fields(mflbm_context& c, int option, double z0) { return MFLBM_POP(init_fields_t, c, option, z0); }
+int init_flow(mflbm_context& c, const void* rho, const void* u, const void* v, const void* w) {
+    return MFLBM_POP(init_flow_t, c, rho, u, v, w);
+}
 
 int monitor(mflbm_context& c, int nex_in, int nex_out, mflbm_monitor* out) {
     return MFLBM_POP(monitor_t, c, nex_in, nex_out, out);

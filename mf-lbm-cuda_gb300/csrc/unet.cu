@@ -1,0 +1,483 @@
+// 3-D U-Net warm start (no counterpart in the reference): network, training
+// step and C ABI.  4 levels of 16 / 32 / 64 / 128 channels, two 3x3x3
+// convolutions with ReLU per level, average pooling down, nearest
+// up-sampling and concatenation with the encoder's output up, a final 3x3x3
+// convolution to the 4 outputs (u, v, w, p).  Activations and weights BF16,
+// accumulation FP32 (unet_kernels.cuh), FP32 master weights with Adam.
+//
+// Inputs carry 2 channels (solid mask, signed distance) and outputs 4; both
+// are stored with 16 channels so every convolution has a multiple of 16 on
+// each side (the padding channels are zero and stay zero: their weights get
+// zero gradients).
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "unet_kernels.cuh"
+#include "unet_tc.cuh"
+
+using mflbm::fail;
+namespace U = mflbm::unet;
+typedef U::bf16 bf16;
+
+namespace {
+
+constexpr int kIn = 2, kOut = 4, kPad = 16;
+inline unsigned nblk(size_t n, int b = 256) { return (unsigned)((n + b - 1) / b); }
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t n = 0;
+    ~DevBuf() { if (p) cudaFree(p); }
+    int alloc(size_t bytes) {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = bytes;
+        MFLBM_CUDA(cudaMalloc(&p, bytes));
+        MFLBM_CUDA(cudaMemset(p, 0, bytes));
+        return MFLBM_OK;
+    }
+    template <class X> X* as() const { return (X*)p; }
+};
+
+struct Tensor {  // D x H x W x C, BF16, with its gradient
+    U::Dims d;
+    int c = 0;
+    DevBuf v, g;
+    size_t count() const { return (size_t)d.D * d.H * d.W * c; }
+    int alloc(U::Dims dd, int cc) {
+        d = dd;
+        c = cc;
+        int rc = v.alloc(count() * sizeof(bf16));
+        return rc == MFLBM_OK ? g.alloc(count() * sizeof(bf16)) : rc;
+    }
+};
+
+struct Conv {
+    int cin, cout;
+    bool relu;
+    DevBuf w32, w16, wt, b, gw, gb, mw, vw, mb, vb;
+    size_t nw() const { return (size_t)cout * 27 * cin; }
+};
+
+template <int NT>
+int launch_conv_tc(const U::Dims& d, const bf16* x, int cin, const bf16* w, const float* b, bf16* y, float* y32,
+                   int cout, bool relu, int* err, cudaStream_t s) {
+    constexpr int smem = U::tc_smem_bytes<NT>();
+    static bool configured = false;
+    if (!configured) {
+        MFLBM_CUDA(cudaFuncSetAttribute(U::conv3d_fwd_tc_kernel<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        configured = true;
+    }
+    const unsigned gx = nblk((size_t)d.vox(), U::TC_M);
+    U::conv3d_fwd_tc_kernel<NT><<<dim3(gx, cout / NT), 128, smem, s>>>(d, x, cin, w, b, y, y32, cout, relu, err);
+    MFLBM_CUDA(cudaGetLastError());
+    mflbm::count_launch();
+    return MFLBM_OK;
+}
+
+// y = act(conv(x, w) + b) on the tensor cores; cin and cout multiples of 16.
+// The output-channel tile is the largest of 128 / 64 / 32 / 16 dividing cout.
+int launch_conv(const U::Dims& d, const bf16* x, int cin, const bf16* w, const float* b, bf16* y, float* y32,
+                int cout, bool relu, int* err, cudaStream_t s) {
+    if (cin % 16 || cout % 16) return fail(MFLBM_E_ARG, "convolution channels must be multiples of 16");
+    if (cout % 128 == 0) return launch_conv_tc<128>(d, x, cin, w, b, y, y32, cout, relu, err, s);
+    if (cout % 64 == 0) return launch_conv_tc<64>(d, x, cin, w, b, y, y32, cout, relu, err, s);
+    if (cout % 32 == 0) return launch_conv_tc<32>(d, x, cin, w, b, y, y32, cout, relu, err, s);
+    return launch_conv_tc<16>(d, x, cin, w, b, y, y32, cout, relu, err, s);
+}
+
+// gradients of a convolution: gw, gb from (x, gy); gx = conv(gy, flipped w)
+int conv_backward(const U::Dims& d, const bf16* x, int cin, const bf16* w, bf16* wt, const bf16* gy, int cout,
+                  float* gw, float* gb, bf16* gx, DevBuf& work, int* err, cudaStream_t s) {
+    const int V = d.D * d.H * d.W;
+    const int chunk = 2048, chunks = (V + chunk - 1) / chunk;
+    const size_t nw = (size_t)cout * 27 * cin;
+    if (work.n < sizeof(float) * (chunks * nw + (size_t)chunks * cout)) {
+        int rc = work.alloc(sizeof(float) * (chunks * nw + (size_t)chunks * cout));
+        if (rc != MFLBM_OK) return rc;
+    }
+    float* part = work.as<float>();
+    U::conv3d_wgrad_kernel<<<dim3(chunks * 27, (cout + 63) / 64, (cin + 31) / 32), 128, 0, s>>>(d, x, cin, gy, cout, chunk, part);
+    MFLBM_CUDA(cudaGetLastError());
+    U::sum_chunks_kernel<<<nblk(nw), 256, 0, s>>>(part, chunks, nw, gw);
+    float* bpart = part + chunks * nw;
+    U::bias_grad_kernel<<<chunks, 128, 0, s>>>(gy, V, cout, chunk, bpart);
+    U::sum_chunks_kernel<<<nblk(cout), 256, 0, s>>>(bpart, chunks, cout, gb);
+    MFLBM_CUDA(cudaGetLastError());
+    mflbm::count_launch();
+    if (gx) {
+        U::flip_weights_kernel<<<nblk(nw), 256, 0, s>>>(w, cout, cin, cout, wt);
+        MFLBM_CUDA(cudaGetLastError());
+        return launch_conv(d, gy, cout, wt, nullptr, gx, nullptr, cin, false, err, s);
+    }
+    return MFLBM_OK;
+}
+
+}  // namespace
+
+struct mflbm_unet {
+    U::Dims d[4];
+    cudaStream_t s = nullptr;
+    std::vector<std::unique_ptr<Conv>> conv;  // enc 0a 0b 1a 1b 2a 2b 3a 3b, dec 2a 2b 1a 1b 0a 0b, final
+    // activations: x, e[l][0..1], p[l], c[l] (concat), dd[l][0..1], out
+    Tensor x, e[4][2], p[4], cc[3], dd[3][2], out;
+    DevBuf out32, tgt, mask, mse_part, work, err;  // err: time-out flag of the tensor-core pipelines
+    int step = 0;
+};
+
+namespace {
+
+int add_conv(mflbm_unet* n, int cin, int cout, bool relu, std::mt19937_64& rng) {
+    auto c = std::make_unique<Conv>();
+    c->cin = cin; c->cout = cout; c->relu = relu;
+    const size_t nw = c->nw();
+    int rc;
+    for (DevBuf* b : {&c->w32, &c->gw, &c->mw, &c->vw})
+        if ((rc = b->alloc(sizeof(float) * nw)) != MFLBM_OK) return rc;
+    for (DevBuf* b : {&c->w16, &c->wt})
+        if ((rc = b->alloc(sizeof(bf16) * nw)) != MFLBM_OK) return rc;
+    for (DevBuf* b : {&c->b, &c->gb, &c->mb, &c->vb})
+        if ((rc = b->alloc(sizeof(float) * cout)) != MFLBM_OK) return rc;
+    // He initialisation over the real fan-in; padding channels start (and stay) zero
+    const int real_in = cin == kPad && n->conv.empty() ? kIn : cin;
+    const int real_out = cout == kPad && c->relu == false ? kOut : cout;
+    std::normal_distribution<float> nd(0.0f, std::sqrt(2.0f / (27.0f * real_in)));
+    std::vector<float> w(nw, 0.0f);
+    for (int co = 0; co < real_out; ++co)
+        for (int t = 0; t < 27; ++t)
+            for (int ci = 0; ci < real_in; ++ci) w[((size_t)co * 27 + t) * cin + ci] = nd(rng);
+    MFLBM_CUDA(cudaMemcpy(c->w32.p, w.data(), sizeof(float) * nw, cudaMemcpyHostToDevice));
+    U::f32_to_bf16_kernel<<<nblk(nw), 256, 0, n->s>>>(c->w32.as<float>(), c->w16.as<bf16>(), nw);
+    MFLBM_CUDA(cudaGetLastError());
+    n->conv.push_back(std::move(c));
+    return MFLBM_OK;
+}
+
+int conv_fwd(mflbm_unet* n, int li, const Tensor& in, Tensor& out, float* y32 = nullptr) {
+    Conv& c = *n->conv[li];
+    return launch_conv(in.d, in.v.as<bf16>(), c.cin, c.w16.as<bf16>(), c.b.as<float>(), out.v.as<bf16>(), y32,
+                       c.cout, c.relu, n->err.as<int>(), n->s);
+}
+
+// gradient of the layer's output in out.g (ReLU applied here); accumulates nothing
+int conv_bwd(mflbm_unet* n, int li, Tensor& in, Tensor& out, bool need_gx) {
+    Conv& c = *n->conv[li];
+    if (c.relu) {
+        U::relu_grad_kernel<<<nblk(out.count()), 256, 0, n->s>>>(out.g.as<bf16>(), out.v.as<bf16>(), out.count());
+        MFLBM_CUDA(cudaGetLastError());
+    }
+    return conv_backward(in.d, in.v.as<bf16>(), c.cin, c.w16.as<bf16>(), c.wt.as<bf16>(), out.g.as<bf16>(), c.cout,
+                         c.gw.as<float>(), c.gb.as<float>(), need_gx ? in.g.as<bf16>() : nullptr, n->work,
+                         n->err.as<int>(), n->s);
+}
+
+int forward(mflbm_unet* n) {
+    int rc, li = 0;
+    const Tensor* in = &n->x;
+    for (int l = 0; l < 4; ++l) {
+        if (l > 0) {
+            const Tensor& src = n->e[l - 1][1];
+            U::pool_fwd_kernel<<<nblk(n->p[l].count()), 256, 0, n->s>>>(src.d, src.v.as<bf16>(), src.c, n->p[l].v.as<bf16>());
+            MFLBM_CUDA(cudaGetLastError());
+            in = &n->p[l];
+        }
+        if ((rc = conv_fwd(n, li++, *in, n->e[l][0])) != MFLBM_OK) return rc;
+        if ((rc = conv_fwd(n, li++, n->e[l][0], n->e[l][1])) != MFLBM_OK) return rc;
+    }
+    const Tensor* low = &n->e[3][1];
+    for (int l = 2; l >= 0; --l) {
+        Tensor& cat = n->cc[l];
+        U::up_fwd_kernel<<<nblk((size_t)cat.d.vox() * low->c), 256, 0, n->s>>>(cat.d, low->v.as<bf16>(), low->c,
+                                                                                cat.v.as<bf16>(), cat.c, 0);
+        const Tensor& skip = n->e[l][1];
+        U::copy_channels_kernel<<<nblk((size_t)cat.d.vox() * skip.c), 256, 0, n->s>>>(
+            skip.v.as<bf16>(), skip.c, 0, cat.v.as<bf16>(), cat.c, low->c, skip.c, (size_t)cat.d.vox());
+        MFLBM_CUDA(cudaGetLastError());
+        if ((rc = conv_fwd(n, li++, cat, n->dd[l][0])) != MFLBM_OK) return rc;
+        if ((rc = conv_fwd(n, li++, n->dd[l][0], n->dd[l][1])) != MFLBM_OK) return rc;
+        low = &n->dd[l][1];
+    }
+    return conv_fwd(n, li, n->dd[0][1], n->out, n->out32.as<float>());
+}
+
+int backward(mflbm_unet* n) {
+    int rc;
+    const int last = (int)n->conv.size() - 1;
+    if ((rc = conv_bwd(n, last, n->dd[0][1], n->out, true)) != MFLBM_OK) return rc;
+    int li = last - 1;
+    for (int l = 0; l <= 2; ++l) {
+        // decoder level l: dd[l][1] <- dd[l][0] <- cat[l]
+        if ((rc = conv_bwd(n, li--, n->dd[l][0], n->dd[l][1], true)) != MFLBM_OK) return rc;
+        if ((rc = conv_bwd(n, li--, n->cc[l], n->dd[l][0], true)) != MFLBM_OK) return rc;
+        Tensor& cat = n->cc[l];
+        Tensor& low = l < 2 ? n->dd[l + 1][1] : n->e[3][1];
+        Tensor& skip = n->e[l][1];
+        U::up_bwd_kernel<<<nblk(low.count()), 256, 0, n->s>>>(cat.d, cat.g.as<bf16>(), cat.c, 0, low.c, low.g.as<bf16>());
+        // skip gradient: stored now, the pooling gradient is added when its level is reached
+        U::copy_channels_kernel<<<nblk(skip.count()), 256, 0, n->s>>>(cat.g.as<bf16>(), cat.c, low.c, skip.g.as<bf16>(),
+                                                                     skip.c, 0, skip.c, (size_t)skip.d.vox());
+        MFLBM_CUDA(cudaGetLastError());
+    }
+    // encoder, deepest first; e[3][1].g came from the up-sampling of level 2
+    for (int l = 3; l >= 0; --l) {
+        const int la = 2 * l, lb = 2 * l + 1;
+        if ((rc = conv_bwd(n, lb, n->e[l][0], n->e[l][1], true)) != MFLBM_OK) return rc;
+        Tensor& in = l > 0 ? n->p[l] : n->x;
+        if ((rc = conv_bwd(n, la, in, n->e[l][0], l > 0)) != MFLBM_OK) return rc;
+        if (l > 0) {
+            // e[l-1][1] feeds the pool of level l and the concatenation of level l-1
+            Tensor& prev = n->e[l - 1][1];
+            U::pool_bwd_add_kernel<<<nblk(prev.count()), 256, 0, n->s>>>(prev.d, n->p[l].g.as<bf16>(), prev.c, prev.g.as<bf16>());
+            MFLBM_CUDA(cudaGetLastError());
+        }
+    }
+    return MFLBM_OK;
+}
+
+int adam(mflbm_unet* n, float lr) {
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    n->step++;
+    const float c1 = 1.0f / (1.0f - std::pow(b1, (float)n->step)), c2 = 1.0f / (1.0f - std::pow(b2, (float)n->step));
+    for (auto& cp : n->conv) {
+        Conv& c = *cp;
+        const size_t nw = c.nw();
+        U::adam_kernel<<<nblk(nw), 256, 0, n->s>>>(c.w32.as<float>(), c.w16.as<bf16>(), c.gw.as<float>(), c.mw.as<float>(),
+                                                   c.vw.as<float>(), nw, lr, b1, b2, c1, c2, eps);
+        U::adam_kernel<<<nblk(c.cout), 256, 0, n->s>>>(c.b.as<float>(), nullptr, c.gb.as<float>(), c.mb.as<float>(),
+                                                       c.vb.as<float>(), c.cout, lr, b1, b2, c1, c2, eps);
+        MFLBM_CUDA(cudaGetLastError());
+    }
+    return MFLBM_OK;
+}
+
+// host (D*H*W*k, FP32) -> device (D*H*W*16, BF16)
+int upload_padded(mflbm_unet* n, const float* h, int k, Tensor& t) {
+    const size_t V = (size_t)t.d.vox();
+    std::vector<bf16> buf(V * kPad);
+    for (size_t v = 0; v < V; ++v)
+        for (int c = 0; c < kPad; ++c) buf[v * kPad + c] = __float2bfloat16_rn(c < k ? h[v * k + c] : 0.0f);
+    MFLBM_CUDA(cudaMemcpyAsync(t.v.p, buf.data(), buf.size() * sizeof(bf16), cudaMemcpyHostToDevice, n->s));
+    MFLBM_CUDA(cudaStreamSynchronize(n->s));
+    return MFLBM_OK;
+}
+
+// the time-out flag of the tensor-core pipelines (after a synchronisation)
+int check_pipeline_flag(const DevBuf& err) {
+    int h = 0;
+    MFLBM_CUDA(cudaMemcpy(&h, err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h) return fail(MFLBM_E_CUDA, "tensor-core convolution: an mbarrier wait timed out");
+    return MFLBM_OK;
+}
+
+// masked MSE of the 4 outputs and the gradients of every layer (no update)
+int loss_and_gradients(mflbm_unet* n, const float* x, const float* target, const float* mask, float* loss) {
+    int rc = upload_padded(n, x, kIn, n->x);
+    if (rc != MFLBM_OK) return rc;
+    const size_t V = (size_t)n->d[0].vox();
+    std::vector<float> t(V * kPad, 0.0f);
+    double count = 0;
+    for (size_t v = 0; v < V; ++v) {
+        for (int c = 0; c < kOut; ++c) t[v * kPad + c] = target[v * kOut + c];
+        count += mask[v];
+    }
+    MFLBM_CUDA(cudaMemcpyAsync(n->tgt.p, t.data(), t.size() * sizeof(float), cudaMemcpyHostToDevice, n->s));
+    MFLBM_CUDA(cudaMemcpyAsync(n->mask.p, mask, V * sizeof(float), cudaMemcpyHostToDevice, n->s));
+    if ((rc = forward(n)) != MFLBM_OK) return rc;
+    const unsigned nb = nblk(V * kPad);
+    const double norm = 1.0 / (std::max(count, 1.0) * kOut);
+    U::mse_kernel<<<nb, 256, 0, n->s>>>(n->out32.as<float>(), n->tgt.as<float>(), n->mask.as<float>(), kPad, V,
+                                        (float)norm, n->out.g.as<bf16>(), n->mse_part.as<float>());
+    MFLBM_CUDA(cudaGetLastError());
+    if ((rc = backward(n)) != MFLBM_OK) return rc;
+    std::vector<float> part(nb);
+    MFLBM_CUDA(cudaMemcpyAsync(part.data(), n->mse_part.p, nb * sizeof(float), cudaMemcpyDeviceToHost, n->s));
+    MFLBM_CUDA(cudaStreamSynchronize(n->s));
+    if ((rc = check_pipeline_flag(n->err)) != MFLBM_OK) return rc;
+    double s = 0;
+    for (float p : part) s += p;
+    if (loss) *loss = (float)(s * norm);
+    return MFLBM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mflbm_unet_create(int D, int H, int W, unsigned long long seed, mflbm_unet** out) {
+    if (!out) return fail(MFLBM_E_ARG, "mflbm_unet_create: null output");
+    *out = nullptr;
+    if (D < 8 || H < 8 || W < 8 || D % 8 || H % 8 || W % 8)
+        return fail(MFLBM_E_ARG, "mflbm_unet_create: dimensions must be multiples of 8 (three poolings)");
+    auto n = std::make_unique<mflbm_unet>();
+    MFLBM_CUDA(cudaStreamCreateWithFlags(&n->s, cudaStreamNonBlocking));
+    static const int ch[4] = {16, 32, 64, 128};
+    for (int l = 0; l < 4; ++l) n->d[l] = U::Dims{D >> l, H >> l, W >> l};
+    std::mt19937_64 rng(seed);
+    int rc;
+    if ((rc = n->x.alloc(n->d[0], kPad)) != MFLBM_OK) return rc;
+    for (int l = 0; l < 4; ++l) {
+        if (l > 0 && (rc = n->p[l].alloc(n->d[l], ch[l - 1])) != MFLBM_OK) return rc;
+        if ((rc = add_conv(n.get(), l == 0 ? kPad : ch[l - 1], ch[l], true, rng)) != MFLBM_OK) return rc;
+        if ((rc = add_conv(n.get(), ch[l], ch[l], true, rng)) != MFLBM_OK) return rc;
+        for (int k = 0; k < 2; ++k)
+            if ((rc = n->e[l][k].alloc(n->d[l], ch[l])) != MFLBM_OK) return rc;
+    }
+    for (int l = 2; l >= 0; --l) {
+        const int low = l == 2 ? ch[3] : ch[l + 1];
+        if ((rc = n->cc[l].alloc(n->d[l], low + ch[l])) != MFLBM_OK) return rc;
+        if ((rc = add_conv(n.get(), low + ch[l], ch[l], true, rng)) != MFLBM_OK) return rc;
+        if ((rc = add_conv(n.get(), ch[l], ch[l], true, rng)) != MFLBM_OK) return rc;
+        for (int k = 0; k < 2; ++k)
+            if ((rc = n->dd[l][k].alloc(n->d[l], ch[l])) != MFLBM_OK) return rc;
+    }
+    if ((rc = add_conv(n.get(), ch[0], kPad, false, rng)) != MFLBM_OK) return rc;
+    if ((rc = n->out.alloc(n->d[0], kPad)) != MFLBM_OK) return rc;
+    const size_t V = (size_t)D * H * W;
+    if ((rc = n->out32.alloc(sizeof(float) * V * kPad)) != MFLBM_OK) return rc;
+    if ((rc = n->tgt.alloc(sizeof(float) * V * kPad)) != MFLBM_OK) return rc;
+    if ((rc = n->mask.alloc(sizeof(float) * V)) != MFLBM_OK) return rc;
+    if ((rc = n->mse_part.alloc(sizeof(float) * nblk(V * kPad))) != MFLBM_OK) return rc;
+    if ((rc = n->err.alloc(sizeof(int))) != MFLBM_OK) return rc;
+    MFLBM_CUDA(cudaStreamSynchronize(n->s));
+    *out = n.release();
+    return MFLBM_OK;
+}
+
+int mflbm_unet_destroy(mflbm_unet* n) {
+    if (!n) return MFLBM_OK;
+    cudaStreamSynchronize(n->s);
+    cudaStream_t s = n->s;
+    delete n;
+    cudaStreamDestroy(s);
+    return MFLBM_OK;
+}
+
+int mflbm_unet_param_count(mflbm_unet* n, long long* count) {
+    if (!n || !count) return fail(MFLBM_E_ARG, "mflbm_unet_param_count: null argument");
+    long long c = 0;
+    for (auto& cp : n->conv) c += (long long)cp->nw() + cp->cout;
+    *count = c;
+    return MFLBM_OK;
+}
+
+int mflbm_unet_get_params(mflbm_unet* n, float* params) {
+    if (!n || !params) return fail(MFLBM_E_ARG, "mflbm_unet_get_params: null argument");
+    MFLBM_CUDA(cudaStreamSynchronize(n->s));
+    for (auto& cp : n->conv) {
+        MFLBM_CUDA(cudaMemcpy(params, cp->w32.p, cp->nw() * sizeof(float), cudaMemcpyDeviceToHost));
+        params += cp->nw();
+        MFLBM_CUDA(cudaMemcpy(params, cp->b.p, cp->cout * sizeof(float), cudaMemcpyDeviceToHost));
+        params += cp->cout;
+    }
+    return MFLBM_OK;
+}
+
+// loads weights and biases and restarts the optimiser (moments zero, step 0)
+int mflbm_unet_set_params(mflbm_unet* n, const float* params) {
+    if (!n || !params) return fail(MFLBM_E_ARG, "mflbm_unet_set_params: null argument");
+    for (auto& cp : n->conv) {
+        Conv& c = *cp;
+        MFLBM_CUDA(cudaMemcpyAsync(c.w32.p, params, c.nw() * sizeof(float), cudaMemcpyHostToDevice, n->s));
+        params += c.nw();
+        MFLBM_CUDA(cudaMemcpyAsync(c.b.p, params, c.cout * sizeof(float), cudaMemcpyHostToDevice, n->s));
+        params += c.cout;
+        U::f32_to_bf16_kernel<<<nblk(c.nw()), 256, 0, n->s>>>(c.w32.as<float>(), c.w16.as<bf16>(), c.nw());
+        MFLBM_CUDA(cudaGetLastError());
+        for (DevBuf* b : {&c.mw, &c.vw, &c.mb, &c.vb}) MFLBM_CUDA(cudaMemsetAsync(b->p, 0, b->n, n->s));
+    }
+    n->step = 0;
+    MFLBM_CUDA(cudaStreamSynchronize(n->s));
+    return MFLBM_OK;
+}
+
+int mflbm_unet_forward(mflbm_unet* n, const float* x, float* y) {
+    if (!n || !x || !y) return fail(MFLBM_E_ARG, "mflbm_unet_forward: null argument");
+    int rc = upload_padded(n, x, kIn, n->x);
+    if (rc != MFLBM_OK || (rc = forward(n)) != MFLBM_OK) return rc;
+    const size_t V = (size_t)n->d[0].vox();
+    std::vector<float> o(V * kPad);
+    MFLBM_CUDA(cudaMemcpyAsync(o.data(), n->out32.p, o.size() * sizeof(float), cudaMemcpyDeviceToHost, n->s));
+    MFLBM_CUDA(cudaStreamSynchronize(n->s));
+    if ((rc = check_pipeline_flag(n->err)) != MFLBM_OK) return rc;
+    for (size_t v = 0; v < V; ++v)
+        for (int c = 0; c < kOut; ++c) y[v * kOut + c] = o[v * kPad + c];
+    return MFLBM_OK;
+}
+
+int mflbm_unet_train_step(mflbm_unet* n, const float* x, const float* target, const float* mask, float lr, float* loss) {
+    if (!n || !x || !target || !mask) return fail(MFLBM_E_ARG, "mflbm_unet_train_step: null argument");
+    int rc = loss_and_gradients(n, x, target, mask, loss);
+    return rc != MFLBM_OK ? rc : adam(n, lr);
+}
+
+int mflbm_unet_gradients(mflbm_unet* n, const float* x, const float* target, const float* mask, float* grads,
+                         float* loss) {
+    if (!n || !x || !target || !mask || !grads) return fail(MFLBM_E_ARG, "mflbm_unet_gradients: null argument");
+    int rc = loss_and_gradients(n, x, target, mask, loss);
+    if (rc != MFLBM_OK) return rc;
+    for (auto& cp : n->conv) {
+        MFLBM_CUDA(cudaMemcpyAsync(grads, cp->gw.p, cp->nw() * sizeof(float), cudaMemcpyDeviceToHost, n->s));
+        grads += cp->nw();
+        MFLBM_CUDA(cudaMemcpyAsync(grads, cp->gb.p, cp->cout * sizeof(float), cudaMemcpyDeviceToHost, n->s));
+        grads += cp->cout;
+    }
+    MFLBM_CUDA(cudaStreamSynchronize(n->s));
+    return MFLBM_OK;
+}
+
+// One convolution and its gradients on host arrays (checks against a CPU
+// restatement): x D*H*W*cin, w cout*27*cin, b cout, gy D*H*W*cout, all FP32
+// (rounded to BF16 on the device); outputs y (FP32 before rounding), gx, gw, gb.
+int mflbm_unet_conv_check(int D, int H, int W, int cin, int cout, const float* x, const float* w, const float* b,
+                          int relu, const float* gy, float* y, float* gx, float* gw, float* gb) {
+    if (cin % 16 || cout % 16 || cin <= 0 || cout <= 0)
+        return fail(MFLBM_E_ARG, "mflbm_unet_conv_check: channels must be positive multiples of 16");
+    const U::Dims d{D, H, W};
+    const size_t V = (size_t)D * H * W, nw = (size_t)cout * 27 * cin;
+    DevBuf dx, dw, db, dy, dy32, dgy, dgx, dgw, dgb, dwt, f32, work, derr;
+    int rc;
+    const size_t ci = (size_t)cin, co = (size_t)cout;
+    struct { DevBuf* b; size_t n; } al[] = {{&dx, V * ci * 2}, {&dw, nw * 2}, {&db, co * 4}, {&dy, V * co * 2},
+                                            {&dy32, V * co * 4}, {&dgy, V * co * 2}, {&dgx, V * ci * 2},
+                                            {&dgw, nw * 4}, {&dgb, co * 4}, {&dwt, nw * 2},
+                                            {&f32, std::max(V * std::max(ci, co), nw) * 4}, {&derr, sizeof(int)}};
+    for (auto& a : al)
+        if ((rc = a.b->alloc(a.n)) != MFLBM_OK) return rc;
+    auto up16 = [&](const float* h, size_t cnt, DevBuf& dst) -> int {
+        MFLBM_CUDA(cudaMemcpy(f32.p, h, cnt * 4, cudaMemcpyHostToDevice));
+        U::f32_to_bf16_kernel<<<nblk(cnt), 256>>>(f32.as<float>(), dst.as<bf16>(), cnt);
+        MFLBM_CUDA(cudaGetLastError());
+        return MFLBM_OK;
+    };
+    if ((rc = up16(x, V * cin, dx)) != MFLBM_OK || (rc = up16(w, nw, dw)) != MFLBM_OK) return rc;
+    MFLBM_CUDA(cudaMemcpy(db.p, b, cout * 4, cudaMemcpyHostToDevice));
+    if ((rc = launch_conv(d, dx.as<bf16>(), cin, dw.as<bf16>(), db.as<float>(), dy.as<bf16>(), dy32.as<float>(), cout,
+                          relu != 0, derr.as<int>(), 0)) != MFLBM_OK)
+        return rc;
+    if (gy) {
+        if ((rc = up16(gy, V * cout, dgy)) != MFLBM_OK) return rc;
+        if ((rc = conv_backward(d, dx.as<bf16>(), cin, dw.as<bf16>(), dwt.as<bf16>(), dgy.as<bf16>(), cout,
+                                dgw.as<float>(), dgb.as<float>(), dgx.as<bf16>(), work, derr.as<int>(), 0)) != MFLBM_OK)
+            return rc;
+    }
+    MFLBM_CUDA(cudaDeviceSynchronize());
+    if ((rc = check_pipeline_flag(derr)) != MFLBM_OK) return rc;
+    if (y) MFLBM_CUDA(cudaMemcpy(y, dy32.p, V * cout * 4, cudaMemcpyDeviceToHost));
+    if (gy) {
+        std::vector<bf16> h(V * cin);
+        MFLBM_CUDA(cudaMemcpy(h.data(), dgx.p, h.size() * 2, cudaMemcpyDeviceToHost));
+        if (gx)
+            for (size_t i = 0; i < h.size(); ++i) gx[i] = __bfloat162float(h[i]);
+        if (gw) MFLBM_CUDA(cudaMemcpy(gw, dgw.p, nw * 4, cudaMemcpyDeviceToHost));
+        if (gb) MFLBM_CUDA(cudaMemcpy(gb, dgb.p, cout * 4, cudaMemcpyDeviceToHost));
+    }
+    return MFLBM_OK;
+}
+
+}  // extern "C"

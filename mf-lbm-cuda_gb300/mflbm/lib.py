@@ -51,6 +51,16 @@ SIGNATURES = {
     "mflbm_write_walls_vtk": (I, [VP, C.c_char_p]),
     "mflbm_write_checkpoint": (I, [VP, I, C.c_char_p]),
     "mflbm_read_checkpoint": (I, [VP, C.c_char_p, VP, C.POINTER(I)]),
+    "mflbm_init_flow": (I, [VP, VP, VP, VP, VP]),
+    "mflbm_unet_create": (I, [I, I, I, C.c_ulonglong, C.POINTER(VP)]),
+    "mflbm_unet_destroy": (I, [VP]),
+    "mflbm_unet_param_count": (I, [VP, C.POINTER(LL)]),
+    "mflbm_unet_forward": (I, [VP, VP, VP]),
+    "mflbm_unet_train_step": (I, [VP, VP, VP, VP, C.c_float, C.POINTER(C.c_float)]),
+    "mflbm_unet_gradients": (I, [VP, VP, VP, VP, VP, C.POINTER(C.c_float)]),
+    "mflbm_unet_get_params": (I, [VP, VP]),
+    "mflbm_unet_set_params": (I, [VP, VP]),
+    "mflbm_unet_conv_check": (I, [I, I, I, I, I, VP, VP, VP, I, VP, VP, VP, VP, VP]),
     "mflbm_node_counts": (I, [VP, C.POINTER(LL)]),
     "mflbm_stream": (VP, [VP]),
     "mflbm_set_kernel_timing": (I, [VP, I]),
@@ -171,6 +181,16 @@ class Context:
         out = {n: self.L.empty(abi.FIELD_KINDS[n], self.T) for n in names}
         check(self.lib.mflbm_download_fields(self.h, *[ptr(out.get(n)) for n in order]), "mflbm_download_fields")
         return out
+
+    def init_flow(self, rho=None, u=None, v=None, w=None):
+        """mflbm_init_flow: equilibrium populations from macroscopic fields
+        (arrays of shape (nz+2, ny+2, nx+2) or flat, any of them None)."""
+        a = [None if f is None else np.ascontiguousarray(f, dtype=self.T).ravel() for f in (rho, u, v, w)]
+        n = (self.params.nx + 2) * (self.params.ny + 2) * (self.params.nz + 2)
+        for f in a:
+            if f is not None and f.size != n:
+                raise ValueError(f"init_flow: expected {n} values per field, got {f.size}")
+        check(self.lib.mflbm_init_flow(self.h, *[ptr(f) for f in a]), "mflbm_init_flow")
 
     def step(self, ntime):
         check(self.lib.mflbm_step(self.h, int(ntime)), "mflbm_step")

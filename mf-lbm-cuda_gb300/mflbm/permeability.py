@@ -42,9 +42,11 @@ def make_samples(n_samples, nmin, nmax, seed=4000, porosity=(0.3, 0.7)):
 
 
 def converge(samples, precision=abi.MFLBM_FP32, fp_mode=abi.MFLBM_FAST, storage=abi.MFLBM_STORE_NATIVE,
-             tol=1e-6, interval=1000, max_steps=200000, batched=True, tune=False):
+             tol=1e-6, interval=1000, max_steps=200000, batched=True, tune=False, on_done=None):
     """Run every sample until k converges.  Returns one dict per sample
-    (k, steps) and the wall time of the stepping."""
+    (k, steps) and the wall time of the stepping.  on_done(i, ctx), when
+    given, receives every context at the end (and then owns it); otherwise
+    the contexts are closed."""
     ctxs = [lib.setup_case(c, precision, fp_mode, storage=storage)[0] for c in samples]
     if tune:
         for c in ctxs:
@@ -76,8 +78,11 @@ def converge(samples, precision=abi.MFLBM_FP32, fp_mode=abi.MFLBM_FAST, storage=
     seconds = time.perf_counter() - t0
     for i in active:
         res[i] = {"case": samples[i].name, "k": k_prev[i], "steps": nt - 1, "converged": False}
-    for c in ctxs:
-        c.close()
+    for i, c in enumerate(ctxs):
+        if on_done:
+            on_done(i, c)
+        else:
+            c.close()
     return res, seconds
 
 

@@ -1,0 +1,246 @@
+"""Learned warm start: the 3-D U-Net of the library (``mflbm_unet_*``) and the
+glue between it and the lattice.
+
+The network maps a pore geometry (solid mask and signed distance to the
+nearest solid, both per lattice node) to a normalised flow field (u, v, w, p).
+A warm start evaluates it, turns the prediction into physical fields and
+fills the populations with their equilibrium (``mflbm_init_flow``, the
+equilibrium fill of the reference's initialization_new_multi_pdf,
+src/Init_multiphase.cpp:389-496); the plain lattice Boltzmann run then
+converges from there.  Normalisation: velocities are stored as u nu / g and
+pressure as (rho - <rho>) / (3 g), each divided by its training-set scale, so
+that a single network serves any body force g and viscosity nu of the Stokes
+regime.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+
+import numpy as np
+
+from . import abi, lib
+from .abi import ptr
+
+N_IN, N_OUT = 2, 4
+
+# D3Q19 directions (includes/Module.h:98-101 of the reference)
+EX = np.array([0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0])
+EY = np.array([0, 0, 0, 1, -1, 0, 0, 1, 1, -1, -1, 0, 0, 0, 0, 1, -1, 1, -1])
+EZ = np.array([0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 1, 1, -1, -1])
+
+
+class UNet:
+    """One network on the current device, sized for D x H x W inputs."""
+
+    def __init__(self, D, H, W, seed=0):
+        self.lib = lib.load()
+        self.shape = (int(D), int(H), int(W))
+        h = C.c_void_p()
+        lib.check(self.lib.mflbm_unet_create(int(D), int(H), int(W), int(seed), C.byref(h)), "mflbm_unet_create")
+        self.h = h
+        n = C.c_longlong()
+        lib.check(self.lib.mflbm_unet_param_count(self.h, C.byref(n)), "mflbm_unet_param_count")
+        self.n_params = int(n.value)
+
+    def close(self):
+        if self.h:
+            self.lib.mflbm_unet_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check_x(self, x, k):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        if x.shape != self.shape + (k,):
+            raise ValueError(f"expected shape {self.shape + (k,)}, got {x.shape}")
+        return x
+
+    def forward(self, x):
+        x = self._check_x(x, N_IN)
+        y = np.empty(self.shape + (N_OUT,), np.float32)
+        lib.check(self.lib.mflbm_unet_forward(self.h, ptr(x), ptr(y)), "mflbm_unet_forward")
+        return y
+
+    def train_step(self, x, target, mask, lr):
+        x = self._check_x(x, N_IN)
+        t = self._check_x(target, N_OUT)
+        m = np.ascontiguousarray(mask, dtype=np.float32)
+        loss = C.c_float()
+        lib.check(self.lib.mflbm_unet_train_step(self.h, ptr(x), ptr(t), ptr(m), C.c_float(lr), C.byref(loss)),
+                  "mflbm_unet_train_step")
+        return float(loss.value)
+
+    def gradients(self, x, target, mask):
+        x = self._check_x(x, N_IN)
+        t = self._check_x(target, N_OUT)
+        m = np.ascontiguousarray(mask, dtype=np.float32)
+        g = np.empty(self.n_params, np.float32)
+        loss = C.c_float()
+        lib.check(self.lib.mflbm_unet_gradients(self.h, ptr(x), ptr(t), ptr(m), ptr(g), C.byref(loss)),
+                  "mflbm_unet_gradients")
+        return float(loss.value), g
+
+    def get_params(self):
+        p = np.empty(self.n_params, np.float32)
+        lib.check(self.lib.mflbm_unet_get_params(self.h, ptr(p)), "mflbm_unet_get_params")
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        if p.size != self.n_params:
+            raise ValueError(f"expected {self.n_params} parameters, got {p.size}")
+        lib.check(self.lib.mflbm_unet_set_params(self.h, ptr(p)), "mflbm_unet_set_params")
+
+
+def conv_check(x, w, b, gy=None, relu=False):
+    """One convolution layer and its gradients through mflbm_unet_conv_check:
+    returns y (FP32 before rounding) and, with gy, (gx, gw, gb)."""
+    D, H, W, cin = x.shape
+    cout = w.shape[0]
+    f = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float32)
+    x, w, b, gy = f(x), f(w), f(b), f(gy)
+    y = np.empty((D, H, W, cout), np.float32)
+    gx = np.empty_like(x) if gy is not None else None
+    gw = np.empty_like(w) if gy is not None else None
+    gb = np.empty(cout, np.float32) if gy is not None else None
+    lib.check(lib.load().mflbm_unet_conv_check(D, H, W, cin, cout, ptr(x), ptr(w), ptr(b), int(relu), ptr(gy),
+                                               ptr(y), ptr(gx), ptr(gw), ptr(gb)), "mflbm_unet_conv_check")
+    return (y, gx, gw, gb) if gy is not None else y
+
+
+# ---------------------------------------------------------------------------
+# geometry -> network inputs
+# ---------------------------------------------------------------------------
+def features(walls_global, shape, periodic=(False, True, True), sdf_scale=0.125):
+    """Inputs of the network for a wall array (the s0 layout of
+    ``lib.set_walls``: nz x ny x nx, non-zero = solid): channel 0 the solid
+    mask, channel 1 the signed Euclidean distance to the nearest solid-fluid
+    boundary (positive in the fluid), times sdf_scale.  periodic: per axis
+    (x, y, z) whether distances wrap around."""
+    from scipy import ndimage
+
+    nx, ny, nz = shape
+    solid = (np.asarray(walls_global).reshape(nz, ny, nx) != 0)
+    pad = 16
+    pw = [(pad if periodic[2] else 0,) * 2, (pad if periodic[1] else 0,) * 2, (pad if periodic[0] else 0,) * 2]
+    s = np.pad(solid, pw, mode="wrap")
+    d_f = ndimage.distance_transform_edt(~s)
+    d_s = ndimage.distance_transform_edt(s)
+    sl = tuple(slice(p[0], p[0] + n) for p, n in zip(pw, (nz, ny, nx)))
+    sdf = (d_f - d_s)[sl]
+    x = np.empty((nz, ny, nx, N_IN), np.float32)
+    x[..., 0] = solid
+    x[..., 1] = sdf * sdf_scale
+    return x
+
+
+# ---------------------------------------------------------------------------
+# lattice <-> flow fields
+# ---------------------------------------------------------------------------
+def macro_fields(ctx):
+    """rho and velocity (j / rho, j the first moment of both components) on
+    the interior nodes, arrays [nz, ny, nx]."""
+    L = ctx.L
+    nx, ny, nz = L.nx, L.ny, L.nz
+    pdf = ctx.download(("pdf",))["pdf"].reshape(2, 19, nz + 2, ny + 2, nx + 2)
+    f = (pdf[0] + pdf[1])[:, 1:nz + 1, 1:ny + 1, 1:nx + 1].astype(np.float64)
+    rho = f.sum(0)
+    jx = np.tensordot(EX, f, 1)
+    jy = np.tensordot(EY, f, 1)
+    jz = np.tensordot(EZ, f, 1)
+    r = np.where(rho > 0, rho, 1.0)
+    return rho, jx / r, jy / r, jz / r
+
+
+def flow_target(ctx, walls_global, nu, g):
+    """Physical flow of a converged single-phase lattice as the network's raw
+    targets (u nu / g, v nu / g, w nu / g, (rho - <rho>) / (3 g)) and the fluid
+    mask; zero in solids."""
+    L = ctx.L
+    rho, u, v, w = macro_fields(ctx)
+    fluid = (np.asarray(walls_global).reshape(L.nz, L.ny, L.nx) == 0)
+    t = np.zeros(rho.shape + (N_OUT,), np.float32)
+    s = nu / g
+    t[..., 0] = u * s
+    t[..., 1] = v * s
+    t[..., 2] = w * s
+    t[..., 3] = (rho - rho[fluid].mean()) / (3.0 * g)
+    t[~fluid] = 0
+    return t, fluid.astype(np.float32)
+
+
+def fill_from_prediction(ctx, y, walls_global, nu, g, scales):
+    """Equilibrium populations from a normalised prediction y [nz, ny, nx, 4]
+    (mflbm_init_flow); velocity zero in solids, halos periodic in y and z."""
+    L = ctx.L
+    nx, ny, nz = L.nx, L.ny, L.nz
+    solid = (np.asarray(walls_global).reshape(nz, ny, nx) != 0)
+    phys = y * np.asarray(scales, np.float32)
+    c = g / nu
+    fields = []
+    for a in range(3):
+        f = np.where(solid, 0.0, phys[..., a] * c)
+        fields.append(f)
+    fields.insert(0, np.where(solid, 1.0, 1.0 + 3.0 * g * phys[..., 3]))
+
+    def halo(f, fill):
+        p = np.pad(f, ((1, 1), (1, 1), (0, 0)), mode="wrap")        # z, y periodic
+        return np.pad(p, ((0, 0), (0, 0), (1, 1)), constant_values=fill)
+    rho, u, v, w = halo(fields[0], 1.0), halo(fields[1], 0.0), halo(fields[2], 0.0), halo(fields[3], 0.0)
+    ctx.init_flow(rho, u, v, w)
+
+
+def predicted_permeability(y, scales, nx, ny, nz):
+    """k of the predicted field: the mean of u_z nu / g over (nx - 2) ny nz."""
+    return float(y[..., 2].astype(np.float64).sum() * scales[2] / ((nx - 2) * ny * nz))
+
+
+# ---------------------------------------------------------------------------
+# training
+# ---------------------------------------------------------------------------
+def augment(x, t, m, flip_x, flip_y):
+    """Mirror images of a sample (walls in x and periodic y are symmetric
+    under x and y reflections; the flow direction z is kept)."""
+    if flip_x:
+        x, t, m = x[:, :, ::-1], t[:, :, ::-1].copy(), m[:, :, ::-1]
+        t[..., 0] *= -1
+    if flip_y:
+        x, t, m = x[:, ::-1], t[:, ::-1].copy(), m[:, ::-1]
+        t[..., 1] *= -1
+    return np.ascontiguousarray(x), np.ascontiguousarray(t), np.ascontiguousarray(m)
+
+
+def train(net, data, epochs, lr=2e-3, lr_end=1e-4, seed=0, log=None):
+    """Adam over the samples (x, t_normalised, mask) for `epochs` passes with
+    random mirror images and a cosine learning-rate decay.  Returns the mean
+    loss of each epoch and the seconds spent."""
+    rng = np.random.default_rng(seed)
+    steps = epochs * len(data)
+    losses = []
+    t0 = time.perf_counter()
+    it = 0
+    for e in range(epochs):
+        tot = 0.0
+        for i in rng.permutation(len(data)):
+            x, t, m = augment(*data[i], bool(rng.integers(2)), bool(rng.integers(2)))
+            a = lr_end + 0.5 * (lr - lr_end) * (1 + np.cos(np.pi * it / max(steps - 1, 1)))
+            tot += net.train_step(x, t, m, a)
+            it += 1
+        losses.append(tot / len(data))
+        if log:
+            log(f"epoch {e}: loss {losses[-1]:.4g}")
+    return losses, time.perf_counter() - t0
+
+
+def save(path, params, scales, meta=None):
+    np.savez(path, params=params, scales=np.asarray(scales, np.float32), **(meta or {}))
+
+
+def load_model(path):
+    z = np.load(path)
+    return z["params"], z["scales"]

@@ -1,0 +1,242 @@
+"""Learned warm start, end to end: training data from the batched lattice
+Boltzmann runs, training of the U-Net on the GPU, and the comparison of
+warm and cold starts on held-out samples.
+
+    python -m mflbm.warmstart --train 192 --eval 24 --n 64 --epochs 20 \
+        --json out.json [--model unet.npz] [--load unet.npz]
+
+Training samples are seeded single-phase grain packs (porosity uniform in
+0.3-0.7) run to a converged permeability by ``mflbm_batch`` (FP32).  For each
+held-out sample the study runs
+  * the FP64 cold start (rest equilibrium; the accuracy reference),
+  * the plain FP32 cold start,
+  * the warm start: network inference, equilibrium fill, FP16 population
+    storage, falling back to the cold start when the permeability after the
+    first check interval differs from the prediction by more than
+    ``--fallback`` (relative),
+each to the same convergence criterion (k changes by less than ``--tol``,
+relative, over ``--interval`` steps), and reports steps, wall time
+(inference included) and the permeability error against the FP64 cold start.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+
+import numpy as np
+
+from . import abi, cases, lib, unet
+from .permeability import converge, permeability
+
+
+def sample_cases(n_samples, n, seed, porosity=(0.3, 0.7), body_force=1e-4):
+    rng = np.random.default_rng(seed)
+    return [cases.permeability_sample(n, float(rng.uniform(*porosity)), seed + 1 + s, body_force=body_force)
+            for s in range(n_samples)]
+
+
+def walls_of(case, precision=abi.MFLBM_FP32):
+    return lib.set_walls(case.control(precision), case.geometry_bytes())
+
+
+def nu_g(case):
+    k = case.control_keys()
+    return float(k["fluid1_viscosity"]), float(k["body_force_0"])
+
+
+def generate(samples, tol, interval, max_steps, log=print):
+    """Converged FP32 flows of `samples` (one batch graph) as (inputs, raw
+    targets, fluid mask) triples, plus the convergence records."""
+    out = []
+    t0 = time.perf_counter()
+    keep = {}
+
+    def grab(i, ctx):
+        keep[i] = ctx
+
+    res, sec = converge(samples, abi.MFLBM_FP32, tol=tol, interval=interval, max_steps=max_steps, batched=True,
+                        on_done=grab)
+    for i, c in enumerate(samples):
+        nu, g = nu_g(c)
+        w = walls_of(c)
+        t, m = unet.flow_target(keep[i], w, nu, g)
+        out.append((unet.features(w, c.shape), t, m))
+        keep[i].close()
+    log(f"generated {len(samples)} samples in {time.perf_counter() - t0:.1f} s (stepping {sec:.1f} s)")
+    return out, res
+
+
+def scales_of(data):
+    """Per-output scale: RMS over fluid nodes of the training targets (u and
+    v share one scale: the packs are statistically symmetric in x and y)."""
+    s = np.zeros(4)
+    for c in range(4):
+        num = sum(float((t[..., c][m > 0] ** 2).sum()) for _, t, m in data)
+        den = sum(float((m > 0).sum()) for _, _, m in data)
+        s[c] = np.sqrt(num / max(den, 1.0))
+    s[0] = s[1] = np.sqrt(0.5 * (s[0] ** 2 + s[1] ** 2))
+    return np.where(s > 0, s, 1.0).astype(np.float32)
+
+
+def run_until_converged(ctx, case, tol, interval, max_steps, nt=1, check=None):
+    """Steps one context until k changes by <= tol (relative) over `interval`
+    steps.  check(k_first) after the first interval may return False to stop
+    early (fallback).  Returns (k, steps, ok)."""
+    k_prev = None
+    steps = 0
+    while steps < max_steps:
+        ctx.run(nt, interval)
+        nt += interval
+        steps += interval
+        k = permeability(ctx, case)
+        if k_prev is None and check is not None and not check(k):
+            return k, steps, False
+        if k_prev is not None and abs(k - k_prev) <= tol * abs(k):
+            return k, steps, True
+        k_prev = k
+    return k_prev, steps, True
+
+
+class WarmStarter:
+    """The trained network with its output scales; one device network per
+    input shape."""
+
+    def __init__(self, params, scales):
+        self.params, self.scales = params, np.asarray(scales, np.float32)
+        self.nets = {}
+
+    def net(self, shape):
+        nx, ny, nz = shape
+        key = (nz, ny, nx)
+        if key not in self.nets:
+            n = unet.UNet(nz, ny, nx)
+            n.set_params(self.params)
+            self.nets[key] = n
+        return self.nets[key]
+
+    def predict(self, case, walls):
+        x = unet.features(walls, case.shape)
+        return self.net(case.shape).forward(x)
+
+    def close(self):
+        for n in self.nets.values():
+            n.close()
+
+
+def cold_start(ctx, info, capture=True):
+    """Rest-state start-up fields (mflbm_init_fields); with capture, two steps
+    first so that the step graph is captured outside the timed region."""
+    if capture:
+        ctx.run(1, 2)
+        ctx.sync()
+    ctl, der = info["control"], info["derived"]
+    ctx.init_fields(ctl.initial_fluid_distribution_option, der.interface_z0, info["W_in"])
+
+
+def evaluate(ws, case, tol, interval, max_steps, fallback, storage=abi.MFLBM_STORE_F16):
+    """FP64 cold, FP32 cold, warm FP32 and warm 16-bit-storage runs of one
+    sample (the last one only when `storage` is not native)."""
+    nu, g = nu_g(case)
+    nx, ny, nz = case.shape
+    rec = {"case": case.name, "porosity_target": case.geometry.porosity}
+    for name, prec in (("fp64_cold", abi.MFLBM_FP64), ("fp32_cold", abi.MFLBM_FP32)):
+        ctx, info = lib.setup_case(case, prec, abi.MFLBM_FAST)
+        cold_start(ctx, info)
+        t0 = time.perf_counter()
+        k, steps, _ = run_until_converged(ctx, case, tol, interval, max_steps)
+        rec[name] = {"k": k, "steps": steps, "seconds": time.perf_counter() - t0}
+        ctx.close()
+    names = {abi.MFLBM_STORE_NATIVE: "fp32", abi.MFLBM_STORE_F16: "f16", abi.MFLBM_STORE_BF16: "bf16"}
+    variants = [("warm_fp32", abi.MFLBM_STORE_NATIVE)] + ([("warm", storage)] if storage != abi.MFLBM_STORE_NATIVE else [])
+    for name, st in variants:
+        ctx, info = lib.setup_case(case, abi.MFLBM_FP32, abi.MFLBM_FAST, storage=st)
+        cold_start(ctx, info)
+        walls = info["walls_global"]
+        ws.net(case.shape)          # device network of this shape, created outside the timed region
+        t0 = time.perf_counter()
+        y = ws.predict(case, walls)
+        k_pred = unet.predicted_permeability(y, ws.scales, nx, ny, nz)
+        unet.fill_from_prediction(ctx, y, walls, nu, g, ws.scales)
+        t_inf = time.perf_counter() - t0
+        k, steps, ok = run_until_converged(ctx, case, tol, interval, max_steps,
+                                           check=lambda k1: abs(k1 - k_pred) <= fallback * abs(k1))
+        fell_back = not ok
+        if fell_back:
+            cold_start(ctx, info, capture=False)
+            k, s2, _ = run_until_converged(ctx, case, tol, interval, max_steps)
+            steps += s2
+        rec[name] = {"k": k, "k_predicted": k_pred, "steps": steps, "seconds": time.perf_counter() - t0,
+                     "inference_seconds": t_inf, "fallback": fell_back, "storage": names[st]}
+        ctx.close()
+    ref = rec["fp64_cold"]["k"]
+    for name in ("fp32_cold",) + tuple(v for v, _ in variants):
+        rec[name]["k_rel_err"] = abs(rec[name]["k"] - ref) / abs(ref)
+    rec["k_pred_rel_err"] = abs(k_pred - ref) / abs(ref)
+    return rec
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--train", type=int, default=192)
+    ap.add_argument("--eval", type=int, default=24)
+    ap.add_argument("--n", type=int, default=64)
+    ap.add_argument("--n-eval", type=int, default=0, help="lattice size of the held-out samples (default --n)")
+    ap.add_argument("--epochs", type=int, default=20)
+    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--tol", type=float, default=1e-5)
+    ap.add_argument("--interval", type=int, default=500)
+    ap.add_argument("--max-steps", type=int, default=100000)
+    ap.add_argument("--fallback", type=float, default=0.5)
+    ap.add_argument("--storage", default="f16", choices=["native", "f16", "bf16"])
+    ap.add_argument("--seed", type=int, default=20000)
+    ap.add_argument("--model", default="", help="write the trained parameters here (.npz)")
+    ap.add_argument("--load", default="", help="skip data generation and training: use these parameters")
+    ap.add_argument("--json", default="")
+    a = ap.parse_args()
+    st = {"native": abi.MFLBM_STORE_NATIVE, "f16": abi.MFLBM_STORE_F16, "bf16": abi.MFLBM_STORE_BF16}[a.storage]
+    out = {"config": vars(a)}
+    log = lambda s: print(s, flush=True)
+    if a.load:
+        params, scales = unet.load_model(a.load)
+    else:
+        train_cases = sample_cases(a.train, a.n, a.seed)
+        data, res = generate(train_cases, a.tol, a.interval, a.max_steps, log)
+        out["train_steps"] = [r["steps"] for r in res]
+        scales = scales_of(data)
+        norm = [(x, t / scales, m) for x, t, m in data]
+        net = unet.UNet(a.n, a.n, a.n, seed=a.seed)
+        losses, sec = unet.train(net, norm, a.epochs, lr=a.lr, log=log)
+        params = net.get_params()
+        net.close()
+        out["training"] = {"losses": losses, "seconds": sec, "samples": a.train, "epochs": a.epochs,
+                           "step_ms": 1e3 * sec / (a.epochs * a.train), "scales": scales.tolist()}
+        if a.model:
+            unet.save(a.model, params, scales)
+    ws = WarmStarter(params, scales)
+    recs = []
+    for c in sample_cases(a.eval, a.n_eval or a.n, a.seed + 100000):
+        r = evaluate(ws, c, a.tol, a.interval, a.max_steps, a.fallback, st)
+        log(json.dumps(r))
+        recs.append(r)
+    ws.close()
+    tot = lambda key, f: float(sum(r[key][f] for r in recs))
+    out["samples"] = recs
+    summ = {"fp64_cold_seconds": tot("fp64_cold", "seconds"), "fp32_cold_seconds": tot("fp32_cold", "seconds"),
+            "fp32_cold_steps": tot("fp32_cold", "steps"),
+            "max_k_rel_err_fp32_cold": max(r["fp32_cold"]["k_rel_err"] for r in recs),
+            "median_k_pred_rel_err": float(np.median([r["k_pred_rel_err"] for r in recs]))}
+    for v in [k for k in ("warm_fp32", "warm") if k in recs[0]]:
+        summ[v] = {"seconds": tot(v, "seconds"), "steps": tot(v, "steps"),
+                   "speedup_vs_fp32_cold": tot("fp32_cold", "seconds") / max(tot(v, "seconds"), 1e-12),
+                   "max_k_rel_err": max(r[v]["k_rel_err"] for r in recs),
+                   "fallbacks": sum(r[v]["fallback"] for r in recs), "storage": recs[0][v]["storage"]}
+    out["summary"] = summ
+    log(json.dumps(out["summary"]))
+    if a.json:
+        with open(a.json, "w") as f:
+            json.dump(out, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()

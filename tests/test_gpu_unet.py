@@ -1,0 +1,124 @@
+"""The U-Net's tensor-core convolutions, their gradients and the whole
+network's gradients against the CPU restatement (oracle/unet_oracle.py),
+plus the warm-start equilibrium fill (mflbm_init_flow).
+
+Tolerances: convolution outputs and weight gradients are FP32 sums of exact
+BF16 products, so they agree with the FP64 sums to 2e-5 of the sum of
+absolute terms; data gradients are rounded to BF16 (2^-8 relative) on both
+sides and may differ by one BF16 step.  Whole-network gradients pass through
+BF16 activations on both sides; single rounding flips propagate, so each
+layer's gradient is compared by relative L2 error (<= 3e-2) and the loss to
+1e-3."""
+import numpy as np
+import pytest
+
+from mflbm import unet
+from oracle import unet_oracle as UO
+
+pytestmark = pytest.mark.gpu
+
+
+def _bf(a):
+    return UO.bf16(np.asarray(a, np.float32)).astype(np.float64)
+
+
+@pytest.mark.parametrize("shape,cin,cout,relu", [((5, 7, 9), 16, 16, False), ((4, 6, 10), 32, 48, True),
+                                                 ((3, 5, 6), 64, 128, False), ((6, 6, 6), 96, 32, True)])
+def test_conv_forward_and_gradients_match_oracle(mflbm_lib, shape, cin, cout, relu):
+    rng = np.random.default_rng(cin + cout)
+    D, H, W = shape
+    x = rng.normal(size=(D, H, W, cin)).astype(np.float32)
+    w = (rng.normal(size=(cout, 27, cin)) / np.sqrt(27 * cin)).astype(np.float32)
+    b = rng.normal(size=cout).astype(np.float32)
+    gy = rng.normal(size=(D, H, W, cout)).astype(np.float32)
+    y, gx, gw, gb = unet.conv_check(x, w, b, gy, relu=relu)
+    xb, wb, gyb = _bf(x), _bf(w), _bf(gy)
+    ref = UO.conv(xb, wb, b.astype(np.float64))
+    scale = UO.conv(np.abs(xb), np.abs(wb))
+    if relu:
+        ref = np.maximum(ref, 0)
+    assert np.all(np.abs(y - ref) <= 2e-5 * scale + 1e-6)
+    gw_ref, gb_ref = UO.conv_wgrad(xb, gyb)
+    gw_scale, _ = UO.conv_wgrad(np.abs(xb), np.abs(gyb))
+    assert np.all(np.abs(gw - gw_ref) <= 2e-5 * gw_scale + 1e-6)
+    assert np.allclose(gb, gb_ref, rtol=1e-5, atol=1e-4)
+    gx_ref = UO.conv_dgrad(gyb, wb)
+    gx_scale = UO.conv_dgrad(np.abs(gyb), np.abs(wb))
+    assert np.all(np.abs(gx - gx_ref) <= 2 ** -8 * np.abs(gx_ref) + 2e-5 * gx_scale + 1e-6)
+
+
+def test_network_gradients_match_oracle(mflbm_lib):
+    D = 16
+    rng = np.random.default_rng(7)
+    net = unet.UNet(D, D, D, seed=3)
+    assert net.n_params == UO.param_count()
+    p = UO.init_params(5)
+    net.set_params(p)
+    assert np.array_equal(net.get_params(), p)
+    x = np.zeros((D, D, D, 2), np.float32)
+    x[..., 0] = rng.random((D, D, D)) < 0.4
+    x[..., 1] = rng.normal(size=(D, D, D))
+    t = rng.normal(size=(D, D, D, 4)).astype(np.float32)
+    m = (x[..., 0] == 0).astype(np.float32)
+    loss, g = net.gradients(x, t, m)
+    loss_ref, g_ref = UO.loss_and_gradients(p, x, t, m)
+    assert abs(loss - loss_ref) <= 1e-3 * loss_ref
+    o = 0
+    for li, (ci, co, _) in enumerate(UO.layer_shapes()):
+        n = co * 27 * ci + co
+        a, r = g[o:o + n].astype(np.float64), g_ref[o:o + n].astype(np.float64)
+        o += n
+        err = np.linalg.norm(a - r) / max(np.linalg.norm(r), 1e-30)
+        assert err <= 3e-2, (li, err)
+    y = net.forward(x)
+    y_ref, _, _ = UO.forward(p, x)
+    assert np.max(np.abs(y - y_ref)) <= 2e-2 * np.max(np.abs(y_ref))
+    net.close()
+
+
+def test_training_reduces_the_loss(mflbm_lib):
+    D = 16
+    rng = np.random.default_rng(11)
+    net = unet.UNet(D, D, D, seed=1)
+    data = []
+    for s in range(4):
+        x = np.zeros((D, D, D, 2), np.float32)
+        x[..., 0] = rng.random((D, D, D)) < 0.3
+        x[..., 1] = rng.normal(size=(D, D, D))
+        t = np.stack([x[..., 1], -x[..., 1], 0.5 * x[..., 0], np.roll(x[..., 1], 1, 0)], -1).astype(np.float32)
+        data.append((x, t, np.ones((D, D, D), np.float32)))
+    first = np.mean([net.gradients(*d)[0] for d in data])
+    losses, _ = unet.train(net, data, epochs=60, lr=3e-3, lr_end=3e-4)
+    assert losses[-1] < 0.5 * first and losses[-1] < losses[0], (first, losses)
+    net.close()
+
+
+def test_init_flow_fills_the_equilibrium(mflbm_lib):
+    from mflbm import abi, cases, lib
+    case = cases.permeability_sample(16, 0.6, 5)
+    ctx, info = lib.setup_case(case, abi.MFLBM_FP64, abi.MFLBM_STRICT, want_host_geometry=True)
+    L = ctx.L
+    shp = (L.nz + 2, L.ny + 2, L.nx + 2)
+    cold = ctx.download(("pdf",))["pdf"].reshape(2, 19, *shp)
+    ctx.init_flow()
+    # rest state: bit-identical to the cold start on the fluid nodes (solid nodes
+    # hold the start-up wetting extrapolation of phi, which the cold start's
+    # fill precedes)
+    walls = info["geometry"]["walls"].reshape(L.nz + 4, L.ny + 4, L.nx + 4)[1:L.nz + 3, 1:L.ny + 3, 1:L.nx + 3]
+    rest = ctx.download(("pdf",))["pdf"].reshape(2, 19, *shp)
+    assert np.array_equal(rest[:, :, walls == 0], cold[:, :, walls == 0])
+    rng = np.random.default_rng(2)
+    rho = 1 + 1e-3 * rng.normal(size=shp)
+    u, v, w = (1e-2 * rng.normal(size=shp) for _ in range(3))
+    ctx.init_flow(rho, u, v, w)
+    pdf = ctx.download(("pdf",))["pdf"].reshape(2, 19, *shp)
+    phi = ctx.download(("phi",))["phi"].reshape(L.nz + 8, L.ny + 8, L.nx + 8)[3:L.nz + 5, 3:L.ny + 5, 3:L.nx + 5]
+    wq = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12)
+    usq = u * u + v * v + w * w
+    for gg, r in enumerate((rho * (1 + phi) * 0.5, rho * (1 - phi) * 0.5)):
+        for q in range(19):
+            cu = unet.EX[q] * u + unet.EY[q] * v + unet.EZ[q] * w
+            ref = r * wq[q] * (1 + 3 * cu + 4.5 * cu * cu - 1.5 * usq)
+            assert np.allclose(pdf[gg, q], ref, rtol=1e-13, atol=1e-16)
+    ctx.close()
+
