@@ -66,55 +66,126 @@ struct Conv {
 };
 
 template <int NT>
-int launch_conv_tc(const U::Dims& d, const bf16* x, int cin, const bf16* w, const float* b, bf16* y, float* y32,
-                   int cout, bool relu, int* err, cudaStream_t s) {
-    constexpr int smem = U::tc_smem_bytes<NT>();
-    static bool configured = false;
-    if (!configured) {
+int configure_tc() {
+    static bool done = false;
+    if (!done) {
+        constexpr int smem = U::tc_smem_bytes<NT>();
         MFLBM_CUDA(cudaFuncSetAttribute(U::conv3d_fwd_tc_kernel<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        configured = true;
+        MFLBM_CUDA(cudaFuncSetAttribute(U::conv3d_wgrad_tc_kernel<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        done = true;
     }
-    const unsigned gx = nblk((size_t)d.vox(), U::TC_M);
-    U::conv3d_fwd_tc_kernel<NT><<<dim3(gx, cout / NT), 128, smem, s>>>(d, x, cin, w, b, y, y32, cout, relu, err);
+    return MFLBM_OK;
+}
+
+// the N tile of a channel count: the count itself (one tile) when it is one
+// of the instantiated sizes, else the largest instantiated divisor
+int tc_tile(int c) {
+    static const int sizes[] = {192, 128, 96, 64, 48, 32, 16};
+    for (int t : sizes)
+        if (c == t) return t;
+    for (int t : sizes)
+        if (t <= 128 && c % t == 0) return t;
+    return 0;
+}
+
+template <int NT>
+int conv_tc(const U::Dims& d, const bf16* x, int cin, const bf16* w, const float* b, bf16* y, float* y32, int cout,
+            bool relu, int* err, DevBuf& split, cudaStream_t s) {
+    int rc = configure_tc<NT>();
+    if (rc != MFLBM_OK) return rc;
+    const int V = d.vox();
+    const unsigned gx = nblk((size_t)V, U::TC_M), gy = cout / NT;
+    // split K over the taps when the grid would leave most SMs idle (deep levels)
+    const int chunks = 27 * (cin / 16);
+    int ksplit = 1;
+    const long long base = (long long)gx * gy;
+    if (base < 2 * 152) ksplit = (int)std::min<long long>((2 * 152 + base - 1) / base, (chunks + 3) / 4);
+    float* part = nullptr;
+    if (ksplit > 1) {
+        const size_t bytes = sizeof(float) * (size_t)ksplit * V * cout;
+        if (split.n < bytes && (rc = split.alloc(bytes)) != MFLBM_OK) return rc;
+        part = split.as<float>();
+    }
+    U::conv3d_fwd_tc_kernel<NT><<<dim3(gx, gy, ksplit), 128, U::tc_smem_bytes<NT>(), s>>>(
+        d, x, cin, w, b, y, y32, cout, relu, ksplit, part, err);
+    MFLBM_CUDA(cudaGetLastError());
+    mflbm::count_launch();
+    if (ksplit > 1) {
+        const size_t n = (size_t)V * cout;
+        U::splitk_reduce_kernel<<<nblk(n), 256, 0, s>>>(part, ksplit, n, cout, b, relu, y, y32);
+        MFLBM_CUDA(cudaGetLastError());
+        mflbm::count_launch();
+    }
+    return MFLBM_OK;
+}
+
+// y = act(conv(x, w) + b) on the tensor cores; cin and cout multiples of 16
+int launch_conv(const U::Dims& d, const bf16* x, int cin, const bf16* w, const float* b, bf16* y, float* y32,
+                int cout, bool relu, int* err, DevBuf& split, cudaStream_t s) {
+    if (cin % 16 || cout % 16 || cin <= 0 || cout <= 0)
+        return fail(MFLBM_E_ARG, "convolution channels must be positive multiples of 16");
+    switch (tc_tile(cout)) {
+    case 192: return conv_tc<192>(d, x, cin, w, b, y, y32, cout, relu, err, split, s);
+    case 128: return conv_tc<128>(d, x, cin, w, b, y, y32, cout, relu, err, split, s);
+    case 96: return conv_tc<96>(d, x, cin, w, b, y, y32, cout, relu, err, split, s);
+    case 64: return conv_tc<64>(d, x, cin, w, b, y, y32, cout, relu, err, split, s);
+    case 48: return conv_tc<48>(d, x, cin, w, b, y, y32, cout, relu, err, split, s);
+    case 32: return conv_tc<32>(d, x, cin, w, b, y, y32, cout, relu, err, split, s);
+    default: return conv_tc<16>(d, x, cin, w, b, y, y32, cout, relu, err, split, s);
+    }
+}
+
+template <int NT>
+int wgrad_tc(const U::Dims& d, const bf16* x, int cin, const bf16* gy, int cout, int chunk, int chunks, float* part,
+             int* err, cudaStream_t s) {
+    int rc = configure_tc<NT>();
+    if (rc != MFLBM_OK) return rc;
+    const int groups = (27 + 128 / cout - 1) / (128 / cout);
+    U::conv3d_wgrad_tc_kernel<NT><<<dim3(chunks, groups, cin / NT), 128, U::tc_smem_bytes<NT>(), s>>>(
+        d, x, cin, gy, cout, chunk, part, err);
     MFLBM_CUDA(cudaGetLastError());
     mflbm::count_launch();
     return MFLBM_OK;
 }
 
-// y = act(conv(x, w) + b) on the tensor cores; cin and cout multiples of 16.
-// The output-channel tile is the largest of 128 / 64 / 32 / 16 dividing cout.
-int launch_conv(const U::Dims& d, const bf16* x, int cin, const bf16* w, const float* b, bf16* y, float* y32,
-                int cout, bool relu, int* err, cudaStream_t s) {
-    if (cin % 16 || cout % 16) return fail(MFLBM_E_ARG, "convolution channels must be multiples of 16");
-    if (cout % 128 == 0) return launch_conv_tc<128>(d, x, cin, w, b, y, y32, cout, relu, err, s);
-    if (cout % 64 == 0) return launch_conv_tc<64>(d, x, cin, w, b, y, y32, cout, relu, err, s);
-    if (cout % 32 == 0) return launch_conv_tc<32>(d, x, cin, w, b, y, y32, cout, relu, err, s);
-    return launch_conv_tc<16>(d, x, cin, w, b, y, y32, cout, relu, err, s);
-}
-
-// gradients of a convolution: gw, gb from (x, gy); gx = conv(gy, flipped w)
+// gradients of a convolution: gw, gb from (x, gy); gx = conv(gy, flipped w).
+// Weight-gradient partials per chunk of voxels on the tensor cores (chunks of
+// 256..2048 voxels, enough to occupy the GPU), folded in chunk order.
 int conv_backward(const U::Dims& d, const bf16* x, int cin, const bf16* w, bf16* wt, const bf16* gy, int cout,
-                  float* gw, float* gb, bf16* gx, DevBuf& work, int* err, cudaStream_t s) {
-    const int V = d.D * d.H * d.W;
-    const int chunk = 2048, chunks = (V + chunk - 1) / chunk;
+                  float* gw, float* gb, bf16* gx, DevBuf& work, DevBuf& split, int* err, cudaStream_t s) {
+    if (cout != 16 && cout != 32 && cout != 64 && cout != 128)
+        return fail(MFLBM_E_ARG, "weight gradient: output channels must be 16, 32, 64 or 128");
+    if (cin % 16 || cin <= 0) return fail(MFLBM_E_ARG, "weight gradient: input channels must be a multiple of 16");
+    const int V = d.vox();
+    const int groups = (27 + 128 / cout - 1) / (128 / cout);
+    int chunk = 2048;
+    while (chunk > 256 && (long long)((V + chunk - 1) / chunk) * groups < 2 * 152) chunk >>= 1;
+    const int chunks = (V + chunk - 1) / chunk;
     const size_t nw = (size_t)cout * 27 * cin;
-    if (work.n < sizeof(float) * (chunks * nw + (size_t)chunks * cout)) {
-        int rc = work.alloc(sizeof(float) * (chunks * nw + (size_t)chunks * cout));
-        if (rc != MFLBM_OK) return rc;
-    }
+    const size_t need = sizeof(float) * (chunks * nw + (size_t)chunks * cout);
+    int rc;
+    if (work.n < need && (rc = work.alloc(need)) != MFLBM_OK) return rc;
     float* part = work.as<float>();
-    U::conv3d_wgrad_kernel<<<dim3(chunks * 27, (cout + 63) / 64, (cin + 31) / 32), 128, 0, s>>>(d, x, cin, gy, cout, chunk, part);
-    MFLBM_CUDA(cudaGetLastError());
+    switch (tc_tile(cin)) {
+    case 192: rc = wgrad_tc<192>(d, x, cin, gy, cout, chunk, chunks, part, err, s); break;
+    case 128: rc = wgrad_tc<128>(d, x, cin, gy, cout, chunk, chunks, part, err, s); break;
+    case 96: rc = wgrad_tc<96>(d, x, cin, gy, cout, chunk, chunks, part, err, s); break;
+    case 64: rc = wgrad_tc<64>(d, x, cin, gy, cout, chunk, chunks, part, err, s); break;
+    case 48: rc = wgrad_tc<48>(d, x, cin, gy, cout, chunk, chunks, part, err, s); break;
+    case 32: rc = wgrad_tc<32>(d, x, cin, gy, cout, chunk, chunks, part, err, s); break;
+    default: rc = wgrad_tc<16>(d, x, cin, gy, cout, chunk, chunks, part, err, s); break;
+    }
+    if (rc != MFLBM_OK) return rc;
     U::sum_chunks_kernel<<<nblk(nw), 256, 0, s>>>(part, chunks, nw, gw);
     float* bpart = part + chunks * nw;
-    U::bias_grad_kernel<<<chunks, 128, 0, s>>>(gy, V, cout, chunk, bpart);
+    U::bias_grad_kernel<<<chunks, 256, 0, s>>>(gy, V, cout, chunk, bpart);
     U::sum_chunks_kernel<<<nblk(cout), 256, 0, s>>>(bpart, chunks, cout, gb);
     MFLBM_CUDA(cudaGetLastError());
     mflbm::count_launch();
     if (gx) {
         U::flip_weights_kernel<<<nblk(nw), 256, 0, s>>>(w, cout, cin, cout, wt);
         MFLBM_CUDA(cudaGetLastError());
-        return launch_conv(d, gy, cout, wt, nullptr, gx, nullptr, cin, false, err, s);
+        return launch_conv(d, gy, cout, wt, nullptr, gx, nullptr, cin, false, err, split, s);
     }
     return MFLBM_OK;
 }
@@ -127,7 +198,8 @@ struct mflbm_unet {
     std::vector<std::unique_ptr<Conv>> conv;  // enc 0a 0b 1a 1b 2a 2b 3a 3b, dec 2a 2b 1a 1b 0a 0b, final
     // activations: x, e[l][0..1], p[l], c[l] (concat), dd[l][0..1], out
     Tensor x, e[4][2], p[4], cc[3], dd[3][2], out;
-    DevBuf out32, tgt, mask, mse_part, work, err;  // err: time-out flag of the tensor-core pipelines
+    DevBuf out32, tgt, mask, mse_part, work, split, err;  // err: time-out flag of the tensor-core pipelines
+    DevBuf raw;                                           // host-layout staging (D*H*W*4 FP32)
     int step = 0;
 };
 
@@ -162,7 +234,7 @@ int add_conv(mflbm_unet* n, int cin, int cout, bool relu, std::mt19937_64& rng) 
 int conv_fwd(mflbm_unet* n, int li, const Tensor& in, Tensor& out, float* y32 = nullptr) {
     Conv& c = *n->conv[li];
     return launch_conv(in.d, in.v.as<bf16>(), c.cin, c.w16.as<bf16>(), c.b.as<float>(), out.v.as<bf16>(), y32,
-                       c.cout, c.relu, n->err.as<int>(), n->s);
+                       c.cout, c.relu, n->err.as<int>(), n->split, n->s);
 }
 
 // gradient of the layer's output in out.g (ReLU applied here); accumulates nothing
@@ -174,7 +246,7 @@ int conv_bwd(mflbm_unet* n, int li, Tensor& in, Tensor& out, bool need_gx) {
     }
     return conv_backward(in.d, in.v.as<bf16>(), c.cin, c.w16.as<bf16>(), c.wt.as<bf16>(), out.g.as<bf16>(), c.cout,
                          c.gw.as<float>(), c.gb.as<float>(), need_gx ? in.g.as<bf16>() : nullptr, n->work,
-                         n->err.as<int>(), n->s);
+                         n->split, n->err.as<int>(), n->s);
 }
 
 int forward(mflbm_unet* n) {
@@ -256,14 +328,12 @@ int adam(mflbm_unet* n, float lr) {
     return MFLBM_OK;
 }
 
-// host (D*H*W*k, FP32) -> device (D*H*W*16, BF16)
+// host (D*H*W*k, FP32) -> device (D*H*W*16, BF16), padded on the device
 int upload_padded(mflbm_unet* n, const float* h, int k, Tensor& t) {
     const size_t V = (size_t)t.d.vox();
-    std::vector<bf16> buf(V * kPad);
-    for (size_t v = 0; v < V; ++v)
-        for (int c = 0; c < kPad; ++c) buf[v * kPad + c] = __float2bfloat16_rn(c < k ? h[v * k + c] : 0.0f);
-    MFLBM_CUDA(cudaMemcpyAsync(t.v.p, buf.data(), buf.size() * sizeof(bf16), cudaMemcpyHostToDevice, n->s));
-    MFLBM_CUDA(cudaStreamSynchronize(n->s));
+    MFLBM_CUDA(cudaMemcpyAsync(n->raw.p, h, V * k * sizeof(float), cudaMemcpyHostToDevice, n->s));
+    U::pad_input_kernel<<<nblk(V * kPad), 256, 0, n->s>>>(n->raw.as<float>(), k, V, t.v.as<bf16>());
+    MFLBM_CUDA(cudaGetLastError());
     return MFLBM_OK;
 }
 
@@ -280,13 +350,11 @@ int loss_and_gradients(mflbm_unet* n, const float* x, const float* target, const
     int rc = upload_padded(n, x, kIn, n->x);
     if (rc != MFLBM_OK) return rc;
     const size_t V = (size_t)n->d[0].vox();
-    std::vector<float> t(V * kPad, 0.0f);
     double count = 0;
-    for (size_t v = 0; v < V; ++v) {
-        for (int c = 0; c < kOut; ++c) t[v * kPad + c] = target[v * kOut + c];
-        count += mask[v];
-    }
-    MFLBM_CUDA(cudaMemcpyAsync(n->tgt.p, t.data(), t.size() * sizeof(float), cudaMemcpyHostToDevice, n->s));
+    for (size_t v = 0; v < V; ++v) count += mask[v];
+    MFLBM_CUDA(cudaMemcpyAsync(n->raw.p, target, V * kOut * sizeof(float), cudaMemcpyHostToDevice, n->s));
+    U::pad_target_kernel<<<nblk(V * kPad), 256, 0, n->s>>>(n->raw.as<float>(), kOut, V, n->tgt.as<float>());
+    MFLBM_CUDA(cudaGetLastError());
     MFLBM_CUDA(cudaMemcpyAsync(n->mask.p, mask, V * sizeof(float), cudaMemcpyHostToDevice, n->s));
     if ((rc = forward(n)) != MFLBM_OK) return rc;
     const unsigned nb = nblk(V * kPad);
@@ -344,6 +412,7 @@ int mflbm_unet_create(int D, int H, int W, unsigned long long seed, mflbm_unet**
     if ((rc = n->mask.alloc(sizeof(float) * V)) != MFLBM_OK) return rc;
     if ((rc = n->mse_part.alloc(sizeof(float) * nblk(V * kPad))) != MFLBM_OK) return rc;
     if ((rc = n->err.alloc(sizeof(int))) != MFLBM_OK) return rc;
+    if ((rc = n->raw.alloc(sizeof(float) * V * kOut)) != MFLBM_OK) return rc;
     MFLBM_CUDA(cudaStreamSynchronize(n->s));
     *out = n.release();
     return MFLBM_OK;
@@ -401,13 +470,11 @@ int mflbm_unet_forward(mflbm_unet* n, const float* x, float* y) {
     int rc = upload_padded(n, x, kIn, n->x);
     if (rc != MFLBM_OK || (rc = forward(n)) != MFLBM_OK) return rc;
     const size_t V = (size_t)n->d[0].vox();
-    std::vector<float> o(V * kPad);
-    MFLBM_CUDA(cudaMemcpyAsync(o.data(), n->out32.p, o.size() * sizeof(float), cudaMemcpyDeviceToHost, n->s));
+    U::take_outputs_kernel<<<nblk(V * kOut), 256, 0, n->s>>>(n->out32.as<float>(), V, kOut, n->raw.as<float>());
+    MFLBM_CUDA(cudaGetLastError());
+    MFLBM_CUDA(cudaMemcpyAsync(y, n->raw.p, V * kOut * sizeof(float), cudaMemcpyDeviceToHost, n->s));
     MFLBM_CUDA(cudaStreamSynchronize(n->s));
-    if ((rc = check_pipeline_flag(n->err)) != MFLBM_OK) return rc;
-    for (size_t v = 0; v < V; ++v)
-        for (int c = 0; c < kOut; ++c) y[v * kOut + c] = o[v * kPad + c];
-    return MFLBM_OK;
+    return check_pipeline_flag(n->err);
 }
 
 int mflbm_unet_train_step(mflbm_unet* n, const float* x, const float* target, const float* mask, float lr, float* loss) {
@@ -440,7 +507,7 @@ int mflbm_unet_conv_check(int D, int H, int W, int cin, int cout, const float* x
         return fail(MFLBM_E_ARG, "mflbm_unet_conv_check: channels must be positive multiples of 16");
     const U::Dims d{D, H, W};
     const size_t V = (size_t)D * H * W, nw = (size_t)cout * 27 * cin;
-    DevBuf dx, dw, db, dy, dy32, dgy, dgx, dgw, dgb, dwt, f32, work, derr;
+    DevBuf dx, dw, db, dy, dy32, dgy, dgx, dgw, dgb, dwt, f32, work, split, derr;
     int rc;
     const size_t ci = (size_t)cin, co = (size_t)cout;
     struct { DevBuf* b; size_t n; } al[] = {{&dx, V * ci * 2}, {&dw, nw * 2}, {&db, co * 4}, {&dy, V * co * 2},
@@ -458,12 +525,12 @@ int mflbm_unet_conv_check(int D, int H, int W, int cin, int cout, const float* x
     if ((rc = up16(x, V * cin, dx)) != MFLBM_OK || (rc = up16(w, nw, dw)) != MFLBM_OK) return rc;
     MFLBM_CUDA(cudaMemcpy(db.p, b, cout * 4, cudaMemcpyHostToDevice));
     if ((rc = launch_conv(d, dx.as<bf16>(), cin, dw.as<bf16>(), db.as<float>(), dy.as<bf16>(), dy32.as<float>(), cout,
-                          relu != 0, derr.as<int>(), 0)) != MFLBM_OK)
+                          relu != 0, derr.as<int>(), split, 0)) != MFLBM_OK)
         return rc;
     if (gy) {
         if ((rc = up16(gy, V * cout, dgy)) != MFLBM_OK) return rc;
         if ((rc = conv_backward(d, dx.as<bf16>(), cin, dw.as<bf16>(), dwt.as<bf16>(), dgy.as<bf16>(), cout,
-                                dgw.as<float>(), dgb.as<float>(), dgx.as<bf16>(), work, derr.as<int>(), 0)) != MFLBM_OK)
+                                dgw.as<float>(), dgb.as<float>(), dgx.as<bf16>(), work, split, derr.as<int>(), 0)) != MFLBM_OK)
             return rc;
     }
     MFLBM_CUDA(cudaDeviceSynchronize());

@@ -1,7 +1,8 @@
-// Kernels of the 3-D U-Net warm start (no counterpart in the reference):
-// 3x3x3 convolutions as implicit GEMMs on the BF16 tensor cores with FP32
-// accumulation, their two gradients, pooling, up-sampling, concatenation,
-// the masked MSE loss and the Adam update.
+// Element-wise kernels of the 3-D U-Net warm start (no counterpart in the
+// reference): chunk folds of the weight gradients, bias gradient, weight
+// flip for the data gradient, ReLU gradient, pooling, up-sampling,
+// concatenation, the masked MSE loss and the Adam update.  The convolutions
+// themselves run on the tensor cores (unet_tc.cuh).
 //
 // Tensors are channels-last: element (z, y, x, c) of a D x H x W x C tensor is
 // at ((z * H + y) * W + x) * C + c; activations and weights are BF16, bias,
@@ -22,19 +23,6 @@ __device__ __forceinline__ uint32_t pack_bf16(bf16 lo, bf16 hi) {
     return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
 }
 
-// D = A (16x16, row) * B (16x8, col) + C on BF16 tensor cores, FP32 accumulate.
-// Fragments per the PTX ISA layout of mma.m16n8k16 (g = lane / 4, t = lane % 4):
-//   a0: (g, 2t..2t+1)  a1: (g+8, 2t..)  a2: (g, 2t+8..)  a3: (g+8, 2t+8..)
-//   b0: (k = 2t..2t+1, n = g)  b1: (k = 2t+8.., n = g)
-//   c0, c1: (g, 2t..2t+1)  c2, c3: (g+8, 2t..2t+1)
-__device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
 struct Dims {
     int D, H, W;
     __host__ __device__ __forceinline__ int vox() const { return D * H * W; }
@@ -48,129 +36,6 @@ __device__ __forceinline__ int neighbour(const Dims& d, int v, int tap) {
     return (zz * d.H + yy) * d.W + xx;
 }
 
-// y = act(conv(x, w) + b).  Block: 4 warps x 16 voxels; each warp computes
-// its 16 voxels for NT output channels (NT / 8 mma tiles).  Grid:
-// (ceil(V / 64), ceil(Cout / NT)).  cout: real output channels (stores
-// beyond it are skipped; weights of the padded channels are read as zero).
-template <int NT>
-__global__ void __launch_bounds__(128) conv3d_fwd_kernel(Dims d, const bf16* __restrict__ x, int cin,
-                                                         const bf16* __restrict__ w, const float* __restrict__ bias,
-                                                         bf16* __restrict__ y, float* __restrict__ y32, int cout,
-                                                         int relu) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int g = lane >> 2, t = lane & 3;
-    const int V = d.vox();
-    const int v0 = (blockIdx.x * 4 + warp) * 16;
-    const int n0 = blockIdx.y * NT;
-    const int va = v0 + g, vb = v0 + g + 8;
-    float acc[NT / 8][4];
-#pragma unroll
-    for (int j = 0; j < NT / 8; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0f;
-    const uint32_t* xw = reinterpret_cast<const uint32_t*>(x);   // pairs of channels
-    const uint32_t* ww = reinterpret_cast<const uint32_t*>(w);
-    for (int tap = 0; tap < 27; ++tap) {
-        const int na = va < V ? neighbour(d, va, tap) : -1;
-        const int nb = vb < V ? neighbour(d, vb, tap) : -1;
-        for (int c0 = 0; c0 < cin; c0 += 16) {
-            uint32_t a[4];
-            a[0] = na >= 0 ? xw[((size_t)na * cin + c0) / 2 + t] : 0u;
-            a[1] = nb >= 0 ? xw[((size_t)nb * cin + c0) / 2 + t] : 0u;
-            a[2] = na >= 0 ? xw[((size_t)na * cin + c0 + 8) / 2 + t] : 0u;
-            a[3] = nb >= 0 ? xw[((size_t)nb * cin + c0 + 8) / 2 + t] : 0u;
-#pragma unroll
-            for (int j = 0; j < NT / 8; ++j) {
-                const int co = n0 + j * 8 + g;
-                uint32_t b[2];
-                const size_t wb = ((size_t)co * 27 + tap) * cin + c0;
-                b[0] = co < cout ? ww[wb / 2 + t] : 0u;
-                b[1] = co < cout ? ww[(wb + 8) / 2 + t] : 0u;
-                mma_bf16(acc[j], a, b);
-            }
-        }
-    }
-#pragma unroll
-    for (int j = 0; j < NT / 8; ++j) {
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int v = h ? vb : va;
-            if (v >= V) continue;
-#pragma unroll
-            for (int e = 0; e < 2; ++e) {
-                const int co = n0 + j * 8 + 2 * t + e;
-                if (co >= cout) continue;
-                float r = acc[j][2 * h + e] + (bias ? bias[co] : 0.0f);
-                if (relu) r = fmaxf(r, 0.0f);
-                y[(size_t)v * cout + co] = __float2bfloat16_rn(r);
-                if (y32) y32[(size_t)v * cout + co] = r;
-            }
-        }
-    }
-}
-
-// Weight gradient, partial over a chunk of voxels:
-//   part[chunk][co][tap][ci] = sum_{v in chunk} gy[v][co] * x[v + tap][ci]
-// as a GEMM with M = Cout (16 per warp), N = Cin (8 per mma), K = voxels.
-// Block: 4 warps, warp w takes output channels 16 w .. 16 w + 15 of the
-// 64-channel tile blockIdx.y; blockIdx.x = chunk * 27 + tap; blockIdx.z: Cin
-// tiles of 32.
-__global__ void __launch_bounds__(128) conv3d_wgrad_kernel(Dims d, const bf16* __restrict__ x, int cin,
-                                                           const bf16* __restrict__ gy, int cout, int chunk_vox,
-                                                           float* __restrict__ part) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int g = lane >> 2, t = lane & 3;
-    const int tap = blockIdx.x % 27, chunk = blockIdx.x / 27;
-    const int co0 = blockIdx.y * 64 + warp * 16;
-    const int ci0 = blockIdx.z * 32;
-    const int V = d.vox();
-    if (co0 >= cout) return;
-    float acc[4][4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0f;
-    const int vb = chunk * chunk_vox, ve = min(V, vb + chunk_vox);
-    for (int k0 = vb; k0 < ve; k0 += 16) {
-        // A (16 co x 16 voxels): a0 (co g, v 2t..2t+1), a1 (co g+8, ...), a2 (co g, v 2t+8..), a3 (co g+8, v 2t+8..)
-        uint32_t a[4];
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            const int co = co0 + g + ((r & 1) ? 8 : 0);
-            const int v = k0 + 2 * t + ((r & 2) ? 8 : 0);
-            const bf16 lo = (v < ve && co < cout) ? gy[(size_t)v * cout + co] : __float2bfloat16_rn(0.0f);
-            const bf16 hi = (v + 1 < ve && co < cout) ? gy[(size_t)(v + 1) * cout + co] : __float2bfloat16_rn(0.0f);
-            a[r] = pack_bf16(lo, hi);
-        }
-        int nbr[4];
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            const int v = k0 + 2 * t + (r & 1) + ((r & 2) ? 8 : 0);
-            nbr[r] = v < ve ? neighbour(d, v, tap) : -1;
-        }
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            // B (16 voxels x 8 ci): b0 (v 2t..2t+1, ci g), b1 (v 2t+8.., ci g)
-            const int ci = ci0 + j * 8 + g;
-            uint32_t b[2];
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int n_lo = nbr[2 * h], n_hi = nbr[2 * h + 1];
-                const bf16 lo = (n_lo >= 0 && ci < cin) ? x[(size_t)n_lo * cin + ci] : __float2bfloat16_rn(0.0f);
-                const bf16 hi = (n_hi >= 0 && ci < cin) ? x[(size_t)n_hi * cin + ci] : __float2bfloat16_rn(0.0f);
-                b[h] = pack_bf16(lo, hi);
-            }
-            mma_bf16(acc[j], a, b);
-        }
-    }
-    float* out = part + (size_t)chunk * cout * 27 * cin;
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-        for (int h = 0; h < 2; ++h)
-#pragma unroll
-            for (int e = 0; e < 2; ++e) {
-                const int co = co0 + g + 8 * h, ci = ci0 + j * 8 + 2 * t + e;
-                if (co < cout && ci < cin) out[((size_t)co * 27 + tap) * cin + ci] = acc[j][2 * h + e];
-            }
-}
-
 // dw[i] = sum over chunks of part[chunk][i], in chunk order (deterministic); db[co] likewise
 __global__ void sum_chunks_kernel(const float* __restrict__ part, int chunks, size_t n, float* __restrict__ out) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -180,13 +45,24 @@ __global__ void sum_chunks_kernel(const float* __restrict__ part, int chunks, si
     out[i] = s;
 }
 
-// bias gradient partials: one block per chunk of voxels, threads over channels
-__global__ void bias_grad_kernel(const bf16* __restrict__ gy, int V, int cout, int chunk_vox, float* __restrict__ part) {
+// bias gradient partials: one block of 256 threads per chunk of voxels;
+// thread (r, c) = (tid / cout, tid % cout) sums channel c over the voxels
+// r, r + 256 / cout, ... of the chunk (coalesced rows), then the rows are
+// folded in shared memory in a fixed order.  cout divides 256.
+__global__ void __launch_bounds__(256) bias_grad_kernel(const bf16* __restrict__ gy, int V, int cout, int chunk_vox,
+                                                        float* __restrict__ part) {
+    __shared__ float sh[256];
+    const int rows = 256 / cout, r = threadIdx.x / cout, c = threadIdx.x - r * cout;
     const int vb = blockIdx.x * chunk_vox, ve = min(V, vb + chunk_vox);
-    for (int co = threadIdx.x; co < cout; co += blockDim.x) {
-        float s = 0.0f;
-        for (int v = vb; v < ve; ++v) s += __bfloat162float(gy[(size_t)v * cout + co]);
-        part[(size_t)blockIdx.x * cout + co] = s;
+    float s = 0.0f;
+    if (r < rows)
+        for (int v = vb + r; v < ve; v += rows) s += __bfloat162float(gy[(size_t)v * cout + c]);
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.x < cout) {
+        float t = 0.0f;
+        for (int k = 0; k < rows; ++k) t += sh[k * cout + threadIdx.x];
+        part[(size_t)blockIdx.x * cout + threadIdx.x] = t;
     }
 }
 
@@ -299,6 +175,26 @@ __global__ void adam_kernel(float* __restrict__ w, bf16* __restrict__ w16, const
     const float wi = w[i] - lr * (mi * c1) / (sqrtf(vi * c2) + eps);
     w[i] = wi;
     if (w16) w16[i] = __float2bfloat16_rn(wi);
+}
+
+// host-side tensors have k channels per voxel; the network's have 16
+// (zero padding), BF16 for inputs, FP32 for targets and outputs
+__global__ void pad_input_kernel(const float* __restrict__ raw, int k, size_t vox, bf16* __restrict__ x) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= vox * 16) return;
+    const int c = (int)(i & 15);
+    x[i] = __float2bfloat16_rn(c < k ? raw[(i >> 4) * k + c] : 0.0f);
+}
+__global__ void pad_target_kernel(const float* __restrict__ raw, int k, size_t vox, float* __restrict__ t) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= vox * 16) return;
+    const int c = (int)(i & 15);
+    t[i] = c < k ? raw[(i >> 4) * k + c] : 0.0f;
+}
+__global__ void take_outputs_kernel(const float* __restrict__ out32, size_t vox, int k, float* __restrict__ dst) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= vox * k) return;
+    dst[i] = out32[(i / k) * 16 + i % k];
 }
 
 __global__ void f32_to_bf16_kernel(const float* __restrict__ a, bf16* __restrict__ b, size_t n) {

@@ -22,8 +22,9 @@ def _bf(a):
     return UO.bf16(np.asarray(a, np.float32)).astype(np.float64)
 
 
-@pytest.mark.parametrize("shape,cin,cout,relu", [((5, 7, 9), 16, 16, False), ((4, 6, 10), 32, 48, True),
-                                                 ((3, 5, 6), 64, 128, False), ((6, 6, 6), 96, 32, True)])
+@pytest.mark.parametrize("shape,cin,cout,relu", [((5, 7, 9), 16, 16, False), ((4, 6, 10), 48, 32, True),
+                                                 ((3, 5, 6), 64, 128, False), ((6, 6, 6), 96, 32, True),
+                                                 ((4, 4, 8), 192, 64, False), ((16, 16, 12), 16, 16, True)])
 def test_conv_forward_and_gradients_match_oracle(mflbm_lib, shape, cin, cout, relu):
     rng = np.random.default_rng(cin + cout)
     D, H, W = shape
