@@ -178,6 +178,24 @@ def drainage_256x256x256(seed=1200):
     }, Geometry(radius=(4.0, 10.0), porosity=0.45, overlap=True, buffer_layers=2, seed=seed))
 
 
+def precision_case(n=(384, 384, 512), seed=1300):
+    """Two-phase drainage for the precision study, default 384 x 384 x 512:
+    walls on x and y, overlapping spheres r ~ U[4, 10] at porosity 0.40 with
+    2-layer buffers, nu1 = 1/6, nu2 = 1/60 (tau 1.0 / 0.55), contact angle
+    60 deg, gamma 0.01, velocity inlet at Ca = 1e-2 (u_in = 6e-4, chosen so
+    that the front advances ~12 lu in 20 000 steps), convective outlet."""
+    nx, ny, nz = n
+    return Case(f"precision_{nx}x{ny}x{nz}", {
+        "nxGlobal": nx, "nyGlobal": ny, "nzGlobal": nz,
+        "inlet_BC": 1, "outlet_BC": 1,
+        "fluid1_viscosity": "0.16666666666666666", "fluid2_viscosity": "0.016666666666666666",
+        "surface_tension": "0.01", "theta": "60", "RK_beta": "0.95",
+        "capillary_number": "1e-2", "saturation_injection": "1.0",
+        "initial_fluid_distribution_option": 1, "initial_interface_position": "2.0",
+        "n_exclude_inlet": 2, "n_exclude_outlet": 2,
+    }, Geometry(radius=(4.0, 10.0), porosity=0.40, overlap=True, buffer_layers=2, seed=seed))
+
+
 def small_case(kind: str, n=(20, 20, 28), seed=7):
     """Small cases covering every boundary kernel, for parity tests."""
     nx, ny, nz = n
@@ -218,9 +236,12 @@ def permeability_sample(n, porosity, seed, body_force=1e-6, radius=(3.0, 6.0)):
     everywhere): an n^3 grain pack of the given porosity, periodic in y and z,
     walled in x, tau = 1 (nu = 1/6), driven by the body force along z.  The
     reference has no single-phase kernel; phi = 1 (initial interface beyond
-    the domain) makes the second component vanish, so neither recolouring nor
-    surface force acts."""
-    keys = {"nxGlobal": n, "nyGlobal": n, "nzGlobal": n,
+    the domain) makes the second component vanish, and a neutral contact
+    angle (90 degrees) makes the wetting extrapolation give phi = 1 on the
+    solid nodes as well, so the phase gradient, recolouring and surface force
+    are zero everywhere (any other angle puts a phase gradient, hence a
+    surface force, on every wall-adjacent fluid node)."""
+    keys = {"nxGlobal": n, "nyGlobal": n, "nzGlobal": n, "theta": "90",
             "jper": 1, "kper": 1, "domain_wall_status_y_min": 0, "domain_wall_status_y_max": 0,
             "domain_wall_status_z_min": 0, "domain_wall_status_z_max": 0,
             "initial_fluid_distribution_option": 1, "initial_interface_position": str(float(n + 10)),

@@ -244,3 +244,37 @@ def save(path, params, scales, meta=None):
 def load_model(path):
     z = np.load(path)
     return z["params"], z["scales"]
+
+
+def main():
+    """Timing of the network on random inputs:
+    python -m mflbm.unet --size 64 --steps 5"""
+    import argparse
+    import json
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--size", type=int, default=64)
+    ap.add_argument("--steps", type=int, default=5)
+    a = ap.parse_args()
+    n = a.size
+    rng = np.random.default_rng(0)
+    net = UNet(n, n, n, seed=1)
+    x = np.zeros((n, n, n, N_IN), np.float32)
+    x[..., 0] = rng.random((n, n, n)) < 0.4
+    x[..., 1] = rng.normal(size=(n, n, n))
+    t = rng.normal(size=(n, n, n, N_OUT)).astype(np.float32)
+    m = np.ones((n, n, n), np.float32)
+    net.train_step(x, t, m, 1e-3)
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        net.train_step(x, t, m, 1e-3)
+    train_ms = 1e3 * (time.perf_counter() - t0) / a.steps
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        net.forward(x)
+    fwd_ms = 1e3 * (time.perf_counter() - t0) / a.steps
+    net.close()
+    print(json.dumps({"size": n, "params": net.n_params, "train_step_ms": train_ms, "forward_ms": fwd_ms}))
+
+
+if __name__ == "__main__":
+    main()

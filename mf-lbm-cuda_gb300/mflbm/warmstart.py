@@ -10,10 +10,12 @@ Training samples are seeded single-phase grain packs (porosity uniform in
 held-out sample the study runs
   * the FP64 cold start (rest equilibrium; the accuracy reference),
   * the plain FP32 cold start,
-  * the warm start: network inference, equilibrium fill, FP16 population
-    storage, falling back to the cold start when the permeability after the
-    first check interval differs from the prediction by more than
-    ``--fallback`` (relative),
+  * the warm starts: network inference and equilibrium fill, with FP32 and
+    with FP16 population storage, falling back to the cold start when the
+    permeability after the first check interval differs from the prediction
+    by more than ``--fallback`` (relative),
+  * the oracle start: the equilibrium fill from the converged FP64 field
+    itself, the bound on what a surrogate can give through this fill,
 each to the same convergence criterion (k changes by less than ``--tol``,
 relative, over ``--interval`` steps), and reports steps, wall time
 (inference included) and the permeability error against the FP64 cold start.
@@ -134,45 +136,86 @@ def cold_start(ctx, info, capture=True):
     ctx.init_fields(ctl.initial_fluid_distribution_option, der.interface_z0, info["W_in"])
 
 
-def evaluate(ws, case, tol, interval, max_steps, fallback, storage=abi.MFLBM_STORE_F16):
-    """FP64 cold, FP32 cold, warm FP32 and warm 16-bit-storage runs of one
-    sample (the last one only when `storage` is not native)."""
+CHECKPOINTS = (0, 10, 24, 50, 100, 200, 400, 800, 1600)
+
+
+def transient(ctx, case, walls, t_ref, k_ref, nu, g):
+    """k / k_ref and the relative L2 error of u_z over the fluid nodes at
+    CHECKPOINTS steps (even step counts: post-even populations)."""
+    fl = (np.asarray(walls).reshape(case.shape[::-1]) == 0)
+    ks, errs, nt, prev = [], [], 1, 0
+    for c in CHECKPOINTS:
+        if c > prev:
+            ctx.run(nt, c - prev)
+            nt += c - prev
+            prev = c
+        ks.append(round(permeability(ctx, case) / k_ref, 4))
+        t, _ = unet.flow_target(ctx, walls, nu, g)
+        errs.append(round(float(np.linalg.norm((t[..., 2] - t_ref[..., 2])[fl]) / np.linalg.norm(t_ref[..., 2][fl])), 4))
+    return {"steps": list(CHECKPOINTS), "k_over_kref": ks, "uz_rel_err": errs}
+
+
+def evaluate(ws, case, tol, interval, max_steps, fallback, storage=abi.MFLBM_STORE_F16, with_transient=False):
+    """One held-out sample: the FP64 cold start (the accuracy reference, and
+    the converged field of the oracle start), the FP32 cold start, the warm
+    starts (FP32 and, unless `storage` is native, 16-bit storage) and the
+    oracle start (equilibrium fill from the converged FP64 field: the best
+    any surrogate could give through the equilibrium fill).  Steps and wall
+    time to convergence, k errors against the FP64 cold start; optionally
+    the transients of the cold, warm and oracle starts (untimed runs)."""
     nu, g = nu_g(case)
     nx, ny, nz = case.shape
     rec = {"case": case.name, "porosity_target": case.geometry.porosity}
-    for name, prec in (("fp64_cold", abi.MFLBM_FP64), ("fp32_cold", abi.MFLBM_FP32)):
-        ctx, info = lib.setup_case(case, prec, abi.MFLBM_FAST)
-        cold_start(ctx, info)
-        t0 = time.perf_counter()
-        k, steps, _ = run_until_converged(ctx, case, tol, interval, max_steps)
-        rec[name] = {"k": k, "steps": steps, "seconds": time.perf_counter() - t0}
-        ctx.close()
+    ctx, info = lib.setup_case(case, abi.MFLBM_FP64, abi.MFLBM_FAST)
+    walls = info["walls_global"]
+    cold_start(ctx, info)
+    t0 = time.perf_counter()
+    k_ref, steps, _ = run_until_converged(ctx, case, tol, interval, max_steps)
+    rec["fp64_cold"] = {"k": k_ref, "steps": steps, "seconds": time.perf_counter() - t0}
+    t_ref, _ = unet.flow_target(ctx, walls, nu, g)
+    ctx.close()
+    ws.net(case.shape)              # device network of this shape, created outside the timed regions
     names = {abi.MFLBM_STORE_NATIVE: "fp32", abi.MFLBM_STORE_F16: "f16", abi.MFLBM_STORE_BF16: "bf16"}
-    variants = [("warm_fp32", abi.MFLBM_STORE_NATIVE)] + ([("warm", storage)] if storage != abi.MFLBM_STORE_NATIVE else [])
-    for name, st in variants:
+    variants = [("fp32_cold", abi.MFLBM_STORE_NATIVE, "cold"), ("warm_fp32", abi.MFLBM_STORE_NATIVE, "warm"),
+                ("oracle_fp32", abi.MFLBM_STORE_NATIVE, "oracle")]
+    if storage != abi.MFLBM_STORE_NATIVE:
+        variants.append(("warm", storage, "warm"))
+    k_pred = None
+
+    def start(ctx, info, how):
+        nonlocal k_pred
+        if how == "warm":
+            y = ws.predict(case, walls)
+            k_pred = unet.predicted_permeability(y, ws.scales, nx, ny, nz)
+            unet.fill_from_prediction(ctx, y, walls, nu, g, ws.scales)
+        elif how == "oracle":
+            unet.fill_from_prediction(ctx, t_ref / ws.scales, walls, nu, g, ws.scales)
+
+    for name, st, how in variants:
         ctx, info = lib.setup_case(case, abi.MFLBM_FP32, abi.MFLBM_FAST, storage=st)
         cold_start(ctx, info)
-        walls = info["walls_global"]
-        ws.net(case.shape)          # device network of this shape, created outside the timed region
         t0 = time.perf_counter()
-        y = ws.predict(case, walls)
-        k_pred = unet.predicted_permeability(y, ws.scales, nx, ny, nz)
-        unet.fill_from_prediction(ctx, y, walls, nu, g, ws.scales)
-        t_inf = time.perf_counter() - t0
-        k, steps, ok = run_until_converged(ctx, case, tol, interval, max_steps,
-                                           check=lambda k1: abs(k1 - k_pred) <= fallback * abs(k1))
-        fell_back = not ok
-        if fell_back:
+        start(ctx, info, how)
+        t_start = time.perf_counter() - t0
+        check = None
+        if how == "warm":
+            kp = k_pred
+            check = lambda k1: abs(k1 - kp) <= fallback * abs(k1)
+        k, steps, ok = run_until_converged(ctx, case, tol, interval, max_steps, check=check)
+        if not ok:
             cold_start(ctx, info, capture=False)
             k, s2, _ = run_until_converged(ctx, case, tol, interval, max_steps)
             steps += s2
-        rec[name] = {"k": k, "k_predicted": k_pred, "steps": steps, "seconds": time.perf_counter() - t0,
-                     "inference_seconds": t_inf, "fallback": fell_back, "storage": names[st]}
+        rec[name] = {"k": k, "steps": steps, "seconds": time.perf_counter() - t0, "start_seconds": t_start,
+                     "fallback": not ok, "storage": names[st], "k_rel_err": abs(k - k_ref) / abs(k_ref)}
         ctx.close()
-    ref = rec["fp64_cold"]["k"]
-    for name in ("fp32_cold",) + tuple(v for v, _ in variants):
-        rec[name]["k_rel_err"] = abs(rec[name]["k"] - ref) / abs(ref)
-    rec["k_pred_rel_err"] = abs(k_pred - ref) / abs(ref)
+        if with_transient and st == abi.MFLBM_STORE_NATIVE:
+            ctx, info = lib.setup_case(case, abi.MFLBM_FP32, abi.MFLBM_FAST)
+            start(ctx, info, how)
+            rec[name]["transient"] = transient(ctx, case, walls, t_ref, k_ref, nu, g)
+            ctx.close()
+    rec["k_predicted"] = k_pred
+    rec["k_pred_rel_err"] = abs(k_pred - k_ref) / abs(k_ref)
     return rec
 
 
@@ -192,6 +235,7 @@ def main():
     ap.add_argument("--seed", type=int, default=20000)
     ap.add_argument("--model", default="", help="write the trained parameters here (.npz)")
     ap.add_argument("--load", default="", help="skip data generation and training: use these parameters")
+    ap.add_argument("--transient", type=int, default=0, help="record the transients of the first N held-out samples")
     ap.add_argument("--json", default="")
     a = ap.parse_args()
     st = {"native": abi.MFLBM_STORE_NATIVE, "f16": abi.MFLBM_STORE_F16, "bf16": abi.MFLBM_STORE_BF16}[a.storage]
@@ -215,18 +259,18 @@ def main():
             unet.save(a.model, params, scales)
     ws = WarmStarter(params, scales)
     recs = []
-    for c in sample_cases(a.eval, a.n_eval or a.n, a.seed + 100000):
-        r = evaluate(ws, c, a.tol, a.interval, a.max_steps, a.fallback, st)
+    for i, c in enumerate(sample_cases(a.eval, a.n_eval or a.n, a.seed + 100000)):
+        r = evaluate(ws, c, a.tol, a.interval, a.max_steps, a.fallback, st, with_transient=i < a.transient)
         log(json.dumps(r))
         recs.append(r)
     ws.close()
     tot = lambda key, f: float(sum(r[key][f] for r in recs))
     out["samples"] = recs
-    summ = {"fp64_cold_seconds": tot("fp64_cold", "seconds"), "fp32_cold_seconds": tot("fp32_cold", "seconds"),
-            "fp32_cold_steps": tot("fp32_cold", "steps"),
+    summ = {"samples": len(recs), "fp64_cold_seconds": tot("fp64_cold", "seconds"),
+            "fp32_cold_seconds": tot("fp32_cold", "seconds"), "fp32_cold_steps": tot("fp32_cold", "steps"),
             "max_k_rel_err_fp32_cold": max(r["fp32_cold"]["k_rel_err"] for r in recs),
             "median_k_pred_rel_err": float(np.median([r["k_pred_rel_err"] for r in recs]))}
-    for v in [k for k in ("warm_fp32", "warm") if k in recs[0]]:
+    for v in [k for k in ("warm_fp32", "oracle_fp32", "warm") if k in recs[0]]:
         summ[v] = {"seconds": tot(v, "seconds"), "steps": tot(v, "steps"),
                    "speedup_vs_fp32_cold": tot("fp32_cold", "seconds") / max(tot(v, "seconds"), 1e-12),
                    "max_k_rel_err": max(r[v]["k_rel_err"] for r in recs),
