@@ -56,11 +56,14 @@ def converge(samples, precision=abi.MFLBM_FP32, fp_mode=abi.MFLBM_FAST, storage=
     active = list(range(len(samples)))
     nt = 1
     t0 = time.perf_counter()
+    batch, batch_set = None, None
     while active and nt <= max_steps:
         if batched:
-            b = lib.Batch([ctxs[i] for i in active])
-            b.run(nt, interval)
-            b.close()
+            if batch_set != active:          # re-captured only when a sample has converged
+                if batch:
+                    batch.close()
+                batch, batch_set = lib.Batch([ctxs[i] for i in active]), list(active)
+            batch.run(nt, interval)
         else:
             for i in active:
                 ctxs[i].run(nt, interval)
@@ -76,6 +79,8 @@ def converge(samples, precision=abi.MFLBM_FP32, fp_mode=abi.MFLBM_FAST, storage=
             k_prev[i] = k
         active = still
     seconds = time.perf_counter() - t0
+    if batch:
+        batch.close()
     for i in active:
         res[i] = {"case": samples[i].name, "k": k_prev[i], "steps": nt - 1, "converged": False}
     for i, c in enumerate(ctxs):
@@ -93,6 +98,8 @@ def main():
     ap.add_argument("--nmax", type=int, default=96)
     ap.add_argument("--tol", type=float, default=1e-6)
     ap.add_argument("--interval", type=int, default=1000)
+    ap.add_argument("--max-steps", type=int, default=100000)
+    ap.add_argument("--json", default="")
     ap.add_argument("--storage", default="native", choices=["native", "f16", "bf16"])
     ap.add_argument("--fp64", action="store_true")
     ap.add_argument("--sequential", action="store_true")
@@ -100,9 +107,15 @@ def main():
     st = {"native": abi.MFLBM_STORE_NATIVE, "f16": abi.MFLBM_STORE_F16, "bf16": abi.MFLBM_STORE_BF16}[a.storage]
     samples = make_samples(a.samples, a.nmin, a.nmax)
     res, sec = converge(samples, abi.MFLBM_FP64 if a.fp64 else abi.MFLBM_FP32, storage=st, tol=a.tol,
-                        interval=a.interval, batched=not a.sequential)
+                        interval=a.interval, max_steps=a.max_steps, batched=not a.sequential)
     nodes = sum(int(np.prod(s.shape)) * r["steps"] for s, r in zip(samples, res))
-    print(json.dumps({"samples": res, "seconds": sec, "aggregate_mlups": nodes / sec / 1e6}))
+    out = {"mode": "sequential" if a.sequential else "batched", "samples": res, "seconds": sec,
+           "lattice_updates": nodes, "aggregate_mlups": nodes / sec / 1e6,
+           "converged": sum(r.get("converged", True) for r in res)}
+    print(json.dumps({k: v for k, v in out.items() if k != "samples"}))
+    if a.json:
+        with open(a.json, "w") as f:
+            json.dump(out, f, indent=1)
 
 
 if __name__ == "__main__":
