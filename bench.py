@@ -206,6 +206,28 @@ def storage_variants(case, geo, steps, nt):
     return out
 
 
+def fp64_variant(case, geo, steps):
+    """The same workload in FP64 (populations and collision): MLUPS and the
+    collision kernel's algorithmic bandwidth (616 B per fluid node + 1 B per
+    node).  On GB300 the FP64 collision is bound by the FP64 pipe, not by HBM."""
+    import torch
+    from mflbm import abi, lib
+    c, _ = lib.setup_case(case, abi.MFLBM_FP64, abi.MFLBM_FAST, geometry=geo)
+    n_fluid, n_all = c.node_counts()
+    c.run(1, 4)
+    stream = torch.cuda.ExternalStream(c.stream())
+    ms = _timed_run(lambda: c.run(5, steps), c.sync, stream)
+    c.set_timing(True)
+    c.run(5 + steps, 4)
+    tc, tg, n = c.kernel_times()
+    c.set_timing(False)
+    coll = tc / max(n, 1)
+    c.close()
+    return {"value": round(n_all * steps / (ms * 1e-3) / 1e6, 2), "unit": "MLUPS", "ms_per_step": round(ms / steps, 5),
+            "collide_ms": round(coll, 5), "gradient_ms": round(tg / max(n, 1), 5),
+            "collide_gbs": round((n_fluid * 616 + n_all) / (coll * 1e-3) / 1e9, 1)}
+
+
 def batch_vs_sequential(steps):
     """16 single-phase samples of 48^3 .. 96^3 (porosity 0.3 .. 0.7): one
     graph launch per step pair for all of them (mflbm_batch) against each
@@ -371,6 +393,7 @@ def main():
     if not args.no_extras:
         ctx.close()
         extra["storage"] = storage_variants(case, geo, min(args.steps, 200), nt)
+        extra["fp64"] = fp64_variant(case, geo, min(args.steps, 40))
         extra["batch"] = batch_vs_sequential(min(args.steps, 200))
 
     if rank != 0:
