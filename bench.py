@@ -428,6 +428,10 @@ def main():
         "gpu_launches": int(launches_per_step * args.steps),
         "clocks": clocks,
         "saturation": round(mon["saturation"], 6),
+        # fluid nodes with a non-zero phase gradient at the end of the e2e leg: the
+        # curvature gathers run only there (elsewhere the surface force is zero)
+        "interface_fraction": round(float(np.count_nonzero(
+            out["c_norm"].reshape(nz + 4, ny + 4, nx + 4)[2:nz + 2, 2:ny + 2, 2:nx + 2])) / n_fluid, 5),
     }
     if cpu:
         line["cpu_baseline"] = cpu

@@ -55,7 +55,7 @@ void free_all(mflbm_context* c) {
     void* ptrs[] = {d.pdf, d.phi, d.cn_x, d.cn_y, d.cn_z, d.c_norm, d.curv, d.W_in, d.f_cv, d.g_cv, d.phi_cv,
                     d.walls, d.walls_type, d.s_nx, d.s_ny, d.s_nz, d.fluid_list, d.list_phi_ext,
                     d.list_cn_ext, d.red, d.staging, d.aux, d.type8, d.cnv4, d.list_norm, d.zpair_off,
-                    d.phi_prev, d.prof, d.dither};
+                    d.phi_prev, d.prof, d.dither, d.iface};
     for (void* p : ptrs) if (p) cudaFree(p);
     d = DeviceState{};
     if (c->pair_graph) cudaGraphExecDestroy(c->pair_graph);
@@ -140,6 +140,7 @@ int build_lists(mflbm_context* c) {
     MFLBM_CUDA(cudaMemset(d.aux, 0, rec * std::max<ll>(1, d.n_fluid)));
     // solid nodes keep a zero normal record (only fluid nodes are rewritten per step)
     MFLBM_CUDA(cudaMemset(d.cnv4, 0, rec * g.n2()));
+    MFLBM_CUDA(cudaMemset(d.iface, 0, g.n2()));
     c->pair_graph_odd_first = -1;  // kernels are launched with the list sizes
     c->generation++;
     return MFLBM_OK;
@@ -308,7 +309,7 @@ int mflbm_create(const mflbm_params* params, mflbm_context** out) {
         {&d.f_cv, T * g.plane1() * 19}, {&d.g_cv, T * g.plane1() * 19}, {&d.phi_cv, T * g.plane1()},
         {(void**)&d.walls, sizeof(int32_t) * g.n2()}, {(void**)&d.walls_type, sizeof(int32_t) * g.n4()},
         {&d.s_nx, T * g.n4()}, {&d.s_ny, T * g.n4()}, {&d.s_nz, T * g.n4()},
-        {(void**)&d.dither, 2 * sizeof(uint32_t)}};
+        {(void**)&d.dither, 2 * sizeof(uint32_t)}, {(void**)&d.iface, (size_t)g.n2()}};
     for (auto& a : allocs) {
         if ((rc = alloc_zero(a.p, a.bytes, c->stream)) != MFLBM_OK) {
             free_all(c);
@@ -661,7 +662,7 @@ int mflbm_autotune(mflbm_context* c, int reps, mflbm_tuning* out) {
     struct { void* p; size_t n; } st[] = {{d.pdf, pop_e * d.b.S * 38}, {d.phi, T * g.n4()},
                                           {d.aux, T * 4 * std::max<ll>(1, d.n_fluid)}, {d.cnv4, T * 4 * g.n2()},
                                           {d.f_cv, T * pl * 19}, {d.g_cv, T * pl * 19}, {d.phi_cv, T * pl},
-                                          {d.dither, 2 * sizeof(uint32_t)}};
+                                          {d.dither, 2 * sizeof(uint32_t)}, {d.iface, (size_t)g.n2()}};
     size_t total = 0;
     for (auto& x : st) total += (x.n + 255) / 256 * 256;
     char* save = nullptr;

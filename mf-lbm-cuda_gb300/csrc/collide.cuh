@@ -180,6 +180,8 @@ template <class T, class E> struct CollideArgs {
     int NX4, NY4;
     T* phi;
     const V4* aux;  // fluid-list order: (n_x, n_y, n_z, 0.5 * gamma * curv * c_norm)
+    const int8_t* iface;  // s2: the record is read only where 1 (elsewhere it is the zero record)
+    int NX2, NY2;
     uint32_t* dither;  // step counter pair of stochastic rounding (16-bit storage)
     Phys<T> ph;
 };
@@ -209,7 +211,9 @@ __global__ void __launch_bounds__(256) collide_stream_kernel(const CollideArgs<T
         g1[q] = Codec::dec(v.x, lat_w<T>(q), lat_winv<T>(q));
         g2[q] = Codec::dec(v.y, lat_w<T>(q), lat_winv<T>(q));
     }
-    const typename Vec4<T>::type av = a.aux[t];
+    typename Vec4<T>::type av;
+    av.x = T(0); av.y = T(0); av.z = T(0); av.w = T(0);
+    if (a.iface[(x + 1) + a.NX2 * ((y + 1) + a.NY2 * (z + 1))]) av = a.aux[t];   // s2 index of (x, y, z)
     // dither seed of 16-bit storage: the node, the step counter and two
     // incoming populations, so that rounding directions are drawn afresh at
     // every step even in a steady flow (a state-only seed freezes them and
@@ -257,6 +261,8 @@ int launch_collide(mflbm_context& c, bool odd) {
     a.NX4 = g.nx + 8; a.NY4 = g.ny + 8;
     a.phi = (T*)d.phi;
     a.aux = (const typename Vec4<T>::type*)d.aux;
+    a.iface = d.iface;
+    a.NX2 = g.nx + 4; a.NY2 = g.ny + 4;
     a.dither = d.dither;
     a.ph = make_phys<T>(c.params);
     if (a.n == 0) return MFLBM_OK;

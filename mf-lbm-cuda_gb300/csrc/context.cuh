@@ -54,6 +54,7 @@ struct DeviceState {
     void* phi_prev = nullptr;          // phi at the previous tracking monitor call (s4)
     double* prof = nullptr;            // per-slice and per-block monitor partials
     uint32_t* dither = nullptr;        // step counter of 16-bit stochastic rounding: [0] read by odd, [1] by even steps
+    int8_t* iface = nullptr;           // s2: 1 where the normal record is non-zero (|grad phi| >= 1e-6, type <= 0)
 };
 
 }  // namespace mflbm

@@ -33,6 +33,7 @@ template <class T> struct GradArgs {
     T* phi;
     V4* cn;    // s2: (n_x, n_y, n_z, |grad phi|)
     V4* aux;   // fluid-list order: (n_x, n_y, n_z, 0.5 * gamma * curv * c_norm)
+    int8_t* iface;  // s2: 1 where the record is non-zero
     T *cnx, *cny, *cnz, *cnorm, *curv;  // reference-layout arrays (export / pack)
     const uint2 *l_phi, *l_cn;
     const uint32_t *l_fluid, *l_norm;
@@ -146,7 +147,9 @@ __global__ void __launch_bounds__(256) normals_kernel(const GradArgs<T> a) {
         if (type == -1 && nrm > T(1e-6)) wetting(a.ph.cos_theta, a.snx[n4], a.sny[n4], a.snz[n4], cx, cy, cz);
         r.x = cx; r.y = cy; r.z = cz; r.w = nrm;
     }
-    a.cn[g.s2(i, j, k)] = r;
+    const ll n2 = g.s2(i, j, k);
+    a.cn[n2] = r;
+    a.iface[n2] = r.w != T(0) ? 1 : 0;
 }
 
 // interface normal on solid boundary nodes = weighted mean over fluid neighbours (:880-906)
@@ -212,7 +215,14 @@ __global__ void __launch_bounds__(256) curvature_kernel(const GradArgs<T> a) {
     const Grid& g = a.g;
     const int sy = g.nx + 4, sz = (g.nx + 4) * (g.ny + 4);
     typename Vec4<T>::type ctr, r;
-    const T cv = curvature_at<T>(a.ph.c, a.cn, (int)g.s2(i, j, k), sy, sz, ctr);
+    const int n2 = (int)g.s2(i, j, k);
+    // Away from interfaces |grad phi| is exactly 0 and the normal record is
+    // all zeros (normals_kernel); the collision's force 0.5 gamma curv
+    // |grad phi| n and its recolouring direction are then zero whatever the
+    // curvature.  Such nodes (iface = 0) get no record: the collision reads
+    // the record only where iface = 1.
+    if (!a.iface[n2]) return;
+    const T cv = curvature_at<T>(a.ph.c, a.cn, n2, sy, sz, ctr);
     r.x = ctr.x; r.y = ctr.y; r.z = ctr.z;
     r.w = T(0.5) * a.ph.gamma * cv * ctr.w;
     a.aux[t] = r;
@@ -255,6 +265,7 @@ __global__ void __launch_bounds__(128) pack_normals_kernel(const GradArgs<T> a) 
         v.x = a.cnx[n]; v.y = a.cny[n]; v.z = a.cnz[n]; v.w = a.cnorm[n];
     }
     a.cn[n] = v;
+    a.iface[n] = v.w != T(0) ? 1 : 0;
 }
 template <class T>
 __global__ void __launch_bounds__(128) aux_from_arrays_kernel(const GradArgs<T> a) {
@@ -280,6 +291,7 @@ GradArgs<T> grad_args(const mflbm_context& c) {
     a.phi = (T*)d.phi;
     a.cn = (typename Vec4<T>::type*)d.cnv4;
     a.aux = (typename Vec4<T>::type*)d.aux;
+    a.iface = d.iface;
     a.cnx = (T*)d.cn_x; a.cny = (T*)d.cn_y; a.cnz = (T*)d.cn_z;
     a.cnorm = (T*)d.c_norm; a.curv = (T*)d.curv;
     a.l_phi = d.list_phi_ext; a.n_phi = (int)d.n_phi_ext;

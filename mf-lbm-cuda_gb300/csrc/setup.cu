@@ -592,8 +592,8 @@ constexpr int kProfSums = 7, kProfExt = 9;  // ext: umax2 usq1 usq2 pre_w pre_nw
 template <class T, class E>
 __global__ void __launch_bounds__(256) monitor_profile_kernel(Grid g, PopView<T, E> P, const uint32_t* list, const int* zoff,
                                                               const T* phi, T* phi_prev,
-                                                              const typename Vec4<T>::type* aux, double force_z,
-                                                              int track, double* out) {
+                                                              const typename Vec4<T>::type* aux, const int8_t* iface,
+                                                              double force_z, int track, double* out) {
     const int kp = blockIdx.x;
     double acc[2 * kProfSums + kProfExt];
 #pragma unroll
@@ -608,7 +608,9 @@ __global__ void __launch_bounds__(256) monitor_profile_kernel(Grid g, PopView<T,
         double rho = 0;
 #pragma unroll
         for (int q = 0; q < 19; ++q) rho += f[q];
-        const typename Vec4<T>::type a = aux[t];
+        typename Vec4<T>::type a;
+        a.x = T(0); a.y = T(0); a.z = T(0); a.w = T(0);
+        if (iface[g.s2(i, j, k)]) a = aux[t];   // the zero record away from interfaces
         const double tmp = (double)a.w;
         const double fx = tmp * (double)a.x, fy = tmp * (double)a.y, fz = tmp * (double)a.z + force_z;
         const double u = f[1] - f[2] + f[7] - f[8] + f[9] - f[10] + f[11] - f[12] + f[13] - f[14] - 0.5 * fx;
@@ -666,7 +668,7 @@ int monitor_profile_t(mflbm_context& c, double* slices, mflbm_monitor_ext* ext, 
     }
     monitor_profile_kernel<T, E><<<nb, 256, 0, c.stream>>>(g, pop_view<T, E>(d), d.fluid_list, d.zpair_off,
                                                         (const T*)d.phi, (T*)d.phi_prev,
-                                                        (const typename Vec4<T>::type*)d.aux,
+                                                        (const typename Vec4<T>::type*)d.aux, d.iface,
                                                         (double)T(c.params.force_z), track ? 1 : 0, d.prof);
     int rc = after_launch("monitor_profile");
     if (rc != MFLBM_OK) return rc;
