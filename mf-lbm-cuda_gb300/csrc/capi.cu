@@ -55,7 +55,7 @@ void free_all(mflbm_context* c) {
     void* ptrs[] = {d.pdf, d.phi, d.cn_x, d.cn_y, d.cn_z, d.c_norm, d.curv, d.W_in, d.f_cv, d.g_cv, d.phi_cv,
                     d.walls, d.walls_type, d.s_nx, d.s_ny, d.s_nz, d.fluid_list, d.list_phi_ext,
                     d.list_cn_ext, d.red, d.staging, d.aux, d.type8, d.cnv4, d.list_norm, d.zpair_off,
-                    d.phi_prev, d.prof, d.dither, d.iface};
+                    d.phi_prev, d.prof, d.dither, d.iface, d.phib};
     for (void* p : ptrs) if (p) cudaFree(p);
     d = DeviceState{};
     if (c->pair_graph) cudaGraphExecDestroy(c->pair_graph);
@@ -309,7 +309,8 @@ int mflbm_create(const mflbm_params* params, mflbm_context** out) {
         {&d.f_cv, T * g.plane1() * 19}, {&d.g_cv, T * g.plane1() * 19}, {&d.phi_cv, T * g.plane1()},
         {(void**)&d.walls, sizeof(int32_t) * g.n2()}, {(void**)&d.walls_type, sizeof(int32_t) * g.n4()},
         {&d.s_nx, T * g.n4()}, {&d.s_ny, T * g.n4()}, {&d.s_nz, T * g.n4()},
-        {(void**)&d.dither, 2 * sizeof(uint32_t)}, {(void**)&d.iface, (size_t)g.n2()}};
+        {(void**)&d.dither, 2 * sizeof(uint32_t)}, {(void**)&d.iface, (size_t)g.n2()},
+        {(void**)&d.phib, (size_t)((g.nx + 9) / 2) * ((g.ny + 9) / 2) * ((g.nz + 9) / 2)}};
     for (auto& a : allocs) {
         if ((rc = alloc_zero(a.p, a.bytes, c->stream)) != MFLBM_OK) {
             free_all(c);

@@ -55,6 +55,7 @@ struct DeviceState {
     double* prof = nullptr;            // per-slice and per-block monitor partials
     uint32_t* dither = nullptr;        // step counter of 16-bit stochastic rounding: [0] read by odd, [1] by even steps
     int8_t* iface = nullptr;           // s2: 1 where the normal record is non-zero (|grad phi| >= 1e-6, type <= 0)
+    int8_t* phib = nullptr;            // per 2x2x2 brick of the s4 lattice: 1 all phi = +1, 2 all phi = -1, else 0
 };
 
 }  // namespace mflbm

@@ -34,6 +34,7 @@ template <class T> struct GradArgs {
     V4* cn;    // s2: (n_x, n_y, n_z, |grad phi|)
     V4* aux;   // fluid-list order: (n_x, n_y, n_z, 0.5 * gamma * curv * c_norm)
     int8_t* iface;  // s2: 1 where the record is non-zero
+    int8_t* phib;   // per 2x2x2 brick of the s4 lattice: 1 all phi = +1, 2 all phi = -1, else 0
     T *cnx, *cny, *cnz, *cnorm, *curv;  // reference-layout arrays (export / pack)
     const uint2 *l_phi, *l_cn;
     const uint32_t *l_fluid, *l_norm;
@@ -123,6 +124,40 @@ __device__ __forceinline__ T iso4_dz(const ModelConsts<T>& c, const T* F, int n,
                       F[n + sy + sz] - F[n - sy - sz] + F[n - sy + sz] - F[n + sy - sz]);
 }
 
+// Bulk detection for the normal pass: per 2x2x2 brick of the s4 lattice
+// (s4-local coordinates 2b, 2b + 1 on each axis; positions past the lattice
+// end are ignored), 1 if every phi is exactly +1, 2 if every phi is exactly -1,
+// 0 otherwise.  Away from interfaces phi is exactly +-1 (one component is
+// exactly zero), so most bricks are uniform.
+template <class T>
+__global__ void __launch_bounds__(256) phi_brick_kernel(const GradArgs<T> a) {
+    typedef typename Vec2<T>::type P;
+    const int NX = a.g.nx + 8, NY = a.g.ny + 8, NZ = a.g.nz + 8;
+    const int BX = (NX + 1) >> 1, BY = (NY + 1) >> 1, BZ = (NZ + 1) >> 1;
+    const ll b = (ll)blockIdx.x * blockDim.x + threadIdx.x;   // bricks in x-fastest order
+    if (b >= (ll)BX * BY * BZ) return;
+    const int bx = (int)(b % BX), by = (int)((b / BX) % BY), bz = (int)(b / ((ll)BX * BY));
+    bool plus = true, minus = true;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        const int y = 2 * by + (e & 1), z = 2 * bz + (e >> 1);
+        if (y >= NY || z >= NZ) continue;
+        const T* row = a.phi + (ll)NX * (y + (ll)NY * z);
+        T v0, v1;
+        if (!(NX & 1)) {            // even rows: every row starts on a pair boundary
+            const P v = reinterpret_cast<const P*>(row)[bx];
+            v0 = v.x;
+            v1 = v.y;
+        } else {
+            v0 = row[2 * bx];
+            v1 = 2 * bx + 1 < NX ? row[2 * bx + 1] : v0;
+        }
+        plus = plus && v0 == T(1) && v1 == T(1);
+        minus = minus && v0 == T(-1) && v1 == T(-1);
+    }
+    a.phib[b] = plus ? 1 : minus ? 2 : 0;
+}
+
 // unit interface normal and |grad phi| at the fluid nodes of [-1, n+2]^3
 // (:757-807) + wetting (:809-878)
 template <class T>
@@ -134,6 +169,25 @@ __global__ void __launch_bounds__(256) normals_kernel(const GradArgs<T> a) {
     const Grid& g = a.g;
     const int sy4 = g.nx + 8, sz4 = (g.nx + 8) * (g.ny + 8);
     const int n4 = (int)g.s4(i, j, k);
+    const ll n2 = g.s2(i, j, k);
+    {
+        // The stencil (s4-local i+2 .. i+4 on each axis) lies in the 2x2x2
+        // bricks (i+2)>>1 .. +1: if they are uniform with one value, every
+        // difference in the ISO4 sums is +0, |grad phi| = 0 and the record is
+        // the zero record -- written without reading the 18 neighbours.
+        const int BX = (g.nx + 9) >> 1, BY = (g.ny + 9) >> 1;
+        const int bx = (i + 2) >> 1, by = (j + 2) >> 1, bz = (k + 2) >> 1;
+        const int8_t* pb = a.phib + bx + (ll)BX * (by + (ll)BY * bz);
+        const int8_t c0 = pb[0];
+        if (c0 != 0 && pb[1] == c0 && pb[BX] == c0 && pb[BX + 1] == c0 && pb[(ll)BX * BY] == c0 &&
+            pb[(ll)BX * BY + 1] == c0 && pb[(ll)BX * BY + BX] == c0 && pb[(ll)BX * BY + BX + 1] == c0) {
+            typename Vec4<T>::type r;
+            r.x = T(0); r.y = T(0); r.z = T(0); r.w = T(0);
+            a.cn[n2] = r;
+            a.iface[n2] = 0;
+            return;
+        }
+    }
     const T x = iso4_dx(a.ph.c, a.phi, n4, sy4, sz4);
     const T y = iso4_dy(a.ph.c, a.phi, n4, sy4, sz4);
     const T z = iso4_dz(a.ph.c, a.phi, n4, sy4, sz4);
@@ -147,7 +201,6 @@ __global__ void __launch_bounds__(256) normals_kernel(const GradArgs<T> a) {
         if (type == -1 && nrm > T(1e-6)) wetting(a.ph.cos_theta, a.snx[n4], a.sny[n4], a.snz[n4], cx, cy, cz);
         r.x = cx; r.y = cy; r.z = cz; r.w = nrm;
     }
-    const ll n2 = g.s2(i, j, k);
     a.cn[n2] = r;
     a.iface[n2] = r.w != T(0) ? 1 : 0;
 }
@@ -162,6 +215,19 @@ __global__ void __launch_bounds__(256) extrapolate_normal_kernel(const GradArgs<
     unpack_xyz(e.x, i, j, k);
     const int sy = a.g.nx + 4, sz = (a.g.nx + 4) * (a.g.ny + 4);
     const int n = (int)a.g.s2(i, j, k);
+    // fluid neighbours whose record is the zero record (interface flag 0)
+    // contribute +0 to every sum: when all of them are such, the mean is +0
+    // and only the flags (1 byte each) are read
+    bool any = false;
+#pragma unroll
+    for (int q = 1; q < 19; ++q)
+        if (e.y & (1u << q)) any = any || a.iface[n + ex(q) + ey(q) * sy + ez(q) * sz];
+    if (!any) {
+        typename Vec4<T>::type r = a.cn[n];
+        r.x = T(0); r.y = T(0); r.z = T(0);
+        a.cn[n] = r;
+        return;
+    }
     T sx = T(0), syy = T(0), szz = T(0), ws = T(0);
 #pragma unroll
     for (int q = 1; q < 19; ++q) {
@@ -292,6 +358,7 @@ GradArgs<T> grad_args(const mflbm_context& c) {
     a.cn = (typename Vec4<T>::type*)d.cnv4;
     a.aux = (typename Vec4<T>::type*)d.aux;
     a.iface = d.iface;
+    a.phib = d.phib;
     a.cnx = (T*)d.cn_x; a.cny = (T*)d.cn_y; a.cnz = (T*)d.cn_z;
     a.cnorm = (T*)d.c_norm; a.curv = (T*)d.curv;
     a.l_phi = d.list_phi_ext; a.n_phi = (int)d.n_phi_ext;
@@ -315,6 +382,9 @@ int launch_gradient(mflbm_context& c) {
         if ((rc = after_launch("extrapolate_phi")) != MFLBM_OK) return rc;
     }
     if (a.n_norm) {
+        const Grid& g = c.d.g;
+        phi_brick_kernel<T><<<grid_for((ll)((g.nx + 9) / 2) * ((g.ny + 9) / 2) * ((g.nz + 9) / 2), 256), 256, 0, s>>>(a);
+        if ((rc = after_launch("phi_brick")) != MFLBM_OK) return rc;
         normals_kernel<T><<<grid_for(a.n_norm, tn.normals), tn.normals, 0, s>>>(a);
         if ((rc = after_launch("normals")) != MFLBM_OK) return rc;
     }

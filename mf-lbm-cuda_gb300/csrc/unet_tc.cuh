@@ -117,14 +117,24 @@ __device__ __forceinline__ uint32_t tc_setup(uint32_t* tslot, uint64_t* bars, ui
     return *tslot;
 }
 
+// one thread waits (bounded) for the phase of a stage's barrier, then the
+// block synchronises on the result, so the other threads do not spend issue
+// slots polling; false (for every thread) on a time-out
+__device__ __forceinline__ bool tc_wait_stage(uint64_t* bar, uint32_t parity) {
+    bool ok = true;
+    if (threadIdx.x == 0) ok = mbar_wait(bar, parity);
+    return __syncthreads_and(ok);
+}
+
 // after `issued` stages (stage s committed to bars[s & 1]): wait (bounded)
 // for the last commit of each barrier; uniform over the block
 __device__ __forceinline__ bool tc_drain(uint64_t* bars, int issued) {
     bool done = true;
-    for (int b = 0; b < 2; ++b) {
-        const int uses = (issued + 1 - b) >> 1;
-        if (uses > 0 && !mbar_wait(&bars[b], (uses - 1) & 1)) done = false;
-    }
+    if (threadIdx.x == 0)
+        for (int b = 0; b < 2; ++b) {
+            const int uses = (issued + 1 - b) >> 1;
+            if (uses > 0 && !mbar_wait(&bars[b], (uses - 1) & 1)) done = false;
+        }
     return __syncthreads_and(done);
 }
 
@@ -173,6 +183,7 @@ __global__ void __launch_bounds__(128) conv3d_fwd_tc_kernel(Dims d, const bf16* 
     const int cb = (int)(((long long)blockIdx.z * chunks) / ksplit), ce = (int)(((long long)(blockIdx.z + 1) * chunks) / ksplit);
     const int stages = (ce - cb + 3) >> 2;
     const int v = m0 + tid;                   // the A row this thread gathers
+    const int vx = v % d.W, vy = (v / d.W) % d.H, vz = v / (d.W * d.H);
     const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
     bool ok = true;
     int issued = 0;
@@ -181,16 +192,17 @@ __global__ void __launch_bounds__(128) conv3d_fwd_tc_kernel(Dims d, const bf16* 
         uint8_t* A = sm + st * STAGE;
         uint8_t* B = A + TC_A_BYTES;
         // the stage's previous MMAs must be done before it is overwritten
-        if (s >= 2 && !__syncthreads_and(mbar_wait(&bars[st], ((s - 2) >> 1) & 1))) { ok = false; break; }
+        if (s >= 2 && !tc_wait_stage(&bars[st], ((s - 2) >> 1) & 1)) { ok = false; break; }
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
             const int ch = cb + 4 * s + i;
             uint4 lo = zero, hi = zero;
             if (ch < ce && v < V) {
                 const int tap = ch / cpt, c0 = (ch - tap * cpt) << 4;
-                const int nb = neighbour(d, v, tap);
-                if (nb >= 0) {
-                    const uint4* src = reinterpret_cast<const uint4*>(x + (size_t)nb * cin + c0);
+                const int xx = vx + tap % 3 - 1, yy = vy + (tap / 3) % 3 - 1, zz = vz + tap / 9 - 1;
+                if (xx >= 0 && yy >= 0 && zz >= 0 && xx < d.W && yy < d.H && zz < d.D) {
+                    const uint4* src =
+                        reinterpret_cast<const uint4*>(x + (((size_t)zz * d.H + yy) * d.W + xx) * cin + c0);
                     lo = src[0];
                     hi = src[1];
                 }
@@ -303,7 +315,7 @@ __global__ void __launch_bounds__(128) conv3d_wgrad_tc_kernel(Dims d, const bf16
         uint8_t* B = A + TC_A_BYTES;
         int* uc = ucoord + st * 64;
         const int u0 = vb + s * TC_K;
-        if (s >= 2 && !__syncthreads_and(mbar_wait(&bars[st], ((s - 2) >> 1) & 1))) { ok = false; break; }
+        if (s >= 2 && !tc_wait_stage(&bars[st], ((s - 2) >> 1) & 1)) { ok = false; break; }
         if (tid < 64) {
             const int u = u0 + tid;
             uc[tid] = u < ve ? ((u % d.W) | (((u / d.W) % d.H) << 10) | ((u / (d.W * d.H)) << 20)) : -1;
