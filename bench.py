@@ -269,6 +269,7 @@ def main():
     ap.add_argument("--size", type=int, default=256, help="lattice edge (default: the 256^3 workload)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the 16-bit storage and batch measurements")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default block sizes (no autotuning)")
     args = ap.parse_args()
     warmup = max(3, args.warmup)
 
@@ -323,6 +324,11 @@ def main():
     ctx.run(nt, warmup)
     nt += warmup
     ctx.sync()
+    # block sizes of the step kernels from the library's autotuner (state unchanged)
+    tuning = None
+    if not args.no_tune:
+        t = ctx.autotune(3)
+        tuning = {k: t[k] for k in ("collide_block", "normals_block", "curvature_block", "extrapolate_block")}
 
     # ---- timed region: K steps, state resident in HBM, graph-replayed ----
     sampler = ClockSampler(local)
@@ -411,7 +417,8 @@ def main():
         "config": {"workload": case.name, "lattice": [nx, ny, nz], "fluid_nodes": n_fluid,
                    "porosity": round(porosity, 4), "precision": "fp32 populations, fp32 collision",
                    "fp_mode": "fast", "l2": "inputs larger than L2 (populations 2.6 GB per replica), no flush",
-                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "block_sizes": tuning or "defaults (128)"},
         "mflups": round(world * n_fluid * args.steps / (t_max * 1e-3) / 1e6, 2),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(achieved / hbm, 4), "peak_kind": peak_kind,
