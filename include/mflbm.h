@@ -216,6 +216,13 @@ int mflbm_init_fields(mflbm_context* ctx, int initial_fluid_distribution_option,
  * (rho = 1, velocity 0).  Call after mflbm_init_fields / mflbm_upload_fields. */
 int mflbm_init_flow(mflbm_context* ctx, const void* rho, const void* u,
                     const void* v, const void* w);
+/* No counterpart in the reference: the same fill with the energy-square
+ * moment of the total populations set to the equilibrium of the collision
+ * itself (the reference's MRT has 0 there at rest, the lattice weights give
+ * 3 rho), so that the state starts on the collision's equilibrium instead of
+ * relaxing that moment in the first steps -- the warm start's fill. */
+int mflbm_init_flow_mrt(mflbm_context* ctx, const void* rho, const void* u,
+                        const void* v, const void* w);
 
 /* Reference: MemAllocate_multi_GPU(1) (src/Init_multiphase_GPU.cu:73-104):
  * upload a full host state.  Any pointer except pdf and phi may be NULL

@@ -422,7 +422,7 @@ int mflbm_init_fields(mflbm_context* c, int option, double interface_z0, const v
     return MFLBM_OK;
 }
 
-int mflbm_init_flow(mflbm_context* c, const void* rho, const void* u, const void* v, const void* w) {
+static int init_flow_entry(mflbm_context* c, const void* rho, const void* u, const void* v, const void* w, int mrt) {
     if (!c) return fail(MFLBM_E_ARG, "null context");
     if (!c->have_fields) return fail(MFLBM_E_STATE, "mflbm_init_flow needs phi (mflbm_init_fields or mflbm_upload_fields first)");
     const Grid& g = c->d.g;
@@ -437,10 +437,18 @@ int mflbm_init_flow(mflbm_context* c, const void* rho, const void* u, const void
         MFLBM_CUDA(cudaMemcpyAsync(dst, host[a], n, cudaMemcpyHostToDevice, c->stream));
         dev[a] = dst;
     }
-    if ((rc = init_flow(*c, dev[0], dev[1], dev[2], dev[3])) != MFLBM_OK) return rc;
+    if ((rc = init_flow(*c, dev[0], dev[1], dev[2], dev[3], mrt)) != MFLBM_OK) return rc;
     MFLBM_CUDA(cudaStreamSynchronize(c->stream));
     c->d.arrays_stale = true;
     return MFLBM_OK;
+}
+
+int mflbm_init_flow(mflbm_context* c, const void* rho, const void* u, const void* v, const void* w) {
+    return init_flow_entry(c, rho, u, v, w, 0);
+}
+
+int mflbm_init_flow_mrt(mflbm_context* c, const void* rho, const void* u, const void* v, const void* w) {
+    return init_flow_entry(c, rho, u, v, w, 1);
 }
 
 int mflbm_upload_fields(mflbm_context* c, const void* pdf, const void* phi, const void* cn_x, const void* cn_y,

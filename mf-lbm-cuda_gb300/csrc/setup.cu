@@ -251,9 +251,17 @@ __global__ void init_phi(Grid g, int option, T z0, int open_z, T phi_inlet, T* p
 // f_q = r w_q (1 + 3 c.u + 4.5 (c.u)^2 - 1.5 u.u) with r = rho (1 +- phi) / 2
 // per component; rho, u, v, w in the (nx+2)(ny+2)(nz+2) layout, NULL for
 // rho = 1 and u = v = w = 0 (the rest state of the cold start).
+// mrt = 1: the energy-square moment of the total populations is set to the
+// collision's own equilibrium, e2 = mrt_e2_coef1 rho + mrt_e2_coef2 j^2 (the
+// MRT of collide(): 0 at rest), instead of the 3 rho that the lattice weights
+// give; the correction lies along that moment's basis vector (12 rest, -4
+// axis, 1 diagonal; no mass or momentum) and is shared between the two
+// components in proportion to their densities.  Without it the first
+// collisions relax that moment from 3 rho to 0, an impulse that shows up as a
+// velocity transient of several times the flow itself.
 template <class T, class E>
 __global__ void init_pdf(Grid g, PopView<T, E> P, ModelConsts<T> c, const T* phi, const T* rho, const T* u,
-                         const T* v, const T* w) {
+                         const T* v, const T* w, int mrt = 0) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y, k = blockIdx.z;
     if (i > g.nx + 1) return;
@@ -263,8 +271,21 @@ __global__ void init_pdf(Grid g, PopView<T, E> P, ModelConsts<T> c, const T* phi
     const T ux = u ? u[n1] : T(0), uy = v ? v[n1] : T(0), uz = w ? w[n1] : T(0);
     const T r[2] = {rh * (T(1.0) + ph) * T(0.5), rh * (T(1.0) - ph) * T(0.5)};
     const T usqrt = ux * ux + uy * uy + uz * uz;
+    T e2_shift = T(0);   // (target - current) / 252 of the total energy-square moment
+    if (mrt) {
+        T e2 = T(0);
+        for (int q = 0; q < 19; ++q) {
+            const T wq = q == 0 ? c.w0 : q < 7 ? c.w1 : c.w2;
+            const T cu = T(ex(q)) * ux + T(ey(q)) * uy + T(ez(q)) * uz;
+            const T feq = rh * wq * (T(1) + T(3) * cu + T(4.5) * cu * cu - T(1.5) * usqrt);
+            e2 += (q == 0 ? T(12) : q < 7 ? T(-4) : T(1)) * feq;
+        }
+        const T jx = rh * ux, jy = rh * uy, jz = rh * uz;
+        e2_shift = (c.mrt_e2_coef1 * rh + c.mrt_e2_coef2 * (jx * jx + jy * jy + jz * jz) - e2) / T(252);
+    }
     for (int gg = 0; gg < 2; ++gg) {
-        P.set(i, j, k, 0, gg, r[gg] * c.w0 + r[gg] * c.w0 * (T(-1.5) * usqrt));
+        const T share = mrt ? r[gg] / rh : T(0);
+        P.set(i, j, k, 0, gg, r[gg] * c.w0 + r[gg] * c.w0 * (T(-1.5) * usqrt) + share * T(12) * e2_shift);
         for (int q = 1; q < 19; ++q) {
             const T wq = q < 7 ? c.w1 : c.w2;
             // the reference's per-direction sums: only the non-zero components, left to right
@@ -278,7 +299,9 @@ __global__ void init_pdf(Grid g, PopView<T, E> P, ModelConsts<T> c, const T* phi
                 cu = first ? term : cu + term;
                 first = false;
             }
-            P.set(i, j, k, q, gg, r[gg] * wq + r[gg] * wq * (T(3.0) * cu + T(4.5) * cu * cu - T(1.5) * usqrt));
+            T f = r[gg] * wq + r[gg] * wq * (T(3.0) * cu + T(4.5) * cu * cu - T(1.5) * usqrt);
+            if (mrt) f += share * (q < 7 ? T(-4) : T(1)) * e2_shift;
+            P.set(i, j, k, q, gg, f);
         }
     }
 }
@@ -329,13 +352,13 @@ int init_fields_t(mflbm_context& c, int option, double z0) {
 // warm-start entry): rho, u, v, w are device arrays of (nx+2)(ny+2)(nz+2) T,
 // any of them NULL.  The convective outlet buffers follow the new populations.
 template <class T, class E>
-int init_flow_t(mflbm_context& c, const void* rho, const void* u, const void* v, const void* w) {
+int init_flow_t(mflbm_context& c, const void* rho, const void* u, const void* v, const void* w, int mrt) {
     DeviceState& d = c.d;
     const Grid g = d.g;
     cudaStream_t s = c.stream;
     int rc;
     init_pdf<T, E><<<dim3(grid_for(g.nx + 2, 128), g.ny + 2, g.nz + 2), 128, 0, s>>>(
-        g, pop_view<T, E>(d), make_consts<T>(), (const T*)d.phi, (const T*)rho, (const T*)u, (const T*)v, (const T*)w);
+        g, pop_view<T, E>(d), make_consts<T>(), (const T*)d.phi, (const T*)rho, (const T*)u, (const T*)v, (const T*)w, mrt);
     if ((rc = after_launch("init_pdf")) != MFLBM_OK) return rc;
     if (c.params.outlet_BC == 1) {
         init_convective<T, E><<<dim3(grid_for(g.nx + 2, 128), g.ny + 2), 128, 0, s>>>(g, pop_view<T, E>(d), (const T*)d.phi, (T*)d.f_cv, (T*)d.g_cv, (T*)d.phi_cv);
@@ -740,8 +763,8 @@ int preprocess_geometry(mflbm_context& c, const int32_t* walls_global, int iper)
 }
 
 int init_fields(mflbm_context& c, int option, double z0) { return MFLBM_POP(init_fields_t, c, option, z0); }
-int init_flow(mflbm_context& c, const void* rho, const void* u, const void* v, const void* w) {
-    return MFLBM_POP(init_flow_t, c, rho, u, v, w);
+int init_flow(mflbm_context& c, const void* rho, const void* u, const void* v, const void* w, int mrt) {
+    return MFLBM_POP(init_flow_t, c, rho, u, v, w, mrt);
 }
 
 int monitor(mflbm_context& c, int nex_in, int nex_out, mflbm_monitor* out) {

@@ -52,6 +52,7 @@ SIGNATURES = {
     "mflbm_write_checkpoint": (I, [VP, I, C.c_char_p]),
     "mflbm_read_checkpoint": (I, [VP, C.c_char_p, VP, C.POINTER(I)]),
     "mflbm_init_flow": (I, [VP, VP, VP, VP, VP]),
+    "mflbm_init_flow_mrt": (I, [VP, VP, VP, VP, VP]),
     "mflbm_unet_create": (I, [I, I, I, C.c_ulonglong, C.POINTER(VP)]),
     "mflbm_unet_destroy": (I, [VP]),
     "mflbm_unet_param_count": (I, [VP, C.POINTER(LL)]),
@@ -182,15 +183,17 @@ class Context:
         check(self.lib.mflbm_download_fields(self.h, *[ptr(out.get(n)) for n in order]), "mflbm_download_fields")
         return out
 
-    def init_flow(self, rho=None, u=None, v=None, w=None):
-        """mflbm_init_flow: equilibrium populations from macroscopic fields
-        (arrays of shape (nz+2, ny+2, nx+2) or flat, any of them None)."""
+    def init_flow(self, rho=None, u=None, v=None, w=None, mrt=False):
+        """mflbm_init_flow (mrt: mflbm_init_flow_mrt): equilibrium populations
+        from macroscopic fields (arrays of shape (nz+2, ny+2, nx+2) or flat,
+        any of them None)."""
         a = [None if f is None else np.ascontiguousarray(f, dtype=self.T).ravel() for f in (rho, u, v, w)]
         n = (self.params.nx + 2) * (self.params.ny + 2) * (self.params.nz + 2)
         for f in a:
             if f is not None and f.size != n:
                 raise ValueError(f"init_flow: expected {n} values per field, got {f.size}")
-        check(self.lib.mflbm_init_flow(self.h, *[ptr(f) for f in a]), "mflbm_init_flow")
+        fn = self.lib.mflbm_init_flow_mrt if mrt else self.lib.mflbm_init_flow
+        check(fn(self.h, *[ptr(f) for f in a]), "mflbm_init_flow")
 
     def step(self, ntime):
         check(self.lib.mflbm_step(self.h, int(ntime)), "mflbm_step")

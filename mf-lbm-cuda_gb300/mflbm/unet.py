@@ -4,10 +4,11 @@ glue between it and the lattice.
 The network maps a pore geometry (solid mask and signed distance to the
 nearest solid, both per lattice node) to a normalised flow field (u, v, w, p).
 A warm start evaluates it, turns the prediction into physical fields and
-fills the populations with their equilibrium (``mflbm_init_flow``, the
+fills the populations with their equilibrium (``mflbm_init_flow_mrt``: the
 equilibrium fill of the reference's initialization_new_multi_pdf,
-src/Init_multiphase.cpp:389-496); the plain lattice Boltzmann run then
-converges from there.  Normalisation: velocities are stored as u nu / g and
+src/Init_multiphase.cpp:389-496, with the energy-square moment on the MRT
+collision's own equilibrium); the plain lattice Boltzmann run then converges
+from there.  Normalisation: velocities are stored as u nu / g and
 pressure as (rho - <rho>) / (3 g), each divided by its training-set scale, so
 that a single network serves any body force g and viscosity nu of the Stokes
 regime.
@@ -174,9 +175,11 @@ def flow_target(ctx, walls_global, nu, g):
     return t, fluid.astype(np.float32)
 
 
-def fill_from_prediction(ctx, y, walls_global, nu, g, scales):
-    """Equilibrium populations from a normalised prediction y [nz, ny, nx, 4]
-    (mflbm_init_flow); velocity zero in solids, halos periodic in y and z."""
+def fill_from_prediction(ctx, y, walls_global, nu, g, scales, mrt=True):
+    """Equilibrium populations from a normalised prediction y [nz, ny, nx, 4];
+    velocity zero in solids, halos periodic in y and z.  mrt: the collision's
+    own equilibrium (mflbm_init_flow_mrt), else the reference's a17 formula
+    with the lattice weights (mflbm_init_flow)."""
     L = ctx.L
     nx, ny, nz = L.nx, L.ny, L.nz
     solid = (np.asarray(walls_global).reshape(nz, ny, nx) != 0)
@@ -192,7 +195,7 @@ def fill_from_prediction(ctx, y, walls_global, nu, g, scales):
         p = np.pad(f, ((1, 1), (1, 1), (0, 0)), mode="wrap")        # z, y periodic
         return np.pad(p, ((0, 0), (0, 0), (1, 1)), constant_values=fill)
     rho, u, v, w = halo(fields[0], 1.0), halo(fields[1], 0.0), halo(fields[2], 0.0), halo(fields[3], 0.0)
-    ctx.init_flow(rho, u, v, w)
+    ctx.init_flow(rho, u, v, w, mrt=mrt)
 
 
 def predicted_permeability(y, scales, nx, ny, nz):

@@ -121,5 +121,17 @@ def test_init_flow_fills_the_equilibrium(mflbm_lib):
             cu = unet.EX[q] * u + unet.EY[q] * v + unet.EZ[q] * w
             ref = r * wq[q] * (1 + 3 * cu + 4.5 * cu * cu - 1.5 * usq)
             assert np.allclose(pdf[gg, q], ref, rtol=1e-13, atol=1e-16)
+    # the MRT-consistent fill: same mass and momentum per node, energy-square
+    # moment of the total on the collision's equilibrium (-475/63 j^2)
+    ctx.init_flow(rho, u, v, w, mrt=True)
+    pm = ctx.download(("pdf",))["pdf"].reshape(2, 19, *shp)
+    for gg in range(2):
+        assert np.allclose(pm[gg].sum(0), pdf[gg].sum(0), rtol=1e-13, atol=1e-15)
+        for E in (unet.EX, unet.EY, unet.EZ):
+            assert np.allclose(np.tensordot(E, pm[gg], 1), np.tensordot(E, pdf[gg], 1), rtol=1e-12, atol=1e-15)
+    f = pm[0] + pm[1]
+    b = np.array([12.0] + [-4.0] * 6 + [1.0] * 12)
+    j2 = sum((rho * c) ** 2 for c in (u, v, w))
+    assert np.allclose(np.tensordot(b, f, 1), -475.0 / 63.0 * j2, rtol=1e-9, atol=1e-13)
     ctx.close()
 
