@@ -55,7 +55,7 @@ void free_all(mflbm_context* c) {
     void* ptrs[] = {d.pdf, d.phi, d.cn_x, d.cn_y, d.cn_z, d.c_norm, d.curv, d.W_in, d.f_cv, d.g_cv, d.phi_cv,
                     d.walls, d.walls_type, d.s_nx, d.s_ny, d.s_nz, d.fluid_list, d.list_phi_ext,
                     d.list_cn_ext, d.red, d.staging, d.aux, d.type8, d.cnv4, d.list_norm, d.zpair_off,
-                    d.phi_prev, d.prof, d.dither, d.iface, d.phib};
+                    d.phi_prev, d.prof, d.dither, d.iface, d.phib, d.tmap, d.ilist, d.ilist_n};
     for (void* p : ptrs) if (p) cudaFree(p);
     d = DeviceState{};
     if (c->pair_graph) cudaGraphExecDestroy(c->pair_graph);
@@ -126,6 +126,21 @@ int build_lists(mflbm_context* c) {
             }
     int rc;
     if ((rc = upload_list(&d.fluid_list, &d.n_fluid, fl)) != MFLBM_OK) return rc;
+    {
+        std::vector<int32_t> tm(g.n2(), -1);
+        for (size_t n = 0; n < fl.size(); ++n) {
+            int x, y, z;
+            unpack_xyz(fl[n], x, y, z);
+            tm[g.s2(x, y, z)] = (int32_t)n;
+        }
+        ll ntm = 0;
+        if ((rc = upload_list(&d.tmap, &ntm, tm)) != MFLBM_OK) return rc;
+        if (d.ilist) cudaFree(d.ilist);
+        d.ilist = nullptr;
+        MFLBM_CUDA(cudaMalloc(&d.ilist, sizeof(uint32_t) * std::max<ll>(1, d.n_fluid)));
+        if (!d.ilist_n) MFLBM_CUDA(cudaMalloc(&d.ilist_n, sizeof(int)));
+        MFLBM_CUDA(cudaMemset(d.ilist_n, 0, sizeof(int)));
+    }
     if ((rc = upload_list(&d.list_phi_ext, &d.n_phi_ext, lphi)) != MFLBM_OK) return rc;
     if ((rc = upload_list(&d.list_cn_ext, &d.n_cn_ext, lcn)) != MFLBM_OK) return rc;
     if ((rc = upload_list(&d.list_norm, &d.n_norm, ln)) != MFLBM_OK) return rc;

@@ -54,8 +54,11 @@ struct DeviceState {
     void* phi_prev = nullptr;          // phi at the previous tracking monitor call (s4)
     double* prof = nullptr;            // per-slice and per-block monitor partials
     uint32_t* dither = nullptr;        // step counter of 16-bit stochastic rounding: [0] read by odd, [1] by even steps
-    int8_t* iface = nullptr;           // s2: 1 where the normal record is non-zero (|grad phi| >= 1e-6, type <= 0)
+    int8_t* iface = nullptr;           // s2: 1 where the normal record may be non-zero (|grad phi| >= 1e-6, type <= 0)
     int8_t* phib = nullptr;            // per 2x2x2 brick of the s4 lattice: 1 all phi = +1, 2 all phi = -1, else 0
+    int32_t* tmap = nullptr;           // s2: fluid-list index of a fluid node of [1, n]^3, else -1
+    uint32_t* ilist = nullptr;         // fluid-list indices of this step's interface nodes (normal pass), n_fluid capacity
+    int* ilist_n = nullptr;            // their count
 };
 
 }  // namespace mflbm

@@ -10,10 +10,12 @@
 //      (n_x, n_y, n_z, |grad phi|) per node of the s2 layout.  Solid nodes
 //      keep the zero record the reference writes there every step (records
 //      are zeroed when the geometry is set and when arrays are packed).
+//      The fluid nodes of [1, n]^3 with a non-zero record are appended to a
+//      compact list (the interface nodes of this step).
 //   3. normal on solid boundary nodes (list with masks)
-//   4. curvature at the fluid nodes of [1, n]^3 and the record the collision
-//      reads, (n_x, n_y, n_z, 0.5 * gamma * curv * c_norm), stored in
-//      fluid-list order so that both kernels access it contiguously
+//   4. curvature at the interface nodes and the record the collision reads,
+//      (n_x, n_y, n_z, 0.5 * gamma * curv * c_norm), stored in fluid-list
+//      order so that the collision reads it contiguously
 //
 // The reference-layout arrays cn_x/y/z, c_norm and curv (curvature on all of
 // [1, n]^3, solid nodes included) are produced from the records only when the
@@ -33,8 +35,11 @@ template <class T> struct GradArgs {
     T* phi;
     V4* cn;    // s2: (n_x, n_y, n_z, |grad phi|)
     V4* aux;   // fluid-list order: (n_x, n_y, n_z, 0.5 * gamma * curv * c_norm)
-    int8_t* iface;  // s2: 1 where the record is non-zero
+    int8_t* iface;  // s2 (fluid nodes): 1 where the record may be non-zero; 0: the zero record
     int8_t* phib;   // per 2x2x2 brick of the s4 lattice: 1 all phi = +1, 2 all phi = -1, else 0
+    const int32_t* tmap;   // s2 -> fluid-list index (or -1)
+    uint32_t* ilist;       // interface nodes of this step (fluid-list indices), appended by the normal pass
+    int* ilist_n;
     T *cnx, *cny, *cnz, *cnorm, *curv;  // reference-layout arrays (export / pack)
     const uint2 *l_phi, *l_cn;
     const uint32_t *l_fluid, *l_norm;
@@ -158,6 +163,32 @@ __global__ void __launch_bounds__(256) phi_brick_kernel(const GradArgs<T> a) {
     a.phib[b] = plus ? 1 : minus ? 2 : 0;
 }
 
+// the normal record of node (i, j, k) of walls_type <= 0 (:757-807) + wetting
+// (:809-878): the unit normal and |grad phi|, or the zero record where
+// |grad phi| < 1e-6
+template <class T>
+__device__ __forceinline__ bool normal_at(const GradArgs<T>& a, int i, int j, int k, int type) {
+    const Grid& g = a.g;
+    const int sy4 = g.nx + 8, sz4 = (g.nx + 8) * (g.ny + 8);
+    const int n4 = (int)g.s4(i, j, k);
+    const T x = iso4_dx(a.ph.c, a.phi, n4, sy4, sz4);
+    const T y = iso4_dy(a.ph.c, a.phi, n4, sy4, sz4);
+    const T z = iso4_dz(a.ph.c, a.phi, n4, sy4, sz4);
+    const T nrm = sqrt(x * x + y * y + z * z);
+    typename Vec4<T>::type r;
+    if (nrm < T(1e-6) || type >= 1) {
+        r.x = T(0); r.y = T(0); r.z = T(0); r.w = T(0);
+    } else {
+        T cx = x / nrm, cy = y / nrm, cz = z / nrm;
+        if (type == -1 && nrm > T(1e-6)) wetting(a.ph.cos_theta, a.snx[n4], a.sny[n4], a.snz[n4], cx, cy, cz);
+        r.x = cx; r.y = cy; r.z = cz; r.w = nrm;
+    }
+    const ll n2 = g.s2(i, j, k);
+    a.cn[n2] = r;
+    a.iface[n2] = r.w != T(0) ? 1 : 0;
+    return r.w != T(0);
+}
+
 // unit interface normal and |grad phi| at the fluid nodes of [-1, n+2]^3
 // (:757-807) + wetting (:809-878)
 template <class T>
@@ -167,7 +198,6 @@ __global__ void __launch_bounds__(256) normals_kernel(const GradArgs<T> a) {
     int i, j, k;
     unpack_xyz(a.l_norm[t], i, j, k);
     const Grid& g = a.g;
-    const int sy4 = g.nx + 8, sz4 = (g.nx + 8) * (g.ny + 8);
     const int n4 = (int)g.s4(i, j, k);
     const ll n2 = g.s2(i, j, k);
     {
@@ -181,28 +211,30 @@ __global__ void __launch_bounds__(256) normals_kernel(const GradArgs<T> a) {
         const int8_t c0 = pb[0];
         if (c0 != 0 && pb[1] == c0 && pb[BX] == c0 && pb[BX + 1] == c0 && pb[(ll)BX * BY] == c0 &&
             pb[(ll)BX * BY + 1] == c0 && pb[(ll)BX * BY + BX] == c0 && pb[(ll)BX * BY + BX + 1] == c0) {
-            typename Vec4<T>::type r;
-            r.x = T(0); r.y = T(0); r.z = T(0); r.w = T(0);
-            a.cn[n2] = r;
-            a.iface[n2] = 0;
+            // a record is non-zero only where the interface flag is set: only
+            // those are cleared, every other one is already the zero record
+            if (a.iface[n2]) {
+                typename Vec4<T>::type r;
+                r.x = T(0); r.y = T(0); r.z = T(0); r.w = T(0);
+                a.cn[n2] = r;
+                a.iface[n2] = 0;
+            }
             return;
         }
     }
-    const T x = iso4_dx(a.ph.c, a.phi, n4, sy4, sz4);
-    const T y = iso4_dy(a.ph.c, a.phi, n4, sy4, sz4);
-    const T z = iso4_dz(a.ph.c, a.phi, n4, sy4, sz4);
-    const T nrm = sqrt(x * x + y * y + z * z);
-    const int type = a.type8[n4];
-    typename Vec4<T>::type r;
-    if (nrm < T(1e-6) || type >= 1) {
-        r.x = T(0); r.y = T(0); r.z = T(0); r.w = T(0);
-    } else {
-        T cx = x / nrm, cy = y / nrm, cz = z / nrm;
-        if (type == -1 && nrm > T(1e-6)) wetting(a.ph.cos_theta, a.snx[n4], a.sny[n4], a.snz[n4], cx, cy, cz);
-        r.x = cx; r.y = cy; r.z = cz; r.w = nrm;
+    const bool on = normal_at<T>(a, i, j, k, a.type8[n4]);
+    // fluid nodes of [1, n]^3 with a non-zero record join the curvature's list
+    // (one atomic per warp; the order of the list does not matter)
+    const int tf = on ? a.tmap[n2] : -1;
+    const unsigned act = __activemask();
+    const unsigned want = __ballot_sync(act, tf >= 0);
+    if (want) {
+        const int lane = threadIdx.x & 31, leader = __ffs(want) - 1;
+        int base = 0;
+        if (lane == leader) base = atomicAdd(a.ilist_n, __popc(want));
+        base = __shfl_sync(act, base, leader);
+        if (tf >= 0) a.ilist[base + __popc(want & ((1u << lane) - 1u))] = (uint32_t)tf;
     }
-    a.cn[n2] = r;
-    a.iface[n2] = r.w != T(0) ? 1 : 0;
 }
 
 // interface normal on solid boundary nodes = weighted mean over fluid neighbours (:880-906)
@@ -271,27 +303,28 @@ __device__ __forceinline__ T curvature_at(const ModelConsts<T>& c, const typenam
            x * y * (kxy + kyx) + x * z * (kxz + kzx) + y * z * (kzy + kyz);
 }
 
-// curvature at the fluid nodes and the collision's record (fluid-list order)
+// Curvature and the collision's record (fluid-list order) at this step's
+// interface nodes: the list the normal pass appended (fluid nodes with a
+// non-zero normal record).  Away from interfaces |grad phi| is exactly 0 and
+// the normal record is all zeros; the collision's force 0.5 gamma curv
+// |grad phi| n and its recolouring direction are then zero whatever the
+// curvature, and the collision reads the record only where the interface
+// flag is set.  Grid-stride loop over the list (its length is on the device).
 template <class T>
 __global__ void __launch_bounds__(256) curvature_kernel(const GradArgs<T> a) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= a.n_fluid) return;
-    int i, j, k;
-    unpack_xyz(a.l_fluid[t], i, j, k);
     const Grid& g = a.g;
     const int sy = g.nx + 4, sz = (g.nx + 4) * (g.ny + 4);
-    typename Vec4<T>::type ctr, r;
-    const int n2 = (int)g.s2(i, j, k);
-    // Away from interfaces |grad phi| is exactly 0 and the normal record is
-    // all zeros (normals_kernel); the collision's force 0.5 gamma curv
-    // |grad phi| n and its recolouring direction are then zero whatever the
-    // curvature.  Such nodes (iface = 0) get no record: the collision reads
-    // the record only where iface = 1.
-    if (!a.iface[n2]) return;
-    const T cv = curvature_at<T>(a.ph.c, a.cn, n2, sy, sz, ctr);
-    r.x = ctr.x; r.y = ctr.y; r.z = ctr.z;
-    r.w = T(0.5) * a.ph.gamma * cv * ctr.w;
-    a.aux[t] = r;
+    const int n = *a.ilist_n;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const int t = (int)a.ilist[p];
+        int i, j, k;
+        unpack_xyz(a.l_fluid[t], i, j, k);
+        typename Vec4<T>::type ctr, r;
+        const T cv = curvature_at<T>(a.ph.c, a.cn, (int)g.s2(i, j, k), sy, sz, ctr);
+        r.x = ctr.x; r.y = ctr.y; r.z = ctr.z;
+        r.w = T(0.5) * a.ph.gamma * cv * ctr.w;
+        a.aux[t] = r;
+    }
 }
 
 // curvature on all of [1, n]^3 into the reference-layout curv array (export)
@@ -331,7 +364,9 @@ __global__ void __launch_bounds__(128) pack_normals_kernel(const GradArgs<T> a) 
         v.x = a.cnx[n]; v.y = a.cny[n]; v.z = a.cnz[n]; v.w = a.cnorm[n];
     }
     a.cn[n] = v;
-    a.iface[n] = v.w != T(0) ? 1 : 0;
+    // 1 where the record may be non-zero: uploaded arrays can carry a normal
+    // with c_norm = 0, and the next normal pass must clear it
+    a.iface[n] = (v.x != T(0) || v.y != T(0) || v.z != T(0) || v.w != T(0)) ? 1 : 0;
 }
 template <class T>
 __global__ void __launch_bounds__(128) aux_from_arrays_kernel(const GradArgs<T> a) {
@@ -359,6 +394,7 @@ GradArgs<T> grad_args(const mflbm_context& c) {
     a.aux = (typename Vec4<T>::type*)d.aux;
     a.iface = d.iface;
     a.phib = d.phib;
+    a.tmap = d.tmap; a.ilist = d.ilist; a.ilist_n = d.ilist_n;
     a.cnx = (T*)d.cn_x; a.cny = (T*)d.cn_y; a.cnz = (T*)d.cn_z;
     a.cnorm = (T*)d.c_norm; a.curv = (T*)d.curv;
     a.l_phi = d.list_phi_ext; a.n_phi = (int)d.n_phi_ext;
@@ -381,6 +417,7 @@ int launch_gradient(mflbm_context& c) {
         extrapolate_phi_kernel<T><<<grid_for(a.n_phi, tn.extrapolate), tn.extrapolate, 0, s>>>(a);
         if ((rc = after_launch("extrapolate_phi")) != MFLBM_OK) return rc;
     }
+    MFLBM_CUDA(cudaMemsetAsync(c.d.ilist_n, 0, sizeof(int), s));
     if (a.n_norm) {
         const Grid& g = c.d.g;
         phi_brick_kernel<T><<<grid_for((ll)((g.nx + 9) / 2) * ((g.ny + 9) / 2) * ((g.nz + 9) / 2), 256), 256, 0, s>>>(a);
@@ -393,7 +430,9 @@ int launch_gradient(mflbm_context& c) {
         if ((rc = after_launch("extrapolate_normal")) != MFLBM_OK) return rc;
     }
     if (!a.n_fluid) return MFLBM_OK;
-    curvature_kernel<T><<<grid_for(a.n_fluid, tn.curvature), tn.curvature, 0, s>>>(a);
+    // a fixed grid (the interface count is known only on the device)
+    const int blocks = (int)std::min<ll>(grid_for(a.n_fluid, tn.curvature), 152 * 8);
+    curvature_kernel<T><<<blocks, tn.curvature, 0, s>>>(a);
     return after_launch("curvature");
 }
 
