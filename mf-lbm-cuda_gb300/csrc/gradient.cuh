@@ -200,6 +200,7 @@ __global__ void __launch_bounds__(256) normals_kernel(const GradArgs<T> a) {
     const Grid& g = a.g;
     const int n4 = (int)g.s4(i, j, k);
     const ll n2 = g.s2(i, j, k);
+    const int8_t was = a.iface[n2];   // issued with the brick loads below
     {
         // The stencil (s4-local i+2 .. i+4 on each axis) lies in the 2x2x2
         // bricks (i+2)>>1 .. +1: if they are uniform with one value, every
@@ -213,7 +214,7 @@ __global__ void __launch_bounds__(256) normals_kernel(const GradArgs<T> a) {
             pb[(ll)BX * BY + 1] == c0 && pb[(ll)BX * BY + BX] == c0 && pb[(ll)BX * BY + BX + 1] == c0) {
             // a record is non-zero only where the interface flag is set: only
             // those are cleared, every other one is already the zero record
-            if (a.iface[n2]) {
+            if (was) {
                 typename Vec4<T>::type r;
                 r.x = T(0); r.y = T(0); r.z = T(0); r.w = T(0);
                 a.cn[n2] = r;
@@ -254,8 +255,12 @@ __global__ void __launch_bounds__(256) extrapolate_normal_kernel(const GradArgs<
 #pragma unroll
     for (int q = 1; q < 19; ++q)
         if (e.y & (1u << q)) any = any || a.iface[n + ex(q) + ey(q) * sy + ez(q) * sz];
+    // |grad phi| of a solid node is 0 in every record (the geometry set-up and
+    // the array packing write solid records as zero records; only the
+    // direction is extrapolated), so the record is written without reading it
+    typename Vec4<T>::type r;
+    r.w = T(0);
     if (!any) {
-        typename Vec4<T>::type r = a.cn[n];
         r.x = T(0); r.y = T(0); r.z = T(0);
         a.cn[n] = r;
         return;
@@ -272,7 +277,6 @@ __global__ void __launch_bounds__(256) extrapolate_normal_kernel(const GradArgs<
             ws += wq;
         }
     }
-    typename Vec4<T>::type r = a.cn[n];
     r.x = sx / ws; r.y = syy / ws; r.z = szz / ws;
     a.cn[n] = r;
 }
