@@ -386,7 +386,7 @@ def main():
     ctx.upload_fields(**host)
     for s in range(e2e_steps):
         ctx.step(nt + s)
-    out = ctx.download()
+    out = ctx.download(out=host)   # into the same pinned buffers
     e2e_s = time.perf_counter() - t0
     barrier(dist)
     nt += e2e_steps
@@ -394,6 +394,7 @@ def main():
     e2e_value = world * n_all * e2e_steps / e2e_s / 1e6
     assert np.isfinite(out["phi"]).all()
 
+    sparse = ctx.interface_stats()
     mon = ctx.monitor(2, 2)
     extra = {}
     if not args.no_extras:
@@ -437,6 +438,9 @@ def main():
         "saturation": round(mon["saturation"], 6),
         # fluid nodes with a non-zero phase gradient at the end of the e2e leg: the
         # curvature gathers run only there (elsewhere the surface force is zero)
+        # sizes of the last gradient pass's sparse sets (interface nodes, solid
+        # nodes given a normal, fluid nodes whose normal was recomputed)
+        "gradient_sets": sparse,
         "interface_fraction": round(float(np.count_nonzero(
             out["c_norm"].reshape(nz + 4, ny + 4, nx + 4)[2:nz + 2, 2:ny + 2, 2:nx + 2])) / n_fluid, 5),
     }

@@ -251,6 +251,13 @@ int mflbm_step(mflbm_context* ctx, int ntime);
  * CUDA graph of one odd+even pair where possible.  Asynchronous. */
 int mflbm_run(mflbm_context* ctx, int ntime_begin, int nsteps);
 int mflbm_synchronize(mflbm_context* ctx);
+/* Sizes of the last gradient pass's sparse sets (no reference counterpart;
+ * diagnostics of the sparse colour-gradient passes): nodes of [-1, n+2]^3
+ * with a non-zero interface normal, solid boundary nodes that received an
+ * extrapolated normal, and fluid nodes whose normals were recomputed.
+ * Synchronises the context's stream.  Any pointer may be NULL. */
+int mflbm_interface_stats(mflbm_context* ctx, long long* interface_nodes, long long* solid_normals,
+                          long long* active_nodes);
 
 /* FP64 device reductions (Monitor quantities) on the current state; the
  * state must be after an even step (src/Misc.cpp:222-274 semantics).

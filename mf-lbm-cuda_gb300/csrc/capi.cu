@@ -55,7 +55,7 @@ void free_all(mflbm_context* c) {
     void* ptrs[] = {d.pdf, d.phi, d.cn_x, d.cn_y, d.cn_z, d.c_norm, d.curv, d.W_in, d.f_cv, d.g_cv, d.phi_cv,
                     d.walls, d.walls_type, d.s_nx, d.s_ny, d.s_nz, d.fluid_list, d.list_phi_ext,
                     d.list_cn_ext, d.red, d.staging, d.aux, d.type8, d.cnv4, d.list_norm, d.zpair_off,
-                    d.phi_prev, d.prof, d.dither, d.iface, d.phib, d.tmap, d.ilist, d.ilist_n};
+                    d.phi_prev, d.prof, d.dither, d.iface, d.phib, d.tmap, d.olist, d.slist, d.nlist, d.smask, d.gcount};
     for (void* p : ptrs) if (p) cudaFree(p);
     d = DeviceState{};
     if (c->pair_graph) cudaGraphExecDestroy(c->pair_graph);
@@ -135,15 +135,29 @@ int build_lists(mflbm_context* c) {
         }
         ll ntm = 0;
         if ((rc = upload_list(&d.tmap, &ntm, tm)) != MFLBM_OK) return rc;
-        if (d.ilist) cudaFree(d.ilist);
-        d.ilist = nullptr;
-        MFLBM_CUDA(cudaMalloc(&d.ilist, sizeof(uint32_t) * std::max<ll>(1, d.n_fluid)));
-        if (!d.ilist_n) MFLBM_CUDA(cudaMalloc(&d.ilist_n, sizeof(int)));
-        MFLBM_CUDA(cudaMemset(d.ilist_n, 0, sizeof(int)));
     }
     if ((rc = upload_list(&d.list_phi_ext, &d.n_phi_ext, lphi)) != MFLBM_OK) return rc;
     if ((rc = upload_list(&d.list_cn_ext, &d.n_cn_ext, lcn)) != MFLBM_OK) return rc;
     if ((rc = upload_list(&d.list_norm, &d.n_norm, ln)) != MFLBM_OK) return rc;
+    {
+        // lists of the sparse gradient passes (all records start as zero records)
+        int dev = 0;
+        MFLBM_CUDA(cudaGetDevice(&dev));
+        MFLBM_CUDA(cudaDeviceGetAttribute(&d.n_sm, cudaDevAttrMultiProcessorCount, dev));
+        for (void** p : {(void**)&d.olist, (void**)&d.slist, (void**)&d.nlist, (void**)&d.smask, (void**)&d.gcount}) {
+            if (*p) cudaFree(*p);
+            *p = nullptr;
+        }
+        d.n_blocks = (ll)(((g.nx + 4) >> 1) + 1) * (((g.ny + 4) >> 1) + 1) * (((g.nz + 4) >> 1) + 1);
+        const size_t nmask = (size_t)(g.n2() / 32 + 1);
+        MFLBM_CUDA(cudaMalloc(&d.olist, sizeof(uint32_t) * std::max<ll>(1, d.n_norm)));
+        MFLBM_CUDA(cudaMalloc(&d.slist, sizeof(uint32_t) * std::max<ll>(1, d.n_cn_ext)));
+        MFLBM_CUDA(cudaMalloc(&d.nlist, sizeof(uint32_t) * std::max<ll>(1, d.n_norm)));
+        MFLBM_CUDA(cudaMalloc(&d.smask, sizeof(uint32_t) * nmask));
+        MFLBM_CUDA(cudaMalloc(&d.gcount, 4 * sizeof(int)));
+        MFLBM_CUDA(cudaMemset(d.smask, 0, sizeof(uint32_t) * nmask));
+        MFLBM_CUDA(cudaMemset(d.gcount, 0, 4 * sizeof(int)));
+    }
     ll nzo = 0;
     if ((rc = upload_list(&d.zpair_off, &nzo, zoff)) != MFLBM_OK) return rc;
     if (d.phi_prev) cudaFree(d.phi_prev);
@@ -569,6 +583,21 @@ int mflbm_synchronize(mflbm_context* c) {
     return MFLBM_OK;
 }
 
+int mflbm_interface_stats(mflbm_context* c, long long* interface_nodes, long long* solid_normals,
+                          long long* active_nodes) {
+    int rc = require_ready(c);
+    if (rc != MFLBM_OK) return rc;
+    int h[3] = {0, 0, 0};
+    if (c->d.gcount) {
+        MFLBM_CUDA(cudaMemcpyAsync(h, c->d.gcount, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+        MFLBM_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    if (interface_nodes) *interface_nodes = h[0];
+    if (solid_normals) *solid_normals = h[1];
+    if (active_nodes) *active_nodes = h[2];
+    return MFLBM_OK;
+}
+
 int mflbm_monitor_reduce(mflbm_context* c, int n_exclude_inlet, int n_exclude_outlet, mflbm_monitor* out) {
     int rc = require_ready(c);
     if (rc != MFLBM_OK) return rc;
@@ -686,7 +715,11 @@ int mflbm_autotune(mflbm_context* c, int reps, mflbm_tuning* out) {
     struct { void* p; size_t n; } st[] = {{d.pdf, pop_e * d.b.S * 38}, {d.phi, T * g.n4()},
                                           {d.aux, T * 4 * std::max<ll>(1, d.n_fluid)}, {d.cnv4, T * 4 * g.n2()},
                                           {d.f_cv, T * pl * 19}, {d.g_cv, T * pl * 19}, {d.phi_cv, T * pl},
-                                          {d.dither, 2 * sizeof(uint32_t)}, {d.iface, (size_t)g.n2()}};
+                                          {d.dither, 2 * sizeof(uint32_t)}, {d.iface, (size_t)g.n2()},
+                                          {d.olist, sizeof(uint32_t) * std::max<ll>(1, d.n_norm)},
+                                          {d.slist, sizeof(uint32_t) * std::max<ll>(1, d.n_cn_ext)},
+                                          {d.smask, sizeof(uint32_t) * (size_t)(g.n2() / 32 + 1)},
+                                          {d.gcount, 4 * sizeof(int)}};
     size_t total = 0;
     for (auto& x : st) total += (x.n + 255) / 256 * 256;
     char* save = nullptr;

@@ -57,8 +57,13 @@ struct DeviceState {
     int8_t* iface = nullptr;           // s2: 1 where the normal record may be non-zero (|grad phi| >= 1e-6, type <= 0)
     int8_t* phib = nullptr;            // per 2x2x2 brick of the s4 lattice: 1 all phi = +1, 2 all phi = -1, else 0
     int32_t* tmap = nullptr;           // s2: fluid-list index of a fluid node of [1, n]^3, else -1
-    uint32_t* ilist = nullptr;         // fluid-list indices of this step's interface nodes (normal pass), n_fluid capacity
-    int* ilist_n = nullptr;            // their count
+    uint32_t* olist = nullptr;         // packed nodes with a non-zero normal record (capacity n_norm)
+    uint32_t* slist = nullptr;         // packed solid boundary nodes that received a normal (capacity n_cn_ext)
+    uint32_t* nlist = nullptr;         // packed fluid nodes of the active 2x2x2 node blocks (capacity n_norm)
+    uint32_t* smask = nullptr;         // bit per s2 node: in slist
+    int* gcount = nullptr;             // lengths of olist, slist, nlist
+    ll n_blocks = 0;                   // node blocks of the normal pass: ((n+4)/2 + 1) per axis
+    int n_sm = 0;                      // multiprocessors of the device (grids of the list passes)
 };
 
 }  // namespace mflbm

@@ -3,19 +3,30 @@
 // launches (:2027-2054).
 //
 //   1. phi on solid boundary nodes (list with precomputed fluid-neighbour masks)
-//   2. unit interface normal + |grad phi| at the fluid nodes of [-1, n+2]^3
-//      (list in brick order), with the geometrical wetting applied in the
-//      same thread at fluid boundary nodes (it only reads its own node's
-//      values, so fusing it is exact); stored as one record
-//      (n_x, n_y, n_z, |grad phi|) per node of the s2 layout.  Solid nodes
-//      keep the zero record the reference writes there every step (records
-//      are zeroed when the geometry is set and when arrays are packed).
-//      The fluid nodes of [1, n]^3 with a non-zero record are appended to a
-//      compact list (the interface nodes of this step).
-//   3. normal on solid boundary nodes (list with masks)
+//   2. unit interface normal + |grad phi| at the fluid nodes of [-1, n+2]^3,
+//      with the geometrical wetting applied in the same thread at fluid
+//      boundary nodes (it only reads its own node's values, so fusing it is
+//      exact); stored as one record (n_x, n_y, n_z, |grad phi|) per node of
+//      the s2 layout.  Solid nodes keep the zero record the reference writes
+//      there every step (records are zeroed when the geometry is set and when
+//      arrays are packed).
+//   3. normal on solid boundary nodes: weighted mean of the fluid
+//      neighbours' normals
 //   4. curvature at the interface nodes and the record the collision reads,
 //      (n_x, n_y, n_z, 0.5 * gamma * curv * c_norm), stored in fluid-list
 //      order so that the collision reads it contiguously
+//
+// Sparse passes.  Away from interfaces phi is exactly +1 or -1, every
+// difference in an ISO4 sum is +0 and the normal record is the zero record;
+// so are the extrapolated normals of solid nodes whose fluid neighbours all
+// have zero records.  The pipeline keeps two lists between passes: the nodes
+// whose record is non-zero (olist) and the solid nodes that received a normal
+// (slist).  A pass resets those records to zero, lists the fluid nodes of the
+// 2x2x2 node blocks whose stencils reach a non-uniform phi brick (nlist),
+// recomputes the normals of those nodes only (rebuilding olist), claims the
+// solid neighbours of olist (rebuilding slist), extrapolates to them and
+// computes the curvature at the fluid nodes of olist.  Every record outside the lists is the zero record, as in the dense
+// passes of the reference.
 //
 // The reference-layout arrays cn_x/y/z, c_norm and curv (curvature on all of
 // [1, n]^3, solid nodes included) are produced from the records only when the
@@ -38,8 +49,11 @@ template <class T> struct GradArgs {
     int8_t* iface;  // s2 (fluid nodes): 1 where the record may be non-zero; 0: the zero record
     int8_t* phib;   // per 2x2x2 brick of the s4 lattice: 1 all phi = +1, 2 all phi = -1, else 0
     const int32_t* tmap;   // s2 -> fluid-list index (or -1)
-    uint32_t* ilist;       // interface nodes of this step (fluid-list indices), appended by the normal pass
-    int* ilist_n;
+    uint32_t* olist;       // packed coordinates of the nodes whose record is non-zero (interface flag set)
+    uint32_t* slist;       // packed coordinates of the solid nodes whose normal may be non-zero
+    uint32_t* nlist;       // packed fluid nodes of this pass's active node blocks
+    uint32_t* smask;       // bit per s2 node: the solid node is in slist
+    int* gcount;           // [0] olist, [1] slist, [2] nlist lengths
     T *cnx, *cny, *cnz, *cnorm, *curv;  // reference-layout arrays (export / pack)
     const uint2 *l_phi, *l_cn;
     const uint32_t *l_fluid, *l_norm;
@@ -139,9 +153,12 @@ __global__ void __launch_bounds__(256) phi_brick_kernel(const GradArgs<T> a) {
     typedef typename Vec2<T>::type P;
     const int NX = a.g.nx + 8, NY = a.g.ny + 8, NZ = a.g.nz + 8;
     const int BX = (NX + 1) >> 1, BY = (NY + 1) >> 1, BZ = (NZ + 1) >> 1;
-    const ll b = (ll)blockIdx.x * blockDim.x + threadIdx.x;   // bricks in x-fastest order
-    if (b >= (ll)BX * BY * BZ) return;
-    const int bx = (int)(b % BX), by = (int)((b / BX) % BY), bz = (int)(b / ((ll)BX * BY));
+    // bricks in x-fastest order; fewer than 2^31 bricks for any lattice the
+    // packed coordinates allow, so 32-bit division
+    const unsigned b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= (unsigned)(BX * BY * BZ)) return;
+    const unsigned bxy = b / (unsigned)BX;
+    const int bx = (int)(b - bxy * (unsigned)BX), by = (int)(bxy % (unsigned)BY), bz = (int)(bxy / (unsigned)BY);
     bool plus = true, minus = true;
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
@@ -189,96 +206,181 @@ __device__ __forceinline__ bool normal_at(const GradArgs<T>& a, int i, int j, in
     return r.w != T(0);
 }
 
-// unit interface normal and |grad phi| at the fluid nodes of [-1, n+2]^3
-// (:757-807) + wetting (:809-878)
-template <class T>
-__global__ void __launch_bounds__(256) normals_kernel(const GradArgs<T> a) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= a.n_norm) return;
-    int i, j, k;
-    unpack_xyz(a.l_norm[t], i, j, k);
-    const Grid& g = a.g;
-    const int n4 = (int)g.s4(i, j, k);
-    const ll n2 = g.s2(i, j, k);
-    const int8_t was = a.iface[n2];   // issued with the brick loads below
-    {
-        // The stencil (s4-local i+2 .. i+4 on each axis) lies in the 2x2x2
-        // bricks (i+2)>>1 .. +1: if they are uniform with one value, every
-        // difference in the ISO4 sums is +0, |grad phi| = 0 and the record is
-        // the zero record -- written without reading the 18 neighbours.
-        const int BX = (g.nx + 9) >> 1, BY = (g.ny + 9) >> 1;
-        const int bx = (i + 2) >> 1, by = (j + 2) >> 1, bz = (k + 2) >> 1;
-        const int8_t* pb = a.phib + bx + (ll)BX * (by + (ll)BY * bz);
-        const int8_t c0 = pb[0];
-        if (c0 != 0 && pb[1] == c0 && pb[BX] == c0 && pb[BX + 1] == c0 && pb[(ll)BX * BY] == c0 &&
-            pb[(ll)BX * BY + 1] == c0 && pb[(ll)BX * BY + BX] == c0 && pb[(ll)BX * BY + BX + 1] == c0) {
-            // a record is non-zero only where the interface flag is set: only
-            // those are cleared, every other one is already the zero record
-            if (was) {
-                typename Vec4<T>::type r;
-                r.x = T(0); r.y = T(0); r.z = T(0); r.w = T(0);
-                a.cn[n2] = r;
-                a.iface[n2] = 0;
-            }
-            return;
-        }
-    }
-    const bool on = normal_at<T>(a, i, j, k, a.type8[n4]);
-    // fluid nodes of [1, n]^3 with a non-zero record join the curvature's list
-    // (one atomic per warp; the order of the list does not matter)
-    const int tf = on ? a.tmap[n2] : -1;
+// Append `value` to `list` where `want` is set: one atomic per warp, the
+// order within the list is arbitrary.
+__device__ __forceinline__ void warp_append(bool want, uint32_t value, uint32_t* list, int* count) {
     const unsigned act = __activemask();
-    const unsigned want = __ballot_sync(act, tf >= 0);
-    if (want) {
-        const int lane = threadIdx.x & 31, leader = __ffs(want) - 1;
-        int base = 0;
-        if (lane == leader) base = atomicAdd(a.ilist_n, __popc(want));
-        base = __shfl_sync(act, base, leader);
-        if (tf >= 0) a.ilist[base + __popc(want & ((1u << lane) - 1u))] = (uint32_t)tf;
+    const unsigned m = __ballot_sync(act, want);
+    if (!m) return;
+    const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(count, __popc(m));
+    base = __shfl_sync(act, base, leader);
+    if (want) list[base + __popc(m & ((1u << lane) - 1u))] = value;
+}
+
+// Reserve `cnt` consecutive slots of a list per thread (warp prefix sum, one
+// atomic per warp); returns the thread's first slot.  Every lane of the warp
+// must call it.
+__device__ __forceinline__ int warp_reserve(int cnt, int* count) {
+    const int lane = threadIdx.x & 31;
+    int incl = cnt;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += v;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    int base = 0;
+    if (lane == 31 && total) base = atomicAdd(count, total);
+    return __shfl_sync(0xffffffffu, base, 31) + incl - cnt;
+}
+
+// Reset the records of the previous pass's lists to the zero record (and
+// their flags), so that every record outside this pass's lists is zero.
+template <class T>
+__global__ void __launch_bounds__(256) clear_records_kernel(const GradArgs<T> a) {
+    const int no = a.gcount[0], ns = a.gcount[1];
+    typename Vec4<T>::type z;
+    z.x = T(0); z.y = T(0); z.z = T(0); z.w = T(0);
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < no + ns; p += gridDim.x * blockDim.x) {
+        const bool solid = p >= no;
+        int i, j, k;
+        unpack_xyz(solid ? a.slist[p - no] : a.olist[p], i, j, k);
+        const ll n2 = a.g.s2(i, j, k);
+        a.cn[n2] = z;
+        if (solid) atomicAnd(&a.smask[n2 >> 5], ~(1u << (n2 & 31)));
+        else a.iface[n2] = 0;
     }
 }
 
-// interface normal on solid boundary nodes = weighted mean over fluid neighbours (:880-906)
+// Node block c (nodes 2c-2 .. 2c-1 on each axis) is active unless the eight
+// phi bricks c .. c+1 that hold its stencils (s4-local i+2 .. i+4) have one
+// common non-zero code.  The fluid nodes (walls_type <= 0) of [-1, n+2]^3 in
+// active blocks are appended to nlist (one atomic per warp).
 template <class T>
-__global__ void __launch_bounds__(256) extrapolate_normal_kernel(const GradArgs<T> a) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= a.n_cn) return;
-    const uint2 e = a.l_cn[t];
-    int i, j, k;
-    unpack_xyz(e.x, i, j, k);
-    const int sy = a.g.nx + 4, sz = (a.g.nx + 4) * (a.g.ny + 4);
-    const int n = (int)a.g.s2(i, j, k);
-    // fluid neighbours whose record is the zero record (interface flag 0)
-    // contribute +0 to every sum: when all of them are such, the mean is +0
-    // and only the flags (1 byte each) are read
-    bool any = false;
+__global__ void __launch_bounds__(256) active_nodes_kernel(const GradArgs<T> a) {
+    const Grid& g = a.g;
+    const int BX = (g.nx + 9) >> 1, BY = (g.ny + 9) >> 1;
+    const int CX = ((g.nx + 4) >> 1) + 1, CY = ((g.ny + 4) >> 1) + 1, CZ = ((g.nz + 4) >> 1) + 1;
+    const unsigned c = blockIdx.x * blockDim.x + threadIdx.x;   // fewer than 2^31 blocks
+    unsigned sel = 0;   // bit e: node e of the block is listed
+    int cx = 0, cy = 0, cz = 0;
+    if (c < (unsigned)(CX * CY * CZ)) {
+        const unsigned cyz = c / (unsigned)CX;
+        cx = (int)(c - cyz * (unsigned)CX); cy = (int)(cyz % (unsigned)CY); cz = (int)(cyz / (unsigned)CY);
+        const int8_t* pb = a.phib + cx + (ll)BX * (cy + (ll)BY * cz);
+        const int8_t c0 = pb[0];
+        const bool quiet = c0 != 0 && pb[1] == c0 && pb[BX] == c0 && pb[BX + 1] == c0 && pb[(ll)BX * BY] == c0 &&
+                           pb[(ll)BX * BY + 1] == c0 && pb[(ll)BX * BY + BX] == c0 && pb[(ll)BX * BY + BX + 1] == c0;
+        if (!quiet) {
 #pragma unroll
-    for (int q = 1; q < 19; ++q)
-        if (e.y & (1u << q)) any = any || a.iface[n + ex(q) + ey(q) * sy + ez(q) * sz];
-    // |grad phi| of a solid node is 0 in every record (the geometry set-up and
-    // the array packing write solid records as zero records; only the
-    // direction is extrapolated), so the record is written without reading it
-    typename Vec4<T>::type r;
-    r.w = T(0);
-    if (!any) {
-        r.x = T(0); r.y = T(0); r.z = T(0);
-        a.cn[n] = r;
-        return;
-    }
-    T sx = T(0), syy = T(0), szz = T(0), ws = T(0);
-#pragma unroll
-    for (int q = 1; q < 19; ++q) {
-        if (e.y & (1u << q)) {
-            const typename Vec4<T>::type v = a.cn[n + ex(q) + ey(q) * sy + ez(q) * sz];
-            const T wq = wq_of(a.ph.c, q);
-            sx += v.x * wq;
-            syy += v.y * wq;
-            szz += v.z * wq;
-            ws += wq;
+            for (int e = 0; e < 8; ++e) {
+                const int i = 2 * cx - 2 + (e & 1), j = 2 * cy - 2 + ((e >> 1) & 1), k = 2 * cz - 2 + (e >> 2);
+                if (i >= -1 && i <= g.nx + 2 && j >= -1 && j <= g.ny + 2 && k >= -1 && k <= g.nz + 2 &&
+                    a.type8[g.s4(i, j, k)] <= 0)
+                    sel |= 1u << e;
+            }
         }
     }
-    r.x = sx / ws; r.y = syy / ws; r.z = szz / ws;
-    a.cn[n] = r;
+    int base = warp_reserve(__popc(sel), &a.gcount[2]);
+    for (int e = 0; e < 8; ++e)
+        if (sel & (1u << e))
+            a.nlist[base++] = pack_xyz(2 * cx - 2 + (e & 1), 2 * cy - 2 + ((e >> 1) & 1), 2 * cz - 2 + (e >> 2));
+}
+
+// unit interface normal and |grad phi| (:757-807) + wetting (:809-878) at the
+// nodes of nlist; nodes with a non-zero record are appended to olist.
+template <class T>
+__global__ void __launch_bounds__(256) normals_kernel(const GradArgs<T> a) {
+    const int nt = a.gcount[2];
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < nt; p += gridDim.x * blockDim.x) {
+        int i, j, k;
+        const uint32_t packed = a.nlist[p];
+        unpack_xyz(packed, i, j, k);
+        const bool on = normal_at<T>(a, i, j, k, a.type8[a.g.s4(i, j, k)]);
+        warp_append(on, packed, a.olist, &a.gcount[0]);
+    }
+}
+
+// Solid boundary nodes (walls_type 2) of [0, n+1]^3 next to a node of olist
+// join slist once (bit mask): the only solid nodes whose extrapolated normal
+// can be non-zero.  Loads, mask reads and atomics of the 18 directions are
+// issued independently; the claims of a warp are appended with one atomic.
+template <class T>
+__global__ void __launch_bounds__(256) claim_solids_kernel(const GradArgs<T> a) {
+    const Grid& g = a.g;
+    const int no = a.gcount[0];
+    const int sy4 = g.nx + 8, sz4 = (g.nx + 8) * (g.ny + 8);
+    const int sy2 = g.nx + 4, sz2 = (g.nx + 4) * (g.ny + 4);
+    const int iters = (no + gridDim.x * blockDim.x - 1) / (gridDim.x * blockDim.x);   // warp-uniform
+    for (int it = 0; it < iters; ++it) {
+        const int p = (it * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x;
+        int i = 0, j = 0, k = 0;
+        unsigned cand = 0;
+        if (p < no) {
+            unpack_xyz(a.olist[p], i, j, k);
+            const int n4 = (int)g.s4(i, j, k);
+#pragma unroll
+            for (int q = 1; q < 19; ++q) {
+                const int si = i + ex(q), sj = j + ey(q), sk = k + ez(q);
+                if (a.type8[n4 + ex(q) + ey(q) * sy4 + ez(q) * sz4] == 2 && si >= 0 && si <= g.nx + 1 && sj >= 0 &&
+                    sj <= g.ny + 1 && sk >= 0 && sk <= g.nz + 1)
+                    cand |= 1u << q;
+            }
+        }
+        // most solid nodes are claimed by several neighbours: a plain read
+        // skips the atomic once the bit is visible
+        const ll n2 = g.s2(i, j, k);
+        uint32_t word[19];
+#pragma unroll
+        for (int q = 1; q < 19; ++q) {
+            const ll s2 = n2 + ex(q) + ey(q) * sy2 + ez(q) * sz2;
+            word[q] = (cand & (1u << q)) ? a.smask[s2 >> 5] : 0xffffffffu;
+        }
+        unsigned mine = 0;
+#pragma unroll
+        for (int q = 1; q < 19; ++q) {
+            const ll s2 = n2 + ex(q) + ey(q) * sy2 + ez(q) * sz2;
+            const uint32_t bit = 1u << (s2 & 31);
+            if ((cand & (1u << q)) && !(word[q] & bit) && !(atomicOr(&a.smask[s2 >> 5], bit) & bit)) mine |= 1u << q;
+        }
+        int at = warp_reserve(__popc(mine), &a.gcount[1]);
+#pragma unroll
+        for (int q = 1; q < 19; ++q)
+            if (mine & (1u << q)) a.slist[at++] = pack_xyz(i + ex(q), j + ey(q), k + ez(q));
+    }
+}
+
+// interface normal on the solid boundary nodes of slist = weighted mean over
+// the fluid neighbours (walls_type <= 0), in direction order (:880-906).
+// |grad phi| of a solid node stays 0.
+template <class T>
+__global__ void __launch_bounds__(256) extrapolate_normal_kernel(const GradArgs<T> a) {
+    const Grid& g = a.g;
+    const int ns = a.gcount[1];
+    const int sy = g.nx + 4, sz = (g.nx + 4) * (g.ny + 4);
+    const int sy4 = g.nx + 8, sz4 = (g.nx + 8) * (g.ny + 8);
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < ns; p += gridDim.x * blockDim.x) {
+        int i, j, k;
+        unpack_xyz(a.slist[p], i, j, k);
+        const int n = (int)g.s2(i, j, k), n4 = (int)g.s4(i, j, k);
+        T sx = T(0), syy = T(0), szz = T(0), ws = T(0);
+#pragma unroll
+        for (int q = 1; q < 19; ++q) {
+            if (a.type8[n4 + ex(q) + ey(q) * sy4 + ez(q) * sz4] <= 0) {
+                const typename Vec4<T>::type v = a.cn[n + ex(q) + ey(q) * sy + ez(q) * sz];
+                const T wq = wq_of(a.ph.c, q);
+                sx += v.x * wq;
+                syy += v.y * wq;
+                szz += v.z * wq;
+                ws += wq;
+            }
+        }
+        typename Vec4<T>::type r;
+        r.x = sx / ws; r.y = syy / ws; r.z = szz / ws; r.w = T(0);
+        a.cn[n] = r;
+    }
 }
 
 // curvature at node n (s2 index) from the nine ISO4 derivatives of the
@@ -308,23 +410,25 @@ __device__ __forceinline__ T curvature_at(const ModelConsts<T>& c, const typenam
 }
 
 // Curvature and the collision's record (fluid-list order) at this step's
-// interface nodes: the list the normal pass appended (fluid nodes with a
-// non-zero normal record).  Away from interfaces |grad phi| is exactly 0 and
-// the normal record is all zeros; the collision's force 0.5 gamma curv
-// |grad phi| n and its recolouring direction are then zero whatever the
-// curvature, and the collision reads the record only where the interface
-// flag is set.  Grid-stride loop over the list (its length is on the device).
+// interface nodes: the fluid nodes of [1, n]^3 in olist (non-zero normal
+// record).  Away from interfaces |grad phi| is exactly 0 and the normal
+// record is all zeros; the collision's force 0.5 gamma curv |grad phi| n and
+// its recolouring direction are then zero whatever the curvature, and the
+// collision reads the record only where the interface flag is set.
+// Grid-stride loop over the list (its length is on the device).
 template <class T>
 __global__ void __launch_bounds__(256) curvature_kernel(const GradArgs<T> a) {
     const Grid& g = a.g;
     const int sy = g.nx + 4, sz = (g.nx + 4) * (g.ny + 4);
-    const int n = *a.ilist_n;
+    const int n = a.gcount[0];
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
-        const int t = (int)a.ilist[p];
         int i, j, k;
-        unpack_xyz(a.l_fluid[t], i, j, k);
+        unpack_xyz(a.olist[p], i, j, k);
+        const int n2 = (int)g.s2(i, j, k);
+        const int t = a.tmap[n2];
+        if (t < 0) continue;   // ghost layers and nodes outside the fluid list
         typename Vec4<T>::type ctr, r;
-        const T cv = curvature_at<T>(a.ph.c, a.cn, (int)g.s2(i, j, k), sy, sz, ctr);
+        const T cv = curvature_at<T>(a.ph.c, a.cn, n2, sy, sz, ctr);
         r.x = ctr.x; r.y = ctr.y; r.z = ctr.z;
         r.w = T(0.5) * a.ph.gamma * cv * ctr.w;
         a.aux[t] = r;
@@ -368,9 +472,12 @@ __global__ void __launch_bounds__(128) pack_normals_kernel(const GradArgs<T> a) 
         v.x = a.cnx[n]; v.y = a.cny[n]; v.z = a.cnz[n]; v.w = a.cnorm[n];
     }
     a.cn[n] = v;
-    // 1 where the record may be non-zero: uploaded arrays can carry a normal
-    // with c_norm = 0, and the next normal pass must clear it
-    a.iface[n] = (v.x != T(0) || v.y != T(0) || v.z != T(0) || v.w != T(0)) ? 1 : 0;
+    // 1 where the record is non-zero (uploaded arrays can carry a normal with
+    // c_norm = 0); such nodes form olist, which the next pass clears first.
+    // Solid records are zero here: slist and its mask start empty.
+    const bool nz = v.x != T(0) || v.y != T(0) || v.z != T(0) || v.w != T(0);
+    a.iface[n] = nz ? 1 : 0;
+    if (nz) a.olist[atomicAdd(&a.gcount[0], 1)] = pack_xyz(i, j, k);
 }
 template <class T>
 __global__ void __launch_bounds__(128) aux_from_arrays_kernel(const GradArgs<T> a) {
@@ -398,7 +505,8 @@ GradArgs<T> grad_args(const mflbm_context& c) {
     a.aux = (typename Vec4<T>::type*)d.aux;
     a.iface = d.iface;
     a.phib = d.phib;
-    a.tmap = d.tmap; a.ilist = d.ilist; a.ilist_n = d.ilist_n;
+    a.tmap = d.tmap;
+    a.olist = d.olist; a.slist = d.slist; a.nlist = d.nlist; a.smask = d.smask; a.gcount = d.gcount;
     a.cnx = (T*)d.cn_x; a.cny = (T*)d.cn_y; a.cnz = (T*)d.cn_z;
     a.cnorm = (T*)d.c_norm; a.curv = (T*)d.curv;
     a.l_phi = d.list_phi_ext; a.n_phi = (int)d.n_phi_ext;
@@ -421,22 +529,36 @@ int launch_gradient(mflbm_context& c) {
         extrapolate_phi_kernel<T><<<grid_for(a.n_phi, tn.extrapolate), tn.extrapolate, 0, s>>>(a);
         if ((rc = after_launch("extrapolate_phi")) != MFLBM_OK) return rc;
     }
-    MFLBM_CUDA(cudaMemsetAsync(c.d.ilist_n, 0, sizeof(int), s));
+    // the list passes run one wave of resident blocks (grid-stride loops: the
+    // list lengths are known only on the device; blocks beyond the resident
+    // ones would start only after the first wave has walked the whole list)
+    const int lb = 256;
+    auto wave = [&](const void* kernel, int bs) {
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, bs, 0) != cudaSuccess || per_sm < 1)
+            per_sm = 1;
+        return std::max(1, c.d.n_sm) * per_sm;
+    };
     if (a.n_norm) {
         const Grid& g = c.d.g;
+        clear_records_kernel<T><<<wave((const void*)clear_records_kernel<T>, lb), lb, 0, s>>>(a);
+        if ((rc = after_launch("clear_records")) != MFLBM_OK) return rc;
+        MFLBM_CUDA(cudaMemsetAsync(c.d.gcount, 0, 3 * sizeof(int), s));
         phi_brick_kernel<T><<<grid_for((ll)((g.nx + 9) / 2) * ((g.ny + 9) / 2) * ((g.nz + 9) / 2), 256), 256, 0, s>>>(a);
         if ((rc = after_launch("phi_brick")) != MFLBM_OK) return rc;
-        normals_kernel<T><<<grid_for(a.n_norm, tn.normals), tn.normals, 0, s>>>(a);
+        active_nodes_kernel<T><<<grid_for(c.d.n_blocks, 256), 256, 0, s>>>(a);
+        if ((rc = after_launch("active_nodes")) != MFLBM_OK) return rc;
+        normals_kernel<T><<<wave((const void*)normals_kernel<T>, tn.normals), tn.normals, 0, s>>>(a);
         if ((rc = after_launch("normals")) != MFLBM_OK) return rc;
-    }
-    if (a.n_cn) {
-        extrapolate_normal_kernel<T><<<grid_for(a.n_cn, tn.extrapolate), tn.extrapolate, 0, s>>>(a);
-        if ((rc = after_launch("extrapolate_normal")) != MFLBM_OK) return rc;
+        if (a.n_cn) {
+            claim_solids_kernel<T><<<wave((const void*)claim_solids_kernel<T>, lb), lb, 0, s>>>(a);
+            if ((rc = after_launch("claim_solids")) != MFLBM_OK) return rc;
+            extrapolate_normal_kernel<T><<<wave((const void*)extrapolate_normal_kernel<T>, lb), lb, 0, s>>>(a);
+            if ((rc = after_launch("extrapolate_normal")) != MFLBM_OK) return rc;
+        }
     }
     if (!a.n_fluid) return MFLBM_OK;
-    // a fixed grid (the interface count is known only on the device)
-    const int blocks = (int)std::min<ll>(grid_for(a.n_fluid, tn.curvature), 152 * 8);
-    curvature_kernel<T><<<blocks, tn.curvature, 0, s>>>(a);
+    curvature_kernel<T><<<wave((const void*)curvature_kernel<T>, tn.curvature), tn.curvature, 0, s>>>(a);
     return after_launch("curvature");
 }
 
@@ -457,6 +579,8 @@ template <class T>
 int launch_refresh_aux(mflbm_context& c) {
     const GradArgs<T> a = grad_args<T>(c);
     const Grid& g = c.d.g;
+    MFLBM_CUDA(cudaMemsetAsync(c.d.gcount, 0, 3 * sizeof(int), c.stream));
+    MFLBM_CUDA(cudaMemsetAsync(c.d.smask, 0, sizeof(uint32_t) * (size_t)(g.n2() / 32 + 1), c.stream));
     pack_normals_kernel<T><<<dim3(grid_for(g.nx + 4, 128), g.ny + 4, g.nz + 4), 128, 0, c.stream>>>(a);
     int rc = after_launch("pack_normals");
     if (rc != MFLBM_OK || !a.n_fluid) return rc;

@@ -39,6 +39,7 @@ SIGNATURES = {
     "mflbm_step": (I, [VP, I]),
     "mflbm_run": (I, [VP, I, I]),
     "mflbm_synchronize": (I, [VP]),
+    "mflbm_interface_stats": (I, [VP, VP, VP, VP]),
     "mflbm_monitor_reduce": (I, [VP, I, I, VP]),
     "mflbm_monitor_reduce_noalloc": (I, [VP, I, I, VP]),
     "mflbm_monitor_profile": (I, [VP, VP, VP, I]),
@@ -176,10 +177,21 @@ class Context:
         check(self.lib.mflbm_upload_fields(self.h, *[ptr(a.get(n)) for n in names]), "mflbm_upload_fields")
 
     def download(self, names=("pdf", "phi", "cn_x", "cn_y", "cn_z", "c_norm", "curv", "f_convec_bc",
-                              "g_convec_bc", "phi_convec_bc")):
+                              "g_convec_bc", "phi_convec_bc"), out=None):
+        """mflbm_download_fields into new arrays, or into the caller's arrays
+        `out` (name -> C-contiguous array of the field's size and the context's
+        dtype, e.g. pinned host buffers)."""
         order = ["pdf", "phi", "cn_x", "cn_y", "cn_z", "c_norm", "curv", "f_convec_bc", "g_convec_bc",
                  "phi_convec_bc"]
-        out = {n: self.L.empty(abi.FIELD_KINDS[n], self.T) for n in names}
+        if out is None:
+            out = {n: self.L.empty(abi.FIELD_KINDS[n], self.T) for n in names}
+        else:
+            out = {n: out[n] for n in names}
+            for n, a in out.items():
+                want = int(np.prod(self.L.shape(abi.FIELD_KINDS[n])))
+                if a.dtype != self.T or a.size != want or not a.flags["C_CONTIGUOUS"]:
+                    raise ValueError(f"download: out[{n!r}] must be a C-contiguous {np.dtype(self.T).name} "
+                                     f"array of {want} values")
         check(self.lib.mflbm_download_fields(self.h, *[ptr(out.get(n)) for n in order]), "mflbm_download_fields")
         return out
 
@@ -203,6 +215,12 @@ class Context:
 
     def sync(self):
         check(self.lib.mflbm_synchronize(self.h), "mflbm_synchronize")
+
+    def interface_stats(self):
+        """mflbm_interface_stats: sizes of the last gradient pass's sparse sets."""
+        v = [C.c_longlong(0) for _ in range(3)]
+        check(self.lib.mflbm_interface_stats(self.h, *[C.byref(x) for x in v]), "mflbm_interface_stats")
+        return {"interface_nodes": v[0].value, "solid_normals": v[1].value, "active_nodes": v[2].value}
 
     def monitor(self, n_exclude_inlet, n_exclude_outlet):
         m = abi.Monitor()

@@ -77,6 +77,14 @@ def test_strict_is_bit_exact_on_odd_sizes(mflbm_lib, kind):
     d = ctx.download()
     for n in STATE:
         assert d[n].tobytes() == o.a[n].tobytes(), f"{n} after 30 steps (max diff {_diff(d[n], o.a[n])})"
+    # the sparse sets of the last gradient pass: the interface nodes are the
+    # nodes with c_norm != 0; every solid node with a non-zero normal is in
+    # the solid set
+    st = ctx.interface_stats()
+    assert st["interface_nodes"] == np.count_nonzero(d["c_norm"]) > 0
+    solid_nz = np.count_nonzero((d["cn_x"] != 0) | (d["cn_y"] != 0) | (d["cn_z"] != 0)) - st["interface_nodes"]
+    assert st["solid_normals"] >= solid_nz
+    assert st["interface_nodes"] <= st["active_nodes"] <= 25 * 25 * 27
     ctx.close()
 
 
@@ -96,6 +104,13 @@ def test_strict_eager_steps_and_upload(mflbm_lib, prec):
     d = ctx2.download()
     for n in STATE:
         assert d[n].tobytes() == o.a[n].tobytes(), n
+    # the same download into the caller's buffers
+    bufs = {n: np.full_like(o.a[n], np.nan) for n in STATE}
+    d_into = ctx2.download(out=bufs)
+    for n in STATE:
+        assert d_into[n] is bufs[n] and bufs[n].tobytes() == o.a[n].tobytes(), n
+    with pytest.raises(ValueError):
+        ctx2.download(names=("phi",), out={"phi": np.zeros(3, dtype=o.a["phi"].dtype)})
     # upload without cn / c_norm / curv: recomputed on the device from phi
     ctx3 = lib.Context(info["params"])
     ctx3.upload_geometry(o.a["walls"], o.a["walls_type"], o.a["s_nx"], o.a["s_ny"], o.a["s_nz"])
