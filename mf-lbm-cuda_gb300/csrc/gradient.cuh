@@ -25,8 +25,8 @@
 // 2x2x2 node blocks whose stencils reach a non-uniform phi brick (nlist),
 // recomputes the normals of those nodes only (rebuilding olist), claims the
 // solid neighbours of olist (rebuilding slist), extrapolates to them and
-// computes the curvature at the fluid nodes of olist.  Every record outside the lists is the zero record, as in the dense
-// passes of the reference.
+// computes the curvature at the fluid nodes of olist.  Every record outside
+// the lists is the zero record, as in the dense passes of the reference.
 //
 // The reference-layout arrays cn_x/y/z, c_norm and curv (curvature on all of
 // [1, n]^3, solid nodes included) are produced from the records only when the
@@ -143,6 +143,25 @@ __device__ __forceinline__ T iso4_dz(const ModelConsts<T>& c, const T* F, int n,
                       F[n + sy + sz] - F[n - sy - sz] + F[n - sy + sz] - F[n + sy - sz]);
 }
 
+// Reset the records of the previous pass's lists to the zero record (and
+// their flags), so that every record outside this pass's lists is zero.
+// Grid-stride over both lists, run by the threads of the brick pass.
+template <class T>
+__device__ __forceinline__ void clear_records(const GradArgs<T>& a, int tid, int nthreads) {
+    const int no = a.gcount[0], ns = a.gcount[1];
+    typename Vec4<T>::type z;
+    z.x = T(0); z.y = T(0); z.z = T(0); z.w = T(0);
+    for (int p = tid; p < no + ns; p += nthreads) {
+        const bool solid = p >= no;
+        int i, j, k;
+        unpack_xyz(solid ? a.slist[p - no] : a.olist[p], i, j, k);
+        const ll n2 = a.g.s2(i, j, k);
+        a.cn[n2] = z;
+        if (solid) atomicAnd(&a.smask[n2 >> 5], ~(1u << (n2 & 31)));
+        else a.iface[n2] = 0;
+    }
+}
+
 // Bulk detection for the normal pass: per 2x2x2 brick of the s4 lattice
 // (s4-local coordinates 2b, 2b + 1 on each axis; positions past the lattice
 // end are ignored), 1 if every phi is exactly +1, 2 if every phi is exactly -1,
@@ -156,6 +175,7 @@ __global__ void __launch_bounds__(256) phi_brick_kernel(const GradArgs<T> a) {
     // bricks in x-fastest order; fewer than 2^31 bricks for any lattice the
     // packed coordinates allow, so 32-bit division
     const unsigned b = blockIdx.x * blockDim.x + threadIdx.x;
+    clear_records<T>(a, (int)b, (int)(gridDim.x * blockDim.x));
     if (b >= (unsigned)(BX * BY * BZ)) return;
     const unsigned bxy = b / (unsigned)BX;
     const int bx = (int)(b - bxy * (unsigned)BX), by = (int)(bxy % (unsigned)BY), bz = (int)(bxy / (unsigned)BY);
@@ -236,24 +256,6 @@ __device__ __forceinline__ int warp_reserve(int cnt, int* count) {
     return __shfl_sync(0xffffffffu, base, 31) + incl - cnt;
 }
 
-// Reset the records of the previous pass's lists to the zero record (and
-// their flags), so that every record outside this pass's lists is zero.
-template <class T>
-__global__ void __launch_bounds__(256) clear_records_kernel(const GradArgs<T> a) {
-    const int no = a.gcount[0], ns = a.gcount[1];
-    typename Vec4<T>::type z;
-    z.x = T(0); z.y = T(0); z.z = T(0); z.w = T(0);
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < no + ns; p += gridDim.x * blockDim.x) {
-        const bool solid = p >= no;
-        int i, j, k;
-        unpack_xyz(solid ? a.slist[p - no] : a.olist[p], i, j, k);
-        const ll n2 = a.g.s2(i, j, k);
-        a.cn[n2] = z;
-        if (solid) atomicAnd(&a.smask[n2 >> 5], ~(1u << (n2 & 31)));
-        else a.iface[n2] = 0;
-    }
-}
-
 // Node block c (nodes 2c-2 .. 2c-1 on each axis) is active unless the eight
 // phi bricks c .. c+1 that hold its stencils (s4-local i+2 .. i+4) have one
 // common non-zero code.  The fluid nodes (walls_type <= 0) of [-1, n+2]^3 in
@@ -332,18 +334,13 @@ __global__ void __launch_bounds__(256) claim_solids_kernel(const GradArgs<T> a) 
         // most solid nodes are claimed by several neighbours: a plain read
         // skips the atomic once the bit is visible
         const ll n2 = g.s2(i, j, k);
-        uint32_t word[19];
-#pragma unroll
-        for (int q = 1; q < 19; ++q) {
-            const ll s2 = n2 + ex(q) + ey(q) * sy2 + ez(q) * sz2;
-            word[q] = (cand & (1u << q)) ? a.smask[s2 >> 5] : 0xffffffffu;
-        }
         unsigned mine = 0;
 #pragma unroll
         for (int q = 1; q < 19; ++q) {
             const ll s2 = n2 + ex(q) + ey(q) * sy2 + ez(q) * sz2;
             const uint32_t bit = 1u << (s2 & 31);
-            if ((cand & (1u << q)) && !(word[q] & bit) && !(atomicOr(&a.smask[s2 >> 5], bit) & bit)) mine |= 1u << q;
+            if ((cand & (1u << q)) && !(a.smask[s2 >> 5] & bit) && !(atomicOr(&a.smask[s2 >> 5], bit) & bit))
+                mine |= 1u << q;
         }
         int at = warp_reserve(__popc(mine), &a.gcount[1]);
 #pragma unroll
@@ -541,11 +538,10 @@ int launch_gradient(mflbm_context& c) {
     };
     if (a.n_norm) {
         const Grid& g = c.d.g;
-        clear_records_kernel<T><<<wave((const void*)clear_records_kernel<T>, lb), lb, 0, s>>>(a);
-        if ((rc = after_launch("clear_records")) != MFLBM_OK) return rc;
-        MFLBM_CUDA(cudaMemsetAsync(c.d.gcount, 0, 3 * sizeof(int), s));
+        // brick codes + reset of the previous lists' records, then the lists restart
         phi_brick_kernel<T><<<grid_for((ll)((g.nx + 9) / 2) * ((g.ny + 9) / 2) * ((g.nz + 9) / 2), 256), 256, 0, s>>>(a);
         if ((rc = after_launch("phi_brick")) != MFLBM_OK) return rc;
+        MFLBM_CUDA(cudaMemsetAsync(c.d.gcount, 0, 3 * sizeof(int), s));
         active_nodes_kernel<T><<<grid_for(c.d.n_blocks, 256), 256, 0, s>>>(a);
         if ((rc = after_launch("active_nodes")) != MFLBM_OK) return rc;
         normals_kernel<T><<<wave((const void*)normals_kernel<T>, tn.normals), tn.normals, 0, s>>>(a);
