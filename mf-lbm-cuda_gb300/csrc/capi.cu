@@ -54,8 +54,8 @@ void free_all(mflbm_context* c) {
     DeviceState& d = c->d;
     void* ptrs[] = {d.pdf, d.phi, d.cn_x, d.cn_y, d.cn_z, d.c_norm, d.curv, d.W_in, d.f_cv, d.g_cv, d.phi_cv,
                     d.walls, d.walls_type, d.s_nx, d.s_ny, d.s_nz, d.fluid_list, d.list_phi_ext,
-                    d.list_cn_ext, d.red, d.staging, d.aux, d.type8, d.cnv4, d.list_norm, d.zpair_off,
-                    d.phi_prev, d.prof, d.dither, d.iface, d.phib, d.tmap, d.olist, d.slist, d.nlist, d.smask, d.gcount};
+                    d.list_cn_ext, d.red, d.staging, d.aux, d.type8, d.cnv4, d.zpair_off,
+                    d.phi_prev, d.prof, d.dither, d.iface, d.phib, d.tmap, d.wmask, d.olist, d.slist, d.nlist, d.smask, d.gcount};
     for (void* p : ptrs) if (p) cudaFree(p);
     d = DeviceState{};
     if (c->pair_graph) cudaGraphExecDestroy(c->pair_graph);
@@ -101,17 +101,6 @@ int build_lists(mflbm_context* c) {
     std::vector<int> zoff(d.b.nbz + 1, 0);
     for (size_t n = 0; n < fe.size(); ++n) zoff[(fe[n].first >> 3) / (d.b.nbx * d.b.nby) + 1]++;
     for (int kp = 0; kp < d.b.nbz; ++kp) zoff[kp + 1] += zoff[kp];
-    // nodes whose normal the step needs: walls_type <= 0 on [-1, n+2]^3, in
-    // brick order of the grid shifted by one (so ghost layer -1 is included)
-    const Bricks bn = make_bricks(g.nx + 2, g.ny + 2, g.nz + 2);
-    std::vector<std::pair<ll, uint32_t>> ne;
-    for (int k = -1; k <= g.nz + 2; ++k)
-        for (int j = -1; j <= g.ny + 2; ++j)
-            for (int i = -1; i <= g.nx + 2; ++i)
-                if (wt[g.s4(i, j, k)] <= 0) ne.emplace_back((ll)bn.elem(i + 1, j + 1, k + 1), pack_xyz(i, j, k));
-    std::sort(ne.begin(), ne.end());
-    std::vector<uint32_t> ln(ne.size());
-    for (size_t n = 0; n < ne.size(); ++n) ln[n] = ne[n].second;
     std::vector<uint2> lphi, lcn;
     for (int k = -2; k <= g.nz + 3; ++k)
         for (int j = -2; j <= g.ny + 3; ++j)
@@ -135,10 +124,30 @@ int build_lists(mflbm_context* c) {
         }
         ll ntm = 0;
         if ((rc = upload_list(&d.tmap, &ntm, tm)) != MFLBM_OK) return rc;
+        // the nodes whose normal the step may need (walls_type <= 0 on
+        // [-1, n+2]^3: their count bounds the sparse lists) and their
+        // solid-boundary neighbours (the claims of the normal extrapolation)
+        std::vector<uint32_t> wm(g.n2(), 0u);
+        d.n_norm = 0;
+        for (int k = -1; k <= g.nz + 2; ++k)
+            for (int j = -1; j <= g.ny + 2; ++j)
+                for (int i = -1; i <= g.nx + 2; ++i) {
+                    if (wt[g.s4(i, j, k)] > 0) continue;
+                    ++d.n_norm;
+                    uint32_t m = 0;
+                    for (int q = 1; q < 19; ++q) {
+                        const int si = i + ex(q), sj = j + ey(q), sk = k + ez(q);
+                        if (si >= 0 && si <= g.nx + 1 && sj >= 0 && sj <= g.ny + 1 && sk >= 0 && sk <= g.nz + 1 &&
+                            wt[g.s4(si, sj, sk)] == 2)
+                            m |= 1u << q;
+                    }
+                    wm[g.s2(i, j, k)] = m;
+                }
+        ll nwm = 0;
+        if ((rc = upload_list(&d.wmask, &nwm, wm)) != MFLBM_OK) return rc;
     }
     if ((rc = upload_list(&d.list_phi_ext, &d.n_phi_ext, lphi)) != MFLBM_OK) return rc;
     if ((rc = upload_list(&d.list_cn_ext, &d.n_cn_ext, lcn)) != MFLBM_OK) return rc;
-    if ((rc = upload_list(&d.list_norm, &d.n_norm, ln)) != MFLBM_OK) return rc;
     {
         // lists of the sparse gradient passes (all records start as zero records)
         int dev = 0;

@@ -21,8 +21,7 @@ struct DeviceState {
     void* staging = nullptr;        // reference-layout (f1) buffer for uploads / downloads
     void* cnv4 = nullptr;           // s2: (n_x, n_y, n_z, |grad phi|) per node
     void* aux = nullptr;            // per fluid node, fluid-list order: (n_x, n_y, n_z, 0.5*gamma*curv*c_norm)
-    uint32_t* list_norm = nullptr;  // walls_type <= 0 on [-1, n+2]^3, in brick order
-    ll n_norm = 0;
+    ll n_norm = 0;                  // walls_type <= 0 nodes on [-1, n+2]^3 (capacity of the sparse lists)
     int8_t* type8 = nullptr;        // walls_type as int8 (s4)
     bool arrays_stale = false;      // cn_x/y/z, c_norm, curv behind the records
     void* phi = nullptr;
@@ -57,6 +56,7 @@ struct DeviceState {
     int8_t* iface = nullptr;           // s2: 1 where the normal record may be non-zero (|grad phi| >= 1e-6, type <= 0)
     int8_t* phib = nullptr;            // per 2x2x2 brick of the s4 lattice: 1 all phi = +1, 2 all phi = -1, else 0
     int32_t* tmap = nullptr;           // s2: fluid-list index of a fluid node of [1, n]^3, else -1
+    uint32_t* wmask = nullptr;         // s2: bit q set where x + e_q is a walls_type-2 node of [0, n+1]^3 (type <= 0 nodes)
     uint32_t* olist = nullptr;         // packed nodes with a non-zero normal record (capacity n_norm)
     uint32_t* slist = nullptr;         // packed solid boundary nodes that received a normal (capacity n_cn_ext)
     uint32_t* nlist = nullptr;         // packed fluid nodes of the active 2x2x2 node blocks (capacity n_norm)

@@ -49,6 +49,7 @@ template <class T> struct GradArgs {
     int8_t* iface;  // s2 (fluid nodes): 1 where the record may be non-zero; 0: the zero record
     int8_t* phib;   // per 2x2x2 brick of the s4 lattice: 1 all phi = +1, 2 all phi = -1, else 0
     const int32_t* tmap;   // s2 -> fluid-list index (or -1)
+    const uint32_t* wmask; // s2: bit q where x + e_q is a solid boundary node (walls_type 2) of [0, n+1]^3
     uint32_t* olist;       // packed coordinates of the nodes whose record is non-zero (interface flag set)
     uint32_t* slist;       // packed coordinates of the solid nodes whose normal may be non-zero
     uint32_t* nlist;       // packed fluid nodes of this pass's active node blocks
@@ -56,7 +57,7 @@ template <class T> struct GradArgs {
     int* gcount;           // [0] olist, [1] slist, [2] nlist lengths
     T *cnx, *cny, *cnz, *cnorm, *curv;  // reference-layout arrays (export / pack)
     const uint2 *l_phi, *l_cn;
-    const uint32_t *l_fluid, *l_norm;
+    const uint32_t* l_fluid;
     int n_phi, n_cn, n_fluid, n_norm;
     Phys<T> ph;
 };
@@ -307,13 +308,13 @@ __global__ void __launch_bounds__(256) normals_kernel(const GradArgs<T> a) {
 
 // Solid boundary nodes (walls_type 2) of [0, n+1]^3 next to a node of olist
 // join slist once (bit mask): the only solid nodes whose extrapolated normal
-// can be non-zero.  Loads, mask reads and atomics of the 18 directions are
-// issued independently; the claims of a warp are appended with one atomic.
+// can be non-zero.  The candidate directions of a node come from its
+// precomputed solid-neighbour mask; the claims of a warp are appended with
+// one atomic.
 template <class T>
 __global__ void __launch_bounds__(256) claim_solids_kernel(const GradArgs<T> a) {
     const Grid& g = a.g;
     const int no = a.gcount[0];
-    const int sy4 = g.nx + 8, sz4 = (g.nx + 8) * (g.ny + 8);
     const int sy2 = g.nx + 4, sz2 = (g.nx + 4) * (g.ny + 4);
     const int iters = (no + gridDim.x * blockDim.x - 1) / (gridDim.x * blockDim.x);   // warp-uniform
     for (int it = 0; it < iters; ++it) {
@@ -322,14 +323,7 @@ __global__ void __launch_bounds__(256) claim_solids_kernel(const GradArgs<T> a) 
         unsigned cand = 0;
         if (p < no) {
             unpack_xyz(a.olist[p], i, j, k);
-            const int n4 = (int)g.s4(i, j, k);
-#pragma unroll
-            for (int q = 1; q < 19; ++q) {
-                const int si = i + ex(q), sj = j + ey(q), sk = k + ez(q);
-                if (a.type8[n4 + ex(q) + ey(q) * sy4 + ez(q) * sz4] == 2 && si >= 0 && si <= g.nx + 1 && sj >= 0 &&
-                    sj <= g.ny + 1 && sk >= 0 && sk <= g.nz + 1)
-                    cand |= 1u << q;
-            }
+            cand = a.wmask[g.s2(i, j, k)];
         }
         // most solid nodes are claimed by several neighbours: a plain read
         // skips the atomic once the bit is visible
@@ -503,13 +497,14 @@ GradArgs<T> grad_args(const mflbm_context& c) {
     a.iface = d.iface;
     a.phib = d.phib;
     a.tmap = d.tmap;
+    a.wmask = d.wmask;
     a.olist = d.olist; a.slist = d.slist; a.nlist = d.nlist; a.smask = d.smask; a.gcount = d.gcount;
     a.cnx = (T*)d.cn_x; a.cny = (T*)d.cn_y; a.cnz = (T*)d.cn_z;
     a.cnorm = (T*)d.c_norm; a.curv = (T*)d.curv;
     a.l_phi = d.list_phi_ext; a.n_phi = (int)d.n_phi_ext;
     a.l_cn = d.list_cn_ext; a.n_cn = (int)d.n_cn_ext;
     a.l_fluid = d.fluid_list; a.n_fluid = (int)d.n_fluid;
-    a.l_norm = d.list_norm; a.n_norm = (int)d.n_norm;
+    a.n_norm = (int)d.n_norm;
     a.ph = make_phys<T>(c.params);
     return a;
 }
