@@ -23,8 +23,8 @@
 // whose record is non-zero (olist) and the solid nodes that received a normal
 // (slist).  A pass resets those records to zero, lists the fluid nodes of the
 // 2x2x2 node blocks whose stencils reach a non-uniform phi brick (nlist),
-// recomputes the normals of those nodes only (rebuilding olist), claims the
-// solid neighbours of olist (rebuilding slist), extrapolates to them and
+// recomputes the normals of those nodes only (rebuilding olist and, from the
+// new interface nodes' solid neighbours, slist), extrapolates to them and
 // computes the curvature at the fluid nodes of olist.  Every record outside
 // the lists is the zero record, as in the dense passes of the reference.
 //
@@ -293,48 +293,41 @@ __global__ void __launch_bounds__(256) active_nodes_kernel(const GradArgs<T> a) 
 }
 
 // unit interface normal and |grad phi| (:757-807) + wetting (:809-878) at the
-// nodes of nlist; nodes with a non-zero record are appended to olist.
+// nodes of nlist; nodes with a non-zero record are appended to olist, and
+// their solid-boundary neighbours of [0, n+1]^3 (the node's precomputed
+// solid-neighbour mask) join slist once (bit mask): the only solid nodes whose
+// extrapolated normal can be non-zero.  The claims of a warp are appended
+// with one atomic; the loop is warp-uniform for that.
 template <class T>
 __global__ void __launch_bounds__(256) normals_kernel(const GradArgs<T> a) {
-    const int nt = a.gcount[2];
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < nt; p += gridDim.x * blockDim.x) {
-        int i, j, k;
-        const uint32_t packed = a.nlist[p];
-        unpack_xyz(packed, i, j, k);
-        const bool on = normal_at<T>(a, i, j, k, a.type8[a.g.s4(i, j, k)]);
-        warp_append(on, packed, a.olist, &a.gcount[0]);
-    }
-}
-
-// Solid boundary nodes (walls_type 2) of [0, n+1]^3 next to a node of olist
-// join slist once (bit mask): the only solid nodes whose extrapolated normal
-// can be non-zero.  The candidate directions of a node come from its
-// precomputed solid-neighbour mask; the claims of a warp are appended with
-// one atomic.
-template <class T>
-__global__ void __launch_bounds__(256) claim_solids_kernel(const GradArgs<T> a) {
     const Grid& g = a.g;
-    const int no = a.gcount[0];
+    const int nt = a.gcount[2];
     const int sy2 = g.nx + 4, sz2 = (g.nx + 4) * (g.ny + 4);
-    const int iters = (no + gridDim.x * blockDim.x - 1) / (gridDim.x * blockDim.x);   // warp-uniform
+    const int iters = (nt + gridDim.x * blockDim.x - 1) / (gridDim.x * blockDim.x);
     for (int it = 0; it < iters; ++it) {
         const int p = (it * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x;
         int i = 0, j = 0, k = 0;
-        unsigned cand = 0;
-        if (p < no) {
-            unpack_xyz(a.olist[p], i, j, k);
+        uint32_t packed = 0, cand = 0;
+        bool on = false;
+        if (p < nt) {
+            packed = a.nlist[p];
+            unpack_xyz(packed, i, j, k);
             cand = a.wmask[g.s2(i, j, k)];
+            on = normal_at<T>(a, i, j, k, a.type8[g.s4(i, j, k)]);
         }
+        warp_append(on, packed, a.olist, &a.gcount[0]);
         // most solid nodes are claimed by several neighbours: a plain read
         // skips the atomic once the bit is visible
         const ll n2 = g.s2(i, j, k);
         unsigned mine = 0;
+        if (on) {
 #pragma unroll
-        for (int q = 1; q < 19; ++q) {
-            const ll s2 = n2 + ex(q) + ey(q) * sy2 + ez(q) * sz2;
-            const uint32_t bit = 1u << (s2 & 31);
-            if ((cand & (1u << q)) && !(a.smask[s2 >> 5] & bit) && !(atomicOr(&a.smask[s2 >> 5], bit) & bit))
-                mine |= 1u << q;
+            for (int q = 1; q < 19; ++q) {
+                const ll s2 = n2 + ex(q) + ey(q) * sy2 + ez(q) * sz2;
+                const uint32_t bit = 1u << (s2 & 31);
+                if ((cand & (1u << q)) && !(a.smask[s2 >> 5] & bit) && !(atomicOr(&a.smask[s2 >> 5], bit) & bit))
+                    mine |= 1u << q;
+            }
         }
         int at = warp_reserve(__popc(mine), &a.gcount[1]);
 #pragma unroll
@@ -542,8 +535,6 @@ int launch_gradient(mflbm_context& c) {
         normals_kernel<T><<<wave((const void*)normals_kernel<T>, tn.normals), tn.normals, 0, s>>>(a);
         if ((rc = after_launch("normals")) != MFLBM_OK) return rc;
         if (a.n_cn) {
-            claim_solids_kernel<T><<<wave((const void*)claim_solids_kernel<T>, lb), lb, 0, s>>>(a);
-            if ((rc = after_launch("claim_solids")) != MFLBM_OK) return rc;
             extrapolate_normal_kernel<T><<<wave((const void*)extrapolate_normal_kernel<T>, lb), lb, 0, s>>>(a);
             if ((rc = after_launch("extrapolate_normal")) != MFLBM_OK) return rc;
         }
