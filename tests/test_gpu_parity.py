@@ -88,6 +88,31 @@ def test_strict_is_bit_exact_on_odd_sizes(mflbm_lib, kind):
     ctx.close()
 
 
+@pytest.mark.parametrize("kind", ["periodic_drop", "plate_drainage"])
+def test_strict_long_run_with_moving_interface(mflbm_lib, kind):
+    """150 steps with a moving interface, graph-replayed and per-step calls
+    mixed: the sparse gradient sets (interface nodes, claimed solid nodes)
+    are rebuilt every pass and every record outside them must stay the zero
+    record, so stale entries would show up as differences here."""
+    case, ctx, info, o = _setup(kind, abi.MFLBM_FP32, abi.MFLBM_STRICT)
+    sizes = []
+    for first, count, eager in [(1, 60, False), (61, 30, True), (91, 60, False)]:
+        if eager:
+            for nt in range(first, first + count):
+                ctx.step(nt)
+        else:
+            ctx.run(first, count)
+        o.run(count)
+        d = ctx.download()
+        for n in STATE:
+            assert d[n].tobytes() == o.a[n].tobytes(), f"{n} after {first + count - 1} steps"
+        st = ctx.interface_stats()
+        assert st["interface_nodes"] == np.count_nonzero(d["c_norm"])
+        sizes.append(st["interface_nodes"])
+    assert min(sizes) > 0
+    ctx.close()
+
+
 @pytest.mark.parametrize("prec", PRECS, ids=["f32", "f64"])
 def test_strict_eager_steps_and_upload(mflbm_lib, prec):
     """Per-step calls (mflbm_step) and a state uploaded from the host in the
