@@ -54,7 +54,7 @@ void free_all(mflbm_context* c) {
     DeviceState& d = c->d;
     void* ptrs[] = {d.pdf, d.phi, d.cn_x, d.cn_y, d.cn_z, d.c_norm, d.curv, d.W_in, d.f_cv, d.g_cv, d.phi_cv,
                     d.walls, d.walls_type, d.s_nx, d.s_ny, d.s_nz, d.fluid_list, d.list_phi_ext,
-                    d.list_cn_ext, d.red, d.staging, d.aux, d.type8, d.cnv4, d.zpair_off,
+                    d.red, d.staging, d.aux, d.type8, d.cnv4, d.zpair_off,
                     d.phi_prev, d.prof, d.dither, d.iface, d.phib, d.tmap, d.wmask, d.olist, d.slist, d.nlist, d.smask, d.gcount};
     for (void* p : ptrs) if (p) cudaFree(p);
     d = DeviceState{};
@@ -101,7 +101,8 @@ int build_lists(mflbm_context* c) {
     std::vector<int> zoff(d.b.nbz + 1, 0);
     for (size_t n = 0; n < fe.size(); ++n) zoff[(fe[n].first >> 3) / (d.b.nbx * d.b.nby) + 1]++;
     for (int kp = 0; kp < d.b.nbz; ++kp) zoff[kp + 1] += zoff[kp];
-    std::vector<uint2> lphi, lcn;
+    std::vector<uint2> lphi;
+    ll ncn = 0;   // walls_type == 2 nodes of [0, n+1]^3: bound of the claimed solid nodes
     for (int k = -2; k <= g.nz + 3; ++k)
         for (int j = -2; j <= g.ny + 3; ++j)
             for (int i = -2; i <= g.nx + 3; ++i) {
@@ -111,7 +112,7 @@ int build_lists(mflbm_context* c) {
                     if (wt[g.s4(i + ex(q), j + ey(q), k + ez(q))] <= 0) mask |= 1u << q;
                 const uint2 e = make_uint2(pack_xyz(i, j, k), mask);
                 lphi.push_back(e);
-                if (i >= 0 && i <= g.nx + 1 && j >= 0 && j <= g.ny + 1 && k >= 0 && k <= g.nz + 1) lcn.push_back(e);
+                if (i >= 0 && i <= g.nx + 1 && j >= 0 && j <= g.ny + 1 && k >= 0 && k <= g.nz + 1) ++ncn;
             }
     int rc;
     if ((rc = upload_list(&d.fluid_list, &d.n_fluid, fl)) != MFLBM_OK) return rc;
@@ -147,7 +148,7 @@ int build_lists(mflbm_context* c) {
         if ((rc = upload_list(&d.wmask, &nwm, wm)) != MFLBM_OK) return rc;
     }
     if ((rc = upload_list(&d.list_phi_ext, &d.n_phi_ext, lphi)) != MFLBM_OK) return rc;
-    if ((rc = upload_list(&d.list_cn_ext, &d.n_cn_ext, lcn)) != MFLBM_OK) return rc;
+    d.n_cn_ext = ncn;
     {
         // lists of the sparse gradient passes (all records start as zero records)
         int dev = 0;

@@ -45,8 +45,7 @@ struct DeviceState {
     ll n_fluid = 0;
     uint2* list_phi_ext = nullptr;     // walls_type == 2 on [-2, n+3]^3: (packed, fluid-neighbour mask)
     ll n_phi_ext = 0;
-    uint2* list_cn_ext = nullptr;      // walls_type == 2 on [0, n+1]^3: (packed, fluid-neighbour mask)
-    ll n_cn_ext = 0;
+    ll n_cn_ext = 0;                   // walls_type == 2 nodes on [0, n+1]^3 (capacity of slist)
     double* red = nullptr;             // reduction scratch
     ll red_len = 0;
     int* zpair_off = nullptr;          // fluid-list offset of each z pair (2 kp, 2 kp + 1), nbz + 1 entries

@@ -56,7 +56,7 @@ template <class T> struct GradArgs {
     uint32_t* smask;       // bit per s2 node: the solid node is in slist
     int* gcount;           // [0] olist, [1] slist, [2] nlist lengths
     T *cnx, *cny, *cnz, *cnorm, *curv;  // reference-layout arrays (export / pack)
-    const uint2 *l_phi, *l_cn;
+    const uint2* l_phi;
     const uint32_t* l_fluid;
     int n_phi, n_cn, n_fluid, n_norm;
     Phys<T> ph;
@@ -495,7 +495,7 @@ GradArgs<T> grad_args(const mflbm_context& c) {
     a.cnx = (T*)d.cn_x; a.cny = (T*)d.cn_y; a.cnz = (T*)d.cn_z;
     a.cnorm = (T*)d.c_norm; a.curv = (T*)d.curv;
     a.l_phi = d.list_phi_ext; a.n_phi = (int)d.n_phi_ext;
-    a.l_cn = d.list_cn_ext; a.n_cn = (int)d.n_cn_ext;
+    a.n_cn = (int)d.n_cn_ext;
     a.l_fluid = d.fluid_list; a.n_fluid = (int)d.n_fluid;
     a.n_norm = (int)d.n_norm;
     a.ph = make_phys<T>(c.params);

@@ -1,0 +1,107 @@
+"""Index arithmetic of the sparse colour-gradient passes
+(mf-lbm-cuda_gb300/csrc/gradient.cuh: phi_brick_kernel, active_nodes_kernel),
+restated in numpy.
+
+The passes skip every node whose ISO4 stencil (the node and its 18 D3Q19
+neighbours, s4-local i+2 .. i+4 on each axis) lies in eight 2x2x2 phi bricks
+of one common code (all exactly +1 or all exactly -1): there every difference
+of the ISO4 sums is +0 and the normal record is the zero record.  These tests
+check, on random phase fields with sharp and diffuse interfaces and on odd and
+even extents, that
+
+  * every node of [-1, n+2]^3 belongs to exactly one node block c
+    (nodes 2c-2 .. 2c-1 per axis), and the blocks range over
+    [0, (n+4)/2] per axis;
+  * the eight bricks c .. c+1 of a block lie inside the brick grid
+    ((n+9)/2 bricks per axis of the s4 lattice) and cover the stencils of all
+    of the block's nodes;
+  * every node outside the active blocks has a stencil of one value (so its
+    gradient is exactly zero), i.e. nothing with a non-zero gradient is
+    skipped.
+"""
+import numpy as np
+import pytest
+
+EX = [0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0]
+EY = [0, 0, 0, 1, -1, 0, 0, 1, 1, -1, -1, 0, 0, 0, 0, 1, -1, 1, -1]
+EZ = [0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 1, 1, -1, -1]
+
+
+def brick_codes(phi4):
+    """Per 2x2x2 brick of the s4 array (x fastest axis last in numpy order:
+    phi4[z, y, x]); positions past the array end are ignored."""
+    NZ, NY, NX = phi4.shape
+    BZ, BY, BX = (NZ + 1) // 2, (NY + 1) // 2, (NX + 1) // 2
+    pad = np.full((2 * BZ, 2 * BY, 2 * BX), np.nan)
+    pad[:NZ, :NY, :NX] = phi4
+    b = pad.reshape(BZ, 2, BY, 2, BX, 2)
+    present = ~np.isnan(b)
+    plus = np.all(np.where(present, b == 1.0, True), axis=(1, 3, 5))
+    minus = np.all(np.where(present, b == -1.0, True), axis=(1, 3, 5))
+    return np.where(plus, 1, np.where(minus, 2, 0)).astype(np.int8)
+
+
+def active_blocks(codes, n):
+    nx, ny, nz = n
+    CX, CY, CZ = (nx + 4) // 2 + 1, (ny + 4) // 2 + 1, (nz + 4) // 2 + 1
+    BZ, BY, BX = codes.shape
+    assert CX + 1 <= BX and CY + 1 <= BY and CZ + 1 <= BZ
+    c0 = codes[:CZ, :CY, :CX]
+    same = np.ones_like(c0, dtype=bool)
+    for dz in (0, 1):
+        for dy in (0, 1):
+            for dx in (0, 1):
+                same &= codes[dz:dz + CZ, dy:dy + CY, dx:dx + CX] == c0
+    quiet = (c0 != 0) & same
+    return ~quiet
+
+
+def random_phase(n, seed, sharp):
+    """phi on the s4 lattice (4 ghost layers): +-1 regions from random balls,
+    with a diffuse band unless `sharp`."""
+    nx, ny, nz = n
+    rng = np.random.default_rng(seed)
+    z, y, x = np.meshgrid(np.arange(nz + 8) - 3, np.arange(ny + 8) - 3, np.arange(nx + 8) - 3, indexing="ij")
+    d = np.full(x.shape, 1e9)
+    for _ in range(4):
+        c = rng.uniform(0, [nx, ny, nz])
+        r = rng.uniform(2, 0.4 * min(n))
+        d = np.minimum(d, np.sqrt((x - c[0]) ** 2 + (y - c[1]) ** 2 + (z - c[2]) ** 2) - r)
+    if sharp:
+        return np.where(d < 0, 1.0, -1.0)
+    phi = np.tanh(-d)
+    phi[d < -2.5] = 1.0      # exactly +-1 away from the band
+    phi[d > 2.5] = -1.0
+    return phi
+
+
+@pytest.mark.parametrize("n", [(20, 20, 28), (21, 19, 23), (16, 17, 9), (32, 24, 12)])
+@pytest.mark.parametrize("sharp", [False, True], ids=["diffuse", "sharp"])
+def test_skipped_nodes_have_uniform_stencils(n, sharp):
+    nx, ny, nz = n
+    phi4 = random_phase(n, seed=nx * 1000 + ny * 10 + nz, sharp=sharp)
+    codes = brick_codes(phi4)
+    assert codes.shape == ((nz + 9) // 2, (ny + 9) // 2, (nx + 9) // 2)
+    act = active_blocks(codes, n)
+    seen = np.zeros((nz + 4, ny + 4, nx + 4), dtype=np.int32)   # nodes -1 .. n+2
+    skipped_nonzero = 0
+    for cz in range(act.shape[0]):
+        for cy in range(act.shape[1]):
+            for cx in range(act.shape[2]):
+                for e in range(8):
+                    i, j, k = 2 * cx - 2 + (e & 1), 2 * cy - 2 + ((e >> 1) & 1), 2 * cz - 2 + (e >> 2)
+                    if not (-1 <= i <= nx + 2 and -1 <= j <= ny + 2 and -1 <= k <= nz + 2):
+                        continue
+                    seen[k + 1, j + 1, i + 1] += 1
+                    # the block's bricks cover the node's stencil
+                    for q in range(19):
+                        si, sj, sk = i + EX[q] + 3, j + EY[q] + 3, k + EZ[q] + 3    # s4-local
+                        assert cx <= si // 2 <= cx + 1 and cy <= sj // 2 <= cy + 1 and cz <= sk // 2 <= cz + 1
+                    if not act[cz, cy, cx]:
+                        c = phi4[k + 3, j + 3, i + 3]
+                        vals = [phi4[k + 3 + EZ[q], j + 3 + EY[q], i + 3 + EX[q]] for q in range(19)]
+                        skipped_nonzero += any(v != c for v in vals)
+    assert np.all(seen == 1), "every node of [-1, n+2]^3 in exactly one block"
+    assert skipped_nonzero == 0
+    # the fields are not trivial: both kinds of blocks occur
+    assert act.any() and not act.all()
