@@ -272,8 +272,9 @@ int mflbm_monitor_reduce(mflbm_context* ctx, int n_exclude_inlet,
  * on it, uses this entry point instead.  Its partials live in one fixed
  * device array of the library (10,250 doubles: 4 partial blocks per SM, up to
  * 256 SMs); a device with more SMs is rejected with MFLBM_E_ARG.
- *   - The first call on each device looks up that array's address (which may
- *     load the library's device code); make it before any stream capture.
+ *   - Every call looks up that array's address on the current device; the
+ *     first lookup on a device may load the library's device code, so make
+ *     the first call before any stream capture.
  *   - All contexts on one device share the array: calls that overlap in time
  *     on the same device (two host threads, or contexts whose streams run
  *     concurrently) race on it and must be serialised by the caller.  Calls
@@ -281,7 +282,8 @@ int mflbm_monitor_reduce(mflbm_context* ctx, int n_exclude_inlet,
  *     the host.
  *   - Nothing in the array needs clearing: each call writes every element it
  *     reads.
- * Same arguments, result and error behaviour as mflbm_monitor_reduce. */
+ * Same arguments and error behaviour as mflbm_monitor_reduce, and the same
+ * result bit for bit (both use 4 partial blocks per SM of the device). */
 int mflbm_monitor_reduce_noalloc(mflbm_context* ctx, int n_exclude_inlet,
                                  int n_exclude_outlet, mflbm_monitor* out);
 

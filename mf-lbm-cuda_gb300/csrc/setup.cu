@@ -3,7 +3,6 @@
 // arithmetic must be the reference's IEEE sequence so masks, solid normals
 // and initial populations are bit-identical to the reference's host code.
 #include <algorithm>
-#include <mutex>
 #include <string>
 #include <type_traits>
 #include <vector>
@@ -471,23 +470,24 @@ __global__ void fold_partials(int nblocks, int stride, const double* partial, do
     if (lane == 0) out[r] = x;
 }
 
+// Partial blocks of the monitor reductions: 4 per SM of the context's
+// device.  mflbm_monitor_reduce and mflbm_monitor_reduce_noalloc use the same
+// count, so their FP64 partial sums group the nodes alike and the two entry
+// points return bit-identical results.
+inline int monitor_blocks(const DeviceState& d) { return 4 * (d.n_sm > 0 ? d.n_sm : 1); }
+// scratch doubles for `blocks` partial blocks: NRED per block for the monitor
+// sums, one per block for the population total, NRED + 1 results
+inline ll monitor_scratch_len(int blocks) { return (ll)NRED * blocks + blocks + NRED + 1; }
+
+// The monitor reductions with their partials and results in `scratch`
+// (monitor_scratch_len(blocks) doubles).
 template <class T, class E>
-int monitor_t(mflbm_context& c, int nex_in, int nex_out, mflbm_monitor* out) {
+int monitor_into(mflbm_context& c, int nex_in, int nex_out, double* scratch, int blocks, mflbm_monitor* out) {
     DeviceState& d = c.d;
     const Grid g = d.g;
     cudaStream_t s = c.stream;
-    const int blocks = 4 * 152;
-    // scratch: NRED*blocks partials, blocks partials, NRED+1 results
-    const ll need = (ll)NRED * blocks + blocks + NRED + 1;
-    if (d.red_len < need) {
-        cudaFree(d.red);
-        d.red = nullptr;
-        d.red_len = 0;
-        MFLBM_CUDA(cudaMalloc(&d.red, sizeof(double) * need));
-        d.red_len = need;
-    }
-    double* part = d.red;
-    double* part2 = d.red + (ll)NRED * blocks;
+    double* part = scratch;
+    double* part2 = scratch + (ll)NRED * blocks;
     double* res = part2 + blocks;
     int rc;
     monitor_partials<T, E><<<blocks, 256, 0, s>>>(g, pop_view<T, E>(d), d.fluid_list, d.n_fluid, (const T*)d.phi,
@@ -515,6 +515,23 @@ int monitor_t(mflbm_context& c, int nex_in, int nex_out, mflbm_monitor* out) {
     return MFLBM_OK;
 }
 
+// mflbm_monitor_reduce: partials in the context's scratch, allocated on the
+// first call.
+template <class T, class E>
+int monitor_t(mflbm_context& c, int nex_in, int nex_out, mflbm_monitor* out) {
+    DeviceState& d = c.d;
+    const int blocks = monitor_blocks(d);
+    const ll need = monitor_scratch_len(blocks);
+    if (d.red_len < need) {
+        cudaFree(d.red);
+        d.red = nullptr;
+        d.red_len = 0;
+        MFLBM_CUDA(cudaMalloc(&d.red, sizeof(double) * need));
+        d.red_len = need;
+    }
+    return monitor_into<T, E>(c, nex_in, nex_out, d.red, blocks, out);
+}
+
 // ---------------------------------------------------------------------------
 // Scratch of mflbm_monitor_reduce_noalloc: a fixed array in the library's
 // device image instead of the context's lazily allocated partials, for callers
@@ -533,73 +550,34 @@ constexpr int kNoallocBlocksMax = 4 * 256;
 constexpr ll kNoallocScratch = (ll)NRED * kNoallocBlocksMax + kNoallocBlocksMax + NRED + 1;
 static __device__ __align__(256) double g_monitor_scratch[kNoallocScratch];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_scratch_mutex;
-double* g_scratch_ptr[kMaxDevices] = {};
-
-// Device address of g_monitor_scratch on the current device, looked up on the
-// first call for that device (which may load the library's device code).
-int noalloc_scratch(double** out, int* sms) {
-    int dev = 0;
-    MFLBM_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kMaxDevices)
-        return fail(MFLBM_E_ARG, "mflbm_monitor_reduce_noalloc: device ordinal " + std::to_string(dev) +
-                                     " beyond the supported " + std::to_string(kMaxDevices));
-    MFLBM_CUDA(cudaDeviceGetAttribute(sms, cudaDevAttrMultiProcessorCount, dev));
-    std::lock_guard<std::mutex> lock(g_scratch_mutex);
-    if (!g_scratch_ptr[dev]) {
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_monitor_scratch);
-        if (e != cudaSuccess)
-            return fail(MFLBM_E_CUDA, std::string("mflbm_monitor_reduce_noalloc: cudaGetSymbolAddress: ") +
-                                          cudaGetErrorString(e));
-        g_scratch_ptr[dev] = (double*)p;
-    }
-    *out = g_scratch_ptr[dev];
+// Device address of g_monitor_scratch on the current device.  The first
+// lookup on a device may load the library's device code there.  The address
+// is looked up on every call rather than cached: a cudaDeviceReset unloads
+// the module, and the next load may place the array elsewhere.
+int noalloc_scratch(double** out) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_monitor_scratch);
+    if (e != cudaSuccess)
+        return fail(MFLBM_E_CUDA, std::string("mflbm_monitor_reduce_noalloc: cudaGetSymbolAddress: ") +
+                                      cudaGetErrorString(e));
+    *out = (double*)p;
     return MFLBM_OK;
 }
 
-// The launches of monitor_t with the partials in g_monitor_scratch.
+// mflbm_monitor_reduce_noalloc: the same launches with the partials in
+// g_monitor_scratch.
 template <class T, class E>
 int monitor_noalloc_t(mflbm_context& c, int nex_in, int nex_out, mflbm_monitor* out) {
-    DeviceState& d = c.d;
-    const Grid g = d.g;
-    cudaStream_t s = c.stream;
-    double* scratch = nullptr;
-    int sms = 0;
-    int rc = noalloc_scratch(&scratch, &sms);
-    if (rc != MFLBM_OK) return rc;
-    const int blocks = 4 * sms;
-    const ll need = (ll)NRED * blocks + blocks + NRED + 1;
+    const int blocks = monitor_blocks(c.d);
+    const ll need = monitor_scratch_len(blocks);
     if (need > kNoallocScratch)
-        return fail(MFLBM_E_ARG, "mflbm_monitor_reduce_noalloc: " + std::to_string(sms) + " SMs need " +
+        return fail(MFLBM_E_ARG, "mflbm_monitor_reduce_noalloc: " + std::to_string(c.d.n_sm) + " SMs need " +
                                      std::to_string(need) + " doubles of scratch, the static array holds " +
                                      std::to_string(kNoallocScratch) + " (at most 256 SMs)");
-    double* part = scratch;
-    double* part2 = scratch + (ll)NRED * blocks;
-    double* res = part2 + blocks;
-    monitor_partials<T, E><<<blocks, 256, 0, s>>>(g, pop_view<T, E>(d), d.fluid_list, d.n_fluid, (const T*)d.phi,
-                                               (const T*)d.cn_x, (const T*)d.cn_y, (const T*)d.cn_z,
-                                               (const T*)d.c_norm, (const T*)d.curv, (double)T(c.params.lbm_gamma),
-                                               (double)T(c.params.force_z), nex_in + 1, g.nz - nex_out, part);
-    if ((rc = after_launch("monitor_partials")) != MFLBM_OK) return rc;
-    fold_partials<<<NRED, 32, 0, s>>>(blocks, NRED, part, res);
-    if ((rc = after_launch("fold_partials")) != MFLBM_OK) return rc;
-    sum_all<T, E><<<blocks, 256, 0, s>>>(g, pop_view<T, E>(d), part2);
-    if ((rc = after_launch("sum_all")) != MFLBM_OK) return rc;
-    fold_partials<<<1, 32, 0, s>>>(blocks, 1, part2, res + NRED);
-    if ((rc = after_launch("fold_partials")) != MFLBM_OK) return rc;
-    double h[NRED + 1];
-    MFLBM_CUDA(cudaMemcpyAsync(h, res, sizeof h, cudaMemcpyDeviceToHost, s));
-    MFLBM_CUDA(cudaStreamSynchronize(s));
-    out->vol1_sum = h[0]; out->vol2_sum = h[1];
-    out->mass1_sum = h[2]; out->mass2_sum = h[3];
-    out->flux1_sum = h[4]; out->flux2_sum = h[5];
-    out->vol1_full = h[6]; out->vol2_full = h[7];
-    out->umax = sqrt(h[8]);
-    out->total_mass = h[9];
-    out->saturation = h[0] / (h[0] + h[1]);
-    return MFLBM_OK;
+    double* scratch = nullptr;
+    int rc = noalloc_scratch(&scratch);
+    if (rc != MFLBM_OK) return rc;
+    return monitor_into<T, E>(c, nex_in, nex_out, scratch, blocks, out);
 }
 
 // ---------------------------------------------------------------------------
