@@ -23,7 +23,10 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 REPO = HERE.parent
-REFERENCE = Path(os.environ.get("MFLBM_REFERENCE", "/root/reference"))
+# The reference checkout: $MFLBM_REFERENCE, else a "reference" folder beside
+# this repository's folder.  Absent (as on a machine without the checkout),
+# the reference-side recipes and tests are skipped.
+REFERENCE = Path(os.environ.get("MFLBM_REFERENCE", str(REPO.parent / "reference")))
 CUDA_INC = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda")) / "include"
 
 FLAGS = ["-O2", "-fPIC", "-fopenmp", "-ffp-contract=off", "-std=c++17"]
