@@ -45,6 +45,51 @@ def force_relevant_pairs(d, ref):
     return out
 
 
+# D3Q19 lattice vectors in the reference's direction order (includes/Module.h:98-100)
+EX = [0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0]
+EY = [0, 0, 0, 1, -1, 0, 0, 1, 1, -1, -1, 0, 0, 0, 0, 1, -1, 1, -1]
+EZ = [0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 1, 1, -1, -1]
+
+
+def live_mass(pdf, walls, shape, jper=0, kper=0):
+    """Total mass of both components held by the populations after an even
+    step (and its boundary update), solid-node slots included, in FP64.
+
+    The reference has no explicit wall bounce-back (src/main_iteration_GPU.cu:
+    73-113, 348-384, 414-452): a population that a fluid node pushes towards a
+    solid neighbour waits in a slot until the same node reads it back, and
+    periodic faces are exchanged by copying slots into ghost layers, which
+    leaves stale duplicates behind.  The live populations after an even step
+    are therefore exactly
+      * those the next odd step pulls: slot q of x - e_q for every fluid node
+        x (a solid node's slot, a ghost copy or a fluid node's slot), and
+      * those parked for the even step after it: slot q of a fluid node y
+        whose neighbour y + e_q (periodic image on a periodic axis) is solid,
+        which that node reads back as its bounced-back population.
+    Each live population is counted once; in a closed domain (walls, periodic
+    axes, no inlet or outlet) their sum is the conserved mass.
+    `pdf` and `walls` are the reference-layout arrays (f1 and s2)."""
+    nx, ny, nz = shape
+    f = pdf.astype(np.float64).reshape(2, 19, nz + 2, ny + 2, nx + 2).sum(axis=0)
+    fluid = walls.reshape(nz + 4, ny + 4, nx + 4)[2:-2, 2:-2, 2:-2] == 0   # nodes [1, n]^3
+    total = 0.0
+    for q in range(19):
+        ex, ey, ez = EX[q], EY[q], EZ[q]
+        pulled = f[q][1 - ez:nz + 1 - ez, 1 - ey:ny + 1 - ey, 1 - ex:nx + 1 - ex]
+        total += float((pulled * fluid).sum())
+        tz, ty, tx = np.arange(1, nz + 1) + ez, np.arange(1, ny + 1) + ey, np.arange(1, nx + 1) + ex
+        if kper:
+            tz = (tz - 1) % nz + 1
+        if jper:
+            ty = (ty - 1) % ny + 1
+        solid_target = np.zeros((nz, ny, nx), bool)
+        iz, iy, ix = (np.where((t >= 1) & (t <= m))[0] for t, m in ((tz, nz), (ty, ny), (tx, nx)))
+        zz, yy, xx = np.ix_(iz, iy, ix)
+        solid_target[zz, yy, xx] = ~fluid[tz[zz] - 1, ty[yy] - 1, tx[xx] - 1]
+        total += float((f[q][1:-1, 1:-1, 1:-1] * (fluid & solid_target)).sum())
+    return total
+
+
 def dtype_of(precision):
     return np.float32 if precision == abi.MFLBM_FP32 else np.float64
 
