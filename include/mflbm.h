@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define MFLBM_ABI_VERSION 2
+#define MFLBM_ABI_VERSION 3
 
 enum {
     MFLBM_OK = 0,
@@ -341,20 +341,29 @@ typedef struct mflbm_tuning {
     int normals_block;                 /* ... of the interface-normal kernel */
     int curvature_block;               /* ... of the curvature kernel */
     int extrapolate_block;             /* ... of the two solid-boundary extrapolations */
-    double step_ms_before;             /* mean step time with the block sizes found on entry */
-    double step_ms_after;              /* ... with the chosen block sizes */
+    double step_ms_before;             /* mean step time with the tuning found on entry */
+    double step_ms_after;              /* ... with the chosen tuning */
+    int tile_x, tile_y, tile_z;        /* population tile extent in 2x2x2 bricks (powers of
+                                          two; x, y 1-32, z 1 or 2); default 8 x 4 x 2 */
 } mflbm_tuning;
 
-/* Times the step kernels of this context with 64, 128 and 256 threads per
- * block, one kernel family at a time, keeps the fastest combination and
- * reports it.  reps: odd + even step pairs timed per candidate (>= 1).  The
- * state is copied aside first (temporary device memory of one state) and
- * restored afterwards, so the simulation's results are unchanged.  Not
- * allowed while kernel timing is on. */
+/* Times the step with several population tile shapes (the layout of the
+ * populations in HBM: tiles of 2x2x2 bricks, each tile storing its 19
+ * directions contiguously), then with 64, 128 and 256 threads per block for
+ * each kernel family, keeps the fastest combination and reports it.  reps:
+ * odd + even step pairs timed per candidate (>= 1).  The state is copied
+ * aside first (temporary device memory of one state) and restored
+ * afterwards; a change of tile shape moves every population exactly, so the
+ * simulation's results are unchanged.  Not allowed while kernel timing is
+ * on. */
 int mflbm_autotune(mflbm_context* ctx, int reps, mflbm_tuning* out);
-/* Sets block sizes (64, 128 or 256; 0 keeps the current value), e.g. to reuse
- * a tuning found on another context of the same size. */
+/* Sets block sizes (64, 128 or 256; 0 keeps the current value) and, when
+ * tile_x/y/z are non-zero, the population tile shape (the populations are
+ * moved to the new layout, results unchanged), e.g. to reuse a tuning found
+ * on another context of the same size. */
 int mflbm_set_tuning(mflbm_context* ctx, const mflbm_tuning* t);
+/* The current block sizes and tile shape (step_ms_* are 0). */
+int mflbm_get_tuning(mflbm_context* ctx, mflbm_tuning* out);
 
 /* A batch of independent contexts on the current device, advanced together:
  * the odd + even step pairs of all of them are captured into one CUDA graph,

@@ -79,28 +79,73 @@ int upload_list(V** dptr, ll* n, const std::vector<V>& h) {
     return MFLBM_OK;
 }
 
-// Node lists from the device geometry: the fluid nodes of [1, n]^3 in
-// brick-element order (consecutive threads touch consecutive elements), and
-// the solid boundary nodes with an 18-bit mask of their fluid neighbours
-// (bit q set when neighbour x + e_q has walls_type <= 0).
+// The fluid list in the order of the population layout (consecutive threads
+// touch consecutive pairs), the fluid-list index of each node (tmap) and the
+// list offset of each layer of population tiles (zpair_off).  With `perm`,
+// perm[t] receives the position in the previous list of the node now at t.
+int order_fluid_list(mflbm_context* c, const std::vector<uint32_t>& nodes, std::vector<int>* perm) {
+    DeviceState& d = c->d;
+    const Grid g = d.g;
+    std::vector<std::pair<ll, uint32_t>> fe;
+    fe.reserve(nodes.size());
+    for (uint32_t p : nodes) {
+        int x, y, z;
+        unpack_xyz(p, x, y, z);
+        fe.emplace_back(d.b.elem(x, y, z), p);
+    }
+    std::sort(fe.begin(), fe.end());
+    std::vector<uint32_t> fl(fe.size());
+    for (size_t n = 0; n < fe.size(); ++n) fl[n] = fe[n].second;
+    // layout order is tile-layer major: offsets of each layer of tiles
+    // (slices 2^(lz+1) kt .. 2^(lz+1) (kt + 1) - 1)
+    std::vector<int> zoff(d.b.ntz + 1, 0);
+    for (size_t n = 0; n < fe.size(); ++n) {
+        int x, y, z;
+        unpack_xyz(fe[n].second, x, y, z);
+        zoff[((z >> 1) >> d.b.lz) + 1]++;
+    }
+    for (int kt = 0; kt < d.b.ntz; ++kt) zoff[kt + 1] += zoff[kt];
+    std::vector<int32_t> tm(g.n2(), -1);
+    if (perm) {
+        // the previous order from the previous tmap
+        std::vector<int32_t> old(g.n2(), -1);
+        if (d.tmap) MFLBM_CUDA(cudaMemcpy(old.data(), d.tmap, sizeof(int32_t) * g.n2(), cudaMemcpyDeviceToHost));
+        perm->assign(fl.size(), 0);
+        for (size_t n = 0; n < fl.size(); ++n) {
+            int x, y, z;
+            unpack_xyz(fl[n], x, y, z);
+            (*perm)[n] = old[g.s2(x, y, z)];
+            if ((*perm)[n] < 0) return fail(MFLBM_E_STATE, "fluid list: a node is missing from the previous order");
+        }
+    }
+    for (size_t n = 0; n < fl.size(); ++n) {
+        int x, y, z;
+        unpack_xyz(fl[n], x, y, z);
+        tm[g.s2(x, y, z)] = (int32_t)n;
+    }
+    int rc;
+    if ((rc = upload_list(&d.fluid_list, &d.n_fluid, fl)) != MFLBM_OK) return rc;
+    ll ntm = 0, nzo = 0;
+    if ((rc = upload_list(&d.tmap, &ntm, tm)) != MFLBM_OK) return rc;
+    if ((rc = upload_list(&d.zpair_off, &nzo, zoff)) != MFLBM_OK) return rc;
+    return MFLBM_OK;
+}
+
+// Node lists from the device geometry: the fluid nodes of [1, n]^3 in the
+// order of the population layout (order_fluid_list), and the solid boundary
+// nodes with an 18-bit mask of their fluid neighbours (bit q set when
+// neighbour x + e_q has walls_type <= 0).
 int build_lists(mflbm_context* c) {
     DeviceState& d = c->d;
     const Grid g = d.g;
     std::vector<int32_t> walls(g.n2()), wt(g.n4());
     MFLBM_CUDA(cudaMemcpy(walls.data(), d.walls, sizeof(int32_t) * g.n2(), cudaMemcpyDeviceToHost));
     MFLBM_CUDA(cudaMemcpy(wt.data(), d.walls_type, sizeof(int32_t) * g.n4(), cudaMemcpyDeviceToHost));
-    std::vector<std::pair<int, uint32_t>> fe;
+    std::vector<uint32_t> nodes;
     for (int k = 1; k <= g.nz; ++k)
         for (int j = 1; j <= g.ny; ++j)
             for (int i = 1; i <= g.nx; ++i)
-                if (walls[g.s2(i, j, k)] == 0) fe.emplace_back(d.b.elem(i, j, k), pack_xyz(i, j, k));
-    std::sort(fe.begin(), fe.end());
-    std::vector<uint32_t> fl(fe.size());
-    for (size_t n = 0; n < fe.size(); ++n) fl[n] = fe[n].second;
-    // brick order is z-pair major: offsets of each pair of slices (2 kp, 2 kp + 1)
-    std::vector<int> zoff(d.b.nbz + 1, 0);
-    for (size_t n = 0; n < fe.size(); ++n) zoff[(fe[n].first >> 3) / (d.b.nbx * d.b.nby) + 1]++;
-    for (int kp = 0; kp < d.b.nbz; ++kp) zoff[kp + 1] += zoff[kp];
+                if (walls[g.s2(i, j, k)] == 0) nodes.push_back(pack_xyz(i, j, k));
     std::vector<uint2> lphi;
     ll ncn = 0;   // walls_type == 2 nodes of [0, n+1]^3: bound of the claimed solid nodes
     for (int k = -2; k <= g.nz + 3; ++k)
@@ -115,16 +160,8 @@ int build_lists(mflbm_context* c) {
                 if (i >= 0 && i <= g.nx + 1 && j >= 0 && j <= g.ny + 1 && k >= 0 && k <= g.nz + 1) ++ncn;
             }
     int rc;
-    if ((rc = upload_list(&d.fluid_list, &d.n_fluid, fl)) != MFLBM_OK) return rc;
+    if ((rc = order_fluid_list(c, nodes, nullptr)) != MFLBM_OK) return rc;
     {
-        std::vector<int32_t> tm(g.n2(), -1);
-        for (size_t n = 0; n < fl.size(); ++n) {
-            int x, y, z;
-            unpack_xyz(fl[n], x, y, z);
-            tm[g.s2(x, y, z)] = (int32_t)n;
-        }
-        ll ntm = 0;
-        if ((rc = upload_list(&d.tmap, &ntm, tm)) != MFLBM_OK) return rc;
         // the nodes whose normal the step may need (walls_type <= 0 on
         // [-1, n+2]^3: their count bounds the sparse lists) and their
         // solid-boundary neighbours (the claims of the normal extrapolation)
@@ -168,8 +205,6 @@ int build_lists(mflbm_context* c) {
         MFLBM_CUDA(cudaMemset(d.smask, 0, sizeof(uint32_t) * nmask));
         MFLBM_CUDA(cudaMemset(d.gcount, 0, 4 * sizeof(int)));
     }
-    ll nzo = 0;
-    if ((rc = upload_list(&d.zpair_off, &nzo, zoff)) != MFLBM_OK) return rc;
     if (d.phi_prev) cudaFree(d.phi_prev);
     d.phi_prev = nullptr;
     if (d.aux) cudaFree(d.aux);
@@ -315,6 +350,60 @@ int capture_batch(mflbm_batch* b) {
 
 int check_block(int v) { return v == 0 || v == 64 || v == 128 || v == 256; }
 
+// log2 of a tile extent (a power of two, 1 .. max); false otherwise
+bool tile_shift(int extent, int max, int* out) {
+    for (int l = 0; (1 << l) <= max; ++l)
+        if (extent == (1 << l)) { *out = l; return true; }
+    return false;
+}
+bool tile_shifts(int tx, int ty, int tz, int* lx, int* ly, int* lz) {
+    return tile_shift(tx, 32, lx) && tile_shift(ty, 32, ly) && tile_shift(tz, 2, lz);
+}
+
+void fill_tuning(const mflbm_context& c, mflbm_tuning* out) {
+    const Tuning& t = c.d.tune;
+    out->collide_block = t.collide; out->normals_block = t.normals;
+    out->curvature_block = t.curvature; out->extrapolate_block = t.extrapolate;
+    out->tile_x = 1 << c.d.b.lx; out->tile_y = 1 << c.d.b.ly; out->tile_z = 1 << c.d.b.lz;
+}
+
+// Switch the population layout to tiles of 2^lx x 2^ly x 2^lz bricks.  The
+// populations move element by element and the collision records follow the
+// fluid list's new order, so the state, and every later step, is unchanged
+// (bit for bit).
+int set_tiling(mflbm_context* c, int lx, int ly, int lz) {
+    DeviceState& d = c->d;
+    if (lx == d.b.lx && ly == d.b.ly && lz == d.b.lz) return MFLBM_OK;
+    const Bricks to = make_bricks(d.g.nx, d.g.ny, d.g.nz, lx, ly, lz);
+    void* pdf = nullptr;
+    int rc = relayout_populations(*c, to, &pdf);
+    if (rc != MFLBM_OK) return rc;
+    MFLBM_CUDA(cudaStreamSynchronize(c->stream));
+    cudaFree(d.pdf);
+    d.pdf = pdf;
+    d.b = to;
+    if (d.fluid_list && d.n_fluid > 0) {
+        std::vector<uint32_t> nodes((size_t)d.n_fluid);
+        MFLBM_CUDA(cudaMemcpy(nodes.data(), d.fluid_list, sizeof(uint32_t) * nodes.size(), cudaMemcpyDeviceToHost));
+        std::vector<int> perm;
+        if ((rc = order_fluid_list(c, nodes, &perm)) != MFLBM_OK) return rc;
+        int* perm_dev = nullptr;
+        MFLBM_CUDA(cudaMalloc(&perm_dev, sizeof(int) * perm.size()));
+        MFLBM_CUDA(cudaMemcpy(perm_dev, perm.data(), sizeof(int) * perm.size(), cudaMemcpyHostToDevice));
+        void* aux = nullptr;
+        rc = permute_records(*c, perm_dev, &aux);
+        cudaStreamSynchronize(c->stream);
+        cudaFree(perm_dev);
+        if (rc != MFLBM_OK) return rc;
+        cudaFree(d.aux);
+        d.aux = aux;
+    }
+    if (c->pair_graph) { cudaGraphExecDestroy(c->pair_graph); c->pair_graph = nullptr; }
+    c->pair_graph_odd_first = -1;
+    c->generation++;
+    return MFLBM_OK;
+}
+
 }  // namespace
 }  // namespace mflbm
 
@@ -337,7 +426,6 @@ int mflbm_create(const mflbm_params* params, mflbm_context** out) {
     d.precision = params->precision;
     const Grid& g = d.g;
     const size_t T = tsize(c);
-    if (d.b.S >= (1ll << 31)) { delete c; return fail(MFLBM_E_ARG, "lattice too large for 32-bit brick indexing"); }
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { delete c; return fail(MFLBM_E_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e)); }
     struct { void** p; size_t bytes; } allocs[] = {
@@ -702,6 +790,15 @@ int mflbm_set_tuning(mflbm_context* c, const mflbm_tuning* t) {
     if (!check_block(t->collide_block) || !check_block(t->normals_block) || !check_block(t->curvature_block) ||
         !check_block(t->extrapolate_block))
         return fail(MFLBM_E_ARG, "mflbm_set_tuning: block sizes must be 64, 128, 256 or 0");
+    const bool tile = t->tile_x || t->tile_y || t->tile_z;
+    int lx = 0, ly = 0, lz = 0;
+    if (tile && !tile_shifts(t->tile_x, t->tile_y, t->tile_z, &lx, &ly, &lz))
+        return fail(MFLBM_E_ARG, "mflbm_set_tuning: tile extents must be powers of two, x and y 1-32, z 1 or 2 "
+                                 "(all three, or all three 0)");
+    if (tile) {
+        const int rc = set_tiling(c, lx, ly, lz);
+        if (rc != MFLBM_OK) return rc;
+    }
     Tuning& tn = c->d.tune;
     if (t->collide_block) tn.collide = t->collide_block;
     if (t->normals_block) tn.normals = t->normals_block;
@@ -709,6 +806,13 @@ int mflbm_set_tuning(mflbm_context* c, const mflbm_tuning* t) {
     if (t->extrapolate_block) tn.extrapolate = t->extrapolate_block;
     if (c->pair_graph) { cudaGraphExecDestroy(c->pair_graph); c->pair_graph = nullptr; }
     c->generation++;
+    return MFLBM_OK;
+}
+
+int mflbm_get_tuning(mflbm_context* c, mflbm_tuning* out) {
+    if (!c || !out) return fail(MFLBM_E_ARG, "mflbm_get_tuning: null argument");
+    fill_tuning(*c, out);
+    out->step_ms_before = out->step_ms_after = 0.0;
     return MFLBM_OK;
 }
 
@@ -721,15 +825,22 @@ int mflbm_autotune(mflbm_context* c, int reps, mflbm_tuning* out) {
     const Grid& g = d.g;
     const size_t T = tsize(c), pl = (size_t)g.plane1();
     const size_t pop_e = c->params.storage == MFLBM_STORE_NATIVE ? T : 2;
+    struct Span { void* p; size_t n; };
     // everything a step writes: populations, phi, records, convective buffers
-    struct { void* p; size_t n; } st[] = {{d.pdf, pop_e * d.b.S * 38}, {d.phi, T * g.n4()},
-                                          {d.aux, T * 4 * std::max<ll>(1, d.n_fluid)}, {d.cnv4, T * 4 * g.n2()},
-                                          {d.f_cv, T * pl * 19}, {d.g_cv, T * pl * 19}, {d.phi_cv, T * pl},
-                                          {d.dither, 2 * sizeof(uint32_t)}, {d.iface, (size_t)g.n2()},
-                                          {d.olist, sizeof(uint32_t) * std::max<ll>(1, d.n_norm)},
-                                          {d.slist, sizeof(uint32_t) * std::max<ll>(1, d.n_cn_ext)},
-                                          {d.smask, sizeof(uint32_t) * (size_t)(g.n2() / 32 + 1)},
-                                          {d.gcount, 4 * sizeof(int)}};
+    // (pointers re-read after every change of tile shape, which reallocates
+    // the populations and the collision records)
+    auto state = [&]() {
+        return std::vector<Span>{{d.pdf, pop_e * d.b.S * 38}, {d.phi, T * g.n4()},
+                                 {d.aux, T * 4 * std::max<ll>(1, d.n_fluid)}, {d.cnv4, T * 4 * g.n2()},
+                                 {d.f_cv, T * pl * 19}, {d.g_cv, T * pl * 19}, {d.phi_cv, T * pl},
+                                 {d.dither, 2 * sizeof(uint32_t)}, {d.iface, (size_t)g.n2()},
+                                 {d.olist, sizeof(uint32_t) * std::max<ll>(1, d.n_norm)},
+                                 {d.slist, sizeof(uint32_t) * std::max<ll>(1, d.n_cn_ext)},
+                                 {d.smask, sizeof(uint32_t) * (size_t)(g.n2() / 32 + 1)},
+                                 {d.gcount, 4 * sizeof(int)}};
+    };
+    const int elx = d.b.lx, ely = d.b.ly, elz = d.b.lz;   // the tile shape on entry (the saved state's layout)
+    std::vector<Span> st = state();
     size_t total = 0;
     for (auto& x : st) total += (x.n + 255) / 256 * 256;
     char* save = nullptr;
@@ -761,6 +872,19 @@ int mflbm_autotune(mflbm_context* c, int reps, mflbm_tuning* out) {
     double before = 0, best_ms = 0;
     rc = measure(best, &before);
     best_ms = before;
+    // tile shape of the population layout (with the entry block sizes), then
+    // block sizes, one kernel family at a time
+    int blx = elx, bly = ely, blz = elz;
+    static const int kTiles[][3] = {{3, 2, 1}, {3, 3, 1}, {1, 1, 1}, {3, 1, 1}, {4, 1, 1}, {2, 2, 1}};
+    for (const auto& tl : kTiles) {
+        if (rc != MFLBM_OK) break;
+        if (tl[0] == elx && tl[1] == ely && tl[2] == elz) continue;
+        if ((rc = set_tiling(c, tl[0], tl[1], tl[2])) != MFLBM_OK) break;
+        double ms = 0;
+        if ((rc = measure(best, &ms)) != MFLBM_OK) break;
+        if (ms < best_ms) { best_ms = ms; blx = tl[0]; bly = tl[1]; blz = tl[2]; }
+    }
+    if (rc == MFLBM_OK) rc = set_tiling(c, blx, bly, blz);
     for (int f = 0; f < 4 && rc == MFLBM_OK; ++f)
         for (int bs : {64, 128, 256}) {
             Tuning t = best;
@@ -772,12 +896,19 @@ int mflbm_autotune(mflbm_context* c, int reps, mflbm_tuning* out) {
             if (ms < best_ms) { best_ms = ms; best = t; }
         }
     d.tune = best;
-    off = 0;
-    for (auto& x : st) {
-        cudaMemcpyAsync(x.p, save + off, x.n, cudaMemcpyDeviceToDevice, c->stream);
-        off += (x.n + 255) / 256 * 256;
+    // back to the entry layout, the saved state, then the chosen layout (both
+    // moves are exact)
+    int rc2 = set_tiling(c, elx, ely, elz);
+    if (rc2 == MFLBM_OK) {
+        st = state();
+        off = 0;
+        for (auto& x : st) {
+            cudaMemcpyAsync(x.p, save + off, x.n, cudaMemcpyDeviceToDevice, c->stream);
+            off += (x.n + 255) / 256 * 256;
+        }
+        cudaStreamSynchronize(c->stream);
+        if (rc == MFLBM_OK) rc2 = set_tiling(c, blx, bly, blz);
     }
-    cudaStreamSynchronize(c->stream);
     cudaFree(save);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -785,9 +916,9 @@ int mflbm_autotune(mflbm_context* c, int reps, mflbm_tuning* out) {
     if (c->pair_graph) { cudaGraphExecDestroy(c->pair_graph); c->pair_graph = nullptr; }
     c->generation++;
     if (rc != MFLBM_OK) return rc;
+    if (rc2 != MFLBM_OK) return rc2;
     if (out) {
-        out->collide_block = best.collide; out->normals_block = best.normals;
-        out->curvature_block = best.curvature; out->extrapolate_block = best.extrapolate;
+        fill_tuning(*c, out);
         out->step_ms_before = before; out->step_ms_after = best_ms;
     }
     return MFLBM_OK;

@@ -161,22 +161,22 @@ __device__ __forceinline__ T collide(const Phys<T>& P, T (&g1)[19], T (&g2)[19],
 
 
 // ===========================================================================
-// Collision + AA streaming over the fluid-node list (brick layout).
+// Collision + AA streaming over the fluid-node list (tiled brick layout).
 //   odd  step: populations pulled from slot q of node x - e_q, pushed to
 //              slot opp(q) of node x + e_q (src/main_iteration_GPU.cu:75-113, 348-384)
 //   even step: read from slot opp(q) of x, written to slot q of x (:414-452, 687-723)
-// In the brick layout the element offset of a neighbour depends only on the
-// parities of (x, y, z): each thread forms six deltas once and every access
-// is slot_base + element.
+// The pair index of a node is separable per axis (Bricks::ax/ay/az), so each
+// thread forms three values per axis (x - 1, x, x + 1, ...) and every
+// neighbour address is a sum of three of them.  I is the index type: 32-bit
+// where the whole population array has fewer than 2^32 pairs.
 // ===========================================================================
 template <class T, class E> struct CollideArgs {
     typedef typename Pop2<E>::type P2;
     typedef typename Vec4<T>::type V4;
-    P2* slot[19];
+    P2* slot[19];   // direction q of tile 0: slot[q][i] is pair i + q * tile
     const uint32_t* list;
     int n;
-    int bx8, bxy8;  // element strides of one brick step in y and z
-    int nbx, nby;
+    Bricks b;
     int NX4, NY4;
     T* phi;
     const V4* aux;  // fluid-list order: (n_x, n_y, n_z, 0.5 * gamma * curv * c_norm)
@@ -195,28 +195,32 @@ template <class E, bool ODD> constexpr int collide_max_regs() {
     return sizeof(E) == 2 ? 64 : sizeof(E) == 4 ? (ODD ? 80 : 64) : 255;
 }
 
-template <class T, class E, bool ODD>
+template <class T, class E, bool ODD, class I>
 __global__ void __launch_bounds__(256) __maxnreg__((collide_max_regs<E, ODD>())) collide_stream_kernel(const CollideArgs<T, E> a) {
     typedef typename Pop2<E>::type P2;
     typedef PopCodec<T, E> Codec;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= a.n) return;
+    const uint32_t node = a.list[t];   // packed coordinates
     int x, y, z;
-    unpack_xyz(a.list[t], x, y, z);
-    const int e0 = (((x >> 1) + a.nbx * ((y >> 1) + a.nby * (z >> 1))) << 3) | (x & 1) | ((y & 1) << 1) | ((z & 1) << 2);
-    // element offsets of the +1 / -1 neighbour along each axis
-    const int dxp = (x & 1) ? 7 : 1, dxm = (x & 1) ? -1 : -7;
-    const int dyp = (y & 1) ? a.bx8 - 2 : 2, dym = (y & 1) ? -2 : 2 - a.bx8;
-    const int dzp = (z & 1) ? a.bxy8 - 4 : 4, dzm = (z & 1) ? -4 : 4 - a.bxy8;
-    auto delta = [&](int q) {  // element offset of x + e_q
-        return (ex(q) > 0 ? dxp : ex(q) < 0 ? dxm : 0) + (ey(q) > 0 ? dyp : ey(q) < 0 ? dym : 0) +
-               (ez(q) > 0 ? dzp : ez(q) < 0 ? dzm : 0);
+    unpack_xyz(node, x, y, z);
+    const Bricks& B = a.b;
+    const I X1 = (I)B.ax(x), Y1 = (I)B.ay(y), Z1 = (I)B.az(z);
+    const I e0 = X1 + Y1 + Z1;
+    I X0 = 0, X2 = 0, Y0 = 0, Y2 = 0, Z0 = 0, Z2 = 0;
+    if (ODD) {
+        X0 = (I)B.ax(x - 1); X2 = (I)B.ax(x + 1);
+        Y0 = (I)B.ay(y - 1); Y2 = (I)B.ay(y + 1);
+        Z0 = (I)B.az(z - 1); Z2 = (I)B.az(z + 1);
+    }
+    auto nb = [&](int q) -> I {  // pair index (direction 0) of x + e_q
+        return (ex(q) > 0 ? X2 : ex(q) < 0 ? X0 : X1) + (ey(q) > 0 ? Y2 : ey(q) < 0 ? Y0 : Y1) +
+               (ez(q) > 0 ? Z2 : ez(q) < 0 ? Z0 : Z1);
     };
-    // the offsets are not antisymmetric (they depend on parity): x - e_q is at delta(opp(q))
     T g1[19], g2[19];
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
-        const P2 v = ODD ? a.slot[q][e0 + delta(opp(q))] : a.slot[opp(q)][e0];
+        const P2 v = ODD ? a.slot[q][nb(opp(q))] : a.slot[opp(q)][e0];
         g1[q] = Codec::dec(v.x, lat_w<T>(q), lat_winv<T>(q));
         g2[q] = Codec::dec(v.y, lat_w<T>(q), lat_winv<T>(q));
     }
@@ -233,7 +237,7 @@ __global__ void __launch_bounds__(256) __maxnreg__((collide_max_regs<E, ODD>()))
     if (!std::is_same<T, E>::value) {
         const uint32_t step = a.dither[ODD ? 0 : 1];
         if (t == 0) a.dither[ODD ? 1 : 0] = step + 1u;
-        seed = mix32((uint32_t)e0 ^ mix32(step * 0x9E3779B9u ^ __float_as_uint((float)g1[1]) ^
+        seed = mix32(node ^ mix32(step * 0x9E3779B9u ^ __float_as_uint((float)g1[1]) ^
                                           mix32(__float_as_uint((float)g2[2]))));
     }
     const T phi = collide<T>(a.ph, g1, g2, av.x, av.y, av.z, av.w);
@@ -249,7 +253,7 @@ __global__ void __launch_bounds__(256) __maxnreg__((collide_max_regs<E, ODD>()))
             v.x = Codec::enc_dither(g1[q], lat_w<T>(q), lat_winv<T>(q), r & 0xffffu);
             v.y = Codec::enc_dither(g2[q], lat_w<T>(q), lat_winv<T>(q), r >> 16);
         }
-        if (ODD) a.slot[opp(q)][e0 + delta(q)] = v;
+        if (ODD) a.slot[opp(q)][nb(q)] = v;
         else a.slot[q][e0] = v;
     }
 }
@@ -261,12 +265,10 @@ int launch_collide(mflbm_context& c, bool odd) {
     const Grid& g = d.g;
     CollideArgs<T, E> a;
     P2* pdf = (P2*)d.pdf;
-    for (int q = 0; q < 19; ++q) a.slot[q] = pdf + d.b.S * q;
+    for (int q = 0; q < 19; ++q) a.slot[q] = pdf + d.b.tile * q;
     a.list = d.fluid_list;
     a.n = (int)d.n_fluid;
-    a.nbx = d.b.nbx; a.nby = d.b.nby;
-    a.bx8 = 8 * d.b.nbx;
-    a.bxy8 = 8 * d.b.nbx * d.b.nby;
+    a.b = d.b;
     a.NX4 = g.nx + 8; a.NY4 = g.ny + 8;
     a.phi = (T*)d.phi;
     a.aux = (const typename Vec4<T>::type*)d.aux;
@@ -276,8 +278,15 @@ int launch_collide(mflbm_context& c, bool odd) {
     a.ph = make_phys<T>(c.params);
     if (a.n == 0) return MFLBM_OK;
     const int bs = d.tune.collide;
-    if (odd) collide_stream_kernel<T, E, true><<<grid_for(a.n, bs), bs, 0, c.stream>>>(a);
-    else collide_stream_kernel<T, E, false><<<grid_for(a.n, bs), bs, 0, c.stream>>>(a);
+    const bool narrow = d.b.pairs() < (1ll << 32);   // 32-bit pair indices suffice
+    const unsigned grid = grid_for(a.n, bs);
+    if (narrow) {
+        if (odd) collide_stream_kernel<T, E, true, uint32_t><<<grid, bs, 0, c.stream>>>(a);
+        else collide_stream_kernel<T, E, false, uint32_t><<<grid, bs, 0, c.stream>>>(a);
+    } else {
+        if (odd) collide_stream_kernel<T, E, true, unsigned long long><<<grid, bs, 0, c.stream>>>(a);
+        else collide_stream_kernel<T, E, false, unsigned long long><<<grid, bs, 0, c.stream>>>(a);
+    }
     return after_launch("collide_stream");
 }
 

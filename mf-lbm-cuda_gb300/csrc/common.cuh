@@ -54,29 +54,62 @@ struct Grid {
     __host__ __device__ ll plane1() const { return (ll)(nx + 2) * (ny + 2); }
 };
 
-// Internal population layout: the lattice [0, n+1]^3 is cut into 2x2x2
-// bricks stored x-fastest; the 8 nodes of a brick are consecutive
-// (bit 0 = x parity, bit 1 = y parity, bit 2 = z parity) and each slot holds
-// both components (g = 0, 1) side by side.  Population (node, e, g) is
-// element 2 * (e * S + elem(node)) + g of the population array.  A 64-byte
-// DRAM line then holds one brick of one direction, so partially fluid lines
-// waste far less than the reference's x-rows (one line = 16 nodes of a row).
+// Internal population layout.  The lattice [0, n+1]^3 is cut into 2x2x2
+// bricks; the 8 nodes of a brick are consecutive (bit 0 = x parity, bit 1 =
+// y parity, bit 2 = z parity) and each slot holds both components (g = 0, 1)
+// side by side, so one 64-byte DRAM burst (FP32) holds one brick of one
+// direction.  Bricks are grouped into tiles of 2^lx x 2^ly x 2^lz bricks;
+// a tile stores its 19 directions one after the other (direction q of the
+// tile: TILE = 8 * 2^(lx+ly+lz) consecutive pairs, bricks x-fastest inside),
+// and tiles are stored x-fastest.  A node's pulls and pushes then stay in its
+// own tile's few tens of kilobytes for most directions (the odd step's
+// neighbours across a z layer of bricks included when lz >= 1), instead of
+// 19 arrays a slot-size apart.
+//
+// The pair index of (node, direction q) is ax(x) + ay(y) + az(z) + q * TILE:
+// separable per axis, so a thread forms its 27 neighbour addresses from
+// three values per axis.
 struct Bricks {
-    int nbx, nby, nbz;
-    ll S;  // elements (nodes incl. padding) per direction
-    __host__ __device__ int elem(int x, int y, int z) const {
-        return (((x >> 1) + nbx * ((y >> 1) + nby * (z >> 1))) << 3) | (x & 1) | ((y & 1) << 1) | ((z & 1) << 2);
+    int nbx, nby, nbz;      // bricks per axis (cover [0, n+1])
+    int lx, ly, lz;         // log2 of the tile extent in bricks
+    int ntx, nty, ntz;      // tiles per axis
+    ll tile;                // pairs per direction of a tile (8 << (lx + ly + lz))
+    ll S;                   // pairs per direction over all tiles (padding included)
+    __host__ __device__ ll ax(int x) const {
+        const int b = x >> 1;
+        return (ll)(b >> lx) * (19 * tile) + ((b & ((1 << lx) - 1)) << 3) + (x & 1);
     }
+    __host__ __device__ ll ay(int y) const {
+        const int b = y >> 1;
+        return (ll)(b >> ly) * (19 * tile) * ntx + ((b & ((1 << ly) - 1)) << (3 + lx)) + ((y & 1) << 1);
+    }
+    __host__ __device__ ll az(int z) const {
+        const int b = z >> 1;
+        return (ll)(b >> lz) * (19 * tile) * ntx * nty + ((b & ((1 << lz) - 1)) << (3 + lx + ly)) + ((z & 1) << 2);
+    }
+    // pair index of direction 0 of node (x, y, z)
+    __host__ __device__ ll elem(int x, int y, int z) const { return ax(x) + ay(y) + az(z); }
+    // element index of component g of direction e of node (x, y, z)
     __host__ __device__ ll at(int x, int y, int z, int e, int g) const {
-        return 2 * ((ll)e * S + elem(x, y, z)) + g;
+        return 2 * (elem(x, y, z) + (ll)e * tile) + g;
     }
+    // pairs of the whole population array (19 directions)
+    __host__ __device__ ll pairs() const { return 19 * S; }
 };
-inline Bricks make_bricks(int nx, int ny, int nz) {
+// The tile extent used unless a tuning chooses another: 8 x 4 x 2 bricks
+// (16 x 8 x 4 nodes).
+constexpr int kTileLx = 3, kTileLy = 2, kTileLz = 1;
+inline Bricks make_bricks(int nx, int ny, int nz, int lx = kTileLx, int ly = kTileLy, int lz = kTileLz) {
     Bricks b;
     b.nbx = (nx + 3) / 2;  // covers x in [0, nx+1]
     b.nby = (ny + 3) / 2;
     b.nbz = (nz + 3) / 2;
-    b.S = (ll)b.nbx * b.nby * b.nbz * 8;
+    b.lx = lx; b.ly = ly; b.lz = lz;
+    b.ntx = (b.nbx + (1 << lx) - 1) >> lx;
+    b.nty = (b.nby + (1 << ly) - 1) >> ly;
+    b.ntz = (b.nbz + (1 << lz) - 1) >> lz;
+    b.tile = (ll)8 << (lx + ly + lz);
+    b.S = b.tile * b.ntx * b.nty * b.ntz;
     return b;
 }
 

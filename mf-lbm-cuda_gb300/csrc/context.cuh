@@ -16,7 +16,7 @@ struct DeviceState {
     Grid g{};
     Bricks b{};
     int precision = MFLBM_FP32;
-    // populations in the brick layout (common.cuh); fields in the reference layouts (s4 / s2 / s1)
+    // populations in the tiled brick layout (common.cuh); fields in the reference layouts (s4 / s2 / s1)
     void* pdf = nullptr;
     void* staging = nullptr;        // reference-layout (f1) buffer for uploads / downloads
     void* cnv4 = nullptr;           // s2: (n_x, n_y, n_z, |grad phi|) per node
@@ -41,16 +41,17 @@ struct DeviceState {
     void* s_ny = nullptr;
     void* s_nz = nullptr;
     // node lists (packed coordinates)
-    uint32_t* fluid_list = nullptr;    // walls == 0 on [1, n]^3, in brick-element order
+    uint32_t* fluid_list = nullptr;    // walls == 0 on [1, n]^3, in population-layout order
     ll n_fluid = 0;
     uint2* list_phi_ext = nullptr;     // walls_type == 2 on [-2, n+3]^3: (packed, fluid-neighbour mask)
     ll n_phi_ext = 0;
     ll n_cn_ext = 0;                   // walls_type == 2 nodes on [0, n+1]^3 (capacity of slist)
     double* red = nullptr;             // reduction scratch
     ll red_len = 0;
-    int* zpair_off = nullptr;          // fluid-list offset of each z pair (2 kp, 2 kp + 1), nbz + 1 entries
+    int* zpair_off = nullptr;          // fluid-list offset of each layer of population tiles, ntz + 1 entries
     void* phi_prev = nullptr;          // phi at the previous tracking monitor call (s4)
     double* prof = nullptr;            // per-slice and per-block monitor partials
+    ll prof_len = 0;
     uint32_t* dither = nullptr;        // step counter of 16-bit stochastic rounding: [0] read by odd, [1] by even steps
     int8_t* iface = nullptr;           // s2: 1 where the normal record may be non-zero (|grad phi| >= 1e-6, type <= 0)
     int8_t* phib = nullptr;            // per 2x2x2 brick of the s4 lattice: 1 all phi = +1, 2 all phi = -1, else 0

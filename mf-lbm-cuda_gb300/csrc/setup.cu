@@ -422,26 +422,20 @@ __global__ void __launch_bounds__(256) monitor_partials(Grid g, PopView<T, E> P,
     }
 }
 
-// sum of every stored population of both components; with 16-bit storage the
-// elements are decoded and the brick padding beyond [0, n+1] is skipped
-// (its zero bits do not encode a zero population)
+// sum of the stored populations of both components over every node of
+// [0, n+1]^3 (the tiles' padding beyond the lattice is not visited), decoded
+// in T and summed in FP64
 template <class T, class E>
 __global__ void __launch_bounds__(256) sum_all(Grid g, PopView<T, E> P, double* partial) {
-    const ll n = P.b.S * 38;
+    const ll n1 = g.n1(), nxy = (ll)(g.nx + 2) * (g.ny + 2);
     double acc = 0;
-    for (ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (ll)gridDim.x * blockDim.x) {
-        if (std::is_same<T, E>::value) {
-            acc += (double)PopCodec<T, E>::dec(P.p[t], T(0), T(0));
-        } else {
-            const ll slot = t >> 1;
-            const int q = (int)(slot / P.b.S);
-            const ll el = slot - (ll)q * P.b.S, brick = el >> 3;
-            const int x = (int)(2 * (brick % P.b.nbx)) + (int)(el & 1);
-            const int y = (int)(2 * ((brick / P.b.nbx) % P.b.nby)) + (int)((el >> 1) & 1);
-            const int z = (int)(2 * (brick / ((ll)P.b.nbx * P.b.nby))) + (int)((el >> 2) & 1);
-            if (x <= g.nx + 1 && y <= g.ny + 1 && z <= g.nz + 1)
-                acc += (double)PopCodec<T, E>::dec(P.p[t], lat_w<T>(q), lat_winv<T>(q));
-        }
+    for (ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x; t < n1 * 19; t += (ll)gridDim.x * blockDim.x) {
+        const int q = (int)(t / n1);
+        const ll r = t - (ll)q * n1;
+        const int z = (int)(r / nxy);
+        const ll rxy = r - (ll)z * nxy;
+        const int y = (int)(rxy / (g.nx + 2)), x = (int)(rxy - (ll)y * (g.nx + 2));
+        acc += (double)P.get(x, y, z, q, 0) + (double)P.get(x, y, z, q, 1);
     }
     __shared__ double sh[8];
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
@@ -497,7 +491,6 @@ int monitor_into(mflbm_context& c, int nex_in, int nex_out, double* scratch, int
     if ((rc = after_launch("monitor_partials")) != MFLBM_OK) return rc;
     fold_partials<<<NRED, 32, 0, s>>>(blocks, NRED, part, res);
     if ((rc = after_launch("fold_partials")) != MFLBM_OK) return rc;
-    // padding elements of the brick layout are zero and never written
     sum_all<T, E><<<blocks, 256, 0, s>>>(g, pop_view<T, E>(d), part2);
     if ((rc = after_launch("sum_all")) != MFLBM_OK) return rc;
     fold_partials<<<1, 32, 0, s>>>(blocks, 1, part2, res + NRED);
@@ -584,22 +577,24 @@ int monitor_noalloc_t(mflbm_context& c, int nex_in, int nex_out, mflbm_monitor* 
 // Per-slice monitor profiles and the other monitor scalars (FP64),
 // src/Monitor.cpp:17-104 (profiles, kinetic energy), :277-351 (phase-field
 // steady state), :355-441 (capillary-pressure steady state), :447-466
-// (breakthrough).  One block per z pair of the fluid list (brick order is
-// z-pair major): every sum is taken in a fixed order, so results repeat
-// exactly.  Thresholds compare phi in the solver precision, as the reference.
+// (breakthrough).  One block per layer of population tiles (SZ = 2 << lz
+// slices; the fluid list is in tile order, hence tile-layer major): every
+// sum is taken in a fixed order, so results repeat exactly.  Thresholds
+// compare phi in the solver precision, as the reference.
 // ---------------------------------------------------------------------------
 constexpr int kProfSums = 7, kProfExt = 9;  // ext: umax2 usq1 usq2 pre_w pre_nw n_w n_nw breakthrough dphi_max
 
-template <class T, class E>
+template <class T, class E, int SZ>
 __global__ void __launch_bounds__(256) monitor_profile_kernel(Grid g, PopView<T, E> P, const uint32_t* list, const int* zoff,
                                                               const T* phi, T* phi_prev,
                                                               const typename Vec4<T>::type* aux, const int8_t* iface,
                                                               double force_z, int track, double* out) {
+    constexpr int NACC = SZ * kProfSums + kProfExt;
     const int kp = blockIdx.x;
-    double acc[2 * kProfSums + kProfExt];
+    double acc[NACC];
 #pragma unroll
-    for (int r = 0; r < 2 * kProfSums + kProfExt; ++r) acc[r] = 0.0;
-    double* ext = acc + 2 * kProfSums;
+    for (int r = 0; r < NACC; ++r) acc[r] = 0.0;
+    double* ext = acc + SZ * kProfSums;
     for (int t = zoff[kp] + threadIdx.x; t < zoff[kp + 1]; t += blockDim.x) {
         int i, j, k;
         unpack_xyz(list[t], i, j, k);
@@ -620,7 +615,7 @@ __global__ void __launch_bounds__(256) monitor_profile_kernel(Grid g, PopView<T,
         const ll n4 = g.s4(i, j, k);
         const T ph = phi[n4];
         const double pd = (double)ph, a1 = 0.5 * (1.0 + pd), a2 = 0.5 * (1.0 - pd);
-        double* sl = acc + (k & 1) * kProfSums;
+        double* sl = acc + (k & (SZ - 1)) * kProfSums;
         sl[0] += w * a1; sl[1] += w * a2; sl[2] += a1; sl[3] += a2;
         sl[4] += rho * a1; sl[5] += rho * a2; sl[6] += rho;
         const double u2 = u * u + v * v + w * w;
@@ -635,11 +630,11 @@ __global__ void __launch_bounds__(256) monitor_profile_kernel(Grid g, PopView<T,
             phi_prev[n4] = ph;
         }
     }
-    __shared__ double sh[2 * kProfSums + kProfExt][8];
+    __shared__ double sh[NACC][8];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-    for (int r = 0; r < 2 * kProfSums + kProfExt; ++r) {
-        const bool is_max = r == 2 * kProfSums || r == 2 * kProfSums + 8;
+    for (int r = 0; r < NACC; ++r) {
+        const bool is_max = r == SZ * kProfSums || r == SZ * kProfSums + 8;
         double x = acc[r];
         for (int o = 16; o > 0; o >>= 1) {
             const double y = __shfl_down_sync(0xffffffffu, x, o);
@@ -648,12 +643,12 @@ __global__ void __launch_bounds__(256) monitor_profile_kernel(Grid g, PopView<T,
         if (lane == 0) sh[r][warp] = x;
     }
     __syncthreads();
-    if (threadIdx.x < 2 * kProfSums + kProfExt) {
+    if (threadIdx.x < NACC) {
         const int r = threadIdx.x;
-        const bool is_max = r == 2 * kProfSums || r == 2 * kProfSums + 8;
+        const bool is_max = r == SZ * kProfSums || r == SZ * kProfSums + 8;
         double x = sh[r][0];
         for (int w = 1; w < (int)(blockDim.x >> 5); ++w) x = is_max ? fmax(x, sh[r][w]) : x + sh[r][w];
-        out[(ll)kp * (2 * kProfSums + kProfExt) + r] = x;
+        out[(ll)kp * NACC + r] = x;
     }
 }
 
@@ -661,28 +656,41 @@ template <class T, class E>
 int monitor_profile_t(mflbm_context& c, double* slices, mflbm_monitor_ext* ext, bool track) {
     DeviceState& d = c.d;
     const Grid g = d.g;
-    const int nb = d.b.nbz, per = 2 * kProfSums + kProfExt;
-    if (!d.prof) MFLBM_CUDA(cudaMalloc(&d.prof, sizeof(double) * nb * per));
+    const int lz = d.b.lz, sz = 2 << lz;   // slices per tile layer
+    if (lz > 1) return fail(MFLBM_E_STATE, "monitor profile: tiles of more than 2 brick layers");
+    const int nb = d.b.ntz, per = sz * kProfSums + kProfExt;
+    if (d.prof_len < (ll)nb * per) {
+        if (d.prof) cudaFree(d.prof);
+        d.prof = nullptr;
+        d.prof_len = 0;
+        MFLBM_CUDA(cudaMalloc(&d.prof, sizeof(double) * nb * per));
+        d.prof_len = (ll)nb * per;
+    }
     if (track && !d.phi_prev) {
         MFLBM_CUDA(cudaMalloc(&d.phi_prev, sizeof(T) * g.n4()));
         MFLBM_CUDA(cudaMemsetAsync(d.phi_prev, 0, sizeof(T) * g.n4(), c.stream));
     }
-    monitor_profile_kernel<T, E><<<nb, 256, 0, c.stream>>>(g, pop_view<T, E>(d), d.fluid_list, d.zpair_off,
-                                                        (const T*)d.phi, (T*)d.phi_prev,
-                                                        (const typename Vec4<T>::type*)d.aux, d.iface,
-                                                        (double)T(c.params.force_z), track ? 1 : 0, d.prof);
+#define MFLBM_PROFILE(SZ)                                                                                         \
+    monitor_profile_kernel<T, E, SZ><<<nb, 256, 0, c.stream>>>(g, pop_view<T, E>(d), d.fluid_list, d.zpair_off,  \
+                                                            (const T*)d.phi, (T*)d.phi_prev,                     \
+                                                            (const typename Vec4<T>::type*)d.aux, d.iface,       \
+                                                            (double)T(c.params.force_z), track ? 1 : 0, d.prof)
+    if (lz == 0) MFLBM_PROFILE(2);
+    else MFLBM_PROFILE(4);
+#undef MFLBM_PROFILE
     int rc = after_launch("monitor_profile");
     if (rc != MFLBM_OK) return rc;
     std::vector<double> h((size_t)nb * per);
     MFLBM_CUDA(cudaMemcpyAsync(h.data(), d.prof, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c.stream));
     MFLBM_CUDA(cudaStreamSynchronize(c.stream));
     for (int m = 0; m < kProfSums; ++m)
-        for (int k = 1; k <= g.nz; ++k) slices[(size_t)m * g.nz + k - 1] = h[(size_t)(k >> 1) * per + (k & 1) * kProfSums + m];
+        for (int k = 1; k <= g.nz; ++k)
+            slices[(size_t)m * g.nz + k - 1] = h[(size_t)(k / sz) * per + (k % sz) * kProfSums + m];
     if (ext) {
         double e[kProfExt] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
         for (int kp = 0; kp < nb; ++kp)
             for (int r = 0; r < kProfExt; ++r) {
-                const double x = h[(size_t)kp * per + 2 * kProfSums + r];
+                const double x = h[(size_t)kp * per + sz * kProfSums + r];
                 e[r] = (r == 0 || r == 8) ? std::max(e[r], x) : e[r] + x;
             }
         ext->umax2 = e[0]; ext->usq1 = e[1]; ext->usq2 = e[2];
@@ -691,6 +699,65 @@ int monitor_profile_t(mflbm_context& c, double* slices, mflbm_monitor_ext* ext, 
         ext->breakthrough = (long long)e[7];
         ext->dphi_max = e[8];
     }
+    return MFLBM_OK;
+}
+
+// Populations moved from one tile shape to another, element by element
+// without decoding (16-bit storage keeps its stored bits), one thread per
+// (node, direction) of [0, n+1]^3.
+template <class P2>
+__global__ void relayout_kernel(Grid g, Bricks from, Bricks to, const P2* src, P2* dst) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, kq = blockIdx.z;
+    const int k = kq % (g.nz + 2), q = kq / (g.nz + 2);
+    if (i > g.nx + 1) return;
+    dst[to.elem(i, j, k) + (ll)q * to.tile] = src[from.elem(i, j, k) + (ll)q * from.tile];
+}
+
+int relayout_impl(mflbm_context& c, const Bricks& to, void** out) {
+    DeviceState& d = c.d;
+    const Grid g = d.g;
+    const size_t pair = c.params.storage != MFLBM_STORE_NATIVE ? 4 : (c.params.precision == MFLBM_FP32 ? 8 : 16);
+    void* dst = nullptr;
+    MFLBM_CUDA(cudaMalloc(&dst, pair * (size_t)to.pairs()));
+    MFLBM_CUDA(cudaMemsetAsync(dst, 0, pair * (size_t)to.pairs(), c.stream));
+    const dim3 grid(grid_for(g.nx + 2, 128), g.ny + 2, (unsigned)((g.nz + 2) * 19));
+    if (pair == 4) relayout_kernel<uint32_t><<<grid, 128, 0, c.stream>>>(g, d.b, to, (const uint32_t*)d.pdf, (uint32_t*)dst);
+    else if (pair == 8) relayout_kernel<uint2><<<grid, 128, 0, c.stream>>>(g, d.b, to, (const uint2*)d.pdf, (uint2*)dst);
+    else relayout_kernel<uint4><<<grid, 128, 0, c.stream>>>(g, d.b, to, (const uint4*)d.pdf, (uint4*)dst);
+    const int rc = after_launch("relayout");
+    if (rc != MFLBM_OK) {
+        cudaFree(dst);
+        return rc;
+    }
+    *out = dst;
+    return MFLBM_OK;
+}
+
+// Collision records gathered into a new fluid-list order: dst[t] = src[perm[t]].
+template <class V>
+__global__ void gather_records(const V* src, const int* perm, V* dst, ll n) {
+    const ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) dst[t] = src[perm[t]];
+}
+
+int permute_impl(mflbm_context& c, const int* perm_dev, void** out) {
+    DeviceState& d = c.d;
+    const ll n = std::max<ll>(1, d.n_fluid);
+    const size_t rec = (c.params.precision == MFLBM_FP32 ? 4 : 8) * 4;
+    void* dst = nullptr;
+    MFLBM_CUDA(cudaMalloc(&dst, rec * n));
+    if (d.n_fluid > 0) {
+        if (c.params.precision == MFLBM_FP32)
+            gather_records<float4><<<grid_for(d.n_fluid, 256), 256, 0, c.stream>>>((const float4*)d.aux, perm_dev, (float4*)dst, d.n_fluid);
+        else
+            gather_records<Double4><<<grid_for(d.n_fluid, 256), 256, 0, c.stream>>>((const Double4*)d.aux, perm_dev, (Double4*)dst, d.n_fluid);
+        const int rc = after_launch("gather_records");
+        if (rc != MFLBM_OK) {
+            cudaFree(dst);
+            return rc;
+        }
+    }
+    *out = dst;
     return MFLBM_OK;
 }
 
@@ -734,6 +801,8 @@ int convert_t(mflbm_context& c, bool to_bricks) {
                                               : fn<float, float>(__VA_ARGS__))
 
 int convert_populations(mflbm_context& c, bool to_bricks) { return MFLBM_POP(convert_t, c, to_bricks); }
+int relayout_populations(mflbm_context& c, const Bricks& to, void** out) { return relayout_impl(c, to, out); }
+int permute_records(mflbm_context& c, const int* perm_dev, void** out) { return permute_impl(c, perm_dev, out); }
 
 int preprocess_geometry(mflbm_context& c, const int32_t* walls_global, int iper) {
     return c.params.precision == MFLBM_FP32 ? preprocess_geometry_t<float>(c, walls_global, iper)

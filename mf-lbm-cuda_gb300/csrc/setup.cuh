@@ -18,4 +18,8 @@ int write_walls_vtk(mflbm_context& c, const char* path);
 int write_checkpoint(mflbm_context& c, int ntime, const char* path);
 // copy populations between d.staging (reference f1 layout) and d.pdf (brick layout)
 int convert_populations(mflbm_context& c, bool to_bricks);
+// the populations in the tile shape `to`, in a new device buffer (*out); d.pdf is unchanged
+int relayout_populations(mflbm_context& c, const Bricks& to, void** out);
+// the collision records in a new fluid-list order, dst[t] = aux[perm[t]], in a new buffer
+int permute_records(mflbm_context& c, const int* perm_dev, void** out);
 }  // namespace mflbm

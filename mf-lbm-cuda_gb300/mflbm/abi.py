@@ -80,7 +80,8 @@ class MonitorExt(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("collide_block", C.c_int), ("normals_block", C.c_int), ("curvature_block", C.c_int),
-                ("extrapolate_block", C.c_int), ("step_ms_before", C.c_double), ("step_ms_after", C.c_double)]
+                ("extrapolate_block", C.c_int), ("step_ms_before", C.c_double), ("step_ms_after", C.c_double),
+                ("tile_x", C.c_int), ("tile_y", C.c_int), ("tile_z", C.c_int)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}

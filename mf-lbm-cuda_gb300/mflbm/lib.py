@@ -45,6 +45,7 @@ SIGNATURES = {
     "mflbm_monitor_profile": (I, [VP, VP, VP, I]),
     "mflbm_autotune": (I, [VP, I, VP]),
     "mflbm_set_tuning": (I, [VP, VP]),
+    "mflbm_get_tuning": (I, [VP, VP]),
     "mflbm_batch_create": (I, [C.POINTER(VP), I, C.POINTER(VP)]),
     "mflbm_batch_run": (I, [VP, I, I]),
     "mflbm_batch_destroy": (I, [VP]),
@@ -247,14 +248,22 @@ class Context:
         return {n: sl[m] for m, n in enumerate(abi.PROFILE_ROWS)}, e.as_dict()
 
     def autotune(self, reps=5):
-        """mflbm_autotune: block sizes of the step kernels; the state is unchanged."""
+        """mflbm_autotune: population tile shape and block sizes of the step
+        kernels; the state is unchanged."""
         t = abi.Tuning()
         check(self.lib.mflbm_autotune(self.h, int(reps), C.byref(t)), "mflbm_autotune")
         return t.as_dict()
 
-    def set_tuning(self, collide=0, normals=0, curvature=0, extrapolate=0):
-        t = abi.Tuning(collide, normals, curvature, extrapolate, 0.0, 0.0)
+    def set_tuning(self, collide=0, normals=0, curvature=0, extrapolate=0, tile=(0, 0, 0)):
+        """mflbm_set_tuning: block sizes (0 keeps one) and, when `tile` is
+        given, the population tile extent in bricks (x, y, z)."""
+        t = abi.Tuning(collide, normals, curvature, extrapolate, 0.0, 0.0, *tile)
         check(self.lib.mflbm_set_tuning(self.h, C.byref(t)), "mflbm_set_tuning")
+
+    def get_tuning(self):
+        t = abi.Tuning()
+        check(self.lib.mflbm_get_tuning(self.h, C.byref(t)), "mflbm_get_tuning")
+        return t.as_dict()
 
     def write_vtk(self, vtk_type, path, precision_cmd=0):
         check(self.lib.mflbm_write_vtk(self.h, int(vtk_type), int(precision_cmd), str(path).encode()), "mflbm_write_vtk")

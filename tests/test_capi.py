@@ -32,7 +32,7 @@ def test_header_declares_the_abi():
 def test_library_exports_every_declared_symbol(mflbm_lib):
     missing = [n for n in declared_functions() if not hasattr(mflbm_lib, n)]
     assert not missing, missing
-    assert mflbm_lib.mflbm_abi_version() == 2
+    assert mflbm_lib.mflbm_abi_version() == 3
 
 
 def test_binding_covers_every_symbol():

@@ -259,3 +259,38 @@ def test_graph_replays_refresh_exported_arrays(mflbm_lib):
     for n in ("cn_x", "c_norm", "curv", "pdf", "phi"):
         assert d[n].tobytes() == o.a[n].tobytes(), n
     ctx.close()
+
+
+@pytest.mark.parametrize("tile", [(1, 1, 1), (2, 2, 2), (32, 32, 2), (4, 8, 1)], ids=lambda t: "x".join(map(str, t)))
+@pytest.mark.parametrize("kind,n", [("velocity_convective", (20, 20, 28)), ("periodic_drop", (21, 21, 23))])
+def test_strict_bit_exact_with_tile_shapes(mflbm_lib, kind, n, tile):
+    """Other population tile shapes: the populations and the collision
+    records move exactly when the shape changes (before the first step and
+    in the middle of a run), so the state stays bit-identical to the oracle;
+    the per-slice monitor profile (one block per layer of tiles) equals the
+    default shape's to FP64 rounding."""
+    from mflbm import lib
+    case = cases.small_case(kind, n=n, seed=11 if n != (20, 20, 28) else 7)
+    geo = read_dat(GOLDEN / f"{case.name}.dat") if n == (20, 20, 28) else case.geometry_bytes()
+    ctx, _ = lib.setup_case(case, abi.MFLBM_FP32, abi.MFLBM_STRICT, geometry=geo)
+    ref, _ = lib.setup_case(case, abi.MFLBM_FP32, abi.MFLBM_STRICT, geometry=geo)
+    o = H.OracleState(case, abi.MFLBM_FP32, geometry=geo)
+    ctx.set_tuning(tile=tile)
+    assert (ctx.get_tuning()["tile_x"], ctx.get_tuning()["tile_y"], ctx.get_tuning()["tile_z"]) == tile
+    for first, count, switch in [(1, 10, (8, 4, 2)), (11, 10, tile)]:
+        ctx.run(first, count)
+        ref.run(first, count)
+        o.run(count)
+        d = ctx.download()
+        for name in STATE:
+            assert d[name].tobytes() == o.a[name].tobytes(), f"{name} after {first + count - 1} steps"
+        # FP64 sums over the same nodes in another order (the list follows the layout)
+        p, e = ctx.monitor_profile()
+        pr, er = ref.monitor_profile()
+        for row in p:
+            assert np.allclose(p[row], pr[row], rtol=1e-12, atol=1e-14), row
+        for key in e:
+            assert e[key] == pytest.approx(er[key], rel=1e-12, abs=1e-14), key
+        ctx.set_tuning(tile=switch)
+    ctx.close()
+    ref.close()
