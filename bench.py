@@ -228,6 +228,88 @@ def fp64_variant(case, geo, steps):
             "collide_gbs": round((n_fluid * 616 + n_all) / (coll * 1e-3) / 1e9, 1)}
 
 
+def late_state(ctx, nt, n_all, n_fluid, target=10001, timed=200):
+    """The same drainage ~10,000 steps in (the front well inside the pack):
+    MLUPS over `timed` steps and the sizes of the sparse gradient sets."""
+    import torch
+    if nt < target:
+        ctx.run(nt, target - nt)
+        nt = target
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    ms = _timed_run(lambda: ctx.run(nt, timed), ctx.sync, stream)
+    nt += timed
+    st = ctx.interface_stats()
+    return nt, {"value": round(n_all * timed / (ms * 1e-3) / 1e6, 2), "unit": "MLUPS", "after_steps": nt - 1,
+                "ms_per_step": round(ms / timed, 5), "gradient_sets": st,
+                "interface_fraction": round(st["interface_nodes"] / n_fluid, 5)}
+
+
+def interface_rich(case, geo, timed=200, settle=20, seed=1206):
+    """The worst case of the sparse colour-gradient passes: the same 256^3
+    pack with phi = +-1 drawn at random per node (the reference's random
+    initial distribution, initial_fluid_distribution_option 6, at saturation
+    0.5; the reference draws from rand() seeded by the clock, this uses a
+    seeded generator), the rest state at that phi, uploaded through the C
+    ABI; MLUPS over `timed` steps after `settle` steps."""
+    import torch
+    from mflbm import abi, lib
+    c, info = lib.setup_case(case, abi.MFLBM_FP32, abi.MFLBM_FAST, geometry=geo)
+    nx, ny, nz = case.shape
+    L = c.L
+    phi = c.download(names=("phi",))["phi"].reshape(nz + 8, ny + 8, nx + 8)
+    rng = np.random.default_rng(seed)
+    core = phi[3:nz + 5, 3:ny + 5, 3:nx + 5]                    # nodes [0, n+1]^3
+    core[...] = np.where(rng.random(core.shape) < 0.5, 1.0, -1.0).astype(np.float32)
+    phi[:4, :, :] = np.float32(info["params"].phi_inlet)         # inlet ghosts k <= 0
+    p1 = phi[3:nz + 5, 3:ny + 5, 3:nx + 5]                      # s1 nodes
+    w = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12, dtype=np.float32)
+    pdf = np.empty((2, 19) + p1.shape, dtype=np.float32)
+    for g, sgn in ((0, 1.0), (1, -1.0)):
+        r = (np.float32(1.0) + np.float32(sgn) * p1) * np.float32(0.5)
+        for q in range(19):
+            np.multiply(r, w[q], out=pdf[g, q])
+    f_cv = np.ascontiguousarray(pdf[0, :, nz, :, :])
+    g_cv = np.ascontiguousarray(pdf[1, :, nz, :, :])
+    phi_cv = np.ascontiguousarray(p1[nz, :, :])                # convective outlet state: z = nz
+    c.upload_fields(pdf=pdf.reshape(-1), phi=phi.reshape(-1), W_in=info["W_in"], f_convec_bc=f_cv.reshape(-1),
+                    g_convec_bc=g_cv.reshape(-1), phi_convec_bc=phi_cv.reshape(-1))
+    del pdf
+    n_fluid, n_all = c.node_counts()
+    c.run(1, settle)
+    stream = torch.cuda.ExternalStream(c.stream())
+    ms = _timed_run(lambda: c.run(1 + settle, timed), c.sync, stream)
+    st = c.interface_stats()
+    c.close()
+    return {"value": round(n_all * timed / (ms * 1e-3) / 1e6, 2), "unit": "MLUPS", "ms_per_step": round(ms / timed, 5),
+            "after_steps": settle + timed, "gradient_sets": st,
+            "interface_fraction": round(st["interface_nodes"] / n_fluid, 5),
+            "how": "random phi = +-1 per node (seeded), rest state, uploaded through mflbm_upload_fields"}
+
+
+def reference_cuda(size):
+    """The reference's own CUDA program (baseline/ref_cuda.py: its kernels and
+    host program compiled for sm_103a with two documented allocation/print
+    patches) on the same workload: MLUPS from its own prints, FP32 and FP64."""
+    sys.path.insert(0, str(REPO / "baseline"))
+    import ref_cuda
+    if not ref_cuda.available("f32"):
+        return {"unavailable": "patched reference sources not present (baseline/ref_cuda.py prepare, "
+                               "on a machine with the reference checkout)"}
+    out = {}
+    for prec, steps, disp in (("f32", 600, 100), ("f64", 200, 50)):
+        try:
+            r = ref_cuda.run(prec, steps=steps, size=size, display=disp)
+            out[prec] = {"value": round(r["mlups"], 2) if r["mlups"] else None, "unit": "MLUPS",
+                         "steps": steps, "mlups_display": r["mlups_display"], "mlups_total": r["mlups_total"],
+                         "block": r["block"]}
+        except Exception as e:   # keep the bench line whatever happens here
+            out[prec] = {"error": str(e)[-400:]}
+    out["patches"] = [p[3] for p in ref_cuda.PATCHES]
+    out["how"] = ("median of the program's own 'simulation speed' prints (all nodes x steps / wall time "
+                  "between prints, src/main.cpp:191-199), block 128x1x1 from the control file")
+    return out
+
+
 def batch_vs_sequential(steps):
     """16 single-phase samples of 48^3 .. 96^3 (porosity 0.3 .. 0.7): one
     graph launch per step pair for all of them (mflbm_batch) against each
@@ -270,6 +352,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the 16-bit storage and batch measurements")
     ap.add_argument("--no-tune", action="store_true", help="keep the default block sizes (no autotuning)")
+    ap.add_argument("--no-reference-cuda", action="store_true",
+                    help="skip the reference's own CUDA program (built from baseline/_ref when present)")
     args = ap.parse_args()
     warmup = max(3, args.warmup)
 
@@ -329,6 +413,7 @@ def main():
     if not args.no_tune:
         t = ctx.autotune(3)
         tuning = {k: t[k] for k in ("collide_block", "normals_block", "curvature_block", "extrapolate_block")}
+        tuning["population_tile_bricks"] = [t["tile_x"], t["tile_y"], t["tile_z"]]
 
     # ---- timed region: K steps, state resident in HBM, graph-replayed ----
     sampler = ClockSampler(local)
@@ -398,10 +483,14 @@ def main():
     mon = ctx.monitor(2, 2)
     extra = {}
     if not args.no_extras:
+        nt, extra["late_state"] = late_state(ctx, nt, n_all, n_fluid)
         ctx.close()
+        extra["interface_rich"] = interface_rich(case, geo)
         extra["storage"] = storage_variants(case, geo, min(args.steps, 200), nt)
         extra["fp64"] = fp64_variant(case, geo, min(args.steps, 40))
         extra["batch"] = batch_vs_sequential(min(args.steps, 200))
+        if not args.no_reference_cuda and world == 1:
+            extra["reference_cuda"] = reference_cuda(nx)
 
     if rank != 0:
         return
