@@ -311,35 +311,50 @@ def reference_cuda(size):
 
 
 def batch_vs_sequential(steps):
-    """16 single-phase samples of 48^3 .. 96^3 (porosity 0.3 .. 0.7): one
-    graph launch per step pair for all of them (mflbm_batch) against each
-    context's own graph replays, one after the other."""
+    """16 single-phase samples of 48^3 .. 96^3 (porosity 0.3 .. 0.7) stepped
+    together by mflbm_batch_run (persistent launches with grid barriers, block
+    size and tile shape from mflbm_batch_autotune) against each context's own
+    graph replays, one context after another (each context autotuned alone)."""
     from mflbm import abi, lib, permeability
     samples = permeability.make_samples(16, 48, 96)
     ctxs = [lib.setup_case(s, abi.MFLBM_FP32, abi.MFLBM_FAST)[0] for s in samples]
+    solo = [lib.setup_case(s, abi.MFLBM_FP32, abi.MFLBM_FAST)[0] for s in samples]
     nodes = sum(int(np.prod(s.shape)) for s in samples)
     steps += steps & 1
     b = lib.Batch(ctxs)
     b.run(1, 4)
-    for c in ctxs:
+    tuned = b.autotune(2)
+    for c in solo:
+        c.run(1, 4)
+        c.autotune(2)
+    b.run(5, 4)
+    for c in solo:
         c.run(5, 4)
         c.sync()
     t0 = time.perf_counter()
     b.run(9, steps)
     t_batch = time.perf_counter() - t0
     t0 = time.perf_counter()
-    for c in ctxs:
-        c.run(9 + steps, steps)
-    for c in ctxs:
+    for c in solo:
+        c.run(9, steps)
+    for c in solo:
         c.sync()
     t_seq = time.perf_counter() - t0
+    opts = b.options()
+    same = all(np.array_equal(x.download(names=("pdf",))["pdf"], y.download(names=("pdf",))["pdf"])
+               for x, y in zip(ctxs, solo))
     b.close()
-    for c in ctxs:
+    for c in ctxs + solo:
         c.close()
     return {"samples": len(samples), "sizes": [s.shape[0] for s in samples], "steps": steps,
             "batched_mlups": round(nodes * steps / t_batch / 1e6, 1),
             "sequential_mlups": round(nodes * steps / t_seq / 1e6, 1),
-            "how": "wall clock, mflbm_batch_run vs mflbm_run per context (each graph-replayed)"}
+            "batched_over_sequential": round(t_seq / t_batch, 3),
+            "mode": {1: "graph", 2: "persistent"}.get(opts["used_mode"], "?"), "grid": opts["grid"],
+            "block": opts["block"], "tile_bricks": [tuned["tile_x"], tuned["tile_y"], tuned["tile_z"]],
+            "results_identical": bool(same),
+            "how": "wall clock, mflbm_batch_run (one persistent launch per 100 steps) vs mflbm_run per context "
+                   "(graph replays), FP32 fast, same start states"}
 
 
 def main():

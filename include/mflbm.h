@@ -39,7 +39,8 @@ enum {
     MFLBM_E_CUDA = -2,     /* a CUDA runtime call failed */
     MFLBM_E_STATE = -3,    /* call out of order (e.g. step before upload) */
     MFLBM_E_NOMEM = -4,    /* device or host allocation failed */
-    MFLBM_E_IO = -5        /* file could not be read or written */
+    MFLBM_E_IO = -5,       /* file could not be read or written */
+    MFLBM_E_TIMEOUT = -6   /* a bounded device-side wait ran out (the state is undefined) */
 };
 
 enum { MFLBM_FP32 = 1, MFLBM_FP64 = 2 };         /* = reference SINGLE/DOUBLE_PRECISION */
@@ -374,9 +375,39 @@ int mflbm_get_tuning(mflbm_context* ctx, mflbm_tuning* out);
 typedef struct mflbm_batch mflbm_batch;
 int mflbm_batch_create(mflbm_context* const* ctxs, int n, mflbm_batch** out);
 /* Steps ntime_begin .. ntime_begin + nsteps - 1 of every context of the
- * batch; ntime_begin must be odd and nsteps even.  Blocks until done. */
+ * batch; ntime_begin must be odd and nsteps even.  Blocks until done.
+ * A batch of single-phase samples (every component-2 population exactly 0,
+ * no interface, no inlet, outlet or plate; same precision, storage and
+ * arithmetic flavour: the single-phase permeability workload) runs as one
+ * persistent cooperative launch per up to 100 steps, every sample's work of
+ * a phase spread over all blocks and the phases (collision, periodic z, y,
+ * z-y) separated by grid barriers with bounded waits; the results are
+ * bit-identical to stepping each context alone.  Other batches run as one
+ * CUDA graph per step pair (a branch per context).  A barrier wait that runs
+ * out returns MFLBM_E_TIMEOUT with the contexts' states undefined. */
 int mflbm_batch_run(mflbm_batch* b, int ntime_begin, int nsteps);
 int mflbm_batch_destroy(mflbm_batch* b);
+
+enum { MFLBM_BATCH_AUTO = 0, MFLBM_BATCH_GRAPH = 1, MFLBM_BATCH_PERSISTENT = 2 };
+typedef struct mflbm_batch_options {
+    int mode;              /* MFLBM_BATCH_AUTO (persistent when the batch allows it), _GRAPH or
+                              _PERSISTENT (an error if the batch does not allow it) */
+    int block;             /* threads per block of the persistent launch: 64, 128 or 256 */
+    double wait_limit_s;   /* bound of every grid-barrier wait, seconds (> 0, <= 60) */
+    int used_mode;         /* out (get): mode of the last run */
+    int grid;              /* out (get): blocks of the last persistent launch */
+} mflbm_batch_options;
+/* Defaults: MFLBM_BATCH_AUTO, 128 threads, 2 s. */
+int mflbm_batch_set_options(mflbm_batch* b, const mflbm_batch_options* o);
+int mflbm_batch_get_options(mflbm_batch* b, mflbm_batch_options* o);
+/* Times the persistent launch with 64, 128 and 256 threads per block and
+ * the population tile shapes 8x4x2, 2x2x2 and 8x8x2 bricks (applied to every
+ * sample), `reps` step pairs each, keeps the fastest and reports it (tile
+ * extents in out->tile_*, the block size in out->collide_block).  Every
+ * context's state is copied aside first and restored; a tile change moves
+ * the populations exactly, so results are unchanged.  Needs a batch that
+ * runs persistent. */
+int mflbm_batch_autotune(mflbm_batch* b, int reps, mflbm_tuning* out);
 
 /* ---- learned warm start: 3-D U-Net --------------------------------------
  * (no counterpart in the reference)  4 levels of 16/32/64/128 channels, two

@@ -225,10 +225,9 @@ __global__ void outlet_pressure_kernel(const BcArgs<T, E> a) {
 __device__ __constant__ const int kZup[5] = {6, 14, 13, 18, 17}, kZdn[5] = {5, 11, 12, 15, 16};
 __device__ __constant__ const int kYup[5] = {4, 10, 9, 16, 18}, kYdn[5] = {3, 7, 8, 15, 17};
 
+// periodic z of column (i, j), i, j >= 1
 template <class T, class E, bool ODD>
-__global__ void periodic_z_kernel(const BcArgs<T, E> a) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1;
-    if (i > a.g.nx) return;
+__device__ __forceinline__ void periodic_z_at(const BcArgs<T, E>& a, int i, int j) {
     const Grid& g = a.g;
     const int nz = g.nz;
 #pragma unroll
@@ -248,11 +247,15 @@ __global__ void periodic_z_kernel(const BcArgs<T, E> a) {
         a.phi[g.s4(i, j, k - 4)] = a.phi[g.s4(i, j, nz + k - 4)];
     }
 }
-
 template <class T, class E, bool ODD>
-__global__ void periodic_y_kernel(const BcArgs<T, E> a) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y + 1;
-    if (i > a.g.nx) return;
+__global__ void periodic_z_kernel(const BcArgs<T, E> a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1;
+    if (i <= a.g.nx) periodic_z_at<T, E, ODD>(a, i, j);
+}
+
+// periodic y of row (i, k), i, k >= 1
+template <class T, class E, bool ODD>
+__device__ __forceinline__ void periodic_y_at(const BcArgs<T, E>& a, int i, int k) {
     const Grid& g = a.g;
     const int ny = g.ny;
 #pragma unroll
@@ -272,11 +275,15 @@ __global__ void periodic_y_kernel(const BcArgs<T, E> a) {
         a.phi[g.s4(i, j - 4, k)] = a.phi[g.s4(i, ny + j - 4, k)];
     }
 }
-
 template <class T, class E, bool ODD>
-__global__ void periodic_zy_kernel(const BcArgs<T, E> a) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    if (i > a.g.nx) return;
+__global__ void periodic_y_kernel(const BcArgs<T, E> a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y + 1;
+    if (i <= a.g.nx) periodic_y_at<T, E, ODD>(a, i, k);
+}
+
+// periodic z-y edges of column i >= 1
+template <class T, class E, bool ODD>
+__device__ __forceinline__ void periodic_zy_at(const BcArgs<T, E>& a, int i) {
     const Grid& g = a.g;
     const int ny = g.ny, nz = g.nz;
 #pragma unroll
@@ -300,6 +307,11 @@ __global__ void periodic_zy_kernel(const BcArgs<T, E> a) {
             a.phi[g.s4(i, j + ny, k + nz)] = a.phi[g.s4(i, j, k)];
             a.phi[g.s4(i, j - 4, k + nz)] = a.phi[g.s4(i, ny + j - 4, k)];
         }
+}
+template <class T, class E, bool ODD>
+__global__ void periodic_zy_kernel(const BcArgs<T, E> a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (i <= a.g.nx) periodic_zy_at<T, E, ODD>(a, i);
 }
 
 // porous plate blocking one component at z = Zplate (:1744-1882); b = blocked component
@@ -361,12 +373,11 @@ __global__ void porous_plate_kernel(const BcArgs<T, E> a) {
 
 
 template <class T, class E>
-int launch_boundaries(mflbm_context& c, bool odd) {
+BcArgs<T, E> bc_args(const mflbm_context& c) {
     const DeviceState& d = c.d;
-    const Grid& g = d.g;
     const mflbm_params& p = c.params;
     BcArgs<T, E> a;
-    a.g = g;
+    a.g = d.g;
     a.P.p = (E*)d.pdf;
     a.P.b = d.b;
     a.walls = d.walls;
@@ -374,6 +385,15 @@ int launch_boundaries(mflbm_context& c, bool odd) {
     a.f_cv = (T*)d.f_cv; a.g_cv = (T*)d.g_cv; a.phi_cv = (T*)d.phi_cv;
     a.ph = make_phys<T>(p);
     a.plate_cmd = p.porous_plate_cmd; a.Zplate = p.Z_porous_plate;
+    return a;
+}
+
+template <class T, class E>
+int launch_boundaries(mflbm_context& c, bool odd) {
+    const DeviceState& d = c.d;
+    const Grid& g = d.g;
+    const mflbm_params& p = c.params;
+    const BcArgs<T, E> a = bc_args<T, E>(c);
     cudaStream_t s = c.stream;
     const unsigned bx = grid_for(g.nx, 128);
     int rc;

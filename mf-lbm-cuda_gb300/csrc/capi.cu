@@ -315,6 +315,16 @@ struct mflbm_batch {
     cudaEvent_t fork = nullptr;
     std::vector<cudaEvent_t> join;
     cudaGraphExec_t exec = nullptr;
+    // persistent launch
+    int mode = MFLBM_BATCH_AUTO, block = 128;
+    double wait_s = 2.0;
+    int used_mode = 0, grid = 0;
+    void* dev_samples = nullptr;
+    size_t samples_cap = 0;
+    int* dev_pre = nullptr;
+    size_t pre_cap = 0;
+    unsigned* dev_bar = nullptr;   // [arrivals, generation]
+    int* dev_err = nullptr;        // [timeout flag, second-component flag]
 };
 
 namespace mflbm {
@@ -345,6 +355,174 @@ int capture_batch(mflbm_batch* b) {
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) return fail(MFLBM_E_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
     for (size_t i = 0; i < b->ctx.size(); ++i) b->gen[i] = b->ctx[i]->generation;
+    return MFLBM_OK;
+}
+
+int set_tiling(mflbm_context* c, int lx, int ly, int lz);
+
+// Everything a step writes (populations, phi, records, convective buffers,
+// sparse-set lists), copied aside in the context's current tile shape.
+struct SavedState {
+    char* buf = nullptr;
+    int lx = 0, ly = 0, lz = 0;
+    bool stale = false;
+};
+struct Span { void* p; size_t n; };
+std::vector<Span> state_spans(mflbm_context* c) {
+    DeviceState& d = c->d;
+    const Grid& g = d.g;
+    const size_t T = tsize(c), pl = (size_t)g.plane1();
+    const size_t pop_e = c->params.storage == MFLBM_STORE_NATIVE ? T : 2;
+    return std::vector<Span>{{d.pdf, pop_e * d.b.S * 38}, {d.phi, T * g.n4()},
+                             {d.aux, T * 4 * std::max<ll>(1, d.n_fluid)}, {d.cnv4, T * 4 * g.n2()},
+                             {d.f_cv, T * pl * 19}, {d.g_cv, T * pl * 19}, {d.phi_cv, T * pl},
+                             {d.dither, 2 * sizeof(uint32_t)}, {d.iface, (size_t)g.n2()},
+                             {d.olist, sizeof(uint32_t) * std::max<ll>(1, d.n_norm)},
+                             {d.slist, sizeof(uint32_t) * std::max<ll>(1, d.n_cn_ext)},
+                             {d.smask, sizeof(uint32_t) * (size_t)(g.n2() / 32 + 1)},
+                             {d.gcount, 4 * sizeof(int)}};
+}
+int save_state(mflbm_context* c, SavedState* s) {
+    const std::vector<Span> st = state_spans(c);
+    size_t total = 0;
+    for (auto& x : st) total += (x.n + 255) / 256 * 256;
+    MFLBM_CUDA(cudaMalloc(&s->buf, total));
+    size_t off = 0;
+    for (auto& x : st) {
+        MFLBM_CUDA(cudaMemcpyAsync(s->buf + off, x.p, x.n, cudaMemcpyDeviceToDevice, c->stream));
+        off += (x.n + 255) / 256 * 256;
+    }
+    s->lx = c->d.b.lx; s->ly = c->d.b.ly; s->lz = c->d.b.lz;
+    s->stale = c->d.arrays_stale;
+    MFLBM_CUDA(cudaStreamSynchronize(c->stream));
+    return MFLBM_OK;
+}
+// Back to the saved tile shape and state; frees the copy.
+int restore_state(mflbm_context* c, SavedState* s) {
+    int rc = set_tiling(c, s->lx, s->ly, s->lz);
+    if (rc == MFLBM_OK) {
+        const std::vector<Span> st = state_spans(c);
+        size_t off = 0;
+        for (auto& x : st) {
+            cudaMemcpyAsync(x.p, s->buf + off, x.n, cudaMemcpyDeviceToDevice, c->stream);
+            off += (x.n + 255) / 256 * 256;
+        }
+        MFLBM_CUDA(cudaStreamSynchronize(c->stream));
+        c->d.arrays_stale = s->stale;
+    }
+    cudaFree(s->buf);
+    s->buf = nullptr;
+    if (c->pair_graph) { cudaGraphExecDestroy(c->pair_graph); c->pair_graph = nullptr; }
+    c->generation++;
+    return rc;
+}
+
+// Whether a batch can run as one persistent launch (batch.cuh): the same
+// precision, storage and flavour everywhere, 32-bit population indices, no
+// inlet, outlet or plate, no interface records, and every component-2
+// population exactly 0.  `why` receives the first reason it cannot.
+int batch_persistent_ok(mflbm_batch* b, bool* ok, std::string* why) {
+    *ok = false;
+    const mflbm_context* c0 = b->ctx[0];
+    for (mflbm_context* c : b->ctx) {
+        const mflbm_params& p = c->params;
+        if (p.precision != c0->params.precision || p.storage != c0->params.storage || p.fp_mode != c0->params.fp_mode) {
+            *why = "contexts differ in precision, storage or arithmetic flavour";
+            return MFLBM_OK;
+        }
+        if (p.kper == 0 && p.domain_wall_status_z_min == 0 && p.domain_wall_status_z_max == 0 &&
+            (p.inlet_BC != 0 || p.outlet_BC != 0)) {
+            *why = "a context has an inlet or outlet boundary";
+            return MFLBM_OK;
+        }
+        if (p.porous_plate_cmd != 0) { *why = "a context has a porous plate"; return MFLBM_OK; }
+        if (c->d.b.pairs() >= (1ll << 32)) { *why = "a context needs 64-bit population indices"; return MFLBM_OK; }
+    }
+    MFLBM_CUDA(cudaMemsetAsync(b->dev_err + 1, 0, sizeof(int), b->origin));
+    MFLBM_CUDA(cudaStreamSynchronize(b->origin));
+    for (mflbm_context* c : b->ctx) {
+        int h[3] = {0, 0, 0};
+        MFLBM_CUDA(cudaMemcpy(h, c->d.gcount, sizeof(h), cudaMemcpyDeviceToHost));
+        if (h[0] != 0 || h[1] != 0) { *why = "a context has interface records (two phases)"; return MFLBM_OK; }
+        const int rc = c->params.fp_mode == MFLBM_STRICT ? strict::second_component(*c, b->dev_err + 1)
+                                                         : fast::second_component(*c, b->dev_err + 1);
+        if (rc != MFLBM_OK) return rc;
+        MFLBM_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    int flag = 0;
+    MFLBM_CUDA(cudaMemcpy(&flag, b->dev_err + 1, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag) { *why = "a context holds the second component"; return MFLBM_OK; }
+    *ok = true;
+    return MFLBM_OK;
+}
+
+// ntime_begin .. ntime_begin + nsteps - 1 of every context as persistent
+// launches of at most 100 steps.
+int batch_run_persistent(mflbm_batch* b, int ntime_begin, int nsteps) {
+    const int ns = (int)b->ctx.size(), bs = b->block;
+    std::vector<int> pre(4 * (ns + 1), 0);
+    int max_units = 1;
+    for (int ph = 0; ph < 4; ++ph) {
+        for (int i = 0; i < ns; ++i) {
+            const mflbm_context& c = *b->ctx[i];
+            const Grid& g = c.d.g;
+            const int xu = (g.nx + bs - 1) / bs;
+            int units = 0;
+            if (ph == 0) units = (int)((c.d.n_fluid + bs - 1) / bs);
+            else if (ph == 1) units = c.params.kper ? g.ny * xu : 0;
+            else if (ph == 2) units = c.params.jper ? g.nz * xu : 0;
+            else units = (c.params.jper && c.params.kper) ? xu : 0;
+            pre[ph * (ns + 1) + i + 1] = pre[ph * (ns + 1) + i] + units;
+        }
+        max_units = std::max(max_units, pre[ph * (ns + 1) + ns]);
+    }
+    if (b->pre_cap < pre.size()) {
+        if (b->dev_pre) cudaFree(b->dev_pre);
+        b->dev_pre = nullptr;
+        b->pre_cap = 0;
+        MFLBM_CUDA(cudaMalloc(&b->dev_pre, sizeof(int) * pre.size()));
+        b->pre_cap = pre.size();
+    }
+    MFLBM_CUDA(cudaMemcpyAsync(b->dev_pre, pre.data(), sizeof(int) * pre.size(), cudaMemcpyHostToDevice, b->origin));
+    const mflbm_context& c0 = *b->ctx[0];
+    const bool strict_mode = c0.params.fp_mode == MFLBM_STRICT;
+    const size_t need = (strict_mode ? strict::batch_sample_bytes(c0) : fast::batch_sample_bytes(c0)) * ns;
+    if (b->samples_cap < need) {
+        if (b->dev_samples) cudaFree(b->dev_samples);
+        b->dev_samples = nullptr;
+        b->samples_cap = 0;
+        MFLBM_CUDA(cudaMalloc(&b->dev_samples, need));
+        b->samples_cap = need;
+    }
+    int grid = 0;
+    int rc = strict_mode ? strict::batch_grid(c0, bs, &grid) : fast::batch_grid(c0, bs, &grid);
+    if (rc != MFLBM_OK) return rc;
+    grid = std::min(grid, max_units);
+    BatchLaunch L;
+    L.samples = b->dev_samples;
+    L.pre = b->dev_pre;
+    L.bar = b->dev_bar;
+    L.error = b->dev_err;
+    L.limit_ns = (unsigned long long)(b->wait_s * 1e9);
+    L.block = bs;
+    L.grid = grid;
+    L.stream = b->origin;
+    for (int done = 0; done < nsteps;) {
+        const int chunk = std::min(100, nsteps - done);
+        L.ntime_begin = ntime_begin + done;
+        L.nsteps = chunk;
+        MFLBM_CUDA(cudaMemsetAsync(b->dev_bar, 0, 2 * sizeof(unsigned), b->origin));
+        MFLBM_CUDA(cudaMemsetAsync(b->dev_err, 0, sizeof(int), b->origin));
+        rc = strict_mode ? strict::batch_persistent(b->ctx.data(), ns, L) : fast::batch_persistent(b->ctx.data(), ns, L);
+        if (rc != MFLBM_OK) return rc;
+        int err = 0;
+        MFLBM_CUDA(cudaMemcpy(&err, b->dev_err, sizeof(int), cudaMemcpyDeviceToHost));
+        if (err) return fail(MFLBM_E_TIMEOUT, "mflbm_batch_run: a grid-barrier wait of the persistent launch ran out after " +
+                                                  std::to_string(b->wait_s) + " s; the contexts' states are undefined");
+        done += chunk;
+    }
+    b->grid = grid;
+    for (mflbm_context* c : b->ctx) c->d.arrays_stale = true;
     return MFLBM_OK;
 }
 
@@ -822,35 +1000,8 @@ int mflbm_autotune(mflbm_context* c, int reps, mflbm_tuning* out) {
     if (c->timing) return fail(MFLBM_E_STATE, "mflbm_autotune: switch kernel timing off first");
     if (reps < 1) reps = 1;
     DeviceState& d = c->d;
-    const Grid& g = d.g;
-    const size_t T = tsize(c), pl = (size_t)g.plane1();
-    const size_t pop_e = c->params.storage == MFLBM_STORE_NATIVE ? T : 2;
-    struct Span { void* p; size_t n; };
-    // everything a step writes: populations, phi, records, convective buffers
-    // (pointers re-read after every change of tile shape, which reallocates
-    // the populations and the collision records)
-    auto state = [&]() {
-        return std::vector<Span>{{d.pdf, pop_e * d.b.S * 38}, {d.phi, T * g.n4()},
-                                 {d.aux, T * 4 * std::max<ll>(1, d.n_fluid)}, {d.cnv4, T * 4 * g.n2()},
-                                 {d.f_cv, T * pl * 19}, {d.g_cv, T * pl * 19}, {d.phi_cv, T * pl},
-                                 {d.dither, 2 * sizeof(uint32_t)}, {d.iface, (size_t)g.n2()},
-                                 {d.olist, sizeof(uint32_t) * std::max<ll>(1, d.n_norm)},
-                                 {d.slist, sizeof(uint32_t) * std::max<ll>(1, d.n_cn_ext)},
-                                 {d.smask, sizeof(uint32_t) * (size_t)(g.n2() / 32 + 1)},
-                                 {d.gcount, 4 * sizeof(int)}};
-    };
-    const int elx = d.b.lx, ely = d.b.ly, elz = d.b.lz;   // the tile shape on entry (the saved state's layout)
-    std::vector<Span> st = state();
-    size_t total = 0;
-    for (auto& x : st) total += (x.n + 255) / 256 * 256;
-    char* save = nullptr;
-    MFLBM_CUDA(cudaMalloc(&save, total));
-    size_t off = 0;
-    for (auto& x : st) {
-        MFLBM_CUDA(cudaMemcpyAsync(save + off, x.p, x.n, cudaMemcpyDeviceToDevice, c->stream));
-        off += (x.n + 255) / 256 * 256;
-    }
-    const bool stale = d.arrays_stale;
+    SavedState saved;
+    if ((rc = save_state(c, &saved)) != MFLBM_OK) return rc;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -874,11 +1025,11 @@ int mflbm_autotune(mflbm_context* c, int reps, mflbm_tuning* out) {
     best_ms = before;
     // tile shape of the population layout (with the entry block sizes), then
     // block sizes, one kernel family at a time
-    int blx = elx, bly = ely, blz = elz;
+    int blx = saved.lx, bly = saved.ly, blz = saved.lz;
     static const int kTiles[][3] = {{3, 2, 1}, {3, 3, 1}, {1, 1, 1}, {3, 1, 1}, {4, 1, 1}, {2, 2, 1}};
     for (const auto& tl : kTiles) {
         if (rc != MFLBM_OK) break;
-        if (tl[0] == elx && tl[1] == ely && tl[2] == elz) continue;
+        if (tl[0] == saved.lx && tl[1] == saved.ly && tl[2] == saved.lz) continue;
         if ((rc = set_tiling(c, tl[0], tl[1], tl[2])) != MFLBM_OK) break;
         double ms = 0;
         if ((rc = measure(best, &ms)) != MFLBM_OK) break;
@@ -896,29 +1047,89 @@ int mflbm_autotune(mflbm_context* c, int reps, mflbm_tuning* out) {
             if (ms < best_ms) { best_ms = ms; best = t; }
         }
     d.tune = best;
-    // back to the entry layout, the saved state, then the chosen layout (both
-    // moves are exact)
-    int rc2 = set_tiling(c, elx, ely, elz);
-    if (rc2 == MFLBM_OK) {
-        st = state();
-        off = 0;
-        for (auto& x : st) {
-            cudaMemcpyAsync(x.p, save + off, x.n, cudaMemcpyDeviceToDevice, c->stream);
-            off += (x.n + 255) / 256 * 256;
-        }
-        cudaStreamSynchronize(c->stream);
-        if (rc == MFLBM_OK) rc2 = set_tiling(c, blx, bly, blz);
-    }
-    cudaFree(save);
+    int rc2 = restore_state(c, &saved);   // the entry layout and state
+    if (rc == MFLBM_OK && rc2 == MFLBM_OK) rc2 = set_tiling(c, blx, bly, blz);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    d.arrays_stale = stale;
     if (c->pair_graph) { cudaGraphExecDestroy(c->pair_graph); c->pair_graph = nullptr; }
     c->generation++;
     if (rc != MFLBM_OK) return rc;
     if (rc2 != MFLBM_OK) return rc2;
     if (out) {
         fill_tuning(*c, out);
+        out->step_ms_before = before; out->step_ms_after = best_ms;
+    }
+    return MFLBM_OK;
+}
+
+int mflbm_batch_autotune(mflbm_batch* b, int reps, mflbm_tuning* out) {
+    if (!b) return fail(MFLBM_E_ARG, "null batch");
+    if (reps < 1) reps = 1;
+    for (mflbm_context* c : b->ctx) {
+        if (c->timing) return fail(MFLBM_E_STATE, "mflbm_batch_autotune: kernel timing is on for a context");
+        MFLBM_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    bool ok = false;
+    std::string why;
+    int rc = batch_persistent_ok(b, &ok, &why);
+    if (rc != MFLBM_OK) return rc;
+    if (!ok) return fail(MFLBM_E_STATE, "mflbm_batch_autotune: no persistent launch: " + why);
+    const size_t n = b->ctx.size();
+    std::vector<SavedState> saved(n);
+    for (size_t i = 0; i < n && rc == MFLBM_OK; ++i) rc = save_state(b->ctx[i], &saved[i]);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    auto tile_all = [&](int lx, int ly, int lz) -> int {
+        for (mflbm_context* c : b->ctx) {
+            const int r = set_tiling(c, lx, ly, lz);
+            if (r != MFLBM_OK) return r;
+        }
+        return MFLBM_OK;
+    };
+    auto measure = [&](int block, double* ms) -> int {
+        b->block = block;
+        int r;
+        if ((r = batch_run_persistent(b, 1, 2)) != MFLBM_OK) return r;   // warm-up pair
+        MFLBM_CUDA(cudaEventRecord(e0, b->origin));
+        if ((r = batch_run_persistent(b, 1, 2 * reps)) != MFLBM_OK) return r;
+        MFLBM_CUDA(cudaEventRecord(e1, b->origin));
+        MFLBM_CUDA(cudaEventSynchronize(e1));
+        float f = 0;
+        MFLBM_CUDA(cudaEventElapsedTime(&f, e0, e1));
+        *ms = f / (2.0 * reps);
+        return MFLBM_OK;
+    };
+    const int entry_block = b->block;
+    double before = 0, best_ms = 0;
+    if (rc == MFLBM_OK) rc = measure(entry_block, &before);
+    best_ms = before;
+    int best_block = entry_block, blx = saved[0].lx, bly = saved[0].ly, blz = saved[0].lz;
+    static const int kTiles[][3] = {{3, 2, 1}, {1, 1, 1}, {3, 3, 1}};
+    for (const auto& tl : kTiles) {
+        if (rc != MFLBM_OK) break;
+        if ((rc = tile_all(tl[0], tl[1], tl[2])) != MFLBM_OK) break;
+        for (int bs : {64, 128, 256}) {
+            double ms = 0;
+            if ((rc = measure(bs, &ms)) != MFLBM_OK) break;
+            if (ms < best_ms) { best_ms = ms; best_block = bs; blx = tl[0]; bly = tl[1]; blz = tl[2]; }
+        }
+    }
+    b->block = best_block;
+    int rc2 = MFLBM_OK;
+    for (size_t i = 0; i < n; ++i) {
+        if (!saved[i].buf) continue;
+        const int r = restore_state(b->ctx[i], &saved[i]);
+        if (rc2 == MFLBM_OK) rc2 = r;
+    }
+    if (rc == MFLBM_OK && rc2 == MFLBM_OK) rc2 = tile_all(blx, bly, blz);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != MFLBM_OK) return rc;
+    if (rc2 != MFLBM_OK) return rc2;
+    if (out) {
+        fill_tuning(*b->ctx[0], out);
+        out->collide_block = best_block;
         out->step_ms_before = before; out->step_ms_after = best_ms;
     }
     return MFLBM_OK;
@@ -939,6 +1150,8 @@ int mflbm_batch_create(mflbm_context* const* ctxs, int n, mflbm_batch** out) {
     b->gen.assign(n, ~0ull);
     b->join.assign(n, nullptr);
     cudaError_t e = cudaStreamCreateWithFlags(&b->origin, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&b->dev_bar, 2 * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMalloc(&b->dev_err, 2 * sizeof(int));
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
     for (int i = 0; i < n && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&b->join[i], cudaEventDisableTiming);
     if (e != cudaSuccess) { mflbm_batch_destroy(b); return fail(MFLBM_E_CUDA, std::string("mflbm_batch_create: ") + cudaGetErrorString(e)); }
@@ -960,9 +1173,57 @@ int mflbm_batch_run(mflbm_batch* b, int ntime_begin, int nsteps) {
         c->d.arrays_stale = true;
     }
     int rc;
+    bool retry = b->mode == MFLBM_BATCH_AUTO;
+    while (b->mode != MFLBM_BATCH_GRAPH) {
+        bool ok = false;
+        std::string why;
+        if ((rc = batch_persistent_ok(b, &ok, &why)) != MFLBM_OK) return rc;
+        if (ok) {
+            b->used_mode = MFLBM_BATCH_PERSISTENT;
+            return batch_run_persistent(b, ntime_begin, nsteps);
+        }
+        if (b->mode == MFLBM_BATCH_PERSISTENT) return fail(MFLBM_E_STATE, "mflbm_batch_run: no persistent launch: " + why);
+        // AUTO: a single-phase state straight from the start-up may still
+        // carry normal records at ghost nodes (the start-up colour gradient
+        // sees the periodic ghost layers before the first exchange fills
+        // them); one graph-launched step pair clears them, then check again.
+        if (!retry || nsteps < 4) break;
+        retry = false;
+        if (stale && (rc = capture_batch(b)) != MFLBM_OK) return rc;
+        stale = false;
+        MFLBM_CUDA(cudaGraphLaunch(b->exec, b->origin));
+        MFLBM_CUDA(cudaStreamSynchronize(b->origin));
+        ntime_begin += 2;
+        nsteps -= 2;
+    }
+    b->used_mode = MFLBM_BATCH_GRAPH;
     if (stale && (rc = capture_batch(b)) != MFLBM_OK) return rc;
     for (int s = 0; s < nsteps; s += 2) MFLBM_CUDA(cudaGraphLaunch(b->exec, b->origin));
     MFLBM_CUDA(cudaStreamSynchronize(b->origin));
+    return MFLBM_OK;
+}
+
+int mflbm_batch_set_options(mflbm_batch* b, const mflbm_batch_options* o) {
+    if (!b || !o) return fail(MFLBM_E_ARG, "mflbm_batch_set_options: null argument");
+    if (o->mode < MFLBM_BATCH_AUTO || o->mode > MFLBM_BATCH_PERSISTENT)
+        return fail(MFLBM_E_ARG, "mflbm_batch_set_options: mode must be MFLBM_BATCH_AUTO, _GRAPH or _PERSISTENT");
+    if (o->block != 64 && o->block != 128 && o->block != 256)
+        return fail(MFLBM_E_ARG, "mflbm_batch_set_options: block must be 64, 128 or 256");
+    if (!(o->wait_limit_s > 0.0) || o->wait_limit_s > 60.0)
+        return fail(MFLBM_E_ARG, "mflbm_batch_set_options: wait_limit_s must be in (0, 60]");
+    b->mode = o->mode;
+    b->block = o->block;
+    b->wait_s = o->wait_limit_s;
+    return MFLBM_OK;
+}
+
+int mflbm_batch_get_options(mflbm_batch* b, mflbm_batch_options* o) {
+    if (!b || !o) return fail(MFLBM_E_ARG, "mflbm_batch_get_options: null argument");
+    o->mode = b->mode;
+    o->block = b->block;
+    o->wait_limit_s = b->wait_s;
+    o->used_mode = b->used_mode;
+    o->grid = b->grid;
     return MFLBM_OK;
 }
 
@@ -973,6 +1234,8 @@ int mflbm_batch_destroy(mflbm_batch* b) {
     if (b->fork) cudaEventDestroy(b->fork);
     for (auto e : b->join) if (e) cudaEventDestroy(e);
     if (b->origin) cudaStreamDestroy(b->origin);
+    for (void* p : {(void*)b->dev_samples, (void*)b->dev_pre, (void*)b->dev_bar, (void*)b->dev_err})
+        if (p) cudaFree(p);
     delete b;
     return MFLBM_OK;
 }

@@ -195,12 +195,11 @@ template <class E, bool ODD> constexpr int collide_max_regs() {
     return sizeof(E) == 2 ? 64 : sizeof(E) == 4 ? (ODD ? 80 : 64) : 255;
 }
 
+// One fluid node of the list (entry t): pull, collide, push.
 template <class T, class E, bool ODD, class I>
-__global__ void __launch_bounds__(256) __maxnreg__((collide_max_regs<E, ODD>())) collide_stream_kernel(const CollideArgs<T, E> a) {
+__device__ __forceinline__ void collide_node(const CollideArgs<T, E>& a, int t) {
     typedef typename Pop2<E>::type P2;
     typedef PopCodec<T, E> Codec;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= a.n) return;
     const uint32_t node = a.list[t];   // packed coordinates
     int x, y, z;
     unpack_xyz(node, x, y, z);
@@ -258,8 +257,14 @@ __global__ void __launch_bounds__(256) __maxnreg__((collide_max_regs<E, ODD>()))
     }
 }
 
+template <class T, class E, bool ODD, class I>
+__global__ void __launch_bounds__(256) __maxnreg__((collide_max_regs<E, ODD>())) collide_stream_kernel(const CollideArgs<T, E> a) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < a.n) collide_node<T, E, ODD, I>(a, t);
+}
+
 template <class T, class E>
-int launch_collide(mflbm_context& c, bool odd) {
+CollideArgs<T, E> collide_args(const mflbm_context& c) {
     typedef typename Pop2<E>::type P2;
     const DeviceState& d = c.d;
     const Grid& g = d.g;
@@ -276,6 +281,13 @@ int launch_collide(mflbm_context& c, bool odd) {
     a.NX2 = g.nx + 4; a.NY2 = g.ny + 4;
     a.dither = d.dither;
     a.ph = make_phys<T>(c.params);
+    return a;
+}
+
+template <class T, class E>
+int launch_collide(mflbm_context& c, bool odd) {
+    const DeviceState& d = c.d;
+    const CollideArgs<T, E> a = collide_args<T, E>(c);
     if (a.n == 0) return MFLBM_OK;
     const int bs = d.tune.collide;
     const bool narrow = d.b.pairs() < (1ll << 32);   // 32-bit pair indices suffice

@@ -287,8 +287,23 @@ inline Phys<T> make_phys(const mflbm_params& p) {
     return h;
 }
 
+// One persistent run of a batch of single-phase samples (batch.cuh).
+struct BatchLaunch {
+    void* samples;               // device array of the flavour's per-sample records
+    const int* pre;              // unit prefix sums, 4 phases x (n + 1)
+    unsigned* bar;               // barrier words [arrivals, generation]
+    int* error;                  // set when a barrier wait ran out
+    unsigned long long limit_ns; // bound of one barrier wait
+    int block, grid, ntime_begin, nsteps;
+    cudaStream_t stream;
+};
+
 // Flavour entry points (step_fast.cu / step_strict.cu).
 namespace fast {
+int batch_persistent(mflbm_context* const* ctx, int n, const BatchLaunch& L);
+int batch_grid(const mflbm_context& c, int block, int* grid);
+size_t batch_sample_bytes(const mflbm_context& c);
+int second_component(mflbm_context& c, int* flag_dev);
 int refresh_aux(mflbm_context& c);
 int export_arrays(mflbm_context& c);
 int collide(mflbm_context& c, bool odd);
@@ -296,6 +311,10 @@ int boundaries(mflbm_context& c, bool odd);
 int gradient(mflbm_context& c);
 }
 namespace strict {
+int batch_persistent(mflbm_context* const* ctx, int n, const BatchLaunch& L);
+int batch_grid(const mflbm_context& c, int block, int* grid);
+size_t batch_sample_bytes(const mflbm_context& c);
+int second_component(mflbm_context& c, int* flag_dev);
 int refresh_aux(mflbm_context& c);
 int export_arrays(mflbm_context& c);
 int collide(mflbm_context& c, bool odd);

@@ -15,3 +15,4 @@
 #include "collide.cuh"
 #include "gradient.cuh"
 #include "boundary.cuh"
+#include "batch.cuh"

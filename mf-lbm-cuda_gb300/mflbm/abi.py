@@ -87,6 +87,18 @@ class Tuning(C.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
 
+MFLBM_BATCH_AUTO, MFLBM_BATCH_GRAPH, MFLBM_BATCH_PERSISTENT = 0, 1, 2
+MFLBM_E_TIMEOUT = -6
+
+
+class BatchOptions(C.Structure):
+    _fields_ = [("mode", C.c_int), ("block", C.c_int), ("wait_limit_s", C.c_double), ("used_mode", C.c_int),
+                ("grid", C.c_int)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
 # rows of the per-slice monitor sums (mflbm_monitor_profile)
 PROFILE_ROWS = ["fl1", "fl2", "vol1", "vol2", "mass1", "mass2", "pre"]
 

@@ -49,6 +49,9 @@ SIGNATURES = {
     "mflbm_batch_create": (I, [C.POINTER(VP), I, C.POINTER(VP)]),
     "mflbm_batch_run": (I, [VP, I, I]),
     "mflbm_batch_destroy": (I, [VP]),
+    "mflbm_batch_set_options": (I, [VP, VP]),
+    "mflbm_batch_get_options": (I, [VP, VP]),
+    "mflbm_batch_autotune": (I, [VP, I, VP]),
     "mflbm_write_vtk": (I, [VP, I, I, C.c_char_p]),
     "mflbm_write_walls_vtk": (I, [VP, C.c_char_p]),
     "mflbm_write_checkpoint": (I, [VP, I, C.c_char_p]),
@@ -300,7 +303,8 @@ class Context:
 
 
 class Batch:
-    """mflbm_batch: contexts advanced together by one CUDA graph launch per step pair."""
+    """mflbm_batch: contexts advanced together, as one persistent launch
+    (single-phase samples) or one CUDA graph launch per step pair."""
 
     def __init__(self, contexts):
         self.lib = load()
@@ -312,6 +316,29 @@ class Batch:
 
     def run(self, ntime_begin, nsteps):
         check(self.lib.mflbm_batch_run(self.h, int(ntime_begin), int(nsteps)), "mflbm_batch_run")
+
+    def options(self):
+        o = abi.BatchOptions()
+        check(self.lib.mflbm_batch_get_options(self.h, C.byref(o)), "mflbm_batch_get_options")
+        return o.as_dict()
+
+    def set_options(self, mode=None, block=None, wait_limit_s=None):
+        o = abi.BatchOptions()
+        check(self.lib.mflbm_batch_get_options(self.h, C.byref(o)), "mflbm_batch_get_options")
+        if mode is not None:
+            o.mode = mode
+        if block is not None:
+            o.block = block
+        if wait_limit_s is not None:
+            o.wait_limit_s = wait_limit_s
+        check(self.lib.mflbm_batch_set_options(self.h, C.byref(o)), "mflbm_batch_set_options")
+
+    def autotune(self, reps=3):
+        """mflbm_batch_autotune: block size of the persistent launch and the
+        population tile shape of every sample; states unchanged."""
+        t = abi.Tuning()
+        check(self.lib.mflbm_batch_autotune(self.h, int(reps), C.byref(t)), "mflbm_batch_autotune")
+        return t.as_dict()
 
     def close(self):
         if self.h:
