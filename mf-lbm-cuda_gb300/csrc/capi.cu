@@ -55,7 +55,8 @@ void free_all(mflbm_context* c) {
     void* ptrs[] = {d.pdf, d.phi, d.cn_x, d.cn_y, d.cn_z, d.c_norm, d.curv, d.W_in, d.f_cv, d.g_cv, d.phi_cv,
                     d.walls, d.walls_type, d.s_nx, d.s_ny, d.s_nz, d.fluid_list, d.list_phi_ext,
                     d.red, d.staging, d.aux, d.type8, d.cnv4, d.zpair_off,
-                    d.phi_prev, d.prof, d.dither, d.iface, d.phib, d.tmap, d.wmask, d.olist, d.slist, d.nlist, d.smask, d.gcount};
+                    d.phi_prev, d.prof, d.dither, d.iface, d.phib, d.tmap, d.wmask, d.olist, d.slist, d.nlist, d.smask, d.gcount,
+                    d.sbcode, d.sbact, d.sblive, d.sbinfo, d.phioff};
     for (void* p : ptrs) if (p) cudaFree(p);
     d = DeviceState{};
     if (c->pair_graph) cudaGraphExecDestroy(c->pair_graph);
@@ -65,6 +66,16 @@ void free_all(mflbm_context* c) {
 int alloc_zero(void** p, size_t bytes, cudaStream_t s) {
     MFLBM_CUDA(cudaMalloc(p, bytes));
     MFLBM_CUDA(cudaMemsetAsync(*p, 0, bytes, s));
+    return MFLBM_OK;
+}
+
+// The next gradient pass processes every super-block: the host has set or
+// replaced phi or the populations (gradient.cuh, super-blocks).
+int request_full_pass(mflbm_context* c) {
+    static const int one = 1;
+    if (!c->d.sbinfo) return MFLBM_OK;
+    MFLBM_CUDA(cudaMemcpyAsync(c->d.sbinfo + 1, &one, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    MFLBM_CUDA(cudaStreamSynchronize(c->stream));
     return MFLBM_OK;
 }
 
@@ -184,6 +195,22 @@ int build_lists(mflbm_context* c) {
         ll nwm = 0;
         if ((rc = upload_list(&d.wmask, &nwm, wm)) != MFLBM_OK) return rc;
     }
+    {
+        // solid boundary nodes grouped by super-block (4 x 4 x 4 phi bricks),
+        // in scan order within each
+        const int nsb = d.SX * d.SY * d.SZ;
+        auto sb_of = [&](uint32_t p) {
+            int x, y, z;
+            unpack_xyz(p, x, y, z);
+            return ((x + 3) >> 3) + d.SX * (((y + 3) >> 3) + d.SY * ((z + 3) >> 3));
+        };
+        std::stable_sort(lphi.begin(), lphi.end(), [&](const uint2& u, const uint2& v) { return sb_of(u.x) < sb_of(v.x); });
+        std::vector<int> off(nsb + 1, 0);
+        for (const uint2& e : lphi) off[sb_of(e.x) + 1]++;
+        for (int b = 0; b < nsb; ++b) off[b + 1] += off[b];
+        ll noff = 0;
+        if ((rc = upload_list(&d.phioff, &noff, off)) != MFLBM_OK) return rc;
+    }
     if ((rc = upload_list(&d.list_phi_ext, &d.n_phi_ext, lphi)) != MFLBM_OK) return rc;
     d.n_cn_ext = ncn;
     {
@@ -217,7 +244,7 @@ int build_lists(mflbm_context* c) {
     MFLBM_CUDA(cudaMemset(d.iface, 0, g.n2()));
     c->pair_graph_odd_first = -1;  // kernels are launched with the list sizes
     c->generation++;
-    return MFLBM_OK;
+    return request_full_pass(c);
 }
 
 int ensure_staging(mflbm_context* c) {
@@ -409,6 +436,7 @@ int restore_state(mflbm_context* c, SavedState* s) {
         }
         MFLBM_CUDA(cudaStreamSynchronize(c->stream));
         c->d.arrays_stale = s->stale;
+        rc = request_full_pass(c);
     }
     cudaFree(s->buf);
     s->buf = nullptr;
@@ -522,7 +550,10 @@ int batch_run_persistent(mflbm_batch* b, int ntime_begin, int nsteps) {
         done += chunk;
     }
     b->grid = grid;
-    for (mflbm_context* c : b->ctx) c->d.arrays_stale = true;
+    for (mflbm_context* c : b->ctx) {
+        c->d.arrays_stale = true;
+        if ((rc = request_full_pass(c)) != MFLBM_OK) return rc;
+    }
     return MFLBM_OK;
 }
 
@@ -606,6 +637,11 @@ int mflbm_create(const mflbm_params* params, mflbm_context** out) {
     const size_t T = tsize(c);
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { delete c; return fail(MFLBM_E_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e)); }
+    // super-blocks of 4 x 4 x 4 phi bricks over the s4 lattice
+    d.SX = ((g.nx + 9) / 2 + 3) / 4;
+    d.SY = ((g.ny + 9) / 2 + 3) / 4;
+    d.SZ = ((g.nz + 9) / 2 + 3) / 4;
+    const size_t nsb = (size_t)d.SX * d.SY * d.SZ;
     struct { void** p; size_t bytes; } allocs[] = {
         {&d.pdf, (params->storage == MFLBM_STORE_NATIVE ? T : 2) * d.b.S * 38}, {&d.cnv4, T * 4 * g.n2()},
         {(void**)&d.type8, (size_t)g.n4()},
@@ -615,7 +651,9 @@ int mflbm_create(const mflbm_params* params, mflbm_context** out) {
         {(void**)&d.walls, sizeof(int32_t) * g.n2()}, {(void**)&d.walls_type, sizeof(int32_t) * g.n4()},
         {&d.s_nx, T * g.n4()}, {&d.s_ny, T * g.n4()}, {&d.s_nz, T * g.n4()},
         {(void**)&d.dither, 2 * sizeof(uint32_t)}, {(void**)&d.iface, (size_t)g.n2()},
-        {(void**)&d.phib, (size_t)((g.nx + 9) / 2) * ((g.ny + 9) / 2) * ((g.nz + 9) / 2)}};
+        {(void**)&d.phib, (size_t)((g.nx + 9) / 2) * ((g.ny + 9) / 2) * ((g.nz + 9) / 2)},
+        {(void**)&d.sbcode, nsb}, {(void**)&d.sbact, nsb}, {(void**)&d.sblive, sizeof(uint32_t) * nsb},
+        {(void**)&d.sbinfo, 2 * sizeof(int)}};
     for (auto& a : allocs) {
         if ((rc = alloc_zero(a.p, a.bytes, c->stream)) != MFLBM_OK) {
             free_all(c);
@@ -624,6 +662,7 @@ int mflbm_create(const mflbm_params* params, mflbm_context** out) {
             return rc == MFLBM_E_CUDA ? MFLBM_E_NOMEM : rc;
         }
     }
+    if ((rc = request_full_pass(c)) != MFLBM_OK) { free_all(c); cudaStreamDestroy(c->stream); delete c; return rc; }
     e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) { free_all(c); cudaStreamDestroy(c->stream); delete c; return fail(MFLBM_E_CUDA, cudaGetErrorString(e)); }
     *out = c;
@@ -721,6 +760,7 @@ int mflbm_init_fields(mflbm_context* c, int option, double interface_z0, const v
     if (W_in) MFLBM_CUDA(cudaMemcpyAsync(c->d.W_in, W_in, tsize(c) * g.plane1(), cudaMemcpyHostToDevice, c->stream));
     int rc = init_fields(*c, option, interface_z0);
     if (rc != MFLBM_OK) return rc;
+    if ((rc = request_full_pass(c)) != MFLBM_OK) return rc;
     if ((rc = flavour_gradient(c)) != MFLBM_OK) return rc;
     MFLBM_CUDA(cudaStreamSynchronize(c->stream));
     c->have_fields = true;
@@ -745,7 +785,7 @@ static int init_flow_entry(mflbm_context* c, const void* rho, const void* u, con
     if ((rc = init_flow(*c, dev[0], dev[1], dev[2], dev[3], mrt)) != MFLBM_OK) return rc;
     MFLBM_CUDA(cudaStreamSynchronize(c->stream));
     c->d.arrays_stale = true;
-    return MFLBM_OK;
+    return request_full_pass(c);
 }
 
 int mflbm_init_flow(mflbm_context* c, const void* rho, const void* u, const void* v, const void* w) {
@@ -767,6 +807,7 @@ int mflbm_upload_fields(mflbm_context* c, const void* pdf, const void* phi, cons
     cudaStream_t s = c->stream;
     int rc = ensure_staging(c);
     if (rc != MFLBM_OK) return rc;
+    if ((rc = request_full_pass(c)) != MFLBM_OK) return rc;
     MFLBM_CUDA(cudaMemcpyAsync(d.staging, pdf, T * g.n1() * 38, cudaMemcpyHostToDevice, s));
     if ((rc = convert_populations(*c, true)) != MFLBM_OK) return rc;
     MFLBM_CUDA(cudaMemcpyAsync(d.phi, phi, T * g.n4(), cudaMemcpyHostToDevice, s));

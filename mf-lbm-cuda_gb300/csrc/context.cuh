@@ -63,6 +63,14 @@ struct DeviceState {
     uint32_t* smask = nullptr;         // bit per s2 node: in slist
     int* gcount = nullptr;             // lengths of olist, slist, nlist
     ll n_blocks = 0;                   // node blocks of the normal pass: ((n+4)/2 + 1) per axis
+    // super-blocks of the normal pass: 4 x 4 x 4 phi bricks (8^3 nodes of the s4 lattice)
+    int SX = 0, SY = 0, SZ = 0;        // super-blocks per axis
+    int8_t* sbcode = nullptr;          // per super-block: the common code of its phi bricks, or 0
+    uint8_t* sbact = nullptr;          // per super-block: 1 if its phi can change at the next step (see gradient.cuh)
+    uint8_t* sbslab = nullptr;         // per super-block: 1 if always processed (open or periodic faces)
+    uint32_t* sblive = nullptr;        // super-blocks processed by the current pass
+    int* sbinfo = nullptr;             // [0] live count, [1] 1: process every super-block at the next pass
+    int* phioff = nullptr;             // offsets of each super-block's nodes in list_phi_ext
     int n_sm = 0;                      // multiprocessors of the device (grids of the list passes)
 };
 

@@ -59,16 +59,53 @@ template <class T> struct GradArgs {
     const uint2* l_phi;
     const uint32_t* l_fluid;
     int n_phi, n_cn, n_fluid, n_norm;
+    // super-blocks (4 x 4 x 4 phi bricks)
+    int SX, SY, SZ;
+    int8_t* sbcode;        // common code of the super-block's phi bricks, or 0
+    uint8_t* sbact;        // 1: the super-block's phi may change at the next step
+    uint32_t* sblive;      // super-blocks of this pass
+    int* sbinfo;           // [0] number of them, [1] 1: every super-block (consumed by this pass)
+    const int* phioff;     // list_phi_ext offsets of each super-block
+    int slab_z, slab_y;    // 1: the two super-block rows at each z (y) face are always processed
     Phys<T> ph;
 };
 
 template <class T> __device__ __forceinline__ T wq_of(const ModelConsts<T>& c, int q) { return q < 7 ? c.w1 : c.w2; }
 
+// Append `value` to `list` where `want` is set: one atomic per warp, the
+// order within the list is arbitrary.
+__device__ __forceinline__ void warp_append(bool want, uint32_t value, uint32_t* list, int* count) {
+    const unsigned act = __activemask();
+    const unsigned m = __ballot_sync(act, want);
+    if (!m) return;
+    const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(count, __popc(m));
+    base = __shfl_sync(act, base, leader);
+    if (want) list[base + __popc(m & ((1u << lane) - 1u))] = value;
+}
+
+// Reserve `cnt` consecutive slots of a list per thread (warp prefix sum, one
+// atomic per warp); returns the thread's first slot.  Every lane of the warp
+// must call it.
+__device__ __forceinline__ int warp_reserve(int cnt, int* count) {
+    const int lane = threadIdx.x & 31;
+    int incl = cnt;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += v;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    int base = 0;
+    if (lane == 31 && total) base = atomicAdd(count, total);
+    return __shfl_sync(0xffffffffu, base, 31) + incl - cnt;
+}
+
+
 // phi on solid boundary nodes = weighted mean over fluid neighbours (:732-755)
 template <class T>
-__global__ void __launch_bounds__(256) extrapolate_phi_kernel(const GradArgs<T> a) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= a.n_phi) return;
+__device__ __forceinline__ void extrapolate_phi_at(const GradArgs<T>& a, int t) {
     const uint2 e = a.l_phi[t];
     int i, j, k;
     unpack_xyz(e.x, i, j, k);
@@ -83,6 +120,77 @@ __global__ void __launch_bounds__(256) extrapolate_phi_kernel(const GradArgs<T> 
         }
     }
     a.phi[n] = s / ws;
+}
+
+// the solid boundary nodes of this pass's super-blocks (one block per super-block)
+template <class T>
+__global__ void __launch_bounds__(256) extrapolate_phi_kernel(const GradArgs<T> a) {
+    const int nl = a.sbinfo[0];
+    for (int w = blockIdx.x; w < nl; w += gridDim.x) {
+        const uint32_t sb = a.sblive[w];
+        for (int t = a.phioff[sb] + threadIdx.x; t < a.phioff[sb + 1]; t += blockDim.x) extrapolate_phi_at<T>(a, t);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Super-blocks.  The dense passes (phi on solid boundary nodes, phi brick
+// codes, node listing) run only over super-blocks of 4 x 4 x 4 phi bricks
+// (8^3 nodes of the s4 lattice) where phi can have changed since the last
+// pass.  Away from the interfaces phi is exactly +1 or -1 and a node keeps
+// its value exactly as long as its D3Q19 neighbourhood holds one value: the
+// absent component's populations are exactly 0 there, and collision,
+// recolouring and streaming keep them 0.  So between two passes phi can
+// change only within one node of a brick that was not uniform, or of a
+// boundary between uniform bricks of opposite sign: within the 3 x 3 x 3
+// super-blocks around a super-block flagged `sbact` (its bricks have no
+// common code, or a neighbour super-block has another code) by the previous
+// pass.  The extrapolated phi of a solid node, a brick code and a node
+// block's activity depend on phi within one node, which stays inside those
+// 27 super-blocks.  Super-blocks at open (inlet / outlet) or periodic faces,
+// whose ghost layers the boundary updates rewrite every step, are always
+// processed, and so is everything after the host set or uploaded a state.
+// Elsewhere phi, the brick codes and the zero records are those of the last
+// pass that processed the super-block.
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void __launch_bounds__(256) sb_live_kernel(const GradArgs<T> a) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    bool live = false;
+    if (s < a.SX * a.SY * a.SZ) {
+        const int sx = s % a.SX, sy = (s / a.SX) % a.SY, sz = s / (a.SX * a.SY);
+        live = a.sbinfo[1] != 0 || (a.slab_z && (sz <= 1 || sz >= a.SZ - 2)) ||
+               (a.slab_y && (sy <= 1 || sy >= a.SY - 2));
+        for (int dz = -1; dz <= 1 && !live; ++dz)
+            for (int dy = -1; dy <= 1 && !live; ++dy)
+                for (int dx = -1; dx <= 1 && !live; ++dx) {
+                    const int x = sx + dx, y = sy + dy, z = sz + dz;
+                    if (x >= 0 && x < a.SX && y >= 0 && y < a.SY && z >= 0 && z < a.SZ &&
+                        a.sbact[x + a.SX * (y + a.SY * z)])
+                        live = true;
+                }
+    }
+    warp_append(live, (uint32_t)s, a.sblive, &a.sbinfo[0]);
+}
+
+// sbact of every super-block from this pass's codes; consumes the
+// every-super-block request
+template <class T>
+__global__ void __launch_bounds__(256) sb_active_kernel(const GradArgs<T> a) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s == 0) a.sbinfo[1] = 0;
+    if (s >= a.SX * a.SY * a.SZ) return;
+    const int sx = s % a.SX, sy = (s / a.SX) % a.SY, sz = s / (a.SX * a.SY);
+    const int8_t c = a.sbcode[s];
+    bool act = c == 0;
+    for (int dz = -1; dz <= 1 && !act; ++dz)
+        for (int dy = -1; dy <= 1 && !act; ++dy)
+            for (int dx = -1; dx <= 1 && !act; ++dx) {
+                const int x = sx + dx, y = sy + dy, z = sz + dz;
+                if (x >= 0 && x < a.SX && y >= 0 && y < a.SY && z >= 0 && z < a.SZ &&
+                    a.sbcode[x + a.SX * (y + a.SY * z)] != c)
+                    act = true;
+            }
+    a.sbact[s] = act ? 1 : 0;
 }
 
 // geometrical wetting: secant iteration turning the interface normal towards
@@ -167,19 +275,14 @@ __device__ __forceinline__ void clear_records(const GradArgs<T>& a, int tid, int
 // (s4-local coordinates 2b, 2b + 1 on each axis; positions past the lattice
 // end are ignored), 1 if every phi is exactly +1, 2 if every phi is exactly -1,
 // 0 otherwise.  Away from interfaces phi is exactly +-1 (one component is
-// exactly zero), so most bricks are uniform.
+// exactly zero), so most bricks are uniform.  One block of 64 threads per
+// super-block of this pass (one brick per thread); the super-block's code is
+// the bricks' common code, or 0.  The threads also reset the records of the
+// previous pass's lists.
 template <class T>
-__global__ void __launch_bounds__(256) phi_brick_kernel(const GradArgs<T> a) {
+__device__ __forceinline__ int8_t phi_brick_code(const GradArgs<T>& a, int bx, int by, int bz) {
     typedef typename Vec2<T>::type P;
     const int NX = a.g.nx + 8, NY = a.g.ny + 8, NZ = a.g.nz + 8;
-    const int BX = (NX + 1) >> 1, BY = (NY + 1) >> 1, BZ = (NZ + 1) >> 1;
-    // bricks in x-fastest order; fewer than 2^31 bricks for any lattice the
-    // packed coordinates allow, so 32-bit division
-    const unsigned b = blockIdx.x * blockDim.x + threadIdx.x;
-    clear_records<T>(a, (int)b, (int)(gridDim.x * blockDim.x));
-    if (b >= (unsigned)(BX * BY * BZ)) return;
-    const unsigned bxy = b / (unsigned)BX;
-    const int bx = (int)(b - bxy * (unsigned)BX), by = (int)(bxy % (unsigned)BY), bz = (int)(bxy / (unsigned)BY);
     bool plus = true, minus = true;
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
@@ -198,7 +301,31 @@ __global__ void __launch_bounds__(256) phi_brick_kernel(const GradArgs<T> a) {
         plus = plus && v0 == T(1) && v1 == T(1);
         minus = minus && v0 == T(-1) && v1 == T(-1);
     }
-    a.phib[b] = plus ? 1 : minus ? 2 : 0;
+    return plus ? 1 : minus ? 2 : 0;
+}
+
+template <class T>
+__global__ void __launch_bounds__(64) phi_brick_kernel(const GradArgs<T> a) {
+    __shared__ int ref;
+    clear_records<T>(a, (int)(blockIdx.x * blockDim.x + threadIdx.x), (int)(gridDim.x * blockDim.x));
+    const int BX = (a.g.nx + 9) >> 1, BY = (a.g.ny + 9) >> 1, BZ = (a.g.nz + 9) >> 1;
+    const int nl = a.sbinfo[0];
+    const int lx = threadIdx.x & 3, ly = (threadIdx.x >> 2) & 3, lz = threadIdx.x >> 4;
+    for (int w = blockIdx.x; w < nl; w += gridDim.x) {
+        const int sb = (int)a.sblive[w];
+        const int bx = 4 * (sb % a.SX) + lx, by = 4 * ((sb / a.SX) % a.SY) + ly, bz = 4 * (sb / (a.SX * a.SY)) + lz;
+        const bool in = bx < BX && by < BY && bz < BZ;
+        int8_t code = 0;
+        if (in) {
+            code = phi_brick_code<T>(a, bx, by, bz);
+            a.phib[bx + (ll)BX * (by + (ll)BY * bz)] = code;
+        }
+        if (threadIdx.x == 0) ref = code;   // brick (4 sx, 4 sy, 4 sz) always exists
+        __syncthreads();
+        const int same = __syncthreads_and(!in || code == ref);
+        if (threadIdx.x == 0) a.sbcode[sb] = same ? (int8_t)ref : 0;
+        __syncthreads();
+    }
 }
 
 // the normal record of node (i, j, k) of walls_type <= 0 (:757-807) + wetting
@@ -227,69 +354,43 @@ __device__ __forceinline__ bool normal_at(const GradArgs<T>& a, int i, int j, in
     return r.w != T(0);
 }
 
-// Append `value` to `list` where `want` is set: one atomic per warp, the
-// order within the list is arbitrary.
-__device__ __forceinline__ void warp_append(bool want, uint32_t value, uint32_t* list, int* count) {
-    const unsigned act = __activemask();
-    const unsigned m = __ballot_sync(act, want);
-    if (!m) return;
-    const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
-    int base = 0;
-    if (lane == leader) base = atomicAdd(count, __popc(m));
-    base = __shfl_sync(act, base, leader);
-    if (want) list[base + __popc(m & ((1u << lane) - 1u))] = value;
-}
-
-// Reserve `cnt` consecutive slots of a list per thread (warp prefix sum, one
-// atomic per warp); returns the thread's first slot.  Every lane of the warp
-// must call it.
-__device__ __forceinline__ int warp_reserve(int cnt, int* count) {
-    const int lane = threadIdx.x & 31;
-    int incl = cnt;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const int v = __shfl_up_sync(0xffffffffu, incl, d);
-        if (lane >= d) incl += v;
-    }
-    const int total = __shfl_sync(0xffffffffu, incl, 31);
-    int base = 0;
-    if (lane == 31 && total) base = atomicAdd(count, total);
-    return __shfl_sync(0xffffffffu, base, 31) + incl - cnt;
-}
-
 // Node block c (nodes 2c-2 .. 2c-1 on each axis) is active unless the eight
 // phi bricks c .. c+1 that hold its stencils (s4-local i+2 .. i+4) have one
 // common non-zero code.  The fluid nodes (walls_type <= 0) of [-1, n+2]^3 in
-// active blocks are appended to nlist (one atomic per warp).
+// active blocks are appended to nlist (one atomic per warp).  One block of 64
+// threads per super-block of this pass: its 4 x 4 x 4 node blocks c (a node
+// block belongs to the super-block of its brick c).
 template <class T>
-__global__ void __launch_bounds__(256) active_nodes_kernel(const GradArgs<T> a) {
+__global__ void __launch_bounds__(64) active_nodes_kernel(const GradArgs<T> a) {
     const Grid& g = a.g;
     const int BX = (g.nx + 9) >> 1, BY = (g.ny + 9) >> 1;
     const int CX = ((g.nx + 4) >> 1) + 1, CY = ((g.ny + 4) >> 1) + 1, CZ = ((g.nz + 4) >> 1) + 1;
-    const unsigned c = blockIdx.x * blockDim.x + threadIdx.x;   // fewer than 2^31 blocks
-    unsigned sel = 0;   // bit e: node e of the block is listed
-    int cx = 0, cy = 0, cz = 0;
-    if (c < (unsigned)(CX * CY * CZ)) {
-        const unsigned cyz = c / (unsigned)CX;
-        cx = (int)(c - cyz * (unsigned)CX); cy = (int)(cyz % (unsigned)CY); cz = (int)(cyz / (unsigned)CY);
-        const int8_t* pb = a.phib + cx + (ll)BX * (cy + (ll)BY * cz);
-        const int8_t c0 = pb[0];
-        const bool quiet = c0 != 0 && pb[1] == c0 && pb[BX] == c0 && pb[BX + 1] == c0 && pb[(ll)BX * BY] == c0 &&
-                           pb[(ll)BX * BY + 1] == c0 && pb[(ll)BX * BY + BX] == c0 && pb[(ll)BX * BY + BX + 1] == c0;
-        if (!quiet) {
+    const int nl = a.sbinfo[0];
+    const int lx = threadIdx.x & 3, ly = (threadIdx.x >> 2) & 3, lz = threadIdx.x >> 4;
+    for (int w = blockIdx.x; w < nl; w += gridDim.x) {
+        const int sb = (int)a.sblive[w];
+        const int cx = 4 * (sb % a.SX) + lx, cy = 4 * ((sb / a.SX) % a.SY) + ly, cz = 4 * (sb / (a.SX * a.SY)) + lz;
+        unsigned sel = 0;   // bit e: node e of the block is listed
+        if (cx < CX && cy < CY && cz < CZ) {
+            const int8_t* pb = a.phib + cx + (ll)BX * (cy + (ll)BY * cz);
+            const int8_t c0 = pb[0];
+            const bool quiet = c0 != 0 && pb[1] == c0 && pb[BX] == c0 && pb[BX + 1] == c0 && pb[(ll)BX * BY] == c0 &&
+                               pb[(ll)BX * BY + 1] == c0 && pb[(ll)BX * BY + BX] == c0 && pb[(ll)BX * BY + BX + 1] == c0;
+            if (!quiet) {
 #pragma unroll
-            for (int e = 0; e < 8; ++e) {
-                const int i = 2 * cx - 2 + (e & 1), j = 2 * cy - 2 + ((e >> 1) & 1), k = 2 * cz - 2 + (e >> 2);
-                if (i >= -1 && i <= g.nx + 2 && j >= -1 && j <= g.ny + 2 && k >= -1 && k <= g.nz + 2 &&
-                    a.type8[g.s4(i, j, k)] <= 0)
-                    sel |= 1u << e;
+                for (int e = 0; e < 8; ++e) {
+                    const int i = 2 * cx - 2 + (e & 1), j = 2 * cy - 2 + ((e >> 1) & 1), k = 2 * cz - 2 + (e >> 2);
+                    if (i >= -1 && i <= g.nx + 2 && j >= -1 && j <= g.ny + 2 && k >= -1 && k <= g.nz + 2 &&
+                        a.type8[g.s4(i, j, k)] <= 0)
+                        sel |= 1u << e;
+                }
             }
         }
+        int base = warp_reserve(__popc(sel), &a.gcount[2]);
+        for (int e = 0; e < 8; ++e)
+            if (sel & (1u << e))
+                a.nlist[base++] = pack_xyz(2 * cx - 2 + (e & 1), 2 * cy - 2 + ((e >> 1) & 1), 2 * cz - 2 + (e >> 2));
     }
-    int base = warp_reserve(__popc(sel), &a.gcount[2]);
-    for (int e = 0; e < 8; ++e)
-        if (sel & (1u << e))
-            a.nlist[base++] = pack_xyz(2 * cx - 2 + (e & 1), 2 * cy - 2 + ((e >> 1) & 1), 2 * cz - 2 + (e >> 2));
 }
 
 // unit interface normal and |grad phi| (:757-807) + wetting (:809-878) at the
@@ -501,6 +602,12 @@ GradArgs<T> grad_args(const mflbm_context& c) {
     a.n_cn = (int)d.n_cn_ext;
     a.l_fluid = d.fluid_list; a.n_fluid = (int)d.n_fluid;
     a.n_norm = (int)d.n_norm;
+    a.SX = d.SX; a.SY = d.SY; a.SZ = d.SZ;
+    a.sbcode = d.sbcode; a.sbact = d.sbact; a.sblive = (uint32_t*)d.sblive; a.sbinfo = d.sbinfo;
+    a.phioff = d.phioff;
+    const mflbm_params& p = c.params;
+    a.slab_z = p.kper || (p.domain_wall_status_z_min == 0 && p.domain_wall_status_z_max == 0);
+    a.slab_y = p.jper;
     a.ph = make_phys<T>(c.params);
     return a;
 }
@@ -513,10 +620,6 @@ int launch_gradient(mflbm_context& c) {
     const Tuning& tn = c.d.tune;
     cudaStream_t s = c.stream;
     int rc;
-    if (a.n_phi) {
-        extrapolate_phi_kernel<T><<<grid_for(a.n_phi, tn.extrapolate), tn.extrapolate, 0, s>>>(a);
-        if ((rc = after_launch("extrapolate_phi")) != MFLBM_OK) return rc;
-    }
     // the list passes run one wave of resident blocks (grid-stride loops: the
     // list lengths are known only on the device; blocks beyond the resident
     // ones would start only after the first wave has walked the whole list)
@@ -527,13 +630,25 @@ int launch_gradient(mflbm_context& c) {
             per_sm = 1;
         return std::max(1, c.d.n_sm) * per_sm;
     };
+    const int nsb = a.SX * a.SY * a.SZ;
+    // this pass's super-blocks
+    MFLBM_CUDA(cudaMemsetAsync(c.d.sbinfo, 0, sizeof(int), s));
+    sb_live_kernel<T><<<grid_for(nsb, 256), 256, 0, s>>>(a);
+    if ((rc = after_launch("sb_live")) != MFLBM_OK) return rc;
+    if (a.n_phi) {
+        extrapolate_phi_kernel<T><<<wave((const void*)extrapolate_phi_kernel<T>, tn.extrapolate), tn.extrapolate, 0, s>>>(a);
+        if ((rc = after_launch("extrapolate_phi")) != MFLBM_OK) return rc;
+    }
     if (a.n_norm) {
-        const Grid& g = c.d.g;
         // brick codes + reset of the previous lists' records, then the lists restart
-        phi_brick_kernel<T><<<grid_for((ll)((g.nx + 9) / 2) * ((g.ny + 9) / 2) * ((g.nz + 9) / 2), 256), 256, 0, s>>>(a);
+        phi_brick_kernel<T><<<wave((const void*)phi_brick_kernel<T>, 64), 64, 0, s>>>(a);
         if ((rc = after_launch("phi_brick")) != MFLBM_OK) return rc;
+    }
+    sb_active_kernel<T><<<grid_for(nsb, 256), 256, 0, s>>>(a);
+    if ((rc = after_launch("sb_active")) != MFLBM_OK) return rc;
+    if (a.n_norm) {
         MFLBM_CUDA(cudaMemsetAsync(c.d.gcount, 0, 3 * sizeof(int), s));
-        active_nodes_kernel<T><<<grid_for(c.d.n_blocks, 256), 256, 0, s>>>(a);
+        active_nodes_kernel<T><<<wave((const void*)active_nodes_kernel<T>, 64), 64, 0, s>>>(a);
         if ((rc = after_launch("active_nodes")) != MFLBM_OK) return rc;
         normals_kernel<T><<<wave((const void*)normals_kernel<T>, tn.normals), tn.normals, 0, s>>>(a);
         if ((rc = after_launch("normals")) != MFLBM_OK) return rc;

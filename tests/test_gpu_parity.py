@@ -88,15 +88,17 @@ def test_strict_is_bit_exact_on_odd_sizes(mflbm_lib, kind):
     ctx.close()
 
 
-@pytest.mark.parametrize("kind", ["periodic_drop", "plate_drainage"])
+@pytest.mark.parametrize("kind", ["periodic_drop", "plate_drainage", "velocity_convective"])
 def test_strict_long_run_with_moving_interface(mflbm_lib, kind):
-    """150 steps with a moving interface, graph-replayed and per-step calls
+    """500 steps with a moving interface, graph-replayed and per-step calls
     mixed: the sparse gradient sets (interface nodes, claimed solid nodes)
-    are rebuilt every pass and every record outside them must stay the zero
-    record, so stale entries would show up as differences here."""
+    are rebuilt every pass over the super-blocks where phi can have changed,
+    and every record, brick code and solid phi outside them must stay what
+    the dense passes give, so stale entries would show up as differences."""
     case, ctx, info, o = _setup(kind, abi.MFLBM_FP32, abi.MFLBM_STRICT)
     sizes = []
-    for first, count, eager in [(1, 60, False), (61, 30, True), (91, 60, False)]:
+    for first, count, eager in [(1, 60, False), (61, 30, True), (91, 210, False), (301, 40, True),
+                                (341, 160, False)]:
         if eager:
             for nt in range(first, first + count):
                 ctx.step(nt)

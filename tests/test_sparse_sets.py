@@ -105,3 +105,86 @@ def test_skipped_nodes_have_uniform_stencils(n, sharp):
     assert skipped_nonzero == 0
     # the fields are not trivial: both kinds of blocks occur
     assert act.any() and not act.all()
+
+
+# ---------------------------------------------------------------------------
+# Super-blocks (gradient.cuh: sb_live_kernel, sb_active_kernel): 4 x 4 x 4
+# phi bricks.  A pass processes only the super-blocks within one super-block
+# of those flagged by the previous pass (no common code among their bricks,
+# or a neighbour super-block with another code).  Restated here: between two
+# passes phi may change only within one node (D3Q19 neighbourhood) of a node
+# whose neighbourhood is not of one value; then every brick whose code can
+# change and every node block whose activity can change lies in a processed
+# super-block.
+# ---------------------------------------------------------------------------
+def super_codes(codes):
+    BZ, BY, BX = codes.shape
+    SZ, SY, SX = (BZ + 3) // 4, (BY + 3) // 4, (BX + 3) // 4
+    pad = np.full((4 * SZ, 4 * SY, 4 * SX), -1, dtype=np.int16)
+    pad[:BZ, :BY, :BX] = codes
+    b = pad.reshape(SZ, 4, SY, 4, SX, 4)
+    first = b[:, 0, :, 0, :, 0]
+    same = np.all((b == first[:, None, :, None, :, None]) | (b == -1), axis=(1, 3, 5))
+    return np.where(same, first, 0)
+
+
+def dilate(mask):
+    out = mask.copy()
+    SZ, SY, SX = mask.shape
+    for dz in (-1, 0, 1):
+        for dy in (-1, 0, 1):
+            for dx in (-1, 0, 1):
+                src = mask[max(0, -dz):SZ - max(0, dz), max(0, -dy):SY - max(0, dy), max(0, -dx):SX - max(0, dx)]
+                out[max(0, dz):SZ - max(0, -dz), max(0, dy):SY - max(0, -dy), max(0, dx):SX - max(0, -dx)] |= src
+    return out
+
+
+def flagged(sc):
+    act = sc == 0
+    SZ, SY, SX = sc.shape
+    for dz in (-1, 0, 1):
+        for dy in (-1, 0, 1):
+            for dx in (-1, 0, 1):
+                a = sc[max(0, -dz):SZ - max(0, dz), max(0, -dy):SY - max(0, dy), max(0, -dx):SX - max(0, dx)]
+                b = sc[max(0, dz):SZ - max(0, -dz), max(0, dy):SY - max(0, -dy), max(0, dx):SX - max(0, -dx)]
+                act[max(0, dz):SZ - max(0, -dz), max(0, dy):SY - max(0, -dy), max(0, dx):SX - max(0, -dx)] |= a != b
+    return act
+
+
+@pytest.mark.parametrize("n", [(40, 40, 56), (33, 29, 47)])
+@pytest.mark.parametrize("sharp", [False, True], ids=["diffuse", "sharp"])
+def test_super_blocks_cover_every_change(n, sharp):
+    nx, ny, nz = n
+    phi = random_phase(n, seed=7 * nx + nz, sharp=sharp)
+    rng = np.random.default_rng(nx)
+
+    def shifted(a, q):
+        """a at x + e_q, edge values repeated past the array (no wrap)."""
+        p = np.pad(a, 1, mode="edge")
+        return p[1 + EZ[q]:1 + EZ[q] + a.shape[0], 1 + EY[q]:1 + EY[q] + a.shape[1], 1 + EX[q]:1 + EX[q] + a.shape[2]]
+
+    # nodes whose D3Q19 neighbourhood (on the s4 array) is not of one value
+    nonuni = np.zeros(phi.shape, dtype=bool)
+    for q in range(1, 19):
+        nonuni |= shifted(phi, q) != phi
+    # phi may change within one node of them: perturb a random subset there
+    near = nonuni.copy()
+    for q in range(1, 19):
+        near |= shifted(nonuni, q)
+    new = phi.copy()
+    pick = near & (rng.random(phi.shape) < 0.5)
+    new[pick] = rng.uniform(-1, 1, size=int(pick.sum()))
+    codes_old, codes_new = brick_codes(phi), brick_codes(new)
+    live = dilate(flagged(super_codes(codes_old)))
+    BZ, BY, BX = codes_old.shape
+    changed = np.argwhere(codes_old != codes_new)
+    for bz, by, bx in changed:
+        assert live[bz // 4, by // 4, bx // 4], ("brick", bz, by, bx)
+    act_old, act_new = active_blocks(codes_old, n), active_blocks(codes_new, n)
+    for cz, cy, cx in np.argwhere(act_old != act_new):
+        assert live[cz // 4, cy // 4, cx // 4], ("block", cz, cy, cx)
+    # changed nodes (and so the solid nodes extrapolating from them) lie in
+    # processed super-blocks or next to one
+    for k, j, i in np.argwhere(new != phi):
+        assert live[(k // 2) // 4, (j // 2) // 4, (i // 2) // 4], ("node", k, j, i)
+    assert len(changed) > 0
