@@ -4,13 +4,12 @@
 // One cooperative launch runs many time steps of every sample of a batch.
 // Each step is a sequence of phases over a work list of (sample, unit)
 // pairs, separated by grid barriers:
-//   collision   units of `blockDim` consecutive fluid-list entries;
-//   periodic z  units of one (j) row of `blockDim` x-columns (kper);
-//   periodic y  units of one (k) row (jper);
-//   periodic zy units of `blockDim` x-columns (jper and kper);
-// the same device functions, in the same order, as the per-sample launches
-// (collide_stream_kernel, periodic_*_kernel), so every sample's state is
-// bit-identical to stepping it alone.
+//   collision  units of `blockDim` consecutive fluid-list entries;
+//   periodic   units of `blockDim` exchange items (periodic_item: z, y and
+//              the z-y edges, which can run at once);
+// the same device functions as the per-sample launches (collide_stream_kernel,
+// periodic_kernel), so every sample's state is bit-identical to stepping it
+// alone.
 //
 // Single phase: the host launches this only for samples whose second
 // component is absent everywhere (every component-2 population exactly 0,
@@ -37,9 +36,10 @@ namespace MFLBM_NS {
 template <class T, class E> struct BatchSample {
     CollideArgs<T, E> c;
     BcArgs<T, E> bc;
+    int jper, kper;
 };
 
-enum { kPhaseCollide = 0, kPhaseZ = 1, kPhaseY = 2, kPhaseZY = 3, kPhases = 4 };
+enum { kPhaseCollide = 0, kPhasePeriodic = 1, kPhases = 2 };
 
 struct BatchSync {
     unsigned* bar;                 // [0] arrivals, [1] generation
@@ -109,20 +109,10 @@ __global__ void __launch_bounds__(256) batch_persistent_kernel(const BatchSample
                         else collide_node<T, E, false, uint32_t>(s.c, t);
                     }
                 } else {
-                    const Grid& g = s.bc.g;
-                    const int xu = (g.nx + blockDim.x - 1) / blockDim.x;   // x-chunks per row
-                    const int i = (r % xu) * blockDim.x + threadIdx.x + 1, row = r / xu + 1;
-                    if (i <= g.nx) {
-                        if (ph == kPhaseZ) {
-                            if (odd) periodic_z_at<T, E, true>(s.bc, i, row);
-                            else periodic_z_at<T, E, false>(s.bc, i, row);
-                        } else if (ph == kPhaseY) {
-                            if (odd) periodic_y_at<T, E, true>(s.bc, i, row);
-                            else periodic_y_at<T, E, false>(s.bc, i, row);
-                        } else {
-                            if (odd) periodic_zy_at<T, E, true>(s.bc, i);
-                            else periodic_zy_at<T, E, false>(s.bc, i);
-                        }
+                    const int item = r * blockDim.x + threadIdx.x;
+                    if (item < periodic_items(s.bc.g, s.jper, s.kper)) {
+                        if (odd) periodic_item<T, E, true>(s.bc, s.jper, s.kper, item);
+                        else periodic_item<T, E, false>(s.bc, s.jper, s.kper, item);
                     }
                 }
             }
@@ -163,6 +153,8 @@ BatchSample<T, E> batch_sample(const mflbm_context& c) {
     BatchSample<T, E> s;
     s.c = collide_args<T, E>(c);
     s.bc = bc_args<T, E>(c);
+    s.jper = c.params.jper;
+    s.kper = c.params.kper;
     return s;
 }
 

@@ -38,9 +38,7 @@ __device__ __constant__ const int kOutlet[5][5] = {{0, 0, 6, 5, 6}, {-1, 0, 13, 
 
 // velocity inlet: bounce-back plus 6 w rho u injection, split by sa_inject (:1009-1077)
 template <class T, class E, bool AFTER_ODD>
-__global__ void inlet_velocity_kernel(const BcArgs<T, E> a) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1;
-    if (i > a.g.nx) return;
+__device__ __forceinline__ void inlet_velocity_at(const BcArgs<T, E>& a, int i, int j) {
     const Grid& g = a.g;
     const int w = a.walls[g.s2(i, j, 1)];
     inlet_phi(a, i, j, w);
@@ -67,9 +65,7 @@ __global__ void inlet_velocity_kernel(const BcArgs<T, E> a) {
 
 // Zou-He pressure inlet per component (:1085-1241)
 template <class T, class E, bool AFTER_ODD>
-__global__ void inlet_pressure_kernel(const BcArgs<T, E> a) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1;
-    if (i > a.g.nx) return;
+__device__ __forceinline__ void inlet_pressure_at(const BcArgs<T, E>& a, int i, int j) {
     const Grid& g = a.g;
     const int w = a.walls[g.s2(i, j, 1)];
     inlet_phi(a, i, j, w);
@@ -117,9 +113,7 @@ __global__ void inlet_pressure_kernel(const BcArgs<T, E> a) {
 
 // convective outflow with the previous-step buffers (:1246-1357)
 template <class T, class E, bool AFTER_ODD>
-__global__ void outlet_convective_kernel(const BcArgs<T, E> a) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1;
-    if (i > a.g.nx) return;
+__device__ __forceinline__ void outlet_convective_at(const BcArgs<T, E>& a, int i, int j) {
     const Grid& g = a.g;
     const int nz = g.nz;
     const T u = a.ph.uin_avg;
@@ -155,9 +149,7 @@ __global__ void outlet_convective_kernel(const BcArgs<T, E> a) {
 
 // Zou-He pressure outlet on the total density, flux split by phi (:1363-1524)
 template <class T, class E, bool AFTER_ODD>
-__global__ void outlet_pressure_kernel(const BcArgs<T, E> a) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1;
-    if (i > a.g.nx) return;
+__device__ __forceinline__ void outlet_pressure_at(const BcArgs<T, E>& a, int i, int j) {
     const Grid& g = a.g;
     const int nz = g.nz;
     const int w = a.walls[g.s2(i, j, nz)];
@@ -222,12 +214,34 @@ __global__ void outlet_pressure_kernel(const BcArgs<T, E> a) {
 
 // Periodic copies across z = 1 / nz, y = 1 / ny and the zy edges (:1529-1733).
 // Directions leaving through the upper face: (ez or ey) = -1 ... see tables.
+// Inlet (1 velocity, 2 pressure, 0 none) and outlet (1 convective, 2 pressure,
+// 0 none) of column (i, j) in one launch.  The inlet reads and writes the z
+// planes 0 .. 2, the outlet nz - 1 .. nz + 1 (and the phi ghosts beyond
+// each): with nz >= 4 they touch no common location, so running them
+// together gives the reference's result of running them one after the other.
+template <class T, class E, bool AFTER_ODD>
+__global__ void inlet_outlet_kernel(const BcArgs<T, E> a, int inlet, int outlet) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1;
+    if (i > a.g.nx) return;
+    if (inlet == 1) inlet_velocity_at<T, E, AFTER_ODD>(a, i, j);
+    else if (inlet == 2) inlet_pressure_at<T, E, AFTER_ODD>(a, i, j);
+    if (outlet == 1) outlet_convective_at<T, E, AFTER_ODD>(a, i, j);
+    else if (outlet == 2) outlet_pressure_at<T, E, AFTER_ODD>(a, i, j);
+}
+
 __device__ __constant__ const int kZup[5] = {6, 14, 13, 18, 17}, kZdn[5] = {5, 11, 12, 15, 16};
 __device__ __constant__ const int kYup[5] = {4, 10, 9, 16, 18}, kYdn[5] = {3, 7, 8, 15, 17};
 
-// periodic z of column (i, j), i, j >= 1
+// Periodic exchanges (:1529-1735).  The reference runs z, then y, then the
+// z-y edges.  Their sources are never another exchange's destinations
+// (before the odd step they copy interior slots to ghosts, after it ghost
+// slots to the interior), and their destinations meet only after the odd
+// step, at the four corner slots of each x column where z and y both write
+// and the edge copy writes last.  `edges` (periodic y and z) makes z and y
+// leave those four slots to the edge copy, so the three can run at once
+// with the reference's result.
 template <class T, class E, bool ODD>
-__device__ __forceinline__ void periodic_z_at(const BcArgs<T, E>& a, int i, int j) {
+__device__ __forceinline__ void periodic_z_at(const BcArgs<T, E>& a, int i, int j, bool edges = false) {
     const Grid& g = a.g;
     const int nz = g.nz;
 #pragma unroll
@@ -238,8 +252,10 @@ __device__ __forceinline__ void periodic_z_at(const BcArgs<T, E>& a, int i, int 
                 a.P.copy(i, j, nz + 1, kZup[s], gg, i, j, 1, kZup[s]);
                 a.P.copy(i, j, 0, kZdn[s], gg, i, j, nz, kZdn[s]);
             } else {
-                a.P.copy(i, j, 1, kZup[s], gg, i, j, nz + 1, kZup[s]);
-                a.P.copy(i, j, nz, kZdn[s], gg, i, j, 0, kZdn[s]);
+                const bool up = !(edges && ((j == 1 && kZup[s] == 18) || (j == g.ny && kZup[s] == 17)));
+                const bool dn = !(edges && ((j == 1 && kZdn[s] == 16) || (j == g.ny && kZdn[s] == 15)));
+                if (up) a.P.copy(i, j, 1, kZup[s], gg, i, j, nz + 1, kZup[s]);
+                if (dn) a.P.copy(i, j, nz, kZdn[s], gg, i, j, 0, kZdn[s]);
             }
         }
     for (int k = 1; k <= 4; ++k) {
@@ -247,15 +263,10 @@ __device__ __forceinline__ void periodic_z_at(const BcArgs<T, E>& a, int i, int 
         a.phi[g.s4(i, j, k - 4)] = a.phi[g.s4(i, j, nz + k - 4)];
     }
 }
-template <class T, class E, bool ODD>
-__global__ void periodic_z_kernel(const BcArgs<T, E> a) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1;
-    if (i <= a.g.nx) periodic_z_at<T, E, ODD>(a, i, j);
-}
 
 // periodic y of row (i, k), i, k >= 1
 template <class T, class E, bool ODD>
-__device__ __forceinline__ void periodic_y_at(const BcArgs<T, E>& a, int i, int k) {
+__device__ __forceinline__ void periodic_y_at(const BcArgs<T, E>& a, int i, int k, bool edges = false) {
     const Grid& g = a.g;
     const int ny = g.ny;
 #pragma unroll
@@ -266,19 +277,16 @@ __device__ __forceinline__ void periodic_y_at(const BcArgs<T, E>& a, int i, int 
                 a.P.copy(i, ny + 1, k, kYup[s], gg, i, 1, k, kYup[s]);
                 a.P.copy(i, 0, k, kYdn[s], gg, i, ny, k, kYdn[s]);
             } else {
-                a.P.copy(i, 1, k, kYup[s], gg, i, ny + 1, k, kYup[s]);
-                a.P.copy(i, ny, k, kYdn[s], gg, i, 0, k, kYdn[s]);
+                const bool up = !(edges && ((k == 1 && kYup[s] == 18) || (k == g.nz && kYup[s] == 16)));
+                const bool dn = !(edges && ((k == 1 && kYdn[s] == 17) || (k == g.nz && kYdn[s] == 15)));
+                if (up) a.P.copy(i, 1, k, kYup[s], gg, i, ny + 1, k, kYup[s]);
+                if (dn) a.P.copy(i, ny, k, kYdn[s], gg, i, 0, k, kYdn[s]);
             }
         }
     for (int j = 1; j <= 4; ++j) {
         a.phi[g.s4(i, j + ny, k)] = a.phi[g.s4(i, j, k)];
         a.phi[g.s4(i, j - 4, k)] = a.phi[g.s4(i, ny + j - 4, k)];
     }
-}
-template <class T, class E, bool ODD>
-__global__ void periodic_y_kernel(const BcArgs<T, E> a) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y + 1;
-    if (i <= a.g.nx) periodic_y_at<T, E, ODD>(a, i, k);
 }
 
 // periodic z-y edges of column i >= 1
@@ -308,10 +316,26 @@ __device__ __forceinline__ void periodic_zy_at(const BcArgs<T, E>& a, int i) {
             a.phi[g.s4(i, j - 4, k + nz)] = a.phi[g.s4(i, ny + j - 4, k)];
         }
 }
+// Work item r of the periodic exchanges (0 <= r < periodic_items): z for
+// (i, j) when kper, then y for (i, k) when jper, then the edges for i when
+// both.
+__host__ __device__ __forceinline__ int periodic_items(const Grid& g, int jper, int kper) {
+    return (kper ? g.nx * g.ny : 0) + (jper ? g.nx * g.nz : 0) + (jper && kper ? g.nx : 0);
+}
 template <class T, class E, bool ODD>
-__global__ void periodic_zy_kernel(const BcArgs<T, E> a) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    if (i <= a.g.nx) periodic_zy_at<T, E, ODD>(a, i);
+__device__ __forceinline__ void periodic_item(const BcArgs<T, E>& a, int jper, int kper, int r) {
+    const Grid& g = a.g;
+    const bool edges = jper && kper;
+    const int nzr = kper ? g.nx * g.ny : 0, nyr = jper ? g.nx * g.nz : 0;
+    if (r < nzr) periodic_z_at<T, E, ODD>(a, r % g.nx + 1, r / g.nx + 1, edges);
+    else if (r < nzr + nyr) periodic_y_at<T, E, ODD>(a, (r - nzr) % g.nx + 1, (r - nzr) / g.nx + 1, edges);
+    else periodic_zy_at<T, E, ODD>(a, r - nzr - nyr + 1);
+}
+// all periodic exchanges of a step in one launch
+template <class T, class E, bool ODD>
+__global__ void periodic_kernel(const BcArgs<T, E> a, int jper, int kper, int n) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < n) periodic_item<T, E, ODD>(a, jper, kper, r);
 }
 
 // porous plate blocking one component at z = Zplate (:1744-1882); b = blocked component
@@ -403,14 +427,20 @@ int launch_boundaries(mflbm_context& c, bool odd) {
         else kernel<T, E, false><<<gridv, 128, 0, s>>>(a);                        \
         if ((rc = after_launch(name)) != MFLBM_OK) return rc;                     \
     } while (0)
-    if (p.kper) MFLBM_BC(periodic_z_kernel, dim3(bx, g.ny), "periodic_z");
-    if (p.jper) MFLBM_BC(periodic_y_kernel, dim3(bx, g.nz), "periodic_y");
-    if (p.jper && p.kper) MFLBM_BC(periodic_zy_kernel, dim3(bx, 1), "periodic_zy");
+    if (p.jper || p.kper) {
+        const int n = periodic_items(g, p.jper, p.kper);
+        if (odd) periodic_kernel<T, E, true><<<grid_for(n, 128), 128, 0, s>>>(a, p.jper, p.kper, n);
+        else periodic_kernel<T, E, false><<<grid_for(n, 128), 128, 0, s>>>(a, p.jper, p.kper, n);
+        if ((rc = after_launch("periodic")) != MFLBM_OK) return rc;
+    }
     if (p.kper == 0 && p.domain_wall_status_z_min == 0 && p.domain_wall_status_z_max == 0) {
-        if (p.inlet_BC == 1) MFLBM_BC(inlet_velocity_kernel, dim3(bx, g.ny), "inlet_velocity");
-        else if (p.inlet_BC == 2) MFLBM_BC(inlet_pressure_kernel, dim3(bx, g.ny), "inlet_pressure");
-        if (p.outlet_BC == 1) MFLBM_BC(outlet_convective_kernel, dim3(bx, g.ny), "outlet_convective");
-        else if (p.outlet_BC == 2) MFLBM_BC(outlet_pressure_kernel, dim3(bx, g.ny), "outlet_pressure");
+        const int in = p.inlet_BC == 1 || p.inlet_BC == 2 ? p.inlet_BC : 0;
+        const int out = p.outlet_BC == 1 || p.outlet_BC == 2 ? p.outlet_BC : 0;
+        if (in || out) {
+            if (odd) inlet_outlet_kernel<T, E, true><<<dim3(bx, g.ny), 128, 0, s>>>(a, in, out);
+            else inlet_outlet_kernel<T, E, false><<<dim3(bx, g.ny), 128, 0, s>>>(a, in, out);
+            if ((rc = after_launch("inlet_outlet")) != MFLBM_OK) return rc;
+        }
     }
     if (p.porous_plate_cmd != 0) MFLBM_BC(porous_plate_kernel, dim3(bx, g.ny), "porous_plate");
 #undef MFLBM_BC

@@ -488,19 +488,17 @@ int batch_persistent_ok(mflbm_batch* b, bool* ok, std::string* why) {
 // launches of at most 100 steps.
 int batch_run_persistent(mflbm_batch* b, int ntime_begin, int nsteps) {
     const int ns = (int)b->ctx.size(), bs = b->block;
-    std::vector<int> pre(4 * (ns + 1), 0);
+    // phase 0: collision units of bs list entries; phase 1: periodic exchange items
+    std::vector<int> pre(2 * (ns + 1), 0);
     int max_units = 1;
-    for (int ph = 0; ph < 4; ++ph) {
+    for (int ph = 0; ph < 2; ++ph) {
         for (int i = 0; i < ns; ++i) {
             const mflbm_context& c = *b->ctx[i];
             const Grid& g = c.d.g;
-            const int xu = (g.nx + bs - 1) / bs;
-            int units = 0;
-            if (ph == 0) units = (int)((c.d.n_fluid + bs - 1) / bs);
-            else if (ph == 1) units = c.params.kper ? g.ny * xu : 0;
-            else if (ph == 2) units = c.params.jper ? g.nz * xu : 0;
-            else units = (c.params.jper && c.params.kper) ? xu : 0;
-            pre[ph * (ns + 1) + i + 1] = pre[ph * (ns + 1) + i] + units;
+            const ll items = ph == 0 ? c.d.n_fluid
+                                     : (ll)(c.params.kper ? g.nx * g.ny : 0) + (c.params.jper ? g.nx * g.nz : 0) +
+                                           (c.params.jper && c.params.kper ? g.nx : 0);
+            pre[ph * (ns + 1) + i + 1] = pre[ph * (ns + 1) + i] + (int)((items + bs - 1) / bs);
         }
         max_units = std::max(max_units, pre[ph * (ns + 1) + ns]);
     }

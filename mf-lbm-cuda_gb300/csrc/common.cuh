@@ -290,7 +290,7 @@ inline Phys<T> make_phys(const mflbm_params& p) {
 // One persistent run of a batch of single-phase samples (batch.cuh).
 struct BatchLaunch {
     void* samples;               // device array of the flavour's per-sample records
-    const int* pre;              // unit prefix sums, 4 phases x (n + 1)
+    const int* pre;              // unit prefix sums, 2 phases x (n + 1)
     unsigned* bar;               // barrier words [arrivals, generation]
     int* error;                  // set when a barrier wait ran out
     unsigned long long limit_ns; // bound of one barrier wait
