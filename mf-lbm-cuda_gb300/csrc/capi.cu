@@ -56,7 +56,7 @@ void free_all(mflbm_context* c) {
                     d.walls, d.walls_type, d.s_nx, d.s_ny, d.s_nz, d.fluid_list, d.list_phi_ext,
                     d.red, d.staging, d.aux, d.type8, d.cnv4, d.zpair_off,
                     d.phi_prev, d.prof, d.dither, d.iface, d.phib, d.tmap, d.wmask, d.olist, d.slist, d.nlist, d.smask, d.gcount,
-                    d.sbcode, d.sbact, d.sblive, d.sbinfo, d.phioff};
+                    d.sbcode, d.sbact, d.sblive, d.sbinfo, d.phioff, d.phibf};
     for (void* p : ptrs) if (p) cudaFree(p);
     d = DeviceState{};
     if (c->pair_graph) cudaGraphExecDestroy(c->pair_graph);
@@ -194,6 +194,21 @@ int build_lists(mflbm_context* c) {
                 }
         ll nwm = 0;
         if ((rc = upload_list(&d.wmask, &nwm, wm)) != MFLBM_OK) return rc;
+    }
+    {
+        // fluid nodes of each phi brick (s4-local 2b, 2b + 1 per axis)
+        const int BX = (g.nx + 9) / 2, BY = (g.ny + 9) / 2, BZ = (g.nz + 9) / 2;
+        std::vector<uint8_t> fm((size_t)BX * BY * BZ, 0);
+        for (int k = 1; k <= g.nz; ++k)
+            for (int j = 1; j <= g.ny; ++j)
+                for (int i = 1; i <= g.nx; ++i)
+                    if (walls[g.s2(i, j, k)] == 0) {
+                        const int x = i + 3, y = j + 3, z = k + 3;   // s4-local
+                        fm[(x >> 1) + (size_t)BX * ((y >> 1) + (size_t)BY * (z >> 1))] |=
+                            (uint8_t)(1u << ((x & 1) | ((y & 1) << 1) | ((z & 1) << 2)));
+                    }
+        ll nfm = 0;
+        if ((rc = upload_list(&d.phibf, &nfm, fm)) != MFLBM_OK) return rc;
     }
     {
         // solid boundary nodes grouped by super-block (4 x 4 x 4 phi bricks),

@@ -65,7 +65,8 @@ struct DeviceState {
     ll n_blocks = 0;                   // node blocks of the normal pass: ((n+4)/2 + 1) per axis
     // super-blocks of the normal pass: 4 x 4 x 4 phi bricks (8^3 nodes of the s4 lattice)
     int SX = 0, SY = 0, SZ = 0;        // super-blocks per axis
-    int8_t* sbcode = nullptr;          // per super-block: the common code of its phi bricks, or 0
+    int8_t* sbcode = nullptr;          // per super-block: the fluid code of its phi bricks (gradient.cuh)
+    uint8_t* phibf = nullptr;          // per phi brick: bit e set where node e is a fluid node of [1, n]^3
     uint8_t* sbact = nullptr;          // per super-block: 1 if its phi can change at the next step (see gradient.cuh)
     uint8_t* sbslab = nullptr;         // per super-block: 1 if always processed (open or periodic faces)
     uint32_t* sblive = nullptr;        // super-blocks processed by the current pass

@@ -61,7 +61,8 @@ template <class T> struct GradArgs {
     int n_phi, n_cn, n_fluid, n_norm;
     // super-blocks (4 x 4 x 4 phi bricks)
     int SX, SY, SZ;
-    int8_t* sbcode;        // common code of the super-block's phi bricks, or 0
+    int8_t* sbcode;        // fluid code of the super-block (below)
+    const uint8_t* phibf;  // per phi brick: bit e set where node e is a fluid node of [1, n]^3
     uint8_t* sbact;        // 1: the super-block's phi may change at the next step
     uint32_t* sblive;      // super-blocks of this pass
     int* sbinfo;           // [0] number of them, [1] 1: every super-block (consumed by this pass)
@@ -136,19 +137,23 @@ __global__ void __launch_bounds__(256) extrapolate_phi_kernel(const GradArgs<T> 
 // Super-blocks.  The dense passes (phi on solid boundary nodes, phi brick
 // codes, node listing) run only over super-blocks of 4 x 4 x 4 phi bricks
 // (8^3 nodes of the s4 lattice) where phi can have changed since the last
-// pass.  Away from the interfaces phi is exactly +1 or -1 and a node keeps
-// its value exactly as long as its D3Q19 neighbourhood holds one value: the
-// absent component's populations are exactly 0 there, and collision,
-// recolouring and streaming keep them 0.  So between two passes phi can
-// change only within one node of a brick that was not uniform, or of a
-// boundary between uniform bricks of opposite sign: within the 3 x 3 x 3
-// super-blocks around a super-block flagged `sbact` (its bricks have no
-// common code, or a neighbour super-block has another code) by the previous
-// pass.  The extrapolated phi of a solid node, a brick code and a node
-// block's activity depend on phi within one node, which stays inside those
-// 27 super-blocks.  Super-blocks at open (inlet / outlet) or periodic faces,
-// whose ghost layers the boundary updates rewrite every step, are always
-// processed, and so is everything after the host set or uploaded a state.
+// pass.  Away from the interfaces phi is exactly +1 or -1 and a fluid node
+// keeps its value exactly as long as its fluid D3Q19 neighbours hold the
+// same value: the absent component's populations are exactly 0 there, and
+// collision, recolouring, streaming and bounce-back keep them 0.  A
+// super-block's fluid code is 1 (2) when all its fluid nodes hold +1 (-1),
+// 3 when it has no fluid node, 0 otherwise; the previous pass flagged it
+// (`sbact`) when its code is 0 or it holds fluid of one sign next to a
+// super-block with fluid of the other.  A fluid node whose phi can change is
+// then in a flagged super-block or one node from one.  Solid and ghost nodes
+// do not count in the codes: the phi of a solid node is extrapolated from
+// fluid nodes within two nodes, and a brick code and a node block's activity
+// depend on phi within one node, so every change lies within four nodes of a
+// flagged super-block: inside the 3 x 3 x 3 super-blocks around it, which
+// this pass processes.  Super-blocks at open (inlet / outlet) or periodic
+// faces, whose ghost layers the boundary updates rewrite every step, are
+// always processed, and so is everything after the host set or uploaded a
+// state.
 // Elsewhere phi, the brick codes and the zero records are those of the last
 // pass that processed the super-block.
 // ---------------------------------------------------------------------------
@@ -160,14 +165,18 @@ __global__ void __launch_bounds__(256) sb_live_kernel(const GradArgs<T> a) {
         const int sx = s % a.SX, sy = (s / a.SX) % a.SY, sz = s / (a.SX * a.SY);
         live = a.sbinfo[1] != 0 || (a.slab_z && (sz <= 1 || sz >= a.SZ - 2)) ||
                (a.slab_y && (sy <= 1 || sy >= a.SY - 2));
-        for (int dz = -1; dz <= 1 && !live; ++dz)
-            for (int dy = -1; dy <= 1 && !live; ++dy)
-                for (int dx = -1; dx <= 1 && !live; ++dx) {
+        unsigned any = 0;
+#pragma unroll
+        for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+            for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+                for (int dx = -1; dx <= 1; ++dx) {
                     const int x = sx + dx, y = sy + dy, z = sz + dz;
-                    if (x >= 0 && x < a.SX && y >= 0 && y < a.SY && z >= 0 && z < a.SZ &&
-                        a.sbact[x + a.SX * (y + a.SY * z)])
-                        live = true;
+                    if (x >= 0 && x < a.SX && y >= 0 && y < a.SY && z >= 0 && z < a.SZ)
+                        any |= a.sbact[x + a.SX * (y + a.SY * z)];
                 }
+        live = live || any != 0;
     }
     warp_append(live, (uint32_t)s, a.sblive, &a.sbinfo[0]);
 }
@@ -181,15 +190,20 @@ __global__ void __launch_bounds__(256) sb_active_kernel(const GradArgs<T> a) {
     if (s >= a.SX * a.SY * a.SZ) return;
     const int sx = s % a.SX, sy = (s / a.SX) % a.SY, sz = s / (a.SX * a.SY);
     const int8_t c = a.sbcode[s];
-    bool act = c == 0;
-    for (int dz = -1; dz <= 1 && !act; ++dz)
-        for (int dy = -1; dy <= 1 && !act; ++dy)
-            for (int dx = -1; dx <= 1 && !act; ++dx) {
+    unsigned seen = 0;   // bit c: code c occurs in the 3 x 3 x 3 super-blocks around
+#pragma unroll
+    for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+        for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+            for (int dx = -1; dx <= 1; ++dx) {
                 const int x = sx + dx, y = sy + dy, z = sz + dz;
-                if (x >= 0 && x < a.SX && y >= 0 && y < a.SY && z >= 0 && z < a.SZ &&
-                    a.sbcode[x + a.SX * (y + a.SY * z)] != c)
-                    act = true;
+                if (x >= 0 && x < a.SX && y >= 0 && y < a.SY && z >= 0 && z < a.SZ)
+                    seen |= 1u << a.sbcode[x + a.SX * (y + a.SY * z)];
             }
+    // flagged: mixed fluid nodes, or fluid of one sign next to fluid of the
+    // other (fluid neighbours lie in the same or adjacent super-blocks)
+    const bool act = c == 0 || (c != 3 && (seen & 6u) == 6u);
     a.sbact[s] = act ? 1 : 0;
 }
 
@@ -280,10 +294,11 @@ __device__ __forceinline__ void clear_records(const GradArgs<T>& a, int tid, int
 // the bricks' common code, or 0.  The threads also reset the records of the
 // previous pass's lists.
 template <class T>
-__device__ __forceinline__ int8_t phi_brick_code(const GradArgs<T>& a, int bx, int by, int bz) {
+__device__ __forceinline__ int8_t phi_brick_code(const GradArgs<T>& a, int bx, int by, int bz, unsigned fmask,
+                                                 int8_t* fcode) {
     typedef typename Vec2<T>::type P;
     const int NX = a.g.nx + 8, NY = a.g.ny + 8, NZ = a.g.nz + 8;
-    bool plus = true, minus = true;
+    bool plus = true, minus = true, fplus = true, fminus = true;
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
         const int y = 2 * by + (e & 1), z = 2 * bz + (e >> 1);
@@ -300,13 +315,16 @@ __device__ __forceinline__ int8_t phi_brick_code(const GradArgs<T>& a, int bx, i
         }
         plus = plus && v0 == T(1) && v1 == T(1);
         minus = minus && v0 == T(-1) && v1 == T(-1);
+        const bool f0 = (fmask >> (2 * e)) & 1u, f1 = (fmask >> (2 * e + 1)) & 1u;
+        fplus = fplus && (!f0 || v0 == T(1)) && (!f1 || v1 == T(1));
+        fminus = fminus && (!f0 || v0 == T(-1)) && (!f1 || v1 == T(-1));
     }
+    *fcode = fmask == 0 ? 3 : fplus ? 1 : fminus ? 2 : 0;
     return plus ? 1 : minus ? 2 : 0;
 }
 
 template <class T>
 __global__ void __launch_bounds__(64) phi_brick_kernel(const GradArgs<T> a) {
-    __shared__ int ref;
     clear_records<T>(a, (int)(blockIdx.x * blockDim.x + threadIdx.x), (int)(gridDim.x * blockDim.x));
     const int BX = (a.g.nx + 9) >> 1, BY = (a.g.ny + 9) >> 1, BZ = (a.g.nz + 9) >> 1;
     const int nl = a.sbinfo[0];
@@ -315,16 +333,16 @@ __global__ void __launch_bounds__(64) phi_brick_kernel(const GradArgs<T> a) {
         const int sb = (int)a.sblive[w];
         const int bx = 4 * (sb % a.SX) + lx, by = 4 * ((sb / a.SX) % a.SY) + ly, bz = 4 * (sb / (a.SX * a.SY)) + lz;
         const bool in = bx < BX && by < BY && bz < BZ;
-        int8_t code = 0;
+        int8_t fcode = 3;   // no fluid node
         if (in) {
-            code = phi_brick_code<T>(a, bx, by, bz);
-            a.phib[bx + (ll)BX * (by + (ll)BY * bz)] = code;
+            const ll b = bx + (ll)BX * (by + (ll)BY * bz);
+            a.phib[b] = phi_brick_code<T>(a, bx, by, bz, a.phibf[b], &fcode);
         }
-        if (threadIdx.x == 0) ref = code;   // brick (4 sx, 4 sy, 4 sz) always exists
-        __syncthreads();
-        const int same = __syncthreads_and(!in || code == ref);
-        if (threadIdx.x == 0) a.sbcode[sb] = same ? (int8_t)ref : 0;
-        __syncthreads();
+        // the super-block's fluid code: 0 if a brick has 0 or both signs occur
+        const int any0 = __syncthreads_or(fcode == 0);
+        const int any1 = __syncthreads_or(fcode == 1);
+        const int any2 = __syncthreads_or(fcode == 2);
+        if (threadIdx.x == 0) a.sbcode[sb] = (any0 || (any1 && any2)) ? 0 : any1 ? 1 : any2 ? 2 : 3;
     }
 }
 
@@ -603,7 +621,7 @@ GradArgs<T> grad_args(const mflbm_context& c) {
     a.l_fluid = d.fluid_list; a.n_fluid = (int)d.n_fluid;
     a.n_norm = (int)d.n_norm;
     a.SX = d.SX; a.SY = d.SY; a.SZ = d.SZ;
-    a.sbcode = d.sbcode; a.sbact = d.sbact; a.sblive = (uint32_t*)d.sblive; a.sbinfo = d.sbinfo;
+    a.sbcode = d.sbcode; a.sbact = d.sbact; a.phibf = d.phibf; a.sblive = (uint32_t*)d.sblive; a.sbinfo = d.sbinfo;
     a.phioff = d.phioff;
     const mflbm_params& p = c.params;
     a.slab_z = p.kper || (p.domain_wall_status_z_min == 0 && p.domain_wall_status_z_max == 0);
@@ -633,7 +651,7 @@ int launch_gradient(mflbm_context& c) {
     const int nsb = a.SX * a.SY * a.SZ;
     // this pass's super-blocks
     MFLBM_CUDA(cudaMemsetAsync(c.d.sbinfo, 0, sizeof(int), s));
-    sb_live_kernel<T><<<grid_for(nsb, 256), 256, 0, s>>>(a);
+    sb_live_kernel<T><<<grid_for(nsb, 64), 64, 0, s>>>(a);
     if ((rc = after_launch("sb_live")) != MFLBM_OK) return rc;
     if (a.n_phi) {
         extrapolate_phi_kernel<T><<<wave((const void*)extrapolate_phi_kernel<T>, tn.extrapolate), tn.extrapolate, 0, s>>>(a);
@@ -644,7 +662,7 @@ int launch_gradient(mflbm_context& c) {
         phi_brick_kernel<T><<<wave((const void*)phi_brick_kernel<T>, 64), 64, 0, s>>>(a);
         if ((rc = after_launch("phi_brick")) != MFLBM_OK) return rc;
     }
-    sb_active_kernel<T><<<grid_for(nsb, 256), 256, 0, s>>>(a);
+    sb_active_kernel<T><<<grid_for(nsb, 64), 64, 0, s>>>(a);
     if ((rc = after_launch("sb_active")) != MFLBM_OK) return rc;
     if (a.n_norm) {
         MFLBM_CUDA(cudaMemsetAsync(c.d.gcount, 0, 3 * sizeof(int), s));

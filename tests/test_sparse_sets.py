@@ -108,27 +108,51 @@ def test_skipped_nodes_have_uniform_stencils(n, sharp):
 
 
 # ---------------------------------------------------------------------------
-# Super-blocks (gradient.cuh: sb_live_kernel, sb_active_kernel): 4 x 4 x 4
-# phi bricks.  A pass processes only the super-blocks within one super-block
-# of those flagged by the previous pass (no common code among their bricks,
-# or a neighbour super-block with another code).  Restated here: between two
-# passes phi may change only within one node (D3Q19 neighbourhood) of a node
-# whose neighbourhood is not of one value; then every brick whose code can
-# change and every node block whose activity can change lies in a processed
-# super-block.
+# Super-blocks (gradient.cuh: phi_brick_kernel, sb_active_kernel,
+# sb_live_kernel): 4 x 4 x 4 phi bricks.  A super-block's fluid code is 1 (2)
+# when every fluid node in it holds +1 (-1), 3 when it has no fluid node, 0
+# otherwise; it is flagged when its code is 0 or it holds fluid of one sign
+# next to a super-block with fluid of the other.  A pass processes the
+# super-blocks within one super-block of those flagged by the previous pass.
+#
+# Restated here: between two passes the phi of a fluid node may change only
+# where the node or one of its fluid D3Q19 neighbours holds another value
+# (populations arrive from fluid neighbours or bounce back); a solid node's
+# phi only where it is extrapolated from fluid nodes that changed (within two
+# nodes); ghost nodes of walled faces never.  Then every changed node, every
+# brick whose code can change and every node block whose activity can change
+# lies in a processed super-block, while static non-uniform phi in solid and
+# ghost nodes flags nothing.
 # ---------------------------------------------------------------------------
-def super_codes(codes):
-    BZ, BY, BX = codes.shape
+def brick_fluid_codes(phi4, fluid4):
+    """Per 2x2x2 brick: 1 / 2 when its fluid nodes are all +1 / -1, 3 without
+    fluid nodes, 0 otherwise (phi_brick_code)."""
+    NZ, NY, NX = phi4.shape
+    BZ, BY, BX = (NZ + 1) // 2, (NY + 1) // 2, (NX + 1) // 2
+    pv = np.zeros((2 * BZ, 2 * BY, 2 * BX))
+    pf = np.zeros((2 * BZ, 2 * BY, 2 * BX), dtype=bool)
+    pv[:NZ, :NY, :NX] = phi4
+    pf[:NZ, :NY, :NX] = fluid4
+    v = pv.reshape(BZ, 2, BY, 2, BX, 2)
+    f = pf.reshape(BZ, 2, BY, 2, BX, 2)
+    anyf = f.any(axis=(1, 3, 5))
+    plus = np.all(~f | (v == 1.0), axis=(1, 3, 5))
+    minus = np.all(~f | (v == -1.0), axis=(1, 3, 5))
+    return np.where(~anyf, 3, np.where(plus, 1, np.where(minus, 2, 0))).astype(np.int8)
+
+
+def super_codes(fcodes):
+    BZ, BY, BX = fcodes.shape
     SZ, SY, SX = (BZ + 3) // 4, (BY + 3) // 4, (BX + 3) // 4
-    pad = np.full((4 * SZ, 4 * SY, 4 * SX), -1, dtype=np.int16)
-    pad[:BZ, :BY, :BX] = codes
+    pad = np.full((4 * SZ, 4 * SY, 4 * SX), 3, dtype=np.int8)   # bricks past the grid: no fluid
+    pad[:BZ, :BY, :BX] = fcodes
     b = pad.reshape(SZ, 4, SY, 4, SX, 4)
-    first = b[:, 0, :, 0, :, 0]
-    same = np.all((b == first[:, None, :, None, :, None]) | (b == -1), axis=(1, 3, 5))
-    return np.where(same, first, 0)
+    any0, any1, any2 = ((b == c).any(axis=(1, 3, 5)) for c in (0, 1, 2))
+    return np.where(any0 | (any1 & any2), 0, np.where(any1, 1, np.where(any2, 2, 3))).astype(np.int8)
 
 
-def dilate(mask):
+def neighbourhood(mask):
+    """OR of mask over the 3 x 3 x 3 super-blocks around each (no wrap)."""
     out = mask.copy()
     SZ, SY, SX = mask.shape
     for dz in (-1, 0, 1):
@@ -140,51 +164,85 @@ def dilate(mask):
 
 
 def flagged(sc):
-    act = sc == 0
-    SZ, SY, SX = sc.shape
-    for dz in (-1, 0, 1):
-        for dy in (-1, 0, 1):
-            for dx in (-1, 0, 1):
-                a = sc[max(0, -dz):SZ - max(0, dz), max(0, -dy):SY - max(0, dy), max(0, -dx):SX - max(0, dx)]
-                b = sc[max(0, dz):SZ - max(0, -dz), max(0, dy):SY - max(0, -dy), max(0, dx):SX - max(0, -dx)]
-                act[max(0, dz):SZ - max(0, -dz), max(0, dy):SY - max(0, -dy), max(0, dx):SX - max(0, -dx)] |= a != b
-    return act
+    both = neighbourhood(sc == 1) & neighbourhood(sc == 2)
+    return (sc == 0) | ((sc != 3) & both)
 
 
-@pytest.mark.parametrize("n", [(40, 40, 56), (33, 29, 47)])
+def shifted(a, q):
+    """a at x + e_q, edge values repeated past the array (no wrap)."""
+    p = np.pad(a, 1, mode="edge")
+    return p[1 + EZ[q]:1 + EZ[q] + a.shape[0], 1 + EY[q]:1 + EY[q] + a.shape[1], 1 + EX[q]:1 + EX[q] + a.shape[2]]
+
+
+def near(mask, hops):
+    out = mask.copy()
+    for _ in range(hops):
+        m = out.copy()
+        for q in range(1, 19):
+            m |= shifted(out, q)
+        out = m
+    return out
+
+
+def porous_fluid(n, seed):
+    """Fluid nodes of [1, n]^3 on the s4 lattice, solid balls removed."""
+    nx, ny, nz = n
+    rng = np.random.default_rng(seed)
+    z, y, x = np.meshgrid(np.arange(nz + 8) - 3, np.arange(ny + 8) - 3, np.arange(nx + 8) - 3, indexing="ij")
+    inside = (x >= 1) & (x <= nx) & (y >= 1) & (y <= ny) & (z >= 1) & (z <= nz)
+    solid = np.zeros(x.shape, dtype=bool)
+    for _ in range(6):
+        c = rng.uniform(0, [nx, ny, nz])
+        solid |= (x - c[0]) ** 2 + (y - c[1]) ** 2 + (z - c[2]) ** 2 < rng.uniform(2, 6) ** 2
+    return inside & ~solid
+
+
+@pytest.mark.parametrize("n", [(40, 40, 56), (33, 29, 47), (64, 48, 40)])
 @pytest.mark.parametrize("sharp", [False, True], ids=["diffuse", "sharp"])
 def test_super_blocks_cover_every_change(n, sharp):
     nx, ny, nz = n
-    phi = random_phase(n, seed=7 * nx + nz, sharp=sharp)
     rng = np.random.default_rng(nx)
+    fluid = porous_fluid(n, seed=3 * nx + ny)
+    phi = random_phase(n, seed=7 * nx + nz, sharp=sharp)
+    # solid nodes: values extrapolated from fluid (arbitrary here); ghost
+    # layers of walled faces: 0
+    solid = ~fluid
+    inside = np.zeros_like(fluid)
+    inside[4:4 + nz, 4:4 + ny, 4:4 + nx] = True
+    phi[solid & inside] = rng.uniform(-1, 1, size=int((solid & inside).sum()))
+    phi[~inside] = 0.0
 
-    def shifted(a, q):
-        """a at x + e_q, edge values repeated past the array (no wrap)."""
-        p = np.pad(a, 1, mode="edge")
-        return p[1 + EZ[q]:1 + EZ[q] + a.shape[0], 1 + EY[q]:1 + EY[q] + a.shape[1], 1 + EX[q]:1 + EX[q] + a.shape[2]]
-
-    # nodes whose D3Q19 neighbourhood (on the s4 array) is not of one value
-    nonuni = np.zeros(phi.shape, dtype=bool)
+    # fluid nodes that may change: the node or a fluid neighbour holds another value
+    may = fluid & ~np.isin(phi, (1.0, -1.0))
     for q in range(1, 19):
-        nonuni |= shifted(phi, q) != phi
-    # phi may change within one node of them: perturb a random subset there
-    near = nonuni.copy()
-    for q in range(1, 19):
-        near |= shifted(nonuni, q)
+        may |= fluid & shifted(fluid, q) & (shifted(phi, q) != phi)
     new = phi.copy()
-    pick = near & (rng.random(phi.shape) < 0.5)
+    pick = may & (rng.random(phi.shape) < 0.5)
     new[pick] = rng.uniform(-1, 1, size=int(pick.sum()))
+    # solid nodes extrapolating from changed fluid nodes
+    ext = solid & inside & near(new != phi, 2) & (rng.random(phi.shape) < 0.5)
+    new[ext] = rng.uniform(-1, 1, size=int(ext.sum()))
+
+    sc = super_codes(brick_fluid_codes(phi, fluid))
+    flag = flagged(sc)
+    live = neighbourhood(flag)
+    # changed fluid nodes lie in flagged super-blocks or one node from one
+    NZ, NY, NX = phi.shape
+    fnode = np.repeat(np.repeat(np.repeat(flag, 8, 0), 8, 1), 8, 2)[:NZ, :NY, :NX]
+    for k, j, i in np.argwhere((new != phi) & fluid & ~near(fnode, 1)):
+        raise AssertionError(("fluid node", k, j, i))
+    # every changed node, brick code and block activity in a processed super-block
+    for k, j, i in np.argwhere(new != phi):
+        assert live[(k // 2) // 4, (j // 2) // 4, (i // 2) // 4], ("node", k, j, i)
     codes_old, codes_new = brick_codes(phi), brick_codes(new)
-    live = dilate(flagged(super_codes(codes_old)))
-    BZ, BY, BX = codes_old.shape
     changed = np.argwhere(codes_old != codes_new)
     for bz, by, bx in changed:
         assert live[bz // 4, by // 4, bx // 4], ("brick", bz, by, bx)
     act_old, act_new = active_blocks(codes_old, n), active_blocks(codes_new, n)
     for cz, cy, cx in np.argwhere(act_old != act_new):
         assert live[cz // 4, cy // 4, cx // 4], ("block", cz, cy, cx)
-    # changed nodes (and so the solid nodes extrapolating from them) lie in
-    # processed super-blocks or next to one
-    for k, j, i in np.argwhere(new != phi):
-        assert live[(k // 2) // 4, (j // 2) // 4, (i // 2) // 4], ("node", k, j, i)
     assert len(changed) > 0
+    # the static non-uniform solid and ghost phi does not keep every
+    # super-block live (it would, counted over all nodes)
+    all_nodes = super_codes(np.where(codes_old == 0, 0, codes_old))
+    assert neighbourhood(flagged(all_nodes)).sum() > live.sum()
