@@ -240,7 +240,7 @@ def late_state(ctx, nt, n_all, n_fluid, target=10001, timed=200):
     nt += timed
     st = ctx.interface_stats()
     return nt, {"value": round(n_all * timed / (ms * 1e-3) / 1e6, 2), "unit": "MLUPS", "after_steps": nt - 1,
-                "ms_per_step": round(ms / timed, 5), "gradient_sets": st,
+                "ms_per_step": round(ms / timed, 5), "gradient_sets": st, "super_blocks": ctx.super_block_stats(),
                 "interface_fraction": round(st["interface_nodes"] / n_fluid, 5)}
 
 
@@ -279,9 +279,10 @@ def interface_rich(case, geo, timed=200, settle=20, seed=1206):
     stream = torch.cuda.ExternalStream(c.stream())
     ms = _timed_run(lambda: c.run(1 + settle, timed), c.sync, stream)
     st = c.interface_stats()
+    sb = c.super_block_stats()
     c.close()
     return {"value": round(n_all * timed / (ms * 1e-3) / 1e6, 2), "unit": "MLUPS", "ms_per_step": round(ms / timed, 5),
-            "after_steps": settle + timed, "gradient_sets": st,
+            "after_steps": settle + timed, "gradient_sets": st, "super_blocks": sb,
             "interface_fraction": round(st["interface_nodes"] / n_fluid, 5),
             "how": "random phi = +-1 per node (seeded), rest state, uploaded through mflbm_upload_fields"}
 
@@ -495,6 +496,7 @@ def main():
     assert np.isfinite(out["phi"]).all()
 
     sparse = ctx.interface_stats()
+    super_blocks = ctx.super_block_stats()
     mon = ctx.monitor(2, 2)
     extra = {}
     if not args.no_extras:
@@ -544,7 +546,7 @@ def main():
         # curvature gathers run only there (elsewhere the surface force is zero)
         # sizes of the last gradient pass's sparse sets (interface nodes, solid
         # nodes given a normal, fluid nodes whose normal was recomputed)
-        "gradient_sets": sparse,
+        "gradient_sets": sparse, "super_blocks": super_blocks,
         "interface_fraction": round(float(np.count_nonzero(
             out["c_norm"].reshape(nz + 4, ny + 4, nx + 4)[2:nz + 2, 2:ny + 2, 2:nx + 2])) / n_fluid, 5),
     }

@@ -259,6 +259,11 @@ int mflbm_synchronize(mflbm_context* ctx);
  * Synchronises the context's stream.  Any pointer may be NULL. */
 int mflbm_interface_stats(mflbm_context* ctx, long long* interface_nodes, long long* solid_normals,
                           long long* active_nodes);
+/* Super-blocks (4 x 4 x 4 bricks of 2 x 2 x 2 phi nodes) of the last
+ * gradient pass: how many it processed, how many it flagged for the next
+ * pass (phi may change within them), and the total.  Synchronises the
+ * context's stream.  No counterpart in the reference. */
+int mflbm_super_block_stats(mflbm_context* ctx, long long* processed, long long* flagged, long long* total);
 
 /* FP64 device reductions (Monitor quantities) on the current state; the
  * state must be after an even step (src/Misc.cpp:222-274 semantics).

@@ -221,6 +221,7 @@ __device__ __forceinline__ void outlet_pressure_at(const BcArgs<T, E>& a, int i,
 // together gives the reference's result of running them one after the other.
 template <class T, class E, bool AFTER_ODD>
 __global__ void inlet_outlet_kernel(const BcArgs<T, E> a, int inlet, int outlet) {
+    pdl_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1;
     if (i > a.g.nx) return;
     if (inlet == 1) inlet_velocity_at<T, E, AFTER_ODD>(a, i, j);
@@ -334,6 +335,7 @@ __device__ __forceinline__ void periodic_item(const BcArgs<T, E>& a, int jper, i
 // all periodic exchanges of a step in one launch
 template <class T, class E, bool ODD>
 __global__ void periodic_kernel(const BcArgs<T, E> a, int jper, int kper, int n) {
+    pdl_wait();
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r < n) periodic_item<T, E, ODD>(a, jper, kper, r);
 }
@@ -341,6 +343,7 @@ __global__ void periodic_kernel(const BcArgs<T, E> a, int jper, int kper, int n)
 // porous plate blocking one component at z = Zplate (:1744-1882); b = blocked component
 template <class T, class E, bool AFTER_ODD>
 __global__ void porous_plate_kernel(const BcArgs<T, E> a) {
+    pdl_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1;
     if (i > a.g.nx) return;
     const Grid& g = a.g;
@@ -421,29 +424,24 @@ int launch_boundaries(mflbm_context& c, bool odd) {
     cudaStream_t s = c.stream;
     const unsigned bx = grid_for(g.nx, 128);
     int rc;
-#define MFLBM_BC(kernel, gridv, name)                                             \
-    do {                                                                          \
-        if (odd) kernel<T, E, true><<<gridv, 128, 0, s>>>(a);                     \
-        else kernel<T, E, false><<<gridv, 128, 0, s>>>(a);                        \
-        if ((rc = after_launch(name)) != MFLBM_OK) return rc;                     \
-    } while (0)
     if (p.jper || p.kper) {
         const int n = periodic_items(g, p.jper, p.kper);
-        if (odd) periodic_kernel<T, E, true><<<grid_for(n, 128), 128, 0, s>>>(a, p.jper, p.kper, n);
-        else periodic_kernel<T, E, false><<<grid_for(n, 128), 128, 0, s>>>(a, p.jper, p.kper, n);
-        if ((rc = after_launch("periodic")) != MFLBM_OK) return rc;
+        rc = launch_pdl("periodic", odd ? periodic_kernel<T, E, true> : periodic_kernel<T, E, false>,
+                        grid_for(n, 128), 128, s, a, p.jper, p.kper, n);
+        if (rc != MFLBM_OK) return rc;
     }
     if (p.kper == 0 && p.domain_wall_status_z_min == 0 && p.domain_wall_status_z_max == 0) {
         const int in = p.inlet_BC == 1 || p.inlet_BC == 2 ? p.inlet_BC : 0;
         const int out = p.outlet_BC == 1 || p.outlet_BC == 2 ? p.outlet_BC : 0;
         if (in || out) {
-            if (odd) inlet_outlet_kernel<T, E, true><<<dim3(bx, g.ny), 128, 0, s>>>(a, in, out);
-            else inlet_outlet_kernel<T, E, false><<<dim3(bx, g.ny), 128, 0, s>>>(a, in, out);
-            if ((rc = after_launch("inlet_outlet")) != MFLBM_OK) return rc;
+            rc = launch_pdl("inlet_outlet", odd ? inlet_outlet_kernel<T, E, true> : inlet_outlet_kernel<T, E, false>,
+                            dim3(bx, g.ny), 128, s, a, in, out);
+            if (rc != MFLBM_OK) return rc;
         }
     }
-    if (p.porous_plate_cmd != 0) MFLBM_BC(porous_plate_kernel, dim3(bx, g.ny), "porous_plate");
-#undef MFLBM_BC
+    if (p.porous_plate_cmd != 0)
+        return launch_pdl("porous_plate", odd ? porous_plate_kernel<T, E, true> : porous_plate_kernel<T, E, false>,
+                          dim3(bx, g.ny), 128, s, a);
     return MFLBM_OK;
 }
 

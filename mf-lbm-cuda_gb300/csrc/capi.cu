@@ -332,10 +332,14 @@ int capture_pair(mflbm_context* c, int first_ntime) {
         c->pair_graph = nullptr;
     }
     cudaGraph_t graph;
+    // a captured pair runs two gradient passes, so the live-count parity is
+    // back where it started after the capture; a failed capture runs nothing
+    const int parity = c->d.grad_parity;
     MFLBM_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     int rc = one_step(c, first_ntime);
     if (rc == MFLBM_OK) rc = one_step(c, first_ntime + 1);
     cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+    if (rc != MFLBM_OK || e != cudaSuccess) c->d.grad_parity = parity;
     if (rc != MFLBM_OK) { if (e == cudaSuccess) cudaGraphDestroy(graph); return rc; }
     if (e != cudaSuccess) return fail(MFLBM_E_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e));
     e = cudaGraphInstantiate(&c->pair_graph, graph, 0);
@@ -377,6 +381,8 @@ namespace {
 int capture_batch(mflbm_batch* b) {
     if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
     cudaGraph_t graph;
+    std::vector<int> parity(b->ctx.size());   // restored if the capture fails (capture_pair)
+    for (size_t i = 0; i < b->ctx.size(); ++i) parity[i] = b->ctx[i]->d.grad_parity;
     MFLBM_CUDA(cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeThreadLocal));
     int rc = MFLBM_OK;
     cudaError_t e = cudaEventRecord(b->fork, b->origin);
@@ -390,6 +396,8 @@ int capture_batch(mflbm_batch* b) {
         e = cudaStreamWaitEvent(b->origin, b->join[i], 0);
     }
     const cudaError_t e2 = cudaStreamEndCapture(b->origin, &graph);
+    if (rc != MFLBM_OK || e != cudaSuccess || e2 != cudaSuccess)
+        for (size_t i = 0; i < b->ctx.size(); ++i) b->ctx[i]->d.grad_parity = parity[i];
     if (rc != MFLBM_OK) { if (e2 == cudaSuccess) cudaGraphDestroy(graph); return rc; }
     if (e != cudaSuccess) { if (e2 == cudaSuccess) cudaGraphDestroy(graph); return fail(MFLBM_E_CUDA, std::string("batch capture: ") + cudaGetErrorString(e)); }
     if (e2 != cudaSuccess) return fail(MFLBM_E_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e2));
@@ -666,7 +674,7 @@ int mflbm_create(const mflbm_params* params, mflbm_context** out) {
         {(void**)&d.dither, 2 * sizeof(uint32_t)}, {(void**)&d.iface, (size_t)g.n2()},
         {(void**)&d.phib, (size_t)((g.nx + 9) / 2) * ((g.ny + 9) / 2) * ((g.nz + 9) / 2)},
         {(void**)&d.sbcode, nsb}, {(void**)&d.sbact, nsb}, {(void**)&d.sblive, sizeof(uint32_t) * nsb},
-        {(void**)&d.sbinfo, 2 * sizeof(int)}};
+        {(void**)&d.sbinfo, 4 * sizeof(int)}};
     for (auto& a : allocs) {
         if ((rc = alloc_zero(a.p, a.bytes, c->stream)) != MFLBM_OK) {
             free_all(c);
@@ -925,6 +933,27 @@ int mflbm_interface_stats(mflbm_context* c, long long* interface_nodes, long lon
     if (interface_nodes) *interface_nodes = h[0];
     if (solid_normals) *solid_normals = h[1];
     if (active_nodes) *active_nodes = h[2];
+    return MFLBM_OK;
+}
+
+int mflbm_super_block_stats(mflbm_context* c, long long* processed, long long* flagged, long long* total) {
+    int rc = require_ready(c);
+    if (rc != MFLBM_OK) return rc;
+    const DeviceState& d = c->d;
+    const size_t nsb = (size_t)d.SX * d.SY * d.SZ;
+    int live[4] = {0, 0, 0, 0};
+    std::vector<uint8_t> act(nsb);
+    MFLBM_CUDA(cudaMemcpyAsync(live, d.sbinfo, sizeof(live), cudaMemcpyDeviceToHost, c->stream));
+    MFLBM_CUDA(cudaMemcpyAsync(act.data(), d.sbact, nsb, cudaMemcpyDeviceToHost, c->stream));
+    MFLBM_CUDA(cudaStreamSynchronize(c->stream));
+    // the last pass counted into the slot the next pass does not use
+    if (processed) *processed = live[d.grad_parity ? 0 : 2];
+    if (flagged) {
+        long long n = 0;
+        for (uint8_t v : act) n += v != 0;
+        *flagged = n;
+    }
+    if (total) *total = (long long)nsb;
     return MFLBM_OK;
 }
 

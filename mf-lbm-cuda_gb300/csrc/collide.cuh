@@ -259,6 +259,7 @@ __device__ __forceinline__ void collide_node(const CollideArgs<T, E>& a, int t) 
 
 template <class T, class E, bool ODD, class I>
 __global__ void __launch_bounds__(256) __maxnreg__((collide_max_regs<E, ODD>())) collide_stream_kernel(const CollideArgs<T, E> a) {
+    pdl_wait();
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t < a.n) collide_node<T, E, ODD, I>(a, t);
 }
@@ -292,14 +293,13 @@ int launch_collide(mflbm_context& c, bool odd) {
     const int bs = d.tune.collide;
     const bool narrow = d.b.pairs() < (1ll << 32);   // 32-bit pair indices suffice
     const unsigned grid = grid_for(a.n, bs);
-    if (narrow) {
-        if (odd) collide_stream_kernel<T, E, true, uint32_t><<<grid, bs, 0, c.stream>>>(a);
-        else collide_stream_kernel<T, E, false, uint32_t><<<grid, bs, 0, c.stream>>>(a);
-    } else {
-        if (odd) collide_stream_kernel<T, E, true, unsigned long long><<<grid, bs, 0, c.stream>>>(a);
-        else collide_stream_kernel<T, E, false, unsigned long long><<<grid, bs, 0, c.stream>>>(a);
-    }
-    return after_launch("collide_stream");
+    if (narrow)
+        return launch_pdl("collide_stream", odd ? collide_stream_kernel<T, E, true, uint32_t>
+                                                : collide_stream_kernel<T, E, false, uint32_t>,
+                          grid, bs, c.stream, a);
+    return launch_pdl("collide_stream", odd ? collide_stream_kernel<T, E, true, unsigned long long>
+                                            : collide_stream_kernel<T, E, false, unsigned long long>,
+                      grid, bs, c.stream, a);
 }
 
 }  // namespace MFLBM_NS

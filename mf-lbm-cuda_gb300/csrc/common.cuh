@@ -242,6 +242,37 @@ inline int after_launch(const char* what) {
 
 inline unsigned grid_for(ll n, int block) { return (unsigned)((n + block - 1) / block); }
 
+// Programmatic dependent launch for the kernels of a time step.  A kernel
+// launched by launch_pdl may be scheduled while the previous kernel of the
+// stream is still running (its blocks are placed as the previous kernel's
+// blocks retire, hiding the launch latency between the short dependent
+// passes); it must call pdl_wait() before its first global memory access.
+// pdl_wait returns once the previous kernel has completed and its writes are
+// visible (griddepcontrol.wait; a no-op for a plain launch), then allows the
+// next kernel to be scheduled.
+__device__ __forceinline__ void pdl_wait() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <class... KArgs, class... Args>
+inline int launch_pdl(const char* what, void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t s,
+                      Args... args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, kernel, args...);
+    if (e != cudaSuccess) return fail(MFLBM_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    return after_launch(what);
+}
+
 }  // namespace mflbm
 
 namespace mflbm {

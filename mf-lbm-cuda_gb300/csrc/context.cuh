@@ -70,7 +70,8 @@ struct DeviceState {
     uint8_t* sbact = nullptr;          // per super-block: 1 if its phi can change at the next step (see gradient.cuh)
     uint8_t* sbslab = nullptr;         // per super-block: 1 if always processed (open or periodic faces)
     uint32_t* sblive = nullptr;        // super-blocks processed by the current pass
-    int* sbinfo = nullptr;             // [0] live count, [1] 1: process every super-block at the next pass
+    int* sbinfo = nullptr;             // [0], [2] live counts of alternate passes; [1] 1: process every super-block at the next pass
+    int grad_parity = 0;               // which live count the next gradient pass uses (launch_gradient)
     int* phioff = nullptr;             // offsets of each super-block's nodes in list_phi_ext
     int n_sm = 0;                      // multiprocessors of the device (grids of the list passes)
 };

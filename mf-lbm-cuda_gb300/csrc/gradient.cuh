@@ -65,7 +65,9 @@ template <class T> struct GradArgs {
     const uint8_t* phibf;  // per phi brick: bit e set where node e is a fluid node of [1, n]^3
     uint8_t* sbact;        // 1: the super-block's phi may change at the next step
     uint32_t* sblive;      // super-blocks of this pass
-    int* sbinfo;           // [0] number of them, [1] 1: every super-block (consumed by this pass)
+    int* sbinfo;           // [1] 1: every super-block (consumed by this pass)
+    int* live_n;           // number of super-blocks of this pass (sbinfo[0] or [2], alternating)
+    int* live_next;        // the next pass's count, zeroed by this pass
     const int* phioff;     // list_phi_ext offsets of each super-block
     int slab_z, slab_y;    // 1: the two super-block rows at each z (y) face are always processed
     Phys<T> ph;
@@ -73,9 +75,12 @@ template <class T> struct GradArgs {
 
 template <class T> __device__ __forceinline__ T wq_of(const ModelConsts<T>& c, int q) { return q < 7 ? c.w1 : c.w2; }
 
-// Append `value` to `list` where `want` is set: one atomic per warp, the
-// order within the list is arbitrary.
-__device__ __forceinline__ void warp_append(bool want, uint32_t value, uint32_t* list, int* count) {
+// Append `value` to `list` (capacity `cap`) where `want` is set: one atomic
+// per warp, the order within the list is arbitrary.  Every list is sized for
+// the most entries a pass can produce; the capacity checks here and the
+// clamped lengths of the readers keep every access inside the buffers even
+// if a count were not reset.
+__device__ __forceinline__ void warp_append(bool want, uint32_t value, uint32_t* list, int* count, int cap) {
     const unsigned act = __activemask();
     const unsigned m = __ballot_sync(act, want);
     if (!m) return;
@@ -83,7 +88,8 @@ __device__ __forceinline__ void warp_append(bool want, uint32_t value, uint32_t*
     int base = 0;
     if (lane == leader) base = atomicAdd(count, __popc(m));
     base = __shfl_sync(act, base, leader);
-    if (want) list[base + __popc(m & ((1u << lane) - 1u))] = value;
+    const int idx = base + __popc(m & ((1u << lane) - 1u));
+    if (want && idx < cap) list[idx] = value;
 }
 
 // Reserve `cnt` consecutive slots of a list per thread (warp prefix sum, one
@@ -126,7 +132,8 @@ __device__ __forceinline__ void extrapolate_phi_at(const GradArgs<T>& a, int t) 
 // the solid boundary nodes of this pass's super-blocks (one block per super-block)
 template <class T>
 __global__ void __launch_bounds__(256) extrapolate_phi_kernel(const GradArgs<T> a) {
-    const int nl = a.sbinfo[0];
+    pdl_wait();
+    const int nl = min(*a.live_n, a.SX * a.SY * a.SZ);
     for (int w = blockIdx.x; w < nl; w += gridDim.x) {
         const uint32_t sb = a.sblive[w];
         for (int t = a.phioff[sb] + threadIdx.x; t < a.phioff[sb + 1]; t += blockDim.x) extrapolate_phi_at<T>(a, t);
@@ -159,6 +166,7 @@ __global__ void __launch_bounds__(256) extrapolate_phi_kernel(const GradArgs<T> 
 // ---------------------------------------------------------------------------
 template <class T>
 __global__ void __launch_bounds__(256) sb_live_kernel(const GradArgs<T> a) {
+    pdl_wait();
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     bool live = false;
     if (s < a.SX * a.SY * a.SZ) {
@@ -178,15 +186,21 @@ __global__ void __launch_bounds__(256) sb_live_kernel(const GradArgs<T> a) {
                 }
         live = live || any != 0;
     }
-    warp_append(live, (uint32_t)s, a.sblive, &a.sbinfo[0]);
+    if (s == 0) *a.live_next = 0;
+    warp_append(live, (uint32_t)s, a.sblive, a.live_n, a.SX * a.SY * a.SZ);
 }
 
 // sbact of every super-block from this pass's codes; consumes the
-// every-super-block request
+// every-super-block request, and restarts the node lists (the brick-code
+// pass has reset the previous lists' records)
 template <class T>
 __global__ void __launch_bounds__(256) sb_active_kernel(const GradArgs<T> a) {
+    pdl_wait();
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s == 0) a.sbinfo[1] = 0;
+    if (s == 0) {
+        a.sbinfo[1] = 0;
+        if (a.n_norm) a.gcount[0] = a.gcount[1] = a.gcount[2] = 0;
+    }
     if (s >= a.SX * a.SY * a.SZ) return;
     const int sx = s % a.SX, sy = (s / a.SX) % a.SY, sz = s / (a.SX * a.SY);
     const int8_t c = a.sbcode[s];
@@ -271,7 +285,7 @@ __device__ __forceinline__ T iso4_dz(const ModelConsts<T>& c, const T* F, int n,
 // Grid-stride over both lists, run by the threads of the brick pass.
 template <class T>
 __device__ __forceinline__ void clear_records(const GradArgs<T>& a, int tid, int nthreads) {
-    const int no = a.gcount[0], ns = a.gcount[1];
+    const int no = min(a.gcount[0], a.n_norm), ns = min(a.gcount[1], a.n_cn);
     typename Vec4<T>::type z;
     z.x = T(0); z.y = T(0); z.z = T(0); z.w = T(0);
     for (int p = tid; p < no + ns; p += nthreads) {
@@ -325,9 +339,10 @@ __device__ __forceinline__ int8_t phi_brick_code(const GradArgs<T>& a, int bx, i
 
 template <class T>
 __global__ void __launch_bounds__(64) phi_brick_kernel(const GradArgs<T> a) {
+    pdl_wait();
     clear_records<T>(a, (int)(blockIdx.x * blockDim.x + threadIdx.x), (int)(gridDim.x * blockDim.x));
     const int BX = (a.g.nx + 9) >> 1, BY = (a.g.ny + 9) >> 1, BZ = (a.g.nz + 9) >> 1;
-    const int nl = a.sbinfo[0];
+    const int nl = min(*a.live_n, a.SX * a.SY * a.SZ);
     const int lx = threadIdx.x & 3, ly = (threadIdx.x >> 2) & 3, lz = threadIdx.x >> 4;
     for (int w = blockIdx.x; w < nl; w += gridDim.x) {
         const int sb = (int)a.sblive[w];
@@ -380,10 +395,11 @@ __device__ __forceinline__ bool normal_at(const GradArgs<T>& a, int i, int j, in
 // block belongs to the super-block of its brick c).
 template <class T>
 __global__ void __launch_bounds__(64) active_nodes_kernel(const GradArgs<T> a) {
+    pdl_wait();
     const Grid& g = a.g;
     const int BX = (g.nx + 9) >> 1, BY = (g.ny + 9) >> 1;
     const int CX = ((g.nx + 4) >> 1) + 1, CY = ((g.ny + 4) >> 1) + 1, CZ = ((g.nz + 4) >> 1) + 1;
-    const int nl = a.sbinfo[0];
+    const int nl = min(*a.live_n, a.SX * a.SY * a.SZ);
     const int lx = threadIdx.x & 3, ly = (threadIdx.x >> 2) & 3, lz = threadIdx.x >> 4;
     for (int w = blockIdx.x; w < nl; w += gridDim.x) {
         const int sb = (int)a.sblive[w];
@@ -406,8 +422,11 @@ __global__ void __launch_bounds__(64) active_nodes_kernel(const GradArgs<T> a) {
         }
         int base = warp_reserve(__popc(sel), &a.gcount[2]);
         for (int e = 0; e < 8; ++e)
-            if (sel & (1u << e))
-                a.nlist[base++] = pack_xyz(2 * cx - 2 + (e & 1), 2 * cy - 2 + ((e >> 1) & 1), 2 * cz - 2 + (e >> 2));
+            if (sel & (1u << e)) {
+                if (base < a.n_norm)
+                    a.nlist[base] = pack_xyz(2 * cx - 2 + (e & 1), 2 * cy - 2 + ((e >> 1) & 1), 2 * cz - 2 + (e >> 2));
+                ++base;
+            }
     }
 }
 
@@ -422,8 +441,9 @@ __global__ void __launch_bounds__(64) active_nodes_kernel(const GradArgs<T> a) {
 // (gradient pipeline 0.175 -> 0.170 ms at 256^3).
 template <class T>
 __global__ void __launch_bounds__(256, 8) normals_kernel(const GradArgs<T> a) {
+    pdl_wait();
     const Grid& g = a.g;
-    const int nt = a.gcount[2];
+    const int nt = min(a.gcount[2], a.n_norm);
     const int sy2 = g.nx + 4, sz2 = (g.nx + 4) * (g.ny + 4);
     const int iters = (nt + gridDim.x * blockDim.x - 1) / (gridDim.x * blockDim.x);
     for (int it = 0; it < iters; ++it) {
@@ -437,7 +457,7 @@ __global__ void __launch_bounds__(256, 8) normals_kernel(const GradArgs<T> a) {
             cand = a.wmask[g.s2(i, j, k)];
             on = normal_at<T>(a, i, j, k, a.type8[g.s4(i, j, k)]);
         }
-        warp_append(on, packed, a.olist, &a.gcount[0]);
+        warp_append(on, packed, a.olist, &a.gcount[0], a.n_norm);
         // most solid nodes are claimed by several neighbours: a plain read
         // skips the atomic once the bit is visible
         const ll n2 = g.s2(i, j, k);
@@ -454,7 +474,10 @@ __global__ void __launch_bounds__(256, 8) normals_kernel(const GradArgs<T> a) {
         int at = warp_reserve(__popc(mine), &a.gcount[1]);
 #pragma unroll
         for (int q = 1; q < 19; ++q)
-            if (mine & (1u << q)) a.slist[at++] = pack_xyz(i + ex(q), j + ey(q), k + ez(q));
+            if (mine & (1u << q)) {
+                if (at < a.n_cn) a.slist[at] = pack_xyz(i + ex(q), j + ey(q), k + ez(q));
+                ++at;
+            }
     }
 }
 
@@ -463,8 +486,9 @@ __global__ void __launch_bounds__(256, 8) normals_kernel(const GradArgs<T> a) {
 // |grad phi| of a solid node stays 0.
 template <class T>
 __global__ void __launch_bounds__(256) extrapolate_normal_kernel(const GradArgs<T> a) {
+    pdl_wait();
     const Grid& g = a.g;
-    const int ns = a.gcount[1];
+    const int ns = min(a.gcount[1], a.n_cn);
     const int sy = g.nx + 4, sz = (g.nx + 4) * (g.ny + 4);
     const int sy4 = g.nx + 8, sz4 = (g.nx + 8) * (g.ny + 8);
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < ns; p += gridDim.x * blockDim.x) {
@@ -524,9 +548,10 @@ __device__ __forceinline__ T curvature_at(const ModelConsts<T>& c, const typenam
 // Grid-stride loop over the list (its length is on the device).
 template <class T>
 __global__ void __launch_bounds__(256) curvature_kernel(const GradArgs<T> a) {
+    pdl_wait();
     const Grid& g = a.g;
     const int sy = g.nx + 4, sz = (g.nx + 4) * (g.ny + 4);
-    const int n = a.gcount[0];
+    const int n = min(a.gcount[0], a.n_norm);
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         int i, j, k;
         unpack_xyz(a.olist[p], i, j, k);
@@ -583,7 +608,10 @@ __global__ void __launch_bounds__(128) pack_normals_kernel(const GradArgs<T> a) 
     // Solid records are zero here: slist and its mask start empty.
     const bool nz = v.x != T(0) || v.y != T(0) || v.z != T(0) || v.w != T(0);
     a.iface[n] = nz ? 1 : 0;
-    if (nz) a.olist[atomicAdd(&a.gcount[0], 1)] = pack_xyz(i, j, k);
+    if (nz) {
+        const int at = atomicAdd(&a.gcount[0], 1);
+        if (at < a.n_norm) a.olist[at] = pack_xyz(i, j, k);
+    }
 }
 template <class T>
 __global__ void __launch_bounds__(128) aux_from_arrays_kernel(const GradArgs<T> a) {
@@ -622,6 +650,7 @@ GradArgs<T> grad_args(const mflbm_context& c) {
     a.n_norm = (int)d.n_norm;
     a.SX = d.SX; a.SY = d.SY; a.SZ = d.SZ;
     a.sbcode = d.sbcode; a.sbact = d.sbact; a.phibf = d.phibf; a.sblive = (uint32_t*)d.sblive; a.sbinfo = d.sbinfo;
+    a.live_n = a.live_next = nullptr;   // set by launch_gradient
     a.phioff = d.phioff;
     const mflbm_params& p = c.params;
     a.slab_z = p.kper || (p.domain_wall_status_z_min == 0 && p.domain_wall_status_z_max == 0);
@@ -631,10 +660,17 @@ GradArgs<T> grad_args(const mflbm_context& c) {
 }
 
 // The per-step pipeline (also the start-up colour_gradient,
-// src/Phase_gradient.cpp:15-216, which performs the same passes).
+// src/Phase_gradient.cpp:15-216, which performs the same passes).  Every
+// kernel is launched with programmatic dependent launch (launch_pdl); the
+// list counters are reset inside the kernels (the super-block count of the
+// next pass by sb_live, the node lists by sb_active), so no memset breaks
+// the chain.
 template <class T>
 int launch_gradient(mflbm_context& c) {
-    const GradArgs<T> a = grad_args<T>(c);
+    GradArgs<T> a = grad_args<T>(c);
+    a.live_n = c.d.sbinfo + (c.d.grad_parity ? 2 : 0);
+    a.live_next = c.d.sbinfo + (c.d.grad_parity ? 0 : 2);
+    c.d.grad_parity ^= 1;
     const Tuning& tn = c.d.tune;
     cudaStream_t s = c.stream;
     int rc;
@@ -646,38 +682,32 @@ int launch_gradient(mflbm_context& c) {
         int per_sm = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, bs, 0) != cudaSuccess || per_sm < 1)
             per_sm = 1;
-        return std::max(1, c.d.n_sm) * per_sm;
+        return (unsigned)(std::max(1, c.d.n_sm) * per_sm);
     };
     const int nsb = a.SX * a.SY * a.SZ;
     // this pass's super-blocks
-    MFLBM_CUDA(cudaMemsetAsync(c.d.sbinfo, 0, sizeof(int), s));
-    sb_live_kernel<T><<<grid_for(nsb, 64), 64, 0, s>>>(a);
-    if ((rc = after_launch("sb_live")) != MFLBM_OK) return rc;
-    if (a.n_phi) {
-        extrapolate_phi_kernel<T><<<wave((const void*)extrapolate_phi_kernel<T>, tn.extrapolate), tn.extrapolate, 0, s>>>(a);
-        if ((rc = after_launch("extrapolate_phi")) != MFLBM_OK) return rc;
-    }
+    if ((rc = launch_pdl("sb_live", sb_live_kernel<T>, grid_for(nsb, 64), 64, s, a)) != MFLBM_OK) return rc;
+    if (a.n_phi &&
+        (rc = launch_pdl("extrapolate_phi", extrapolate_phi_kernel<T>,
+                         wave((const void*)extrapolate_phi_kernel<T>, tn.extrapolate), tn.extrapolate, s, a)) != MFLBM_OK)
+        return rc;
+    // brick codes + reset of the previous lists' records
+    if (a.n_norm && (rc = launch_pdl("phi_brick", phi_brick_kernel<T>, wave((const void*)phi_brick_kernel<T>, 64), 64,
+                                     s, a)) != MFLBM_OK)
+        return rc;
+    if ((rc = launch_pdl("sb_active", sb_active_kernel<T>, grid_for(nsb, 64), 64, s, a)) != MFLBM_OK) return rc;
     if (a.n_norm) {
-        // brick codes + reset of the previous lists' records, then the lists restart
-        phi_brick_kernel<T><<<wave((const void*)phi_brick_kernel<T>, 64), 64, 0, s>>>(a);
-        if ((rc = after_launch("phi_brick")) != MFLBM_OK) return rc;
-    }
-    sb_active_kernel<T><<<grid_for(nsb, 64), 64, 0, s>>>(a);
-    if ((rc = after_launch("sb_active")) != MFLBM_OK) return rc;
-    if (a.n_norm) {
-        MFLBM_CUDA(cudaMemsetAsync(c.d.gcount, 0, 3 * sizeof(int), s));
-        active_nodes_kernel<T><<<wave((const void*)active_nodes_kernel<T>, 64), 64, 0, s>>>(a);
-        if ((rc = after_launch("active_nodes")) != MFLBM_OK) return rc;
-        normals_kernel<T><<<wave((const void*)normals_kernel<T>, tn.normals), tn.normals, 0, s>>>(a);
-        if ((rc = after_launch("normals")) != MFLBM_OK) return rc;
-        if (a.n_cn) {
-            extrapolate_normal_kernel<T><<<wave((const void*)extrapolate_normal_kernel<T>, lb), lb, 0, s>>>(a);
-            if ((rc = after_launch("extrapolate_normal")) != MFLBM_OK) return rc;
-        }
+        rc = launch_pdl("active_nodes", active_nodes_kernel<T>, wave((const void*)active_nodes_kernel<T>, 64), 64, s, a);
+        if (rc != MFLBM_OK) return rc;
+        rc = launch_pdl("normals", normals_kernel<T>, wave((const void*)normals_kernel<T>, tn.normals), tn.normals, s, a);
+        if (rc != MFLBM_OK) return rc;
+        if (a.n_cn && (rc = launch_pdl("extrapolate_normal", extrapolate_normal_kernel<T>,
+                                       wave((const void*)extrapolate_normal_kernel<T>, lb), lb, s, a)) != MFLBM_OK)
+            return rc;
     }
     if (!a.n_fluid) return MFLBM_OK;
-    curvature_kernel<T><<<wave((const void*)curvature_kernel<T>, tn.curvature), tn.curvature, 0, s>>>(a);
-    return after_launch("curvature");
+    return launch_pdl("curvature", curvature_kernel<T>, wave((const void*)curvature_kernel<T>, tn.curvature),
+                      tn.curvature, s, a);
 }
 
 // Reference-layout cn_x/y/z, c_norm, curv from the records.

@@ -40,6 +40,7 @@ SIGNATURES = {
     "mflbm_run": (I, [VP, I, I]),
     "mflbm_synchronize": (I, [VP]),
     "mflbm_interface_stats": (I, [VP, VP, VP, VP]),
+    "mflbm_super_block_stats": (I, [VP, VP, VP, VP]),
     "mflbm_monitor_reduce": (I, [VP, I, I, VP]),
     "mflbm_monitor_reduce_noalloc": (I, [VP, I, I, VP]),
     "mflbm_monitor_profile": (I, [VP, VP, VP, I]),
@@ -225,6 +226,13 @@ class Context:
         v = [C.c_longlong(0) for _ in range(3)]
         check(self.lib.mflbm_interface_stats(self.h, *[C.byref(x) for x in v]), "mflbm_interface_stats")
         return {"interface_nodes": v[0].value, "solid_normals": v[1].value, "active_nodes": v[2].value}
+
+    def super_block_stats(self):
+        """mflbm_super_block_stats: super-blocks the last gradient pass processed
+        and flagged, and their total."""
+        v = [C.c_longlong(0) for _ in range(3)]
+        check(self.lib.mflbm_super_block_stats(self.h, *[C.byref(x) for x in v]), "mflbm_super_block_stats")
+        return {"processed": v[0].value, "flagged": v[1].value, "total": v[2].value}
 
     def monitor(self, n_exclude_inlet, n_exclude_outlet):
         m = abi.Monitor()

@@ -111,6 +111,10 @@ def test_strict_long_run_with_moving_interface(mflbm_lib, kind):
         st = ctx.interface_stats()
         assert st["interface_nodes"] == np.count_nonzero(d["c_norm"])
         sizes.append(st["interface_nodes"])
+        # the super-block counts of the last pass (its list count alternates
+        # between two counters across graph-replayed and per-step passes)
+        sb = ctx.super_block_stats()
+        assert 0 < sb["processed"] <= sb["total"] and sb["flagged"] <= sb["total"], sb
     assert min(sizes) > 0
     ctx.close()
 
