@@ -38,7 +38,7 @@ UNITS = {
     "unet.cu": [],
 }
 HEADERS = ["common.cuh", "context.cuh", "step_kernels.cuh", "collide.cuh", "gradient.cuh", "boundary.cuh", "setup.cuh",
-           "unet_kernels.cuh", "unet_tc.cuh"]
+           "batch.cuh", "unet_kernels.cuh", "unet_tc.cuh", "unet_halo.cuh"]
 
 
 def _run(cmd):

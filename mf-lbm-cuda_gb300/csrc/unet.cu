@@ -18,6 +18,9 @@
 #include <vector>
 
 #include "common.cuh"
+#include <cudaTypedefs.h>
+
+#include "unet_halo.cuh"
 #include "unet_kernels.cuh"
 #include "unet_tc.cuh"
 
@@ -119,11 +122,97 @@ int conv_tc(const U::Dims& d, const bf16* x, int cin, const bf16* w, const float
     return MFLBM_OK;
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library)
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    return fn;
+}
+
+// multiprocessors of the current device (0 if the query fails)
+int sm_count() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            n = 0;
+    }
+    return n;
+}
+
+// The halo-tiled kernel's z extent for a convolution, or 0 where the gather
+// kernel serves it better or the halo kernel cannot take it: cout must be
+// one instantiated tile (16, 32 or 48), the weights of all taps and two
+// halo buffers must fit in shared memory, the tensor map needs a 16-byte
+// aligned input, and there must be at least one tile per multiprocessor.
+int halo_tz(const U::Dims& d, const bf16* x, int cin, int cout) {
+    if (cout != 16 && cout != 32 && cout != 48) return 0;
+    if (reinterpret_cast<uintptr_t>(x) % 16 || !tensor_map_encoder()) return 0;
+    const int nsm = sm_count();
+    if (nsm <= 0) return 0;
+    const long long txy = (long long)((d.W + 7) / 8) * ((d.H + 15) / 16);
+    for (int tz : {4, 2, 1}) {
+        if (U::halo_smem_bytes(cin, cout, tz) > 227 * 1024 || tz * cout > 256) continue;
+        const long long tiles = txy * ((d.D + tz - 1) / tz);
+        if (tiles >= 2LL * nsm || (tz == 1 && tiles >= nsm)) return tz;
+    }
+    return 0;
+}
+
+template <int NT>
+int conv_halo(const U::Dims& d, const bf16* x, int cin, int tz, const bf16* w, const float* b, bf16* y, float* y32,
+              bool relu, int* err, cudaStream_t s) {
+    static bool configured = false;
+    if (!configured) {
+        MFLBM_CUDA(cudaFuncSetAttribute(U::conv3d_halo_tc_kernel<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        227 * 1024));
+        configured = true;
+    }
+    CUtensorMap map;
+    const cuuint64_t dims[4] = {(cuuint64_t)cin, (cuuint64_t)d.W, (cuuint64_t)d.H, (cuuint64_t)d.D};
+    const cuuint64_t strides[3] = {(cuuint64_t)cin * 2, (cuuint64_t)cin * 2 * d.W, (cuuint64_t)cin * 2 * d.W * d.H};
+    const cuuint32_t box[4] = {8, U::HALO_X, U::HALO_Y, (cuuint32_t)(tz + 2)};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const CUresult cr = tensor_map_encoder()(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void*)x, dims, strides, box,
+                                             estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (cr != CUDA_SUCCESS) return fail(MFLBM_E_CUDA, "cuTensorMapEncodeTiled failed for the convolution input");
+    const int smem = U::halo_smem_bytes(cin, NT, tz);
+    int per_sm = 0;
+    MFLBM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, U::conv3d_halo_tc_kernel<NT>, 128, smem));
+    if (per_sm < 1) return fail(MFLBM_E_CUDA, "halo convolution does not fit on a multiprocessor");
+    // at most 512 tensor-memory columns per multiprocessor
+    const int cols = tz * NT <= 32 ? 32 : tz * NT <= 64 ? 64 : tz * NT <= 128 ? 128 : 256;
+    per_sm = std::min(per_sm, 512 / cols);
+    const long long tiles = (long long)((d.W + 7) / 8) * ((d.H + 15) / 16) * ((d.D + tz - 1) / tz);
+    const int grid = (int)std::min<long long>(tiles, (long long)per_sm * sm_count());
+    U::conv3d_halo_tc_kernel<NT><<<grid, 128, smem, s>>>(map, d, cin, tz, w, b, y, y32, relu ? 1 : 0, err);
+    MFLBM_CUDA(cudaGetLastError());
+    mflbm::count_launch();
+    return MFLBM_OK;
+}
+
 // y = act(conv(x, w) + b) on the tensor cores; cin and cout multiples of 16
 int launch_conv(const U::Dims& d, const bf16* x, int cin, const bf16* w, const float* b, bf16* y, float* y32,
                 int cout, bool relu, int* err, DevBuf& split, cudaStream_t s) {
     if (cin % 16 || cout % 16 || cin <= 0 || cout <= 0)
         return fail(MFLBM_E_ARG, "convolution channels must be positive multiples of 16");
+    if (const int tz = halo_tz(d, x, cin, cout)) {
+        switch (cout) {
+        case 16: return conv_halo<16>(d, x, cin, tz, w, b, y, y32, relu, err, s);
+        case 32: return conv_halo<32>(d, x, cin, tz, w, b, y, y32, relu, err, s);
+        default: return conv_halo<48>(d, x, cin, tz, w, b, y, y32, relu, err, s);
+        }
+    }
     switch (tc_tile(cout)) {
     case 192: return conv_tc<192>(d, x, cin, w, b, y, y32, cout, relu, err, split, s);
     case 128: return conv_tc<128>(d, x, cin, w, b, y, y32, cout, relu, err, split, s);

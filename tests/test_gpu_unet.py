@@ -26,6 +26,21 @@ def _bf(a):
                                                  ((3, 5, 6), 64, 128, False), ((6, 6, 6), 96, 32, True),
                                                  ((4, 4, 8), 192, 64, False), ((16, 16, 12), 16, 16, True)])
 def test_conv_forward_and_gradients_match_oracle(mflbm_lib, shape, cin, cout, relu):
+    _check_conv(shape, cin, cout, relu)
+
+
+# Volumes with at least one halo tile (8 x 16 x tz voxels) per multiprocessor
+# of a GB300 (152): the halo-tiled kernel (unet_halo.cuh) serves the forward
+# pass and the data gradient here, with partial tiles at the x, y and z ends;
+# tz = 4 for (62, 60, 36) with 16 -> 16, tz = 1 elsewhere; 48 -> 16 has six
+# channel groups, its data gradient 48 output channels.
+@pytest.mark.parametrize("shape,cin,cout,relu", [((62, 60, 36), 16, 16, True), ((40, 48, 36), 48, 16, False),
+                                                 ((40, 30, 20), 32, 32, True), ((34, 32, 24), 16, 32, False)])
+def test_halo_conv_forward_and_gradients_match_oracle(mflbm_lib, shape, cin, cout, relu):
+    _check_conv(shape, cin, cout, relu)
+
+
+def _check_conv(shape, cin, cout, relu):
     rng = np.random.default_rng(cin + cout)
     D, H, W = shape
     x = rng.normal(size=(D, H, W, cin)).astype(np.float32)
