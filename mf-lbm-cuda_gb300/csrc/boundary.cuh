@@ -21,6 +21,16 @@ template <class T, class E> struct BcArgs {
 
 template <class T> __device__ __forceinline__ T keep(T v_new, T v_old, int w) { return v_new * T(1 - w) + v_old * T(w); }
 
+// Column (i, j) of a thread of the face kernels: a block of 128 threads
+// covers 16 x 8 columns, a warp 16 x 2, so that the warp's accesses to a z
+// plane use half of each 2 x 2 x 2 population brick it touches (a warp
+// along one x row would use a quarter).
+__device__ __forceinline__ void face_column(int& i, int& j) {
+    i = blockIdx.x * 16 + (threadIdx.x & 15) + 1;
+    j = blockIdx.y * 8 + (threadIdx.x >> 4) + 1;
+}
+inline dim3 face_grid(const Grid& g) { return dim3((g.nx + 15) / 16, (g.ny + 7) / 8); }
+
 template <class T, class E>
 __device__ __forceinline__ void inlet_phi(const BcArgs<T, E>& a, int i, int j, int w) {
     const Grid& g = a.g;
@@ -222,8 +232,9 @@ __device__ __forceinline__ void outlet_pressure_at(const BcArgs<T, E>& a, int i,
 template <class T, class E, bool AFTER_ODD>
 __global__ void inlet_outlet_kernel(const BcArgs<T, E> a, int inlet, int outlet) {
     pdl_wait();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1;
-    if (i > a.g.nx) return;
+    int i, j;
+    face_column(i, j);
+    if (i > a.g.nx || j > a.g.ny) return;
     if (inlet == 1) inlet_velocity_at<T, E, AFTER_ODD>(a, i, j);
     else if (inlet == 2) inlet_pressure_at<T, E, AFTER_ODD>(a, i, j);
     if (outlet == 1) outlet_convective_at<T, E, AFTER_ODD>(a, i, j);
@@ -344,8 +355,9 @@ __global__ void periodic_kernel(const BcArgs<T, E> a, int jper, int kper, int n)
 template <class T, class E, bool AFTER_ODD>
 __global__ void porous_plate_kernel(const BcArgs<T, E> a) {
     pdl_wait();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1;
-    if (i > a.g.nx) return;
+    int i, j;
+    face_column(i, j);
+    if (i > a.g.nx || j > a.g.ny) return;
     const Grid& g = a.g;
     const int zp = a.Zplate;
     if (!(zp >= 1 && zp <= g.nz) || (a.plate_cmd != 1 && a.plate_cmd != 2)) return;
@@ -422,7 +434,6 @@ int launch_boundaries(mflbm_context& c, bool odd) {
     const mflbm_params& p = c.params;
     const BcArgs<T, E> a = bc_args<T, E>(c);
     cudaStream_t s = c.stream;
-    const unsigned bx = grid_for(g.nx, 128);
     int rc;
     if (p.jper || p.kper) {
         const int n = periodic_items(g, p.jper, p.kper);
@@ -435,13 +446,13 @@ int launch_boundaries(mflbm_context& c, bool odd) {
         const int out = p.outlet_BC == 1 || p.outlet_BC == 2 ? p.outlet_BC : 0;
         if (in || out) {
             rc = launch_pdl("inlet_outlet", odd ? inlet_outlet_kernel<T, E, true> : inlet_outlet_kernel<T, E, false>,
-                            dim3(bx, g.ny), 128, s, a, in, out);
+                            face_grid(g), 128, s, a, in, out);
             if (rc != MFLBM_OK) return rc;
         }
     }
     if (p.porous_plate_cmd != 0)
         return launch_pdl("porous_plate", odd ? porous_plate_kernel<T, E, true> : porous_plate_kernel<T, E, false>,
-                          dim3(bx, g.ny), 128, s, a);
+                          face_grid(g), 128, s, a);
     return MFLBM_OK;
 }
 

@@ -55,8 +55,8 @@ void free_all(mflbm_context* c) {
     void* ptrs[] = {d.pdf, d.phi, d.cn_x, d.cn_y, d.cn_z, d.c_norm, d.curv, d.W_in, d.f_cv, d.g_cv, d.phi_cv,
                     d.walls, d.walls_type, d.s_nx, d.s_ny, d.s_nz, d.fluid_list, d.list_phi_ext,
                     d.red, d.staging, d.aux, d.type8, d.cnv4, d.zpair_off,
-                    d.phi_prev, d.prof, d.dither, d.iface, d.phib, d.tmap, d.wmask, d.olist, d.slist, d.nlist, d.smask, d.gcount,
-                    d.sbcode, d.sbact, d.sblive, d.sbinfo, d.phioff, d.phibf};
+                    d.phi_prev, d.prof, d.dither, d.iface, d.pmask, d.fmask, d.cmask, d.tmap, d.wmask, d.olist, d.slist, d.nlist, d.smask, d.gcount,
+                    d.sbcode, d.sbact, d.sblive, d.sbinfo, d.phioff};
     for (void* p : ptrs) if (p) cudaFree(p);
     d = DeviceState{};
     if (c->pair_graph) cudaGraphExecDestroy(c->pair_graph);
@@ -196,19 +196,23 @@ int build_lists(mflbm_context* c) {
         if ((rc = upload_list(&d.wmask, &nwm, wm)) != MFLBM_OK) return rc;
     }
     {
-        // fluid nodes of each phi brick (s4-local 2b, 2b + 1 per axis)
-        const int BX = (g.nx + 9) / 2, BY = (g.ny + 9) / 2, BZ = (g.nz + 9) / 2;
-        std::vector<uint8_t> fm((size_t)BX * BY * BZ, 0);
-        for (int k = 1; k <= g.nz; ++k)
-            for (int j = 1; j <= g.ny; ++j)
-                for (int i = 1; i <= g.nx; ++i)
-                    if (walls[g.s2(i, j, k)] == 0) {
-                        const int x = i + 3, y = j + 3, z = k + 3;   // s4-local
-                        fm[(x >> 1) + (size_t)BX * ((y >> 1) + (size_t)BY * (z >> 1))] |=
-                            (uint8_t)(1u << ((x & 1) | ((y & 1) << 1) | ((z & 1) << 2)));
-                    }
+        // row masks over the s4 lattice (row (y, z), byte b: x = 8b .. 8b + 7):
+        // the fluid nodes of [1, n]^3 (super-block codes) and the nodes whose
+        // normal may be non-zero (walls_type <= 0 on [-1, n+2]^3)
+        const int NY4 = g.ny + 8, NZ4 = g.nz + 8;
+        std::vector<uint8_t> fm((size_t)d.SX * NY4 * NZ4, 0), cm(fm.size(), 0);
+        auto at = [&](int i, int j, int k) { return (size_t)((i + 3) >> 3) + (size_t)d.SX * ((j + 3) + (size_t)NY4 * (k + 3)); };
+        for (int k = -1; k <= g.nz + 2; ++k)
+            for (int j = -1; j <= g.ny + 2; ++j)
+                for (int i = -1; i <= g.nx + 2; ++i) {
+                    const uint8_t bit = (uint8_t)(1u << ((i + 3) & 7));
+                    if (wt[g.s4(i, j, k)] <= 0) cm[at(i, j, k)] |= bit;
+                    if (i >= 1 && i <= g.nx && j >= 1 && j <= g.ny && k >= 1 && k <= g.nz && walls[g.s2(i, j, k)] == 0)
+                        fm[at(i, j, k)] |= bit;
+                }
         ll nfm = 0;
-        if ((rc = upload_list(&d.phibf, &nfm, fm)) != MFLBM_OK) return rc;
+        if ((rc = upload_list(&d.fmask, &nfm, fm)) != MFLBM_OK) return rc;
+        if ((rc = upload_list(&d.cmask, &nfm, cm)) != MFLBM_OK) return rc;
     }
     {
         // solid boundary nodes grouped by super-block (4 x 4 x 4 phi bricks),
@@ -672,7 +676,7 @@ int mflbm_create(const mflbm_params* params, mflbm_context** out) {
         {(void**)&d.walls, sizeof(int32_t) * g.n2()}, {(void**)&d.walls_type, sizeof(int32_t) * g.n4()},
         {&d.s_nx, T * g.n4()}, {&d.s_ny, T * g.n4()}, {&d.s_nz, T * g.n4()},
         {(void**)&d.dither, 2 * sizeof(uint32_t)}, {(void**)&d.iface, (size_t)g.n2()},
-        {(void**)&d.phib, (size_t)((g.nx + 9) / 2) * ((g.ny + 9) / 2) * ((g.nz + 9) / 2)},
+        {(void**)&d.pmask, sizeof(uint16_t) * (size_t)d.SX * (g.ny + 8) * (g.nz + 8)},
         {(void**)&d.sbcode, nsb}, {(void**)&d.sbact, nsb}, {(void**)&d.sblive, sizeof(uint32_t) * nsb},
         {(void**)&d.sbinfo, 4 * sizeof(int)}};
     for (auto& a : allocs) {

@@ -54,7 +54,9 @@ struct DeviceState {
     ll prof_len = 0;
     uint32_t* dither = nullptr;        // step counter of 16-bit stochastic rounding: [0] read by odd, [1] by even steps
     int8_t* iface = nullptr;           // s2: 1 where the normal record may be non-zero (|grad phi| >= 1e-6, type <= 0)
-    int8_t* phib = nullptr;            // per 2x2x2 brick of the s4 lattice: 1 all phi = +1, 2 all phi = -1, else 0
+    uint16_t* pmask = nullptr;         // s4 rows x super-block columns: phi == +1 / -1 bits (gradient.cuh)
+    uint8_t* fmask = nullptr;          // the same rows: fluid nodes of [1, n]^3
+    uint8_t* cmask = nullptr;          // the same rows: walls_type <= 0 on [-1, n+2]^3
     int32_t* tmap = nullptr;           // s2: fluid-list index of a fluid node of [1, n]^3, else -1
     uint32_t* wmask = nullptr;         // s2: bit q set where x + e_q is a walls_type-2 node of [0, n+1]^3 (type <= 0 nodes)
     uint32_t* olist = nullptr;         // packed nodes with a non-zero normal record (capacity n_norm)
@@ -66,7 +68,6 @@ struct DeviceState {
     // super-blocks of the normal pass: 4 x 4 x 4 phi bricks (8^3 nodes of the s4 lattice)
     int SX = 0, SY = 0, SZ = 0;        // super-blocks per axis
     int8_t* sbcode = nullptr;          // per super-block: the fluid code of its phi bricks (gradient.cuh)
-    uint8_t* phibf = nullptr;          // per phi brick: bit e set where node e is a fluid node of [1, n]^3
     uint8_t* sbact = nullptr;          // per super-block: 1 if its phi can change at the next step (see gradient.cuh)
     uint8_t* sbslab = nullptr;         // per super-block: 1 if always processed (open or periodic faces)
     uint32_t* sblive = nullptr;        // super-blocks processed by the current pass

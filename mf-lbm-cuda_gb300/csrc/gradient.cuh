@@ -47,7 +47,9 @@ template <class T> struct GradArgs {
     V4* cn;    // s2: (n_x, n_y, n_z, |grad phi|)
     V4* aux;   // fluid-list order: (n_x, n_y, n_z, 0.5 * gamma * curv * c_norm)
     int8_t* iface;  // s2 (fluid nodes): 1 where the record may be non-zero; 0: the zero record
-    int8_t* phib;   // per 2x2x2 brick of the s4 lattice: 1 all phi = +1, 2 all phi = -1, else 0
+    uint16_t* pmask;       // s4 rows (y, z) x super-block columns: phi == +1 bits (low byte), == -1 (high byte)
+    const uint8_t* fmask;  // the same rows: fluid nodes of [1, n]^3
+    const uint8_t* cmask;  // the same rows: walls_type <= 0 on [-1, n+2]^3 (the nodes whose normal may be non-zero)
     const int32_t* tmap;   // s2 -> fluid-list index (or -1)
     const uint32_t* wmask; // s2: bit q where x + e_q is a solid boundary node (walls_type 2) of [0, n+1]^3
     uint32_t* olist;       // packed coordinates of the nodes whose record is non-zero (interface flag set)
@@ -62,7 +64,6 @@ template <class T> struct GradArgs {
     // super-blocks (4 x 4 x 4 phi bricks)
     int SX, SY, SZ;
     int8_t* sbcode;        // fluid code of the super-block (below)
-    const uint8_t* phibf;  // per phi brick: bit e set where node e is a fluid node of [1, n]^3
     uint8_t* sbact;        // 1: the super-block's phi may change at the next step
     uint32_t* sblive;      // super-blocks of this pass
     int* sbinfo;           // [1] 1: every super-block (consumed by this pass)
@@ -299,65 +300,106 @@ __device__ __forceinline__ void clear_records(const GradArgs<T>& a, int tid, int
     }
 }
 
-// Bulk detection for the normal pass: per 2x2x2 brick of the s4 lattice
-// (s4-local coordinates 2b, 2b + 1 on each axis; positions past the lattice
-// end are ignored), 1 if every phi is exactly +1, 2 if every phi is exactly -1,
-// 0 otherwise.  Away from interfaces phi is exactly +-1 (one component is
-// exactly zero), so most bricks are uniform.  One block of 64 threads per
-// super-block of this pass (one brick per thread); the super-block's code is
-// the bricks' common code, or 0.  The threads also reset the records of the
+// Row masks of the s4 lattice: for row (y, z) and byte b (x = 8b .. 8b + 7,
+// the x extent of super-block column b), pmask holds bit x & 7 where phi is
+// exactly +1 (low byte) and exactly -1 (high byte).  Away from interfaces
+// phi is exactly +-1 (one component is exactly zero), so most stencils are
+// of one value.  One block of 64 threads per super-block of this pass (one
+// row of 8 nodes per thread); the super-block's fluid code follows from the
+// rows' fluid masks (fmask).  The threads also reset the records of the
 // previous pass's lists.
 template <class T>
-__device__ __forceinline__ int8_t phi_brick_code(const GradArgs<T>& a, int bx, int by, int bz, unsigned fmask,
-                                                 int8_t* fcode) {
-    typedef typename Vec2<T>::type P;
-    const int NX = a.g.nx + 8, NY = a.g.ny + 8, NZ = a.g.nz + 8;
-    bool plus = true, minus = true, fplus = true, fminus = true;
-#pragma unroll
-    for (int e = 0; e < 4; ++e) {
-        const int y = 2 * by + (e & 1), z = 2 * bz + (e >> 1);
-        if (y >= NY || z >= NZ) continue;
-        const T* row = a.phi + (ll)NX * (y + (ll)NY * z);
-        T v0, v1;
-        if (!(NX & 1)) {            // even rows: every row starts on a pair boundary
-            const P v = reinterpret_cast<const P*>(row)[bx];
-            v0 = v.x;
-            v1 = v.y;
-        } else {
-            v0 = row[2 * bx];
-            v1 = 2 * bx + 1 < NX ? row[2 * bx + 1] : v0;
-        }
-        plus = plus && v0 == T(1) && v1 == T(1);
-        minus = minus && v0 == T(-1) && v1 == T(-1);
-        const bool f0 = (fmask >> (2 * e)) & 1u, f1 = (fmask >> (2 * e + 1)) & 1u;
-        fplus = fplus && (!f0 || v0 == T(1)) && (!f1 || v1 == T(1));
-        fminus = fminus && (!f0 || v0 == T(-1)) && (!f1 || v1 == T(-1));
-    }
-    *fcode = fmask == 0 ? 3 : fplus ? 1 : fminus ? 2 : 0;
-    return plus ? 1 : minus ? 2 : 0;
-}
-
-template <class T>
-__global__ void __launch_bounds__(64) phi_brick_kernel(const GradArgs<T> a) {
+__global__ void __launch_bounds__(64) phi_mask_kernel(const GradArgs<T> a) {
     pdl_wait();
     clear_records<T>(a, (int)(blockIdx.x * blockDim.x + threadIdx.x), (int)(gridDim.x * blockDim.x));
-    const int BX = (a.g.nx + 9) >> 1, BY = (a.g.ny + 9) >> 1, BZ = (a.g.nz + 9) >> 1;
+    const int NX = a.g.nx + 8, NY = a.g.ny + 8, NZ = a.g.nz + 8;
     const int nl = min(*a.live_n, a.SX * a.SY * a.SZ);
-    const int lx = threadIdx.x & 3, ly = (threadIdx.x >> 2) & 3, lz = threadIdx.x >> 4;
+    const int ly = threadIdx.x & 7, lz = threadIdx.x >> 3;
     for (int w = blockIdx.x; w < nl; w += gridDim.x) {
         const int sb = (int)a.sblive[w];
-        const int bx = 4 * (sb % a.SX) + lx, by = 4 * ((sb / a.SX) % a.SY) + ly, bz = 4 * (sb / (a.SX * a.SY)) + lz;
-        const bool in = bx < BX && by < BY && bz < BZ;
-        int8_t fcode = 3;   // no fluid node
-        if (in) {
-            const ll b = bx + (ll)BX * (by + (ll)BY * bz);
-            a.phib[b] = phi_brick_code<T>(a, bx, by, bz, a.phibf[b], &fcode);
+        const int sx = sb % a.SX, y = 8 * ((sb / a.SX) % a.SY) + ly, z = 8 * (sb / (a.SX * a.SY)) + lz;
+        unsigned F = 0, P = 0, M = 0;
+        if (y < NY && z < NZ) {
+            const ll r = sx + (ll)a.SX * (y + (ll)NY * z);
+            const T* row = a.phi + (ll)NX * (y + (ll)NY * z) + 8 * sx;
+            const int nb = min(8, NX - 8 * sx);
+#pragma unroll
+            for (int b = 0; b < 8; ++b)
+                if (b < nb) {
+                    const T v = row[b];
+                    P |= (v == T(1) ? 1u : 0u) << b;
+                    M |= (v == T(-1) ? 1u : 0u) << b;
+                }
+            a.pmask[r] = (uint16_t)(P | (M << 8));
+            F = a.fmask[r];
         }
-        // the super-block's fluid code: 0 if a brick has 0 or both signs occur
-        const int any0 = __syncthreads_or(fcode == 0);
-        const int any1 = __syncthreads_or(fcode == 1);
-        const int any2 = __syncthreads_or(fcode == 2);
-        if (threadIdx.x == 0) a.sbcode[sb] = (any0 || (any1 && any2)) ? 0 : any1 ? 1 : any2 ? 2 : 3;
+        // fluid code: 3 without fluid nodes, 1 (2) when all of them are +1 (-1), else 0
+        const int anyf = __syncthreads_or(F != 0);
+        const int notp = __syncthreads_or((F & ~P) != 0);
+        const int notm = __syncthreads_or((F & ~M) != 0);
+        if (threadIdx.x == 0) a.sbcode[sb] = !anyf ? 3 : !notp ? 1 : !notm ? 2 : 0;
+    }
+}
+
+// 24-bit windows of a row's +1 and -1 masks around byte b: bytes b - 1, b,
+// b + 1 (0 past the row ends) at bits 0, 8, 16.
+__device__ __forceinline__ void mask_window(const uint16_t* pm, ll r, int b, int SX, uint32_t& wp, uint32_t& wm) {
+    const uint32_t c = pm[r], l = b > 0 ? pm[r - 1] : 0u, h = b + 1 < SX ? pm[r + 1] : 0u;
+    wp = (l & 0xFFu) | ((c & 0xFFu) << 8) | ((h & 0xFFu) << 16);
+    wm = (l >> 8) | ((c >> 8) << 8) | ((h >> 8) << 16);
+}
+
+// The nodes whose normal this pass recomputes: the candidates (walls_type <=
+// 0 on [-1, n+2]^3, cmask) whose ISO4 stencil (the node and its 18 D3Q19
+// neighbours) is not all exactly +1 or all exactly -1; elsewhere every
+// difference of the stencil is +0 and the record is the zero record.  Per
+// row of 8 nodes, bit-parallel: with a window w of a row's mask (byte b at
+// bits 8..15), w >> 8, w >> 7 and w >> 9 hold x, x - 1 and x + 1; the
+// stencil is x +- 1 of row (y, z), x and x +- 1 of rows (y +- 1, z) and
+// (y, z +- 1), and x of rows (y +- 1, z +- 1).  Appended to nlist (one atomic
+// per warp).  One block of 64 threads per super-block of this pass.
+template <class T>
+__global__ void __launch_bounds__(64) active_nodes_kernel(const GradArgs<T> a) {
+    pdl_wait();
+    const int NY = a.g.ny + 8, NZ = a.g.nz + 8;
+    const int nl = min(*a.live_n, a.SX * a.SY * a.SZ);
+    const int ly = threadIdx.x & 7, lz = threadIdx.x >> 3;
+    const ll RY = a.SX, RZ = (ll)a.SX * NY;   // row strides of the masks
+    for (int w = blockIdx.x; w < nl; w += gridDim.x) {
+        const int sb = (int)a.sblive[w];
+        const int sx = sb % a.SX, y = 8 * ((sb / a.SX) % a.SY) + ly, z = 8 * (sb / (a.SX * a.SY)) + lz;
+        unsigned sel = 0;   // bit b: node x = 8 sx + b of the row is listed
+        if (y >= 1 && y < NY - 1 && z >= 1 && z < NZ - 1) {
+            const ll r = sx + RY * y + RZ * z;
+            const unsigned cand = a.cmask[r];
+            if (cand) {
+                uint32_t up = 0xFFFFFFFFu, um = 0xFFFFFFFFu, wp, wm;
+                mask_window(a.pmask, r, sx, a.SX, wp, wm);
+                up &= (wp >> 7) & (wp >> 8) & (wp >> 9);
+                um &= (wm >> 7) & (wm >> 8) & (wm >> 9);
+                const ll side[4] = {-RY, RY, -RZ, RZ};
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    mask_window(a.pmask, r + side[e], sx, a.SX, wp, wm);
+                    up &= (wp >> 7) & (wp >> 8) & (wp >> 9);
+                    um &= (wm >> 7) & (wm >> 8) & (wm >> 9);
+                }
+                const ll diag[4] = {-RY - RZ, RY - RZ, -RY + RZ, RY + RZ};
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const uint32_t c = a.pmask[r + diag[e]];
+                    up &= c;
+                    um &= c >> 8;
+                }
+                sel = cand & ~(up | um) & 0xFFu;
+            }
+        }
+        int base = warp_reserve(__popc(sel), &a.gcount[2]);
+        for (int b = 0; b < 8; ++b)
+            if (sel & (1u << b)) {
+                if (base < a.n_norm) a.nlist[base] = pack_xyz(8 * sx + b - 3, y - 3, z - 3);
+                ++base;
+            }
     }
 }
 
@@ -385,49 +427,6 @@ __device__ __forceinline__ bool normal_at(const GradArgs<T>& a, int i, int j, in
     a.cn[n2] = r;
     a.iface[n2] = r.w != T(0) ? 1 : 0;
     return r.w != T(0);
-}
-
-// Node block c (nodes 2c-2 .. 2c-1 on each axis) is active unless the eight
-// phi bricks c .. c+1 that hold its stencils (s4-local i+2 .. i+4) have one
-// common non-zero code.  The fluid nodes (walls_type <= 0) of [-1, n+2]^3 in
-// active blocks are appended to nlist (one atomic per warp).  One block of 64
-// threads per super-block of this pass: its 4 x 4 x 4 node blocks c (a node
-// block belongs to the super-block of its brick c).
-template <class T>
-__global__ void __launch_bounds__(64) active_nodes_kernel(const GradArgs<T> a) {
-    pdl_wait();
-    const Grid& g = a.g;
-    const int BX = (g.nx + 9) >> 1, BY = (g.ny + 9) >> 1;
-    const int CX = ((g.nx + 4) >> 1) + 1, CY = ((g.ny + 4) >> 1) + 1, CZ = ((g.nz + 4) >> 1) + 1;
-    const int nl = min(*a.live_n, a.SX * a.SY * a.SZ);
-    const int lx = threadIdx.x & 3, ly = (threadIdx.x >> 2) & 3, lz = threadIdx.x >> 4;
-    for (int w = blockIdx.x; w < nl; w += gridDim.x) {
-        const int sb = (int)a.sblive[w];
-        const int cx = 4 * (sb % a.SX) + lx, cy = 4 * ((sb / a.SX) % a.SY) + ly, cz = 4 * (sb / (a.SX * a.SY)) + lz;
-        unsigned sel = 0;   // bit e: node e of the block is listed
-        if (cx < CX && cy < CY && cz < CZ) {
-            const int8_t* pb = a.phib + cx + (ll)BX * (cy + (ll)BY * cz);
-            const int8_t c0 = pb[0];
-            const bool quiet = c0 != 0 && pb[1] == c0 && pb[BX] == c0 && pb[BX + 1] == c0 && pb[(ll)BX * BY] == c0 &&
-                               pb[(ll)BX * BY + 1] == c0 && pb[(ll)BX * BY + BX] == c0 && pb[(ll)BX * BY + BX + 1] == c0;
-            if (!quiet) {
-#pragma unroll
-                for (int e = 0; e < 8; ++e) {
-                    const int i = 2 * cx - 2 + (e & 1), j = 2 * cy - 2 + ((e >> 1) & 1), k = 2 * cz - 2 + (e >> 2);
-                    if (i >= -1 && i <= g.nx + 2 && j >= -1 && j <= g.ny + 2 && k >= -1 && k <= g.nz + 2 &&
-                        a.type8[g.s4(i, j, k)] <= 0)
-                        sel |= 1u << e;
-                }
-            }
-        }
-        int base = warp_reserve(__popc(sel), &a.gcount[2]);
-        for (int e = 0; e < 8; ++e)
-            if (sel & (1u << e)) {
-                if (base < a.n_norm)
-                    a.nlist[base] = pack_xyz(2 * cx - 2 + (e & 1), 2 * cy - 2 + ((e >> 1) & 1), 2 * cz - 2 + (e >> 2));
-                ++base;
-            }
-    }
 }
 
 // unit interface normal and |grad phi| (:757-807) + wetting (:809-878) at the
@@ -638,7 +637,7 @@ GradArgs<T> grad_args(const mflbm_context& c) {
     a.cn = (typename Vec4<T>::type*)d.cnv4;
     a.aux = (typename Vec4<T>::type*)d.aux;
     a.iface = d.iface;
-    a.phib = d.phib;
+    a.pmask = d.pmask; a.fmask = d.fmask; a.cmask = d.cmask;
     a.tmap = d.tmap;
     a.wmask = d.wmask;
     a.olist = d.olist; a.slist = d.slist; a.nlist = d.nlist; a.smask = d.smask; a.gcount = d.gcount;
@@ -649,7 +648,7 @@ GradArgs<T> grad_args(const mflbm_context& c) {
     a.l_fluid = d.fluid_list; a.n_fluid = (int)d.n_fluid;
     a.n_norm = (int)d.n_norm;
     a.SX = d.SX; a.SY = d.SY; a.SZ = d.SZ;
-    a.sbcode = d.sbcode; a.sbact = d.sbact; a.phibf = d.phibf; a.sblive = (uint32_t*)d.sblive; a.sbinfo = d.sbinfo;
+    a.sbcode = d.sbcode; a.sbact = d.sbact; a.sblive = (uint32_t*)d.sblive; a.sbinfo = d.sbinfo;
     a.live_n = a.live_next = nullptr;   // set by launch_gradient
     a.phioff = d.phioff;
     const mflbm_params& p = c.params;
@@ -691,8 +690,8 @@ int launch_gradient(mflbm_context& c) {
         (rc = launch_pdl("extrapolate_phi", extrapolate_phi_kernel<T>,
                          wave((const void*)extrapolate_phi_kernel<T>, tn.extrapolate), tn.extrapolate, s, a)) != MFLBM_OK)
         return rc;
-    // brick codes + reset of the previous lists' records
-    if (a.n_norm && (rc = launch_pdl("phi_brick", phi_brick_kernel<T>, wave((const void*)phi_brick_kernel<T>, 64), 64,
+    // row masks + reset of the previous lists' records
+    if (a.n_norm && (rc = launch_pdl("phi_mask", phi_mask_kernel<T>, wave((const void*)phi_mask_kernel<T>, 64), 64,
                                      s, a)) != MFLBM_OK)
         return rc;
     if ((rc = launch_pdl("sb_active", sb_active_kernel<T>, grid_for(nsb, 64), 64, s, a)) != MFLBM_OK) return rc;

@@ -151,7 +151,7 @@ int sm_count() {
 
 // CTAs of the halo-tiled kernel per multiprocessor: shared memory (with the
 // per-block reservation), 16 blocks of 128 threads, 512 tensor-memory columns
-int halo_per_sm(int cin, int cout, int tz) {
+int halo_per_sm(int cin, int cout, int tz, int nbuf) {
     static int smem_sm = 0, reserved = 0;
     if (!smem_sm) {
         int dev = 0;
@@ -160,46 +160,55 @@ int halo_per_sm(int cin, int cout, int tz) {
             cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev) != cudaSuccess)
             return 0;
     }
-    const int by_smem = smem_sm / (U::halo_smem_bytes(cin, cout, tz) + reserved);
+    const int bytes = U::halo_smem_bytes(cin, cout, tz, nbuf);
+    if (bytes > 227 * 1024) return 0;
+    const int by_smem = smem_sm / (bytes + reserved);
     return std::min(std::min(by_smem, 16), 512 / U::halo_tmem_cols(cout, tz));
 }
 
-// The halo-tiled kernel's z extent for a convolution, or 0 where the gather
-// kernel serves it better or the halo kernel cannot take it: cout must be
-// one instantiated tile (16, 32 or 48), the weights of all taps and two
-// halo buffers must fit in shared memory, the tensor map needs a 16-byte
-// aligned input, and there must be at least one tile per multiprocessor.
-// Among the extents that qualify, the one with the fewest z slices per CTA
-// (rounds of resident CTAs x tz) wins, the larger extent on a tie.
-int halo_tz(const U::Dims& d, const bf16* x, int cin, int cout) {
-    if (cout != 16 && cout != 32 && cout != 48) return 0;
-    if (reinterpret_cast<uintptr_t>(x) % 16 || !tensor_map_encoder()) return 0;
+struct HaloPlan {
+    int tz = 0, nbuf = 2;
+};
+
+// The halo-tiled kernel's z extent and halo buffers for a convolution, or
+// tz = 0 where it cannot take it: cout must be one instantiated tile (16, 32
+// or 48), the weights of all taps and the halo buffers must fit in shared
+// memory, the tensor map needs a 16-byte aligned input, and there must be at
+// least one tile per multiprocessor.  Two halo buffers unless one buffer
+// lets more CTAs share a multiprocessor (one issuing thread each).  Among the
+// extents that qualify, the one with the fewest z slices per CTA (rounds of
+// resident CTAs x tz) wins, the larger extent on a tie.
+HaloPlan halo_plan(const U::Dims& d, const bf16* x, int cin, int cout) {
+    HaloPlan best;
+    if (cout != 16 && cout != 32 && cout != 48) return best;
+    if (reinterpret_cast<uintptr_t>(x) % 16 || !tensor_map_encoder()) return best;
     const int nsm = sm_count();
-    if (nsm <= 0) return 0;
+    if (nsm <= 0) return best;
     const long long txy = (long long)((d.W + 7) / 8) * ((d.H + 15) / 16);
-    int best = 0;
     long long best_cost = 0;
     for (int tz : {4, 2, 1}) {
-        if (U::halo_smem_bytes(cin, cout, tz) > 227 * 1024) continue;
-        const int per_sm = halo_per_sm(cin, cout, tz);
+        const int two = halo_per_sm(cin, cout, tz, 2), one = halo_per_sm(cin, cout, tz, 1);
+        const int nbuf = two >= 2 || two >= one ? 2 : 1;
+        const int per_sm = nbuf == 2 ? two : one;
         const long long tiles = txy * ((d.D + tz - 1) / tz);
         if (per_sm < 1 || tiles < nsm) continue;
         const long long resident = (long long)per_sm * nsm;
         const long long cost = (tiles + resident - 1) / resident * tz;
-        if (!best || cost < best_cost) { best = tz; best_cost = cost; }
+        if (!best.tz || cost < best_cost) { best.tz = tz; best.nbuf = nbuf; best_cost = cost; }
     }
     return best;
 }
 
 template <int NT>
-int conv_halo(const U::Dims& d, const bf16* x, int cin, int tz, const bf16* w, const float* b, bf16* y, float* y32,
-              bool relu, int* err, DevBuf& scratch, cudaStream_t s) {
+int conv_halo(const U::Dims& d, const bf16* x, int cin, const HaloPlan& plan, const bf16* w, const float* b, bf16* y,
+              float* y32, bool relu, int* err, DevBuf& scratch, cudaStream_t s) {
     static bool configured = false;
     if (!configured) {
         MFLBM_CUDA(cudaFuncSetAttribute(U::conv3d_halo_tc_kernel<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         227 * 1024));
         configured = true;
     }
+    const int tz = plan.tz;
     // the weights' shared-memory image
     const int rows = 27 * (cin / 8) * NT;
     int rc;
@@ -216,13 +225,13 @@ int conv_halo(const U::Dims& d, const bf16* x, int cin, int tz, const bf16* w, c
                                              estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (cr != CUDA_SUCCESS) return fail(MFLBM_E_CUDA, "cuTensorMapEncodeTiled failed for the convolution input");
-    const int smem = U::halo_smem_bytes(cin, NT, tz);
-    const int per_sm = halo_per_sm(cin, NT, tz);
+    const int smem = U::halo_smem_bytes(cin, NT, tz, plan.nbuf);
+    const int per_sm = halo_per_sm(cin, NT, tz, plan.nbuf);
     if (per_sm < 1) return fail(MFLBM_E_CUDA, "halo convolution does not fit on a multiprocessor");
     const long long tiles = (long long)((d.W + 7) / 8) * ((d.H + 15) / 16) * ((d.D + tz - 1) / tz);
     const int grid = (int)std::min<long long>(tiles, (long long)per_sm * sm_count());
-    U::conv3d_halo_tc_kernel<NT><<<grid, 128, smem, s>>>(map, d, cin, tz, scratch.as<bf16>(), b, y, y32, relu ? 1 : 0,
-                                                         err);
+    U::conv3d_halo_tc_kernel<NT><<<grid, 128, smem, s>>>(map, d, cin, tz, plan.nbuf, scratch.as<bf16>(), b, y, y32,
+                                                         relu ? 1 : 0, err);
     MFLBM_CUDA(cudaGetLastError());
     mflbm::count_launch();
     return MFLBM_OK;
@@ -233,11 +242,12 @@ int launch_conv(const U::Dims& d, const bf16* x, int cin, const bf16* w, const f
                 int cout, bool relu, int* err, DevBuf& split, cudaStream_t s) {
     if (cin % 16 || cout % 16 || cin <= 0 || cout <= 0)
         return fail(MFLBM_E_ARG, "convolution channels must be positive multiples of 16");
-    if (const int tz = halo_tz(d, x, cin, cout)) {
+    const HaloPlan plan = halo_plan(d, x, cin, cout);
+    if (plan.tz) {
         switch (cout) {
-        case 16: return conv_halo<16>(d, x, cin, tz, w, b, y, y32, relu, err, split, s);
-        case 32: return conv_halo<32>(d, x, cin, tz, w, b, y, y32, relu, err, split, s);
-        default: return conv_halo<48>(d, x, cin, tz, w, b, y, y32, relu, err, split, s);
+        case 16: return conv_halo<16>(d, x, cin, plan, w, b, y, y32, relu, err, split, s);
+        case 32: return conv_halo<32>(d, x, cin, plan, w, b, y, y32, relu, err, split, s);
+        default: return conv_halo<48>(d, x, cin, plan, w, b, y, y32, relu, err, split, s);
         }
     }
     switch (tc_tile(cout)) {

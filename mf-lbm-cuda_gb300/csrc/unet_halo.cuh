@@ -26,10 +26,12 @@
 // precomputed increments.  Several CTAs share a multiprocessor, each with its
 // own issuing thread.
 //
-// The CTA is persistent over tiles; the halo is double-buffered, so the TMA
-// of the next tile overlaps the MMAs and the epilogue of this one.  The
-// epilogue reads the accumulators with tcgen05.ld (one row per thread), adds
-// the bias, applies the ReLU and writes BF16 (and FP32) outputs.  Every wait
+// The CTA is persistent over tiles.  With two halo buffers the TMA of the
+// next tile overlaps the MMAs and the epilogue of this one; with one (wide
+// inputs, so that two CTAs fit on a multiprocessor) it overlaps the
+// epilogue.  The epilogue reads the accumulators with tcgen05.ld (one row
+// per thread), adds the bias, applies the ReLU and writes BF16 (and FP32)
+// outputs.  Every wait
 // is bounded: on a time-out the kernel records an error, waits (bounded) for
 // its copies and MMAs in flight, frees its tensor memory and returns.
 #pragma once
@@ -55,10 +57,10 @@ __host__ __device__ constexpr int halo_tmem_cols(int nt, int tz) {
     return tz * halo_splits(tz) * nt <= 32 ? 32 : tz * halo_splits(tz) * nt <= 64 ? 64
          : tz * halo_splits(tz) * nt <= 128 ? 128 : tz * halo_splits(tz) * nt <= 256 ? 256 : 512;
 }
-// weights, two halo buffers, the bias (up to 64 floats), then 64 bytes of
+// weights, nbuf halo buffers, the bias (up to 64 floats), then 64 bytes of
 // barriers and the TMEM slot
-__host__ __device__ constexpr int halo_smem_bytes(int cin, int nt, int tz) {
-    return halo_weight_bytes(cin, nt) + 2 * (cin / 8) * halo_plane_bytes(tz) + 256 + 64;
+__host__ __device__ constexpr int halo_smem_bytes(int cin, int nt, int tz, int nbuf) {
+    return halo_weight_bytes(cin, nt) + nbuf * (cin / 8) * halo_plane_bytes(tz) + 256 + 64;
 }
 
 __device__ __forceinline__ void tma_expect(uint64_t* bar, uint32_t bytes) {
@@ -92,11 +94,11 @@ __global__ void arrange_halo_weights_kernel(const bf16* __restrict__ w, int cin,
 
 // y = act(conv(x, w) + b) for cout == NT.  x is read through `xmap`: a 4-D
 // tensor map over (channel, x, y, z) of the BF16 input with a box of
-// (8, 10, 18, tz + 2); `wimg` is the weights' shared-memory image.  Tiles:
-// ceil(W / 8) x ceil(H / 16) x ceil(D / tz).
+// (8, 10, 18, tz + 2); `wimg` is the weights' shared-memory image; nbuf
+// halo buffers (1 or 2).  Tiles: ceil(W / 8) x ceil(H / 16) x ceil(D / tz).
 template <int NT>
 __global__ void __launch_bounds__(128) conv3d_halo_tc_kernel(const __grid_constant__ CUtensorMap xmap, Dims d, int cin,
-                                                             int tz, const bf16* __restrict__ wimg,
+                                                             int tz, int nbuf, const bf16* __restrict__ wimg,
                                                              const float* __restrict__ bias, bf16* __restrict__ y,
                                                              float* __restrict__ y32, int relu, int* __restrict__ err) {
     constexpr uint32_t IDESC = tc_idesc_bf16(TC_M, NT);
@@ -107,8 +109,8 @@ __global__ void __launch_bounds__(128) conv3d_halo_tc_kernel(const __grid_consta
     const int WB = halo_weight_bytes(cin, NT), P = halo_plane_bytes(tz);
     const int HB = KG * P;                        // one halo buffer
     uint8_t* halo = sm + WB;
-    float* sbias = reinterpret_cast<float*>(sm + WB + 2 * HB);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(sm + WB + 2 * HB + 256);   // [0], [1] halo, [2] MMA, [3] weights
+    float* sbias = reinterpret_cast<float*>(sm + WB + nbuf * HB);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sm + WB + nbuf * HB + 256);   // [0], [1] halo, [2] MMA, [3] weights
     uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 4);
     const uint32_t ncols = (uint32_t)halo_tmem_cols(NT, tz);
 
@@ -138,12 +140,13 @@ __global__ void __launch_bounds__(128) conv3d_halo_tc_kernel(const __grid_consta
         y0 = ((tile / TXn) % TYn) * 16;
         z0 = (tile / (TXn * TYn)) * tz;
     };
-    auto load = [&](int i) {   // thread 0: the halo of this CTA's i-th tile into buffer i & 1
+    // tile i's halo goes to buffer i % nbuf, completing phase (i / nbuf) & 1 of its barrier
+    auto load = [&](int i) {   // thread 0
         int x0, y0, z0;
         origin(blockIdx.x + i * gridDim.x, x0, y0, z0);
-        uint64_t* bar = &bars[i & 1];
+        uint64_t* bar = &bars[i % nbuf];
         tma_expect(bar, tx_bytes);
-        const uint32_t dst = smem_addr(halo + (i & 1) * HB);
+        const uint32_t dst = smem_addr(halo + (i % nbuf) * HB);
         for (int kg = 0; kg < KG; ++kg) tma_load_4d(dst + kg * P, &xmap, kg * 8, x0 - 1, y0 - 1, z0 - 1, bar);
     };
 
@@ -157,13 +160,14 @@ __global__ void __launch_bounds__(128) conv3d_halo_tc_kernel(const __grid_consta
     }
     for (int i = 0; i < mine && ok; ++i) {
         if (tid == 0) {
-            if (i + 1 < mine) { load(i + 1); ++loads; }   // its buffer's MMAs (tile i - 1) are done
+            // two buffers: the next tile's (its MMAs, of tile i - 1, are done)
+            if (nbuf == 2 && i + 1 < mine) { load(i + 1); ++loads; }
             if (!wready) ok = wready = mbar_wait(&bars[3], 0);
-            if (ok && !mbar_wait(&bars[i & 1], (i >> 1) & 1)) ok = false;
+            if (ok && !mbar_wait(&bars[i % nbuf], (i / nbuf) & 1)) ok = false;
             if (ok) {
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 // descriptors advance in 16-byte units (start address field)
-                const uint64_t a0 = tc_desc(smem_addr(halo + (i & 1) * HB), P, HALO_X * 16);
+                const uint64_t a0 = tc_desc(smem_addr(halo + (i % nbuf) * HB), P, HALO_X * 16);
                 const uint64_t b0 = tc_desc(smem_addr(sm), NT * 16, 128);
                 const uint32_t zstep = HALO_X * HALO_Y, gstep = (uint32_t)P >> 4;
                 for (int t = 0; t < 27; ++t) {
@@ -183,6 +187,8 @@ __global__ void __launch_bounds__(128) conv3d_halo_tc_kernel(const __grid_consta
         }
         if (!__syncthreads_and(ok)) { ok = false; break; }
         if (!tc_wait_stage(&bars[2], i & 1)) { ok = false; break; }
+        // one buffer: the next tile's, now that this tile's MMAs are done
+        if (tid == 0 && nbuf == 1 && i + 1 < mine) { load(i + 1); ++loads; }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         // epilogue: row m = 32 * warp + lane of every z slice
         int x0, y0, z0;
@@ -231,8 +237,8 @@ __global__ void __launch_bounds__(128) conv3d_halo_tc_kernel(const __grid_consta
         if (tid == 0) {
             atomicExch(err, 1);
             if (mine > 0 && !wready) mbar_wait(&bars[3], 0);
-            // halo loads: the i-th load completes phase (i >> 1) & 1 of bars[i & 1]
-            for (int i = loads - 2 < 0 ? 0 : loads - 2; i < loads; ++i) mbar_wait(&bars[i & 1], (i >> 1) & 1);
+            // halo loads: the i-th load completes phase (i / nbuf) & 1 of bars[i % nbuf]
+            for (int i = loads - nbuf < 0 ? 0 : loads - nbuf; i < loads; ++i) mbar_wait(&bars[i % nbuf], (i / nbuf) & 1);
             if (mmas > 0) mbar_wait(&bars[2], (mmas - 1) & 1);
         }
         __syncthreads();

@@ -1,23 +1,17 @@
 """Index arithmetic of the sparse colour-gradient passes
-(mf-lbm-cuda_gb300/csrc/gradient.cuh: phi_brick_kernel, active_nodes_kernel),
-restated in numpy.
+(mf-lbm-cuda_gb300/csrc/gradient.cuh: phi_mask_kernel, active_nodes_kernel,
+sb_active_kernel, sb_live_kernel), restated in numpy.
 
-The passes skip every node whose ISO4 stencil (the node and its 18 D3Q19
-neighbours, s4-local i+2 .. i+4 on each axis) lies in eight 2x2x2 phi bricks
-of one common code (all exactly +1 or all exactly -1): there every difference
-of the ISO4 sums is +0 and the normal record is the zero record.  These tests
-check, on random phase fields with sharp and diffuse interfaces and on odd and
-even extents, that
-
-  * every node of [-1, n+2]^3 belongs to exactly one node block c
-    (nodes 2c-2 .. 2c-1 per axis), and the blocks range over
-    [0, (n+4)/2] per axis;
-  * the eight bricks c .. c+1 of a block lie inside the brick grid
-    ((n+9)/2 bricks per axis of the s4 lattice) and cover the stencils of all
-    of the block's nodes;
-  * every node outside the active blocks has a stencil of one value (so its
-    gradient is exactly zero), i.e. nothing with a non-zero gradient is
-    skipped.
+The normal pass skips every node whose ISO4 stencil (the node and its 18
+D3Q19 neighbours) is all exactly +1 or all exactly -1: there every
+difference of the ISO4 sums is +0 and the normal record is the zero record.
+The node listing decides this bit-parallel from per-row masks of the s4
+lattice (8 nodes per byte); these tests check, on random phase fields with
+sharp and diffuse interfaces and on odd and even extents, that the bitwise
+rule lists exactly the candidate nodes with a non-uniform stencil, and (the
+super-blocks) that every node, row mask and listing decision that can change
+between two passes lies in a super-block the pass processes.  The 2x2x2
+brick codes restated first are the super-blocks' fluid codes.
 """
 import numpy as np
 import pytest
@@ -41,21 +35,6 @@ def brick_codes(phi4):
     return np.where(plus, 1, np.where(minus, 2, 0)).astype(np.int8)
 
 
-def active_blocks(codes, n):
-    nx, ny, nz = n
-    CX, CY, CZ = (nx + 4) // 2 + 1, (ny + 4) // 2 + 1, (nz + 4) // 2 + 1
-    BZ, BY, BX = codes.shape
-    assert CX + 1 <= BX and CY + 1 <= BY and CZ + 1 <= BZ
-    c0 = codes[:CZ, :CY, :CX]
-    same = np.ones_like(c0, dtype=bool)
-    for dz in (0, 1):
-        for dy in (0, 1):
-            for dx in (0, 1):
-                same &= codes[dz:dz + CZ, dy:dy + CY, dx:dx + CX] == c0
-    quiet = (c0 != 0) & same
-    return ~quiet
-
-
 def random_phase(n, seed, sharp):
     """phi on the s4 lattice (4 ghost layers): +-1 regions from random balls,
     with a diffuse band unless `sharp`."""
@@ -75,36 +54,77 @@ def random_phase(n, seed, sharp):
     return phi
 
 
-@pytest.mark.parametrize("n", [(20, 20, 28), (21, 19, 23), (16, 17, 9), (32, 24, 12)])
+def row_masks(phi4, SX):
+    """pmask of phi_mask_kernel: per row (z, y) and byte b, bit x & 7 where phi
+    is exactly +1 (P) and exactly -1 (M); x = 8b + bit, zero past the row end."""
+    NZ, NY, NX = phi4.shape
+    pad = np.zeros((NZ, NY, 8 * SX))
+    pad[:, :, :NX] = phi4
+    valid = np.zeros(8 * SX, bool)
+    valid[:NX] = True
+    bits = (1 << np.arange(8)).astype(np.uint32)
+    P = ((pad == 1.0) & valid).reshape(NZ, NY, SX, 8) @ bits
+    M = ((pad == -1.0) & valid).reshape(NZ, NY, SX, 8) @ bits
+    return P.astype(np.uint32), M.astype(np.uint32)
+
+
+def listed_rows(P, M, C):
+    """active_nodes_kernel's bitwise rule: candidates (C) whose 19-node stencil
+    is not all +1 and not all -1, per row byte (rows 1 .. N-2 only)."""
+    NZ, NY, SX = P.shape
+
+    def window(A):   # bytes b-1, b, b+1 at bits 0, 8, 16
+        lo = np.zeros_like(A)
+        hi = np.zeros_like(A)
+        lo[:, :, 1:] = A[:, :, :-1]
+        hi[:, :, :-1] = A[:, :, 1:]
+        return lo | (A << 8) | (hi << 16)
+
+    out = np.zeros_like(P)
+    zs, ys = slice(1, NZ - 1), slice(1, NY - 1)
+    for A, acc in ((P, "up"), (M, "um")):
+        w = window(A)
+        u = np.full((NZ - 2, NY - 2, SX), 0xFFFFFFFF, np.uint32)
+        for dz, dy in ((0, 0), (0, -1), (0, 1), (-1, 0), (1, 0)):
+            ww = w[1 + dz:NZ - 1 + dz, 1 + dy:NY - 1 + dy]
+            u &= (ww >> 7) & (ww >> 8) & (ww >> 9)
+        for dz, dy in ((-1, -1), (-1, 1), (1, -1), (1, 1)):
+            u &= A[1 + dz:NZ - 1 + dz, 1 + dy:NY - 1 + dy]
+        if acc == "up":
+            up = u
+        else:
+            um = u
+    out[zs, ys] = C[zs, ys] & ~(up | um) & 0xFF
+    return out
+
+
+@pytest.mark.parametrize("n", [(20, 20, 28), (21, 19, 23), (16, 17, 9), (33, 24, 12)])
 @pytest.mark.parametrize("sharp", [False, True], ids=["diffuse", "sharp"])
-def test_skipped_nodes_have_uniform_stencils(n, sharp):
+def test_row_masks_list_exactly_the_non_uniform_stencils(n, sharp):
     nx, ny, nz = n
     phi4 = random_phase(n, seed=nx * 1000 + ny * 10 + nz, sharp=sharp)
-    codes = brick_codes(phi4)
-    assert codes.shape == ((nz + 9) // 2, (ny + 9) // 2, (nx + 9) // 2)
-    act = active_blocks(codes, n)
-    seen = np.zeros((nz + 4, ny + 4, nx + 4), dtype=np.int32)   # nodes -1 .. n+2
-    skipped_nonzero = 0
-    for cz in range(act.shape[0]):
-        for cy in range(act.shape[1]):
-            for cx in range(act.shape[2]):
-                for e in range(8):
-                    i, j, k = 2 * cx - 2 + (e & 1), 2 * cy - 2 + ((e >> 1) & 1), 2 * cz - 2 + (e >> 2)
-                    if not (-1 <= i <= nx + 2 and -1 <= j <= ny + 2 and -1 <= k <= nz + 2):
-                        continue
-                    seen[k + 1, j + 1, i + 1] += 1
-                    # the block's bricks cover the node's stencil
-                    for q in range(19):
-                        si, sj, sk = i + EX[q] + 3, j + EY[q] + 3, k + EZ[q] + 3    # s4-local
-                        assert cx <= si // 2 <= cx + 1 and cy <= sj // 2 <= cy + 1 and cz <= sk // 2 <= cz + 1
-                    if not act[cz, cy, cx]:
-                        c = phi4[k + 3, j + 3, i + 3]
-                        vals = [phi4[k + 3 + EZ[q], j + 3 + EY[q], i + 3 + EX[q]] for q in range(19)]
-                        skipped_nonzero += any(v != c for v in vals)
-    assert np.all(seen == 1), "every node of [-1, n+2]^3 in exactly one block"
-    assert skipped_nonzero == 0
-    # the fields are not trivial: both kinds of blocks occur
-    assert act.any() and not act.all()
+    rng = np.random.default_rng(nx + ny)
+    SX = ((nx + 9) // 2 + 3) // 4
+    assert 8 * SX >= nx + 8
+    # candidates: a random subset of [-1, n+2]^3 (walls_type <= 0), s4 x 2 .. n+5
+    cand = np.zeros(phi4.shape, bool)
+    cand[2:nz + 6, 2:ny + 6, 2:nx + 6] = rng.random((nz + 4, ny + 4, nx + 4)) < 0.8
+    padc = np.zeros(phi4.shape[:2] + (8 * SX,), bool)
+    padc[:, :, :nx + 8] = cand
+    C = (padc.reshape(nz + 8, ny + 8, SX, 8) @ (1 << np.arange(8))).astype(np.uint32)
+    P, M = row_masks(phi4, SX)
+    L = listed_rows(P, M, C)
+    listed = ((L[..., None] >> np.arange(8)) & 1).astype(bool).reshape(nz + 8, ny + 8, 8 * SX)[:, :, :nx + 8]
+    # the direct rule
+    uni = np.zeros(phi4.shape, bool)
+    core = (slice(1, nz + 7), slice(1, ny + 7), slice(1, nx + 7))
+    for val in (1.0, -1.0):
+        u = np.ones((nz + 6, ny + 6, nx + 6), bool)
+        for q in range(19):
+            u &= phi4[1 + EZ[q]:nz + 7 + EZ[q], 1 + EY[q]:ny + 7 + EY[q], 1 + EX[q]:nx + 7 + EX[q]] == val
+        uni[core] |= u
+    assert np.array_equal(listed, cand & ~uni)
+    assert listed.any() and (cand & uni).any()
 
 
 # ---------------------------------------------------------------------------
@@ -238,9 +258,13 @@ def test_super_blocks_cover_every_change(n, sharp):
     changed = np.argwhere(codes_old != codes_new)
     for bz, by, bx in changed:
         assert live[bz // 4, by // 4, bx // 4], ("brick", bz, by, bx)
-    act_old, act_new = active_blocks(codes_old, n), active_blocks(codes_new, n)
-    for cz, cy, cx in np.argwhere(act_old != act_new):
-        assert live[cz // 4, cy // 4, cx // 4], ("block", cz, cy, cx)
+    # listing decisions of the node pass (row masks, every node a candidate)
+    SX = ((nx + 9) // 2 + 3) // 4
+    C = np.full((nz + 8, ny + 8, SX), 0xFF, np.uint32)
+    L_old = listed_rows(*row_masks(phi, SX), C)
+    L_new = listed_rows(*row_masks(new, SX), C)
+    for z, y, b in np.argwhere(L_old != L_new):
+        assert live[(z // 2) // 4, (y // 2) // 4, b], ("listing", z, y, b)
     assert len(changed) > 0
     # the static non-uniform solid and ghost phi does not keep every
     # super-block live (it would, counted over all nodes)
