@@ -484,11 +484,16 @@ def main():
     barrier(dist)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    ctx.upload_fields(**host)
+    ctx.upload_fields(**host)      # blocks until the state is on the device
+    t1 = time.perf_counter()
     for s in range(e2e_steps):
         ctx.step(nt + s)
+    ctx.sync()
+    t2 = time.perf_counter()
     out = ctx.download(out=host)   # into the same pinned buffers
     e2e_s = time.perf_counter() - t0
+    e2e_parts = {"upload_s": round(t1 - t0, 5), "steps_s": round(t2 - t1, 5),
+                 "download_s": round(time.perf_counter() - t2, 5)}
     barrier(dist)
     nt += e2e_steps
     e2e_s = max_over_ranks(dist, e2e_s)
@@ -538,6 +543,8 @@ def main():
                           "algorithmic_bytes_per_step": step_bytes, "gradient_ms": round(gradient_ms, 5)},
         "e2e": {"value": round(e2e_value, 2), "unit": "MLUPS", "steps": e2e_steps,
                 "h2d_bytes_per_step": int(h2d / e2e_steps), "d2h_bytes_per_step": int(d2h / e2e_steps),
+                "parts": e2e_parts, "h2d_gbs": round(h2d / e2e_parts["upload_s"] / 1e9, 1),
+                "d2h_gbs": round(d2h / e2e_parts["download_s"] / 1e9, 1),
                 "how": "mflbm_upload_fields from pinned host buffers, mflbm_step per step, mflbm_download_fields"},
         "gpu_launches": int(launches_per_step * args.steps),
         "clocks": clocks,
