@@ -247,9 +247,9 @@ int build_lists(mflbm_context* c) {
         MFLBM_CUDA(cudaMalloc(&d.slist, sizeof(uint32_t) * std::max<ll>(1, d.n_cn_ext)));
         MFLBM_CUDA(cudaMalloc(&d.nlist, sizeof(uint32_t) * std::max<ll>(1, d.n_norm)));
         MFLBM_CUDA(cudaMalloc(&d.smask, sizeof(uint32_t) * nmask));
-        MFLBM_CUDA(cudaMalloc(&d.gcount, 4 * sizeof(int)));
+        MFLBM_CUDA(cudaMalloc(&d.gcount, 8 * sizeof(int)));
         MFLBM_CUDA(cudaMemset(d.smask, 0, sizeof(uint32_t) * nmask));
-        MFLBM_CUDA(cudaMemset(d.gcount, 0, 4 * sizeof(int)));
+        MFLBM_CUDA(cudaMemset(d.gcount, 0, 8 * sizeof(int)));
     }
     if (d.phi_prev) cudaFree(d.phi_prev);
     d.phi_prev = nullptr;
@@ -434,7 +434,7 @@ std::vector<Span> state_spans(mflbm_context* c) {
                              {d.olist, sizeof(uint32_t) * std::max<ll>(1, d.n_norm)},
                              {d.slist, sizeof(uint32_t) * std::max<ll>(1, d.n_cn_ext)},
                              {d.smask, sizeof(uint32_t) * (size_t)(g.n2() / 32 + 1)},
-                             {d.gcount, 4 * sizeof(int)}};
+                             {d.gcount, 8 * sizeof(int)}};
 }
 int save_state(mflbm_context* c, SavedState* s) {
     const std::vector<Span> st = state_spans(c);
@@ -821,6 +821,21 @@ int mflbm_init_flow_mrt(mflbm_context* c, const void* rho, const void* u, const 
     return init_flow_entry(c, rho, u, v, w, 1);
 }
 
+// The device address of a page-locked host range [p, p + bytes) (allocated
+// or registered with CUDA, so the device can read and write it over the host
+// link), or nullptr for other memory.
+void* device_view(const void* p, size_t bytes) {
+    if (!p || !bytes) return nullptr;
+    cudaPointerAttributes a, b;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess || a.type != cudaMemoryTypeHost || !a.devicePointer ||
+        cudaPointerGetAttributes(&b, (const char*)p + bytes - 1) != cudaSuccess || b.type != cudaMemoryTypeHost ||
+        (const char*)b.devicePointer - (const char*)a.devicePointer != (ptrdiff_t)(bytes - 1)) {
+        cudaGetLastError();   // an unregistered pointer may leave an error behind
+        return nullptr;
+    }
+    return a.devicePointer;
+}
+
 int mflbm_upload_fields(mflbm_context* c, const void* pdf, const void* phi, const void* cn_x, const void* cn_y,
                         const void* cn_z, const void* c_norm, const void* curv, const void* W_in,
                         const void* f_convec_bc, const void* g_convec_bc, const void* phi_convec_bc) {
@@ -830,11 +845,17 @@ int mflbm_upload_fields(mflbm_context* c, const void* pdf, const void* phi, cons
     const Grid& g = d.g;
     const size_t T = tsize(c);
     cudaStream_t s = c->stream;
-    int rc = ensure_staging(c);
+    int rc = request_full_pass(c);
     if (rc != MFLBM_OK) return rc;
-    if ((rc = request_full_pass(c)) != MFLBM_OK) return rc;
-    MFLBM_CUDA(cudaMemcpyAsync(d.staging, pdf, T * g.n1() * 38, cudaMemcpyHostToDevice, s));
-    if ((rc = convert_populations(*c, true)) != MFLBM_OK) return rc;
+    // populations: page-locked host memory is read by the relayout kernel
+    // directly; other memory goes through the staging buffer
+    if (void* dv = device_view(pdf, T * g.n1() * 38)) {
+        if ((rc = convert_populations(*c, true, dv)) != MFLBM_OK) return rc;
+    } else {
+        if ((rc = ensure_staging(c)) != MFLBM_OK) return rc;
+        MFLBM_CUDA(cudaMemcpyAsync(d.staging, pdf, T * g.n1() * 38, cudaMemcpyHostToDevice, s));
+        if ((rc = convert_populations(*c, true)) != MFLBM_OK) return rc;
+    }
     MFLBM_CUDA(cudaMemcpyAsync(d.phi, phi, T * g.n4(), cudaMemcpyHostToDevice, s));
     if (W_in) MFLBM_CUDA(cudaMemcpyAsync(d.W_in, W_in, T * g.plane1(), cudaMemcpyHostToDevice, s));
     const bool have_grad = cn_x && cn_y && cn_z && c_norm && curv;
@@ -867,17 +888,20 @@ int mflbm_download_fields(mflbm_context* c, void* pdf, void* phi, void* cn_x, vo
     const Grid& g = d.g;
     const size_t T = tsize(c);
     cudaStream_t s = c->stream;
+    // populations: written by the relayout kernel straight into page-locked
+    // host memory, else through the staging buffer
+    void* pdf_direct = pdf ? device_view(pdf, T * g.n1() * 38) : nullptr;
     if (pdf) {
-        int rc = ensure_staging(c);
-        if (rc != MFLBM_OK) return rc;
-        if ((rc = convert_populations(*c, false)) != MFLBM_OK) return rc;
+        int rc = MFLBM_OK;
+        if (!pdf_direct && (rc = ensure_staging(c)) != MFLBM_OK) return rc;
+        if ((rc = convert_populations(*c, false, pdf_direct)) != MFLBM_OK) return rc;
     }
     if (cn_x || cn_y || cn_z || c_norm || curv) {
         int rc = export_arrays(c);
         if (rc != MFLBM_OK) return rc;
     }
     struct { void* dst; const void* src; size_t n; } cp[] = {
-        {pdf, d.staging, T * g.n1() * 38}, {phi, d.phi, T * g.n4()}, {cn_x, d.cn_x, T * g.n2()}, {cn_y, d.cn_y, T * g.n2()},
+        {pdf_direct ? nullptr : pdf, d.staging, T * g.n1() * 38}, {phi, d.phi, T * g.n4()}, {cn_x, d.cn_x, T * g.n2()}, {cn_y, d.cn_y, T * g.n2()},
         {cn_z, d.cn_z, T * g.n2()}, {c_norm, d.c_norm, T * g.n2()}, {curv, d.curv, T * g.n1()},
         {f_convec_bc, d.f_cv, T * g.plane1() * 19}, {g_convec_bc, d.g_cv, T * g.plane1() * 19},
         {phi_convec_bc, d.phi_cv, T * g.plane1()}};

@@ -21,8 +21,8 @@
 // so are the extrapolated normals of solid nodes whose fluid neighbours all
 // have zero records.  The pipeline keeps two lists between passes: the nodes
 // whose record is non-zero (olist) and the solid nodes that received a normal
-// (slist).  A pass resets those records to zero, lists the fluid nodes of the
-// 2x2x2 node blocks whose stencils reach a non-uniform phi brick (nlist),
+// (slist).  A pass resets those records to zero, lists the fluid nodes whose
+// stencil is not all +1 or all -1 (nlist, from per-row bit masks of phi),
 // recomputes the normals of those nodes only (rebuilding olist and, from the
 // new interface nodes' solid neighbours, slist), extrapolates to them and
 // computes the curvature at the fluid nodes of olist.  Every record outside
@@ -54,9 +54,9 @@ template <class T> struct GradArgs {
     const uint32_t* wmask; // s2: bit q where x + e_q is a solid boundary node (walls_type 2) of [0, n+1]^3
     uint32_t* olist;       // packed coordinates of the nodes whose record is non-zero (interface flag set)
     uint32_t* slist;       // packed coordinates of the solid nodes whose normal may be non-zero
-    uint32_t* nlist;       // packed fluid nodes of this pass's active node blocks
+    uint32_t* nlist;       // packed fluid nodes whose normal this pass recomputes
     uint32_t* smask;       // bit per s2 node: the solid node is in slist
-    int* gcount;           // [0] olist, [1] slist, [2] nlist lengths
+    int* gcount;           // [0] olist, [1] slist, [2] nlist lengths; [4], [5] the previous pass's [0], [1]
     T *cnx, *cny, *cnz, *cnorm, *curv;  // reference-layout arrays (export / pack)
     const uint2* l_phi;
     const uint32_t* l_fluid;
@@ -130,20 +130,9 @@ __device__ __forceinline__ void extrapolate_phi_at(const GradArgs<T>& a, int t) 
     a.phi[n] = s / ws;
 }
 
-// the solid boundary nodes of this pass's super-blocks (one block per super-block)
-template <class T>
-__global__ void __launch_bounds__(256) extrapolate_phi_kernel(const GradArgs<T> a) {
-    pdl_wait();
-    const int nl = min(*a.live_n, a.SX * a.SY * a.SZ);
-    for (int w = blockIdx.x; w < nl; w += gridDim.x) {
-        const uint32_t sb = a.sblive[w];
-        for (int t = a.phioff[sb] + threadIdx.x; t < a.phioff[sb + 1]; t += blockDim.x) extrapolate_phi_at<T>(a, t);
-    }
-}
-
 // ---------------------------------------------------------------------------
-// Super-blocks.  The dense passes (phi on solid boundary nodes, phi brick
-// codes, node listing) run only over super-blocks of 4 x 4 x 4 phi bricks
+// Super-blocks.  The dense passes (phi on solid boundary nodes, phi row
+// masks, node listing) run only over super-blocks of 4 x 4 x 4 phi bricks
 // (8^3 nodes of the s4 lattice) where phi can have changed since the last
 // pass.  Away from the interfaces phi is exactly +1 or -1 and a fluid node
 // keeps its value exactly as long as its fluid D3Q19 neighbours hold the
@@ -155,14 +144,14 @@ __global__ void __launch_bounds__(256) extrapolate_phi_kernel(const GradArgs<T> 
 // super-block with fluid of the other.  A fluid node whose phi can change is
 // then in a flagged super-block or one node from one.  Solid and ghost nodes
 // do not count in the codes: the phi of a solid node is extrapolated from
-// fluid nodes within two nodes, and a brick code and a node block's activity
+// fluid nodes within two nodes, and a node's row-mask bits and listing
 // depend on phi within one node, so every change lies within four nodes of a
 // flagged super-block: inside the 3 x 3 x 3 super-blocks around it, which
 // this pass processes.  Super-blocks at open (inlet / outlet) or periodic
 // faces, whose ghost layers the boundary updates rewrite every step, are
 // always processed, and so is everything after the host set or uploaded a
 // state.
-// Elsewhere phi, the brick codes and the zero records are those of the last
+// Elsewhere phi, the row masks and the zero records are those of the last
 // pass that processed the super-block.
 // ---------------------------------------------------------------------------
 template <class T>
@@ -187,22 +176,21 @@ __global__ void __launch_bounds__(256) sb_live_kernel(const GradArgs<T> a) {
                 }
         live = live || any != 0;
     }
-    if (s == 0) *a.live_next = 0;
+    if (s == 0) {
+        *a.live_next = 0;
+        // the node lists restart; the previous olist / slist lengths stay for
+        // the reset of their records (clear_records)
+        a.gcount[4] = a.gcount[0];
+        a.gcount[5] = a.gcount[1];
+        a.gcount[0] = a.gcount[1] = a.gcount[2] = 0;
+    }
     warp_append(live, (uint32_t)s, a.sblive, a.live_n, a.SX * a.SY * a.SZ);
 }
 
-// sbact of every super-block from this pass's codes; consumes the
-// every-super-block request, and restarts the node lists (the brick-code
-// pass has reset the previous lists' records)
+// sbact of super-block s from this pass's codes (run by the node-listing
+// kernel over every super-block)
 template <class T>
-__global__ void __launch_bounds__(256) sb_active_kernel(const GradArgs<T> a) {
-    pdl_wait();
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s == 0) {
-        a.sbinfo[1] = 0;
-        if (a.n_norm) a.gcount[0] = a.gcount[1] = a.gcount[2] = 0;
-    }
-    if (s >= a.SX * a.SY * a.SZ) return;
+__device__ __forceinline__ void sb_active_at(const GradArgs<T>& a, int s) {
     const int sx = s % a.SX, sy = (s / a.SX) % a.SY, sz = s / (a.SX * a.SY);
     const int8_t c = a.sbcode[s];
     unsigned seen = 0;   // bit c: code c occurs in the 3 x 3 x 3 super-blocks around
@@ -286,7 +274,7 @@ __device__ __forceinline__ T iso4_dz(const ModelConsts<T>& c, const T* F, int n,
 // Grid-stride over both lists, run by the threads of the brick pass.
 template <class T>
 __device__ __forceinline__ void clear_records(const GradArgs<T>& a, int tid, int nthreads) {
-    const int no = min(a.gcount[0], a.n_norm), ns = min(a.gcount[1], a.n_cn);
+    const int no = min(a.gcount[4], a.n_norm), ns = min(a.gcount[5], a.n_cn);
     typename Vec4<T>::type z;
     z.x = T(0); z.y = T(0); z.z = T(0); z.w = T(0);
     for (int p = tid; p < no + ns; p += nthreads) {
@@ -300,14 +288,16 @@ __device__ __forceinline__ void clear_records(const GradArgs<T>& a, int tid, int
     }
 }
 
-// Row masks of the s4 lattice: for row (y, z) and byte b (x = 8b .. 8b + 7,
-// the x extent of super-block column b), pmask holds bit x & 7 where phi is
+// Per super-block of this pass (one block of 64 threads): the phi of its
+// solid boundary nodes (extrapolated from fluid neighbours, which this
+// kernel does not write, so the super-blocks are independent), then the row
+// masks of the s4 lattice: for row (y, z) and byte b (x = 8b .. 8b + 7, the
+// x extent of super-block column b), pmask holds bit x & 7 where phi is
 // exactly +1 (low byte) and exactly -1 (high byte).  Away from interfaces
 // phi is exactly +-1 (one component is exactly zero), so most stencils are
-// of one value.  One block of 64 threads per super-block of this pass (one
-// row of 8 nodes per thread); the super-block's fluid code follows from the
-// rows' fluid masks (fmask).  The threads also reset the records of the
-// previous pass's lists.
+// of one value.  One row of 8 nodes per thread; the super-block's fluid code
+// follows from the rows' fluid masks (fmask).  The threads also reset the
+// records of the previous pass's lists.
 template <class T>
 __global__ void __launch_bounds__(64) phi_mask_kernel(const GradArgs<T> a) {
     pdl_wait();
@@ -317,6 +307,12 @@ __global__ void __launch_bounds__(64) phi_mask_kernel(const GradArgs<T> a) {
     const int ly = threadIdx.x & 7, lz = threadIdx.x >> 3;
     for (int w = blockIdx.x; w < nl; w += gridDim.x) {
         const int sb = (int)a.sblive[w];
+        // phi of the super-block's solid boundary nodes (from fluid phi only),
+        // then its rows
+        if (a.n_phi) {
+            for (int t = a.phioff[sb] + threadIdx.x; t < a.phioff[sb + 1]; t += blockDim.x) extrapolate_phi_at<T>(a, t);
+            __syncthreads();
+        }
         const int sx = sb % a.SX, y = 8 * ((sb / a.SX) % a.SY) + ly, z = 8 * (sb / (a.SX * a.SY)) + lz;
         unsigned F = 0, P = 0, M = 0;
         if (y < NY && z < NZ) {
@@ -357,7 +353,9 @@ __device__ __forceinline__ void mask_window(const uint16_t* pm, ll r, int b, int
 // bits 8..15), w >> 8, w >> 7 and w >> 9 hold x, x - 1 and x + 1; the
 // stencil is x +- 1 of row (y, z), x and x +- 1 of rows (y +- 1, z) and
 // (y, z +- 1), and x of rows (y +- 1, z +- 1).  Appended to nlist (one atomic
-// per warp).  One block of 64 threads per super-block of this pass.
+// per warp).  One block of 64 threads per super-block of this pass.  The
+// same launch first flags every super-block for the next pass (sb_active_at:
+// it needs the codes of this pass, which the mask kernel has written).
 template <class T>
 __global__ void __launch_bounds__(64) active_nodes_kernel(const GradArgs<T> a) {
     pdl_wait();
@@ -365,6 +363,10 @@ __global__ void __launch_bounds__(64) active_nodes_kernel(const GradArgs<T> a) {
     const int nl = min(*a.live_n, a.SX * a.SY * a.SZ);
     const int ly = threadIdx.x & 7, lz = threadIdx.x >> 3;
     const ll RY = a.SX, RZ = (ll)a.SX * NY;   // row strides of the masks
+    const int nsb = a.SX * a.SY * a.SZ;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nsb; s += gridDim.x * blockDim.x) sb_active_at<T>(a, s);
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.sbinfo[1] = 0;   // the every-super-block request is consumed
+    if (!a.n_norm) return;
     for (int w = blockIdx.x; w < nl; w += gridDim.x) {
         const int sb = (int)a.sblive[w];
         const int sx = sb % a.SX, y = 8 * ((sb / a.SX) % a.SY) + ly, z = 8 * (sb / (a.SX * a.SY)) + lz;
@@ -676,7 +678,6 @@ int launch_gradient(mflbm_context& c) {
     // the list passes run one wave of resident blocks (grid-stride loops: the
     // list lengths are known only on the device; blocks beyond the resident
     // ones would start only after the first wave has walked the whole list)
-    const int lb = 256;
     auto wave = [&](const void* kernel, int bs) {
         int per_sm = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, bs, 0) != cudaSuccess || per_sm < 1)
@@ -686,22 +687,19 @@ int launch_gradient(mflbm_context& c) {
     const int nsb = a.SX * a.SY * a.SZ;
     // this pass's super-blocks
     if ((rc = launch_pdl("sb_live", sb_live_kernel<T>, grid_for(nsb, 64), 64, s, a)) != MFLBM_OK) return rc;
-    if (a.n_phi &&
-        (rc = launch_pdl("extrapolate_phi", extrapolate_phi_kernel<T>,
-                         wave((const void*)extrapolate_phi_kernel<T>, tn.extrapolate), tn.extrapolate, s, a)) != MFLBM_OK)
+    // solid phi + row masks + super-block codes + reset of the previous lists' records
+    if ((rc = launch_pdl("phi_mask", phi_mask_kernel<T>, wave((const void*)phi_mask_kernel<T>, 64), 64, s, a)) !=
+        MFLBM_OK)
         return rc;
-    // row masks + reset of the previous lists' records
-    if (a.n_norm && (rc = launch_pdl("phi_mask", phi_mask_kernel<T>, wave((const void*)phi_mask_kernel<T>, 64), 64,
-                                     s, a)) != MFLBM_OK)
-        return rc;
-    if ((rc = launch_pdl("sb_active", sb_active_kernel<T>, grid_for(nsb, 64), 64, s, a)) != MFLBM_OK) return rc;
+    // flags for the next pass + node listing
+    rc = launch_pdl("active_nodes", active_nodes_kernel<T>, wave((const void*)active_nodes_kernel<T>, 64), 64, s, a);
+    if (rc != MFLBM_OK) return rc;
     if (a.n_norm) {
-        rc = launch_pdl("active_nodes", active_nodes_kernel<T>, wave((const void*)active_nodes_kernel<T>, 64), 64, s, a);
-        if (rc != MFLBM_OK) return rc;
         rc = launch_pdl("normals", normals_kernel<T>, wave((const void*)normals_kernel<T>, tn.normals), tn.normals, s, a);
         if (rc != MFLBM_OK) return rc;
         if (a.n_cn && (rc = launch_pdl("extrapolate_normal", extrapolate_normal_kernel<T>,
-                                       wave((const void*)extrapolate_normal_kernel<T>, lb), lb, s, a)) != MFLBM_OK)
+                                       wave((const void*)extrapolate_normal_kernel<T>, tn.extrapolate), tn.extrapolate,
+                                       s, a)) != MFLBM_OK)
             return rc;
     }
     if (!a.n_fluid) return MFLBM_OK;

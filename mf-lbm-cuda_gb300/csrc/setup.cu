@@ -762,6 +762,8 @@ int permute_impl(mflbm_context& c, const int* perm_dev, void** out) {
 }
 
 // Reference layout (f1) <-> brick layout, one thread per (node, direction).
+// f1 is the staging buffer, or page-locked host memory that the kernel reads
+// or writes over the host link directly.
 template <class T, class E>
 __global__ void f1_to_bricks(Grid g, PopView<T, E> P, const T* f1) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, kq = blockIdx.z;
@@ -782,12 +784,13 @@ __global__ void bricks_to_f1(Grid g, PopView<T, E> P, T* f1) {
 }
 
 template <class T, class E>
-int convert_t(mflbm_context& c, bool to_bricks) {
+int convert_t(mflbm_context& c, bool to_bricks, void* f1) {
     DeviceState& d = c.d;
     const Grid g = d.g;
     const dim3 grid(grid_for(g.nx + 2, 128), g.ny + 2, (g.nz + 2) * 19);
-    if (to_bricks) f1_to_bricks<T, E><<<grid, 128, 0, c.stream>>>(g, pop_view<T, E>(d), (const T*)d.staging);
-    else bricks_to_f1<T, E><<<grid, 128, 0, c.stream>>>(g, pop_view<T, E>(d), (T*)d.staging);
+    T* src = (T*)(f1 ? f1 : d.staging);
+    if (to_bricks) f1_to_bricks<T, E><<<grid, 128, 0, c.stream>>>(g, pop_view<T, E>(d), src);
+    else bricks_to_f1<T, E><<<grid, 128, 0, c.stream>>>(g, pop_view<T, E>(d), src);
     return after_launch(to_bricks ? "f1_to_bricks" : "bricks_to_f1");
 }
 
@@ -800,7 +803,7 @@ int convert_t(mflbm_context& c, bool to_bricks) {
      : c.params.storage == MFLBM_STORE_BF16   ? fn<float, __nv_bfloat16>(__VA_ARGS__)   \
                                               : fn<float, float>(__VA_ARGS__))
 
-int convert_populations(mflbm_context& c, bool to_bricks) { return MFLBM_POP(convert_t, c, to_bricks); }
+int convert_populations(mflbm_context& c, bool to_bricks, void* f1) { return MFLBM_POP(convert_t, c, to_bricks, f1); }
 int relayout_populations(mflbm_context& c, const Bricks& to, void** out) { return relayout_impl(c, to, out); }
 int permute_records(mflbm_context& c, const int* perm_dev, void** out) { return permute_impl(c, perm_dev, out); }
 

@@ -16,8 +16,9 @@ int monitor_noalloc(mflbm_context& c, int nex_in, int nex_out, mflbm_monitor* ou
 int write_vtk(mflbm_context& c, int vtk_type, int precision_cmd, const char* path);
 int write_walls_vtk(mflbm_context& c, const char* path);
 int write_checkpoint(mflbm_context& c, int ntime, const char* path);
-// copy populations between d.staging (reference f1 layout) and d.pdf (brick layout)
-int convert_populations(mflbm_context& c, bool to_bricks);
+// copy populations between the reference f1 layout (d.staging, or `f1`:
+// page-locked host memory the device can address) and d.pdf (brick layout)
+int convert_populations(mflbm_context& c, bool to_bricks, void* f1 = nullptr);
 // the populations in the tile shape `to`, in a new device buffer (*out); d.pdf is unchanged
 int relayout_populations(mflbm_context& c, const Bricks& to, void** out);
 // the collision records in a new fluid-list order, dst[t] = aux[perm[t]], in a new buffer
