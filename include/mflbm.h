@@ -449,6 +449,12 @@ int mflbm_unet_set_params(mflbm_unet* net, const float* params);
 int mflbm_unet_conv_check(int D, int H, int W, int cin, int cout, const float* x,
                           const float* w, const float* b, int relu, const float* gy,
                           float* y, float* gx, float* gw, float* gb);
+/* Bound of the tensor-core convolutions' waits for their pipeline stages,
+ * in mbarrier polls (default 1048576).  A wait that runs out makes the call
+ * return MFLBM_E_CUDA; the copies and MMAs still in flight are waited for
+ * with the default bound before tensor memory is freed, so the device stays
+ * usable.  0 makes every stage wait run out (a test of that path). */
+int mflbm_unet_set_wait_limit(unsigned int polls);
 
 /* ---- introspection ---------------------------------------------------- */
 /* Counts of lattice nodes: [0] fluid nodes in [1,n]^3, [1] all nodes n^3. */

@@ -627,6 +627,11 @@ int mflbm_unet_gradients(mflbm_unet* n, const float* x, const float* target, con
 // One convolution and its gradients on host arrays (checks against a CPU
 // restatement): x D*H*W*cin, w cout*27*cin, b cout, gy D*H*W*cout, all FP32
 // (rounded to BF16 on the device); outputs y (FP32 before rounding), gx, gw, gb.
+int mflbm_unet_set_wait_limit(unsigned int polls) {
+    MFLBM_CUDA(cudaMemcpyToSymbol(U::g_tc_stage_wait, &polls, sizeof(polls)));
+    return MFLBM_OK;
+}
+
 int mflbm_unet_conv_check(int D, int H, int W, int cin, int cout, const float* x, const float* w, const float* b,
                           int relu, const float* gy, float* y, float* gx, float* gw, float* gb) {
     if (cin % 16 || cout % 16 || cin <= 0 || cout <= 0)

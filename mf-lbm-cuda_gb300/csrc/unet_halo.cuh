@@ -31,9 +31,9 @@
 // inputs, so that two CTAs fit on a multiprocessor) it overlaps the
 // epilogue.  The epilogue reads the accumulators with tcgen05.ld (one row
 // per thread), adds the bias, applies the ReLU and writes BF16 (and FP32)
-// outputs.  Every wait
-// is bounded: on a time-out the kernel records an error, waits (bounded) for
-// its copies and MMAs in flight, frees its tensor memory and returns.
+// outputs.  Every wait is bounded: on a time-out the kernel records an
+// error, waits (bounded) for its copies and MMAs in flight, frees its tensor
+// memory and returns.
 #pragma once
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -162,8 +162,8 @@ __global__ void __launch_bounds__(128) conv3d_halo_tc_kernel(const __grid_consta
         if (tid == 0) {
             // two buffers: the next tile's (its MMAs, of tile i - 1, are done)
             if (nbuf == 2 && i + 1 < mine) { load(i + 1); ++loads; }
-            if (!wready) ok = wready = mbar_wait(&bars[3], 0);
-            if (ok && !mbar_wait(&bars[i % nbuf], (i / nbuf) & 1)) ok = false;
+            if (!wready) ok = wready = mbar_wait_stage(&bars[3], 0);
+            if (ok && !mbar_wait_stage(&bars[i % nbuf], (i / nbuf) & 1)) ok = false;
             if (ok) {
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 // descriptors advance in 16-byte units (start address field)

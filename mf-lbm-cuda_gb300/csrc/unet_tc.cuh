@@ -69,11 +69,25 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
+// Bound of the waits for pipeline stages (polls; mflbm_unet_set_wait_limit
+// lowers it to exercise the error path).  The waits for copies and MMAs
+// still in flight on the way out always use TC_WAIT_LIMIT, so a short bound
+// never frees tensor or shared memory under an operation.
+__device__ uint32_t g_tc_stage_wait = TC_WAIT_LIMIT;
+
 // bounded wait for the phase of the given parity; false on time-out
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-    for (uint32_t i = 0; i < TC_WAIT_LIMIT; ++i)
+__device__ __forceinline__ bool mbar_wait_for(uint64_t* bar, uint32_t parity, uint32_t limit) {
+    for (uint32_t i = 0; i < limit; ++i)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
+}
+// the drain waits (full bound)
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    return mbar_wait_for(bar, parity, TC_WAIT_LIMIT);
+}
+// the waits of the pipeline stages
+__device__ __forceinline__ bool mbar_wait_stage(uint64_t* bar, uint32_t parity) {
+    return mbar_wait_for(bar, parity, *(volatile uint32_t*)&g_tc_stage_wait);
 }
 
 __device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
@@ -122,7 +136,7 @@ __device__ __forceinline__ uint32_t tc_setup(uint32_t* tslot, uint64_t* bars, ui
 // slots polling; false (for every thread) on a time-out
 __device__ __forceinline__ bool tc_wait_stage(uint64_t* bar, uint32_t parity) {
     bool ok = true;
-    if (threadIdx.x == 0) ok = mbar_wait(bar, parity);
+    if (threadIdx.x == 0) ok = mbar_wait_stage(bar, parity);
     return __syncthreads_and(ok);
 }
 

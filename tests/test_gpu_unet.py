@@ -40,6 +40,30 @@ def test_halo_conv_forward_and_gradients_match_oracle(mflbm_lib, shape, cin, cou
     _check_conv(shape, cin, cout, relu)
 
 
+@pytest.mark.parametrize("shape,cin,cout", [((5, 7, 9), 16, 16), ((40, 30, 20), 32, 32)], ids=["gather", "halo"])
+def test_stage_wait_that_runs_out_is_reported(mflbm_lib, shape, cin, cout):
+    """A bound of 0 polls makes every pipeline-stage wait of the tensor-core
+    convolutions run out (the gather kernels and, at the second shape, the
+    halo-tiled kernel): the call fails with the time-out error, the kernels
+    still wait (with the full bound) for their copies and MMAs before freeing
+    tensor memory, and with the default bound the next call is exact again."""
+    from mflbm import lib
+    L = lib.load()
+    rng = np.random.default_rng(5)
+    D, H, W = shape
+    x = rng.normal(size=(D, H, W, cin)).astype(np.float32)
+    w = (rng.normal(size=(cout, 27, cin)) / np.sqrt(27 * cin)).astype(np.float32)
+    b = rng.normal(size=cout).astype(np.float32)
+    gy = rng.normal(size=(D, H, W, cout)).astype(np.float32)
+    lib.check(L.mflbm_unet_set_wait_limit(0), "mflbm_unet_set_wait_limit")
+    try:
+        with pytest.raises(lib.MflbmError, match="timed out"):
+            unet.conv_check(x, w, b, gy, relu=False)
+    finally:
+        lib.check(L.mflbm_unet_set_wait_limit(1 << 20), "mflbm_unet_set_wait_limit")
+    _check_conv(shape, cin, cout, False)
+
+
 def _check_conv(shape, cin, cout, relu):
     rng = np.random.default_rng(cin + cout)
     D, H, W = shape
