@@ -368,6 +368,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the 16-bit storage and batch measurements")
     ap.add_argument("--no-tune", action="store_true", help="keep the default block sizes (no autotuning)")
+    ap.add_argument("--storage", default="native", choices=["native", "f16", "bf16"],
+                    help="population storage of the main run (default: FP32 populations; f16 / bf16 for "
+                         "one-kernel captures of the 16-bit collision)")
     ap.add_argument("--no-reference-cuda", action="store_true",
                     help="skip the reference's own CUDA program (built from baseline/_ref when present)")
     args = ap.parse_args()
@@ -410,7 +413,9 @@ def main():
     from mflbm import lib
     lib.load()
     geo = case.geometry_bytes()
-    ctx, info = lib.setup_case(case, abi.MFLBM_FP32, abi.MFLBM_FAST, geometry=geo)
+    storage = {"native": abi.MFLBM_STORE_NATIVE, "f16": abi.MFLBM_STORE_F16, "bf16": abi.MFLBM_STORE_BF16}[args.storage]
+    pop_bytes = POP_BYTES if storage == abi.MFLBM_STORE_NATIVE else 2
+    ctx, info = lib.setup_case(case, abi.MFLBM_FP32, abi.MFLBM_FAST, geometry=geo, storage=storage)
     n_fluid, _ = ctx.node_counts()
     porosity = n_fluid / n_all
 
@@ -461,10 +466,10 @@ def main():
     collide_ms = tc / max(ncoll, 1)
     gradient_ms = tg / max(ncoll, 1)
     hbm, peak_kind = peaks()
-    coll_bytes = n_fluid * COLLIDE_BYTES_PER_FLUID + n_all * MASK_BYTES_PER_NODE
+    coll_bytes = n_fluid * (2 * 38 * pop_bytes + 4) + n_all * MASK_BYTES_PER_NODE
     achieved = coll_bytes / (collide_ms * 1e-3) / 1e9
-    traffic_per_fluid, traffic_src = read_traffic_profile()
-    step_bytes = n_fluid * STEP_BYTES_PER_FLUID + n_all * MASK_BYTES_PER_NODE
+    traffic_per_fluid, traffic_src = read_traffic_profile() if storage == abi.MFLBM_STORE_NATIVE else (None, None)
+    step_bytes = n_fluid * (2 * 38 * pop_bytes + 2 * 4) + n_all * MASK_BYTES_PER_NODE
     step_ms = t_max / args.steps
 
     # ---- end to end through the C ABI with pinned host buffers ----
@@ -527,7 +532,9 @@ def main():
         "warmup": warmup, "ms_per_step": round(step_ms, 5), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": data,
         "config": {"workload": case.name, "lattice": [nx, ny, nz], "fluid_nodes": n_fluid,
-                   "porosity": round(porosity, 4), "precision": "fp32 populations, fp32 collision",
+                   "porosity": round(porosity, 4),
+                   "precision": ("fp32 populations, fp32 collision" if storage == abi.MFLBM_STORE_NATIVE
+                                 else f"{args.storage} shifted populations, fp32 collision"),
                    "fp_mode": "fast", "l2": "inputs larger than L2 (populations 2.6 GB per replica), no flush",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "block_sizes": tuning or "defaults (128)"},
