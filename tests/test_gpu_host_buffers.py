@@ -1,9 +1,9 @@
 """mflbm_upload_fields / mflbm_download_fields with page-locked host buffers.
 
-With page-locked (pinned) host memory the population relayout kernels read
-and write the caller's reference-layout array directly over the host link;
-with ordinary memory the copy goes through the device staging buffer.  Both
-paths must move exactly the same bytes: a state uploaded from pinned memory
+With page-locked (pinned) host memory the upload's population relayout
+kernel reads the caller's reference-layout array directly over the host
+link; with ordinary memory the copy goes through the device staging buffer.
+Both paths must move exactly the same bytes: a state uploaded from pinned memory
 and stepped must equal the same state uploaded from ordinary memory, bit for
 bit, and a download into pinned buffers must equal a download into ordinary
 arrays.
