@@ -87,9 +87,12 @@ __device__ __forceinline__ bool grid_sync(const BatchSync& s) {
     return ok != 0;
 }
 
-// pre: kPhases arrays of (ns + 1) unit prefix sums, phase-major.
+// pre: kPhases arrays of (ns + 1) unit prefix sums, phase-major.  At least
+// 3 resident blocks of 256 (2 in FP64): with the bare thread bound the
+// compiler held the FP32 kernel to 64 registers and spilled 28 bytes; with
+// this one it uses 80 without spills, as the collision kernel does.
 template <class T, class E>
-__global__ void __launch_bounds__(256) batch_persistent_kernel(const BatchSample<T, E>* S, int ns, const int* pre,
+__global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : 3) batch_persistent_kernel(const BatchSample<T, E>* S, int ns, const int* pre,
                                                                BatchSync sync, int ntime_begin, int nsteps) {
     for (int step = 0; step < nsteps; ++step) {
         const bool odd = ((ntime_begin + step) & 1) != 0;
