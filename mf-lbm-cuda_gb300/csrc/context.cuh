@@ -54,7 +54,7 @@ struct DeviceState {
     ll prof_len = 0;
     uint32_t* dither = nullptr;        // step counter of 16-bit stochastic rounding: [0] read by odd, [1] by even steps
     int8_t* iface = nullptr;           // s2: 1 where the normal record may be non-zero (|grad phi| >= 1e-6, type <= 0)
-    uint16_t* pmask = nullptr;         // s4 rows x super-block columns: phi == +1 / -1 bits (gradient.cuh)
+    uint16_t* pmask = nullptr;         // s4 rows x super-block columns: phi near +1 / -1 bits (gradient.cuh)
     uint8_t* fmask = nullptr;          // the same rows: fluid nodes of [1, n]^3
     uint8_t* cmask = nullptr;          // the same rows: walls_type <= 0 on [-1, n+2]^3
     int32_t* tmap = nullptr;           // s2: fluid-list index of a fluid node of [1, n]^3, else -1

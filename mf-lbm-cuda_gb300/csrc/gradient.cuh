@@ -22,7 +22,8 @@
 // have zero records.  The pipeline keeps two lists between passes: the nodes
 // whose record is non-zero (olist) and the solid nodes that received a normal
 // (slist).  A pass resets those records to zero, lists the fluid nodes whose
-// stencil is not all +1 or all -1 (nlist, from per-row bit masks of phi),
+// stencil is not all (to within 7e-7) +1 or -1 (nlist, from per-row bit
+// masks of phi),
 // recomputes the normals of those nodes only (rebuilding olist and, from the
 // new interface nodes' solid neighbours, slist), extrapolates to them and
 // computes the curvature at the fluid nodes of olist.  Every record outside
@@ -47,7 +48,7 @@ template <class T> struct GradArgs {
     V4* cn;    // s2: (n_x, n_y, n_z, |grad phi|)
     V4* aux;   // fluid-list order: (n_x, n_y, n_z, 0.5 * gamma * curv * c_norm)
     int8_t* iface;  // s2 (fluid nodes): 1 where the record may be non-zero; 0: the zero record
-    uint16_t* pmask;       // s4 rows (y, z) x super-block columns: phi == +1 bits (low byte), == -1 (high byte)
+    uint16_t* pmask;       // s4 rows (y, z) x super-block columns: phi near +1 bits (low byte), near -1 (high byte)
     const uint8_t* fmask;  // the same rows: fluid nodes of [1, n]^3
     const uint8_t* cmask;  // the same rows: walls_type <= 0 on [-1, n+2]^3 (the nodes whose normal may be non-zero)
     const int32_t* tmap;   // s2 -> fluid-list index (or -1)
@@ -75,6 +76,10 @@ template <class T> struct GradArgs {
 };
 
 template <class T> __device__ __forceinline__ T wq_of(const ModelConsts<T>& c, int q) { return q < 7 ? c.w1 : c.w2; }
+
+// Distance from +-1 within which a stencil value counts as +-1 for the node
+// listing (phi_mask_kernel): 3 * 2^-22, exact in FP32 and FP64.
+constexpr double kNearOne = 7.152557373046875e-07;
 
 // Append `value` to `list` (capacity `cap`) where `want` is set: one atomic
 // per warp, the order within the list is arbitrary.  Every list is sized for
@@ -293,11 +298,23 @@ __device__ __forceinline__ void clear_records(const GradArgs<T>& a, int tid, int
 // kernel does not write, so the super-blocks are independent), then the row
 // masks of the s4 lattice: for row (y, z) and byte b (x = 8b .. 8b + 7, the
 // x extent of super-block column b), pmask holds bit x & 7 where phi is
-// exactly +1 (low byte) and exactly -1 (high byte).  Away from interfaces
-// phi is exactly +-1 (one component is exactly zero), so most stencils are
-// of one value.  One row of 8 nodes per thread; the super-block's fluid code
-// follows from the rows' fluid masks (fmask).  The threads also reset the
-// records of the previous pass's lists.
+// within kNearOne of +1 (low byte) and of -1 (high byte).  One row of 8
+// nodes per thread; the super-block's fluid code follows from the rows'
+// fluid masks (fmask) and exact comparisons with +-1.  The threads also
+// reset the records of the previous pass's lists.
+//
+// Why "within kNearOne" suffices: with every stencil value phi_q = s + e_q,
+// s = +-1 and |e_q| <= d, the ISO4 gradient is 3 sum_q w_q e_q e_q-vector,
+// whose length is at most d * max over sign choices |sum_q 3 w_q (+-e_q)| =
+// d * sqrt(14) / 3 = 1.2472 d (attained along (1, 2/3, 1/3)).  In the
+// arithmetic of iso4_d*: the face difference is exact (Sterbenz), the
+// running edge sum rounds at most three times by half an ulp of 1 (2^-24 in
+// FP32), times iso4b = 1/12, and the products and the final sum round
+// values of order d; so the computed |grad phi| is below 1.2472 d + 3e-8.
+// With d = 3 * 2^-22 (7.15e-7, exact in FP32) that is below 9.3e-7 < 1e-6,
+// the cut-off under which the normal pass writes the zero record: such a
+// node need not be listed.  Away from interfaces phi is exactly +-1 or
+// within a few ulps of it, so most stencils qualify.
 template <class T>
 __global__ void __launch_bounds__(64) phi_mask_kernel(const GradArgs<T> a) {
     pdl_wait();
@@ -314,19 +331,22 @@ __global__ void __launch_bounds__(64) phi_mask_kernel(const GradArgs<T> a) {
             __syncthreads();
         }
         const int sx = sb % a.SX, y = 8 * ((sb / a.SX) % a.SY) + ly, z = 8 * (sb / (a.SX * a.SY)) + lz;
-        unsigned F = 0, P = 0, M = 0;
+        unsigned F = 0, P = 0, M = 0, NP = 0, NM = 0;   // exactly +-1 (codes), within kNearOne (listing)
         if (y < NY && z < NZ) {
             const ll r = sx + (ll)a.SX * (y + (ll)NY * z);
             const T* row = a.phi + (ll)NX * (y + (ll)NY * z) + 8 * sx;
             const int nb = min(8, NX - 8 * sx);
+            const T d = T(kNearOne);
 #pragma unroll
             for (int b = 0; b < 8; ++b)
                 if (b < nb) {
                     const T v = row[b];
                     P |= (v == T(1) ? 1u : 0u) << b;
                     M |= (v == T(-1) ? 1u : 0u) << b;
+                    NP |= (v >= T(1) - d && v <= T(1) + d ? 1u : 0u) << b;
+                    NM |= (v >= T(-1) - d && v <= T(-1) + d ? 1u : 0u) << b;
                 }
-            a.pmask[r] = (uint16_t)(P | (M << 8));
+            a.pmask[r] = (uint16_t)(NP | (NM << 8));
             F = a.fmask[r];
         }
         // fluid code: 3 without fluid nodes, 1 (2) when all of them are +1 (-1), else 0
@@ -347,8 +367,9 @@ __device__ __forceinline__ void mask_window(const uint16_t* pm, ll r, int b, int
 
 // The nodes whose normal this pass recomputes: the candidates (walls_type <=
 // 0 on [-1, n+2]^3, cmask) whose ISO4 stencil (the node and its 18 D3Q19
-// neighbours) is not all exactly +1 or all exactly -1; elsewhere every
-// difference of the stencil is +0 and the record is the zero record.  Per
+// neighbours) is not all within kNearOne of +1 or all within it of -1;
+// elsewhere |grad phi| < 1e-6 and the record is the zero record
+// (phi_mask_kernel gives the bound).  Per
 // row of 8 nodes, bit-parallel: with a window w of a row's mask (byte b at
 // bits 8..15), w >> 8, w >> 7 and w >> 9 hold x, x - 1 and x + 1; the
 // stencil is x +- 1 of row (y, z), x and x +- 1 of rows (y +- 1, z) and
