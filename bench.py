@@ -371,6 +371,9 @@ def main():
     ap.add_argument("--storage", default="native", choices=["native", "f16", "bf16"],
                     help="population storage of the main run (default: FP32 populations; f16 / bf16 for "
                          "one-kernel captures of the 16-bit collision)")
+    ap.add_argument("--interface-rich-only", action="store_true",
+                    help="run only the interface-rich state (random +-1 phi) for --warmup + --steps steps and "
+                         "print its line (for launch lists of the sparse passes' worst case)")
     ap.add_argument("--no-reference-cuda", action="store_true",
                     help="skip the reference's own CUDA program (built from baseline/_ref when present)")
     args = ap.parse_args()
@@ -413,6 +416,9 @@ def main():
     from mflbm import lib
     lib.load()
     geo = case.geometry_bytes()
+    if args.interface_rich_only:
+        print(json.dumps({"interface_rich": interface_rich(case, geo, timed=args.steps, settle=max(args.warmup, 2) // 2 * 2)}))
+        return
     storage = {"native": abi.MFLBM_STORE_NATIVE, "f16": abi.MFLBM_STORE_F16, "bf16": abi.MFLBM_STORE_BF16}[args.storage]
     pop_bytes = POP_BYTES if storage == abi.MFLBM_STORE_NATIVE else 2
     ctx, info = lib.setup_case(case, abi.MFLBM_FP32, abi.MFLBM_FAST, geometry=geo, storage=storage)
