@@ -288,7 +288,9 @@ __device__ __forceinline__ void clear_records(const GradArgs<T>& a, int tid, int
         unpack_xyz(solid ? a.slist[p - no] : a.olist[p], i, j, k);
         const ll n2 = a.g.s2(i, j, k);
         a.cn[n2] = z;
-        if (solid) atomicAnd(&a.smask[n2 >> 5], ~(1u << (n2 & 31)));
+        // every set bit of smask belongs to an slist entry, so zeroing the
+        // whole words of the entries clears them all (plain stores, no atomics)
+        if (solid) a.smask[n2 >> 5] = 0u;
         else a.iface[n2] = 0;
     }
 }
@@ -480,8 +482,12 @@ __global__ void __launch_bounds__(256, 8) normals_kernel(const GradArgs<T> a) {
             on = normal_at<T>(a, i, j, k, a.type8[g.s4(i, j, k)]);
         }
         warp_append(on, packed, a.olist, &a.gcount[0], a.n_norm);
-        // most solid nodes are claimed by several neighbours: a plain read
-        // skips the atomic once the bit is visible
+        // most solid nodes are claimed by several neighbours: a read skips
+        // the atomic once the bit is set.  The read goes to L2 (ld.cg), where
+        // the other multiprocessors' atomics land: a line cached in this
+        // multiprocessor's L1 would keep showing the bit clear, and with an
+        // interface at every node the redundant atomics on the same words
+        // dominate the pass.
         const ll n2 = g.s2(i, j, k);
         unsigned mine = 0;
         if (on) {
@@ -489,7 +495,7 @@ __global__ void __launch_bounds__(256, 8) normals_kernel(const GradArgs<T> a) {
             for (int q = 1; q < 19; ++q) {
                 const ll s2 = n2 + ex(q) + ey(q) * sy2 + ez(q) * sz2;
                 const uint32_t bit = 1u << (s2 & 31);
-                if ((cand & (1u << q)) && !(a.smask[s2 >> 5] & bit) && !(atomicOr(&a.smask[s2 >> 5], bit) & bit))
+                if ((cand & (1u << q)) && !(__ldcg(&a.smask[s2 >> 5]) & bit) && !(atomicOr(&a.smask[s2 >> 5], bit) & bit))
                     mine |= 1u << q;
             }
         }
