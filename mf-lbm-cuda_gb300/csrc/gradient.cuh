@@ -484,20 +484,27 @@ __global__ void __launch_bounds__(256, 8) normals_kernel(const GradArgs<T> a) {
         warp_append(on, packed, a.olist, &a.gcount[0], a.n_norm);
         // most solid nodes are claimed by several neighbours: a read skips
         // the atomic once the bit is set.  The read goes to L2 (ld.cg), where
-        // the other multiprocessors' atomics land: a line cached in this
-        // multiprocessor's L1 would keep showing the bit clear, and with an
-        // interface at every node the redundant atomics on the same words
-        // dominate the pass.
+        // the other multiprocessors' atomics land (a line cached in this
+        // multiprocessor's L1 could keep showing the bit clear).  The reads
+        // are issued first (their results folded into one mask), then the
+        // needed atomics, none waiting on another: with an interface at every
+        // node, a chain of up to 18 L2 round trips per node dominated the pass.
         const ll n2 = g.s2(i, j, k);
         unsigned mine = 0;
-        if (on) {
+        if (on && cand) {
+            unsigned need = 0;
 #pragma unroll
-            for (int q = 1; q < 19; ++q) {
-                const ll s2 = n2 + ex(q) + ey(q) * sy2 + ez(q) * sz2;
-                const uint32_t bit = 1u << (s2 & 31);
-                if ((cand & (1u << q)) && !(__ldcg(&a.smask[s2 >> 5]) & bit) && !(atomicOr(&a.smask[s2 >> 5], bit) & bit))
-                    mine |= 1u << q;
-            }
+            for (int q = 1; q < 19; ++q)
+                if (cand & (1u << q)) {
+                    const ll s2 = n2 + ex(q) + ey(q) * sy2 + ez(q) * sz2;
+                    if (!((__ldcg(&a.smask[s2 >> 5]) >> (s2 & 31)) & 1u)) need |= 1u << q;
+                }
+#pragma unroll
+            for (int q = 1; q < 19; ++q)
+                if (need & (1u << q)) {
+                    const ll s2 = n2 + ex(q) + ey(q) * sy2 + ez(q) * sz2;
+                    if (!((atomicOr(&a.smask[s2 >> 5], 1u << (s2 & 31)) >> (s2 & 31)) & 1u)) mine |= 1u << q;
+                }
         }
         int at = warp_reserve(__popc(mine), &a.gcount[1]);
 #pragma unroll
