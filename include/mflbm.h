@@ -254,8 +254,10 @@ int mflbm_run(mflbm_context* ctx, int ntime_begin, int nsteps);
 int mflbm_synchronize(mflbm_context* ctx);
 /* Sizes of the last gradient pass's sparse sets (no reference counterpart;
  * diagnostics of the sparse colour-gradient passes): nodes of [-1, n+2]^3
- * with a non-zero interface normal, solid boundary nodes that received an
- * extrapolated normal, and fluid nodes whose normals were recomputed.
+ * with a non-zero interface normal, solid boundary nodes given a non-zero
+ * extrapolated normal by that pass (the solid nodes of the super-blocks it
+ * processed; elsewhere the solid normals are unchanged), and fluid nodes
+ * whose normals were recomputed.
  * Synchronises the context's stream.  Any pointer may be NULL. */
 int mflbm_interface_stats(mflbm_context* ctx, long long* interface_nodes, long long* solid_normals,
                           long long* active_nodes);

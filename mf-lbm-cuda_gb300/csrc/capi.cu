@@ -55,7 +55,7 @@ void free_all(mflbm_context* c) {
     void* ptrs[] = {d.pdf, d.phi, d.cn_x, d.cn_y, d.cn_z, d.c_norm, d.curv, d.W_in, d.f_cv, d.g_cv, d.phi_cv,
                     d.walls, d.walls_type, d.s_nx, d.s_ny, d.s_nz, d.fluid_list, d.list_phi_ext,
                     d.red, d.staging, d.aux, d.type8, d.cnv4, d.zpair_off,
-                    d.phi_prev, d.prof, d.dither, d.iface, d.pmask, d.fmask, d.cmask, d.tmap, d.wmask, d.olist, d.slist, d.nlist, d.smask, d.gcount,
+                    d.phi_prev, d.prof, d.dither, d.iface, d.pmask, d.fmask, d.cmask, d.tmap, d.olist, d.nlist, d.gcount,
                     d.sbcode, d.sbact, d.sblive, d.sbinfo, d.phioff};
     for (void* p : ptrs) if (p) cudaFree(p);
     d = DeviceState{};
@@ -158,7 +158,7 @@ int build_lists(mflbm_context* c) {
             for (int i = 1; i <= g.nx; ++i)
                 if (walls[g.s2(i, j, k)] == 0) nodes.push_back(pack_xyz(i, j, k));
     std::vector<uint2> lphi;
-    ll ncn = 0;   // walls_type == 2 nodes of [0, n+1]^3: bound of the claimed solid nodes
+    ll ncn = 0;   // walls_type == 2 nodes of [0, n+1]^3: the nodes of the normal extrapolation
     for (int k = -2; k <= g.nz + 3; ++k)
         for (int j = -2; j <= g.ny + 3; ++j)
             for (int i = -2; i <= g.nx + 3; ++i) {
@@ -172,29 +172,13 @@ int build_lists(mflbm_context* c) {
             }
     int rc;
     if ((rc = order_fluid_list(c, nodes, nullptr)) != MFLBM_OK) return rc;
-    {
-        // the nodes whose normal the step may need (walls_type <= 0 on
-        // [-1, n+2]^3: their count bounds the sparse lists) and their
-        // solid-boundary neighbours (the claims of the normal extrapolation)
-        std::vector<uint32_t> wm(g.n2(), 0u);
-        d.n_norm = 0;
-        for (int k = -1; k <= g.nz + 2; ++k)
-            for (int j = -1; j <= g.ny + 2; ++j)
-                for (int i = -1; i <= g.nx + 2; ++i) {
-                    if (wt[g.s4(i, j, k)] > 0) continue;
-                    ++d.n_norm;
-                    uint32_t m = 0;
-                    for (int q = 1; q < 19; ++q) {
-                        const int si = i + ex(q), sj = j + ey(q), sk = k + ez(q);
-                        if (si >= 0 && si <= g.nx + 1 && sj >= 0 && sj <= g.ny + 1 && sk >= 0 && sk <= g.nz + 1 &&
-                            wt[g.s4(si, sj, sk)] == 2)
-                            m |= 1u << q;
-                    }
-                    wm[g.s2(i, j, k)] = m;
-                }
-        ll nwm = 0;
-        if ((rc = upload_list(&d.wmask, &nwm, wm)) != MFLBM_OK) return rc;
-    }
+    // the nodes whose normal the step may need: walls_type <= 0 on
+    // [-1, n+2]^3 (their count bounds the sparse lists)
+    d.n_norm = 0;
+    for (int k = -1; k <= g.nz + 2; ++k)
+        for (int j = -1; j <= g.ny + 2; ++j)
+            for (int i = -1; i <= g.nx + 2; ++i)
+                if (wt[g.s4(i, j, k)] <= 0) ++d.n_norm;
     {
         // row masks over the s4 lattice (row (y, z), byte b: x = 8b .. 8b + 7):
         // the fluid nodes of [1, n]^3 (super-block codes) and the nodes whose
@@ -237,18 +221,13 @@ int build_lists(mflbm_context* c) {
         int dev = 0;
         MFLBM_CUDA(cudaGetDevice(&dev));
         MFLBM_CUDA(cudaDeviceGetAttribute(&d.n_sm, cudaDevAttrMultiProcessorCount, dev));
-        for (void** p : {(void**)&d.olist, (void**)&d.slist, (void**)&d.nlist, (void**)&d.smask, (void**)&d.gcount}) {
+        for (void** p : {(void**)&d.olist, (void**)&d.nlist, (void**)&d.gcount}) {
             if (*p) cudaFree(*p);
             *p = nullptr;
         }
-        d.n_blocks = (ll)(((g.nx + 4) >> 1) + 1) * (((g.ny + 4) >> 1) + 1) * (((g.nz + 4) >> 1) + 1);
-        const size_t nmask = (size_t)(g.n2() / 32 + 1);
         MFLBM_CUDA(cudaMalloc(&d.olist, sizeof(uint32_t) * std::max<ll>(1, d.n_norm)));
-        MFLBM_CUDA(cudaMalloc(&d.slist, sizeof(uint32_t) * std::max<ll>(1, d.n_cn_ext)));
         MFLBM_CUDA(cudaMalloc(&d.nlist, sizeof(uint32_t) * std::max<ll>(1, d.n_norm)));
-        MFLBM_CUDA(cudaMalloc(&d.smask, sizeof(uint32_t) * nmask));
         MFLBM_CUDA(cudaMalloc(&d.gcount, 8 * sizeof(int)));
-        MFLBM_CUDA(cudaMemset(d.smask, 0, sizeof(uint32_t) * nmask));
         MFLBM_CUDA(cudaMemset(d.gcount, 0, 8 * sizeof(int)));
     }
     if (d.phi_prev) cudaFree(d.phi_prev);
@@ -432,8 +411,6 @@ std::vector<Span> state_spans(mflbm_context* c) {
                              {d.f_cv, T * pl * 19}, {d.g_cv, T * pl * 19}, {d.phi_cv, T * pl},
                              {d.dither, 2 * sizeof(uint32_t)}, {d.iface, (size_t)g.n2()},
                              {d.olist, sizeof(uint32_t) * std::max<ll>(1, d.n_norm)},
-                             {d.slist, sizeof(uint32_t) * std::max<ll>(1, d.n_cn_ext)},
-                             {d.smask, sizeof(uint32_t) * (size_t)(g.n2() / 32 + 1)},
                              {d.gcount, 8 * sizeof(int)}};
 }
 int save_state(mflbm_context* c, SavedState* s) {

@@ -45,7 +45,7 @@ struct DeviceState {
     ll n_fluid = 0;
     uint2* list_phi_ext = nullptr;     // walls_type == 2 on [-2, n+3]^3: (packed, fluid-neighbour mask)
     ll n_phi_ext = 0;
-    ll n_cn_ext = 0;                   // walls_type == 2 nodes on [0, n+1]^3 (capacity of slist)
+    ll n_cn_ext = 0;                   // walls_type == 2 nodes on [0, n+1]^3 (normal extrapolation)
     double* red = nullptr;             // reduction scratch
     ll red_len = 0;
     int* zpair_off = nullptr;          // fluid-list offset of each layer of population tiles, ntz + 1 entries
@@ -58,13 +58,9 @@ struct DeviceState {
     uint8_t* fmask = nullptr;          // the same rows: fluid nodes of [1, n]^3
     uint8_t* cmask = nullptr;          // the same rows: walls_type <= 0 on [-1, n+2]^3
     int32_t* tmap = nullptr;           // s2: fluid-list index of a fluid node of [1, n]^3, else -1
-    uint32_t* wmask = nullptr;         // s2: bit q set where x + e_q is a walls_type-2 node of [0, n+1]^3 (type <= 0 nodes)
     uint32_t* olist = nullptr;         // packed nodes with a non-zero normal record (capacity n_norm)
-    uint32_t* slist = nullptr;         // packed solid boundary nodes that received a normal (capacity n_cn_ext)
     uint32_t* nlist = nullptr;         // packed fluid nodes of the active 2x2x2 node blocks (capacity n_norm)
-    uint32_t* smask = nullptr;         // bit per s2 node: in slist
-    int* gcount = nullptr;             // lengths of olist, slist, nlist
-    ll n_blocks = 0;                   // node blocks of the normal pass: ((n+4)/2 + 1) per axis
+    int* gcount = nullptr;             // [0] olist, [1] solid normals written, [2] nlist, [4] previous olist
     // super-blocks of the normal pass: 4 x 4 x 4 phi bricks (8^3 nodes of the s4 lattice)
     int SX = 0, SY = 0, SZ = 0;        // super-blocks per axis
     int8_t* sbcode = nullptr;          // per super-block: the fluid code of its phi bricks (gradient.cuh)

@@ -19,15 +19,15 @@
 // Sparse passes.  Away from interfaces phi is exactly +1 or -1, every
 // difference in an ISO4 sum is +0 and the normal record is the zero record;
 // so are the extrapolated normals of solid nodes whose fluid neighbours all
-// have zero records.  The pipeline keeps two lists between passes: the nodes
-// whose record is non-zero (olist) and the solid nodes that received a normal
-// (slist).  A pass resets those records to zero, lists the fluid nodes whose
-// stencil is not all (to within 7e-7) +1 or -1 (nlist, from per-row bit
-// masks of phi),
-// recomputes the normals of those nodes only (rebuilding olist and, from the
-// new interface nodes' solid neighbours, slist), extrapolates to them and
-// computes the curvature at the fluid nodes of olist.  Every record outside
-// the lists is the zero record, as in the dense passes of the reference.
+// have zero records.  The pipeline keeps the list of the fluid nodes whose
+// record is non-zero (olist) between passes.  A pass resets those records to
+// zero, lists the fluid nodes whose stencil is not all (to within 7e-7) +1
+// or -1 (nlist, from per-row bit masks of phi), recomputes the normals of
+// those nodes only (rebuilding olist), extrapolates normals to the solid
+// boundary nodes of the super-blocks where phi can have changed and computes
+// the curvature at the fluid nodes of olist.  Every fluid record outside the
+// list is the zero record and every solid record is the dense passes' value,
+// as in the reference.
 //
 // The reference-layout arrays cn_x/y/z, c_norm and curv (curvature on all of
 // [1, n]^3, solid nodes included) are produced from the records only when the
@@ -52,12 +52,10 @@ template <class T> struct GradArgs {
     const uint8_t* fmask;  // the same rows: fluid nodes of [1, n]^3
     const uint8_t* cmask;  // the same rows: walls_type <= 0 on [-1, n+2]^3 (the nodes whose normal may be non-zero)
     const int32_t* tmap;   // s2 -> fluid-list index (or -1)
-    const uint32_t* wmask; // s2: bit q where x + e_q is a solid boundary node (walls_type 2) of [0, n+1]^3
     uint32_t* olist;       // packed coordinates of the nodes whose record is non-zero (interface flag set)
-    uint32_t* slist;       // packed coordinates of the solid nodes whose normal may be non-zero
     uint32_t* nlist;       // packed fluid nodes whose normal this pass recomputes
-    uint32_t* smask;       // bit per s2 node: the solid node is in slist
-    int* gcount;           // [0] olist, [1] slist, [2] nlist lengths; [4], [5] the previous pass's [0], [1]
+    int* gcount;           // [0] olist, [2] nlist lengths, [1] solid nodes given a non-zero normal by this
+                           // pass; [4] the previous pass's [0]
     T *cnx, *cny, *cnz, *cnorm, *curv;  // reference-layout arrays (export / pack)
     const uint2* l_phi;
     const uint32_t* l_fluid;
@@ -183,10 +181,9 @@ __global__ void __launch_bounds__(256) sb_live_kernel(const GradArgs<T> a) {
     }
     if (s == 0) {
         *a.live_next = 0;
-        // the node lists restart; the previous olist / slist lengths stay for
-        // the reset of their records (clear_records)
+        // the node lists restart; the previous olist length stays for the
+        // reset of its records (clear_records)
         a.gcount[4] = a.gcount[0];
-        a.gcount[5] = a.gcount[1];
         a.gcount[0] = a.gcount[1] = a.gcount[2] = 0;
     }
     warp_append(live, (uint32_t)s, a.sblive, a.live_n, a.SX * a.SY * a.SZ);
@@ -274,24 +271,20 @@ __device__ __forceinline__ T iso4_dz(const ModelConsts<T>& c, const T* F, int n,
                       F[n + sy + sz] - F[n - sy - sz] + F[n - sy + sz] - F[n + sy - sz]);
 }
 
-// Reset the records of the previous pass's lists to the zero record (and
-// their flags), so that every record outside this pass's lists is zero.
-// Grid-stride over both lists, run by the threads of the brick pass.
+// Reset the records of the previous pass's interface list to the zero record
+// (and their flags), so that every fluid record outside this pass's list is
+// zero.  Grid-stride, run by the threads of the mask pass.
 template <class T>
 __device__ __forceinline__ void clear_records(const GradArgs<T>& a, int tid, int nthreads) {
-    const int no = min(a.gcount[4], a.n_norm), ns = min(a.gcount[5], a.n_cn);
+    const int no = min(a.gcount[4], a.n_norm);
     typename Vec4<T>::type z;
     z.x = T(0); z.y = T(0); z.z = T(0); z.w = T(0);
-    for (int p = tid; p < no + ns; p += nthreads) {
-        const bool solid = p >= no;
+    for (int p = tid; p < no; p += nthreads) {
         int i, j, k;
-        unpack_xyz(solid ? a.slist[p - no] : a.olist[p], i, j, k);
+        unpack_xyz(a.olist[p], i, j, k);
         const ll n2 = a.g.s2(i, j, k);
         a.cn[n2] = z;
-        // every set bit of smask belongs to an slist entry, so zeroing the
-        // whole words of the entries clears them all (plain stores, no atomics)
-        if (solid) a.smask[n2 >> 5] = 0u;
-        else a.iface[n2] = 0;
+        a.iface[n2] = 0;
     }
 }
 
@@ -455,97 +448,79 @@ __device__ __forceinline__ bool normal_at(const GradArgs<T>& a, int i, int j, in
 }
 
 // unit interface normal and |grad phi| (:757-807) + wetting (:809-878) at the
-// nodes of nlist; nodes with a non-zero record are appended to olist, and
-// their solid-boundary neighbours of [0, n+1]^3 (the node's precomputed
-// solid-neighbour mask) join slist once (bit mask): the only solid nodes whose
-// extrapolated normal can be non-zero.  The claims of a warp are appended
-// with one atomic; the loop is warp-uniform for that.
-// 32 registers (8 blocks of 256 per SM): the pass is bound by the latency of
-// its dependent loads, and full occupancy outweighs the 48 bytes it spills
-// (gradient pipeline 0.175 -> 0.170 ms at 256^3).
+// nodes of nlist; nodes with a non-zero record are appended to olist (one
+// atomic per warp).
 template <class T>
 __global__ void __launch_bounds__(256, 8) normals_kernel(const GradArgs<T> a) {
     pdl_wait();
     const Grid& g = a.g;
     const int nt = min(a.gcount[2], a.n_norm);
-    const int sy2 = g.nx + 4, sz2 = (g.nx + 4) * (g.ny + 4);
     const int iters = (nt + gridDim.x * blockDim.x - 1) / (gridDim.x * blockDim.x);
     for (int it = 0; it < iters; ++it) {
         const int p = (it * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x;
-        int i = 0, j = 0, k = 0;
-        uint32_t packed = 0, cand = 0;
+        uint32_t packed = 0;
         bool on = false;
         if (p < nt) {
+            int i, j, k;
             packed = a.nlist[p];
             unpack_xyz(packed, i, j, k);
-            cand = a.wmask[g.s2(i, j, k)];
             on = normal_at<T>(a, i, j, k, a.type8[g.s4(i, j, k)]);
         }
         warp_append(on, packed, a.olist, &a.gcount[0], a.n_norm);
-        // most solid nodes are claimed by several neighbours: a read skips
-        // the atomic once the bit is set.  The read goes to L2 (ld.cg), where
-        // the other multiprocessors' atomics land (a line cached in this
-        // multiprocessor's L1 could keep showing the bit clear).  The reads
-        // are issued first (their results folded into one mask), then the
-        // needed atomics, none waiting on another: with an interface at every
-        // node, a chain of up to 18 L2 round trips per node dominated the pass.
-        const ll n2 = g.s2(i, j, k);
-        unsigned mine = 0;
-        if (on && cand) {
-            unsigned need = 0;
-#pragma unroll
-            for (int q = 1; q < 19; ++q)
-                if (cand & (1u << q)) {
-                    const ll s2 = n2 + ex(q) + ey(q) * sy2 + ez(q) * sz2;
-                    if (!((__ldcg(&a.smask[s2 >> 5]) >> (s2 & 31)) & 1u)) need |= 1u << q;
-                }
-#pragma unroll
-            for (int q = 1; q < 19; ++q)
-                if (need & (1u << q)) {
-                    const ll s2 = n2 + ex(q) + ey(q) * sy2 + ez(q) * sz2;
-                    if (!((atomicOr(&a.smask[s2 >> 5], 1u << (s2 & 31)) >> (s2 & 31)) & 1u)) mine |= 1u << q;
-                }
-        }
-        int at = warp_reserve(__popc(mine), &a.gcount[1]);
-#pragma unroll
-        for (int q = 1; q < 19; ++q)
-            if (mine & (1u << q)) {
-                if (at < a.n_cn) a.slist[at] = pack_xyz(i + ex(q), j + ey(q), k + ez(q));
-                ++at;
-            }
     }
 }
 
-// interface normal on the solid boundary nodes of slist = weighted mean over
-// the fluid neighbours (walls_type <= 0), in direction order (:880-906).
-// |grad phi| of a solid node stays 0.
+// Interface normal on the solid boundary nodes (walls_type 2) of [0, n+1]^3
+// = weighted mean over the fluid neighbours (walls_type <= 0), in direction
+// order (:880-906), for every solid boundary node of this pass's
+// super-blocks: zero or not, its record is written, so no list of the solid
+// nodes that received a normal is kept.  A solid node's normal depends on the
+// records of its fluid neighbours, which change only within two nodes of a
+// phi that changed: within three nodes of a flagged super-block, inside the
+// processed ones.  Neighbours whose interface flag is clear hold the zero
+// record: their +0 terms are skipped (only their weights are summed), which
+// leaves every sum bit-identical.  One block per super-block of this pass;
+// gcount[1] counts the non-zero results.
 template <class T>
 __global__ void __launch_bounds__(256) extrapolate_normal_kernel(const GradArgs<T> a) {
     pdl_wait();
     const Grid& g = a.g;
-    const int ns = min(a.gcount[1], a.n_cn);
     const int sy = g.nx + 4, sz = (g.nx + 4) * (g.ny + 4);
-    const int sy4 = g.nx + 8, sz4 = (g.nx + 8) * (g.ny + 8);
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < ns; p += gridDim.x * blockDim.x) {
-        int i, j, k;
-        unpack_xyz(a.slist[p], i, j, k);
-        const int n = (int)g.s2(i, j, k), n4 = (int)g.s4(i, j, k);
-        T sx = T(0), syy = T(0), szz = T(0), ws = T(0);
+    const int nl = min(*a.live_n, a.SX * a.SY * a.SZ);
+    int nonzero = 0;
+    for (int w = blockIdx.x; w < nl; w += gridDim.x) {
+        const uint32_t sb = a.sblive[w];
+        for (int t = a.phioff[sb] + threadIdx.x; t < a.phioff[sb + 1]; t += blockDim.x) {
+            const uint2 e = a.l_phi[t];
+            int i, j, k;
+            unpack_xyz(e.x, i, j, k);
+            if (i < 0 || j < 0 || k < 0 || i > g.nx + 1 || j > g.ny + 1 || k > g.nz + 1) continue;
+            const int n = (int)g.s2(i, j, k);
+            T sx = T(0), syy = T(0), szz = T(0), ws = T(0);
 #pragma unroll
-        for (int q = 1; q < 19; ++q) {
-            if (a.type8[n4 + ex(q) + ey(q) * sy4 + ez(q) * sz4] <= 0) {
-                const typename Vec4<T>::type v = a.cn[n + ex(q) + ey(q) * sy + ez(q) * sz];
-                const T wq = wq_of(a.ph.c, q);
-                sx += v.x * wq;
-                syy += v.y * wq;
-                szz += v.z * wq;
-                ws += wq;
+            for (int q = 1; q < 19; ++q) {
+                if (e.y & (1u << q)) {
+                    const int m = n + ex(q) + ey(q) * sy + ez(q) * sz;
+                    const T wq = wq_of(a.ph.c, q);
+                    if (a.iface[m]) {
+                        const typename Vec4<T>::type v = a.cn[m];
+                        sx += v.x * wq;
+                        syy += v.y * wq;
+                        szz += v.z * wq;
+                    }
+                    ws += wq;
+                }
             }
+            typename Vec4<T>::type r;
+            r.x = sx / ws; r.y = syy / ws; r.z = szz / ws; r.w = T(0);
+            a.cn[n] = r;
+            nonzero += (r.x != T(0) || r.y != T(0) || r.z != T(0)) ? 1 : 0;
         }
-        typename Vec4<T>::type r;
-        r.x = sx / ws; r.y = syy / ws; r.z = szz / ws; r.w = T(0);
-        a.cn[n] = r;
     }
+    // one atomic per warp
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) nonzero += __shfl_xor_sync(0xffffffffu, nonzero, o);
+    if ((threadIdx.x & 31) == 0 && nonzero) atomicAdd(&a.gcount[1], nonzero);
 }
 
 // curvature at node n (s2 index) from the nine ISO4 derivatives of the
@@ -640,7 +615,7 @@ __global__ void __launch_bounds__(128) pack_normals_kernel(const GradArgs<T> a) 
     a.cn[n] = v;
     // 1 where the record is non-zero (uploaded arrays can carry a normal with
     // c_norm = 0); such nodes form olist, which the next pass clears first.
-    // Solid records are zero here: slist and its mask start empty.
+    // Solid records are zero here; the next pass (every super-block) extrapolates them.
     const bool nz = v.x != T(0) || v.y != T(0) || v.z != T(0) || v.w != T(0);
     a.iface[n] = nz ? 1 : 0;
     if (nz) {
@@ -675,8 +650,7 @@ GradArgs<T> grad_args(const mflbm_context& c) {
     a.iface = d.iface;
     a.pmask = d.pmask; a.fmask = d.fmask; a.cmask = d.cmask;
     a.tmap = d.tmap;
-    a.wmask = d.wmask;
-    a.olist = d.olist; a.slist = d.slist; a.nlist = d.nlist; a.smask = d.smask; a.gcount = d.gcount;
+    a.olist = d.olist; a.nlist = d.nlist; a.gcount = d.gcount;
     a.cnx = (T*)d.cn_x; a.cny = (T*)d.cn_y; a.cnz = (T*)d.cn_z;
     a.cnorm = (T*)d.c_norm; a.curv = (T*)d.curv;
     a.l_phi = d.list_phi_ext; a.n_phi = (int)d.n_phi_ext;
@@ -759,7 +733,6 @@ int launch_refresh_aux(mflbm_context& c) {
     const GradArgs<T> a = grad_args<T>(c);
     const Grid& g = c.d.g;
     MFLBM_CUDA(cudaMemsetAsync(c.d.gcount, 0, 3 * sizeof(int), c.stream));
-    MFLBM_CUDA(cudaMemsetAsync(c.d.smask, 0, sizeof(uint32_t) * (size_t)(g.n2() / 32 + 1), c.stream));
     pack_normals_kernel<T><<<dim3(grid_for(g.nx + 4, 128), g.ny + 4, g.nz + 4), 128, 0, c.stream>>>(a);
     int rc = after_launch("pack_normals");
     if (rc != MFLBM_OK || !a.n_fluid) return rc;
