@@ -46,31 +46,34 @@ __device__ __constant__ const int kInlet[5][4] = {{0, 0, 5, 6}, {-1, 0, 11, 14},
 // (dx, dy, slot at z=nz+1 of (i+dx, j+dy), slot at z=nz of (i, j), convective buffer slot)
 __device__ __constant__ const int kOutlet[5][5] = {{0, 0, 6, 5, 6}, {-1, 0, 13, 12, 13}, {1, 0, 14, 11, 14}, {0, -1, 17, 16, 17}, {0, 1, 18, 15, 18}};
 
-// velocity inlet: bounce-back plus 6 w rho u injection, split by sa_inject (:1009-1077)
+// velocity inlet: bounce-back plus 6 w rho u injection, split by sa_inject
+// (:1009-1077).  One link s (kInlet) of component gg; the links of a column
+// touch distinct slots, so they can run in separate threads.
 template <class T, class E, bool AFTER_ODD>
-__device__ __forceinline__ void inlet_velocity_at(const BcArgs<T, E>& a, int i, int j) {
+__device__ __forceinline__ void inlet_velocity_link(const BcArgs<T, E>& a, int i, int j, int gg, int s) {
     const Grid& g = a.g;
     const int w = a.walls[g.s2(i, j, 1)];
-    inlet_phi(a, i, j, w);
     T t2 = a.W_in[g.s1(i, j, 0)] * a.ph.relaxation;
     const T t1 = t2 * a.ph.sa_inject;
     t2 = t2 - t1;
-#pragma unroll
-    for (int gg = 0; gg < 2; ++gg) {
-        const T inj = gg == 0 ? t1 : t2;
-#pragma unroll
-        for (int s = 0; s < 5; ++s) {
-            const T wq = s == 0 ? a.ph.c.w1 : a.ph.c.w2;
-            const int dx = kInlet[s][0], dy = kInlet[s][1], s0 = kInlet[s][2], s1 = kInlet[s][3];
-            if (!AFTER_ODD) {
-                const T d = a.P.get(i + dx, j + dy, 0, s0, gg);
-                a.P.set(i + dx, j + dy, 0, s0, gg, keep((a.P.get(i, j, 1, s1, gg) + T(6.0) * wq * inj), d, w));
-            } else {
-                const T d = a.P.get(i, j, 1, s1, gg);
-                a.P.set(i, j, 1, s1, gg, keep((a.P.get(i + dx, j + dy, 0, s0, gg) + T(6.0) * wq * inj), d, w));
-            }
-        }
+    const T inj = gg == 0 ? t1 : t2;
+    const T wq = s == 0 ? a.ph.c.w1 : a.ph.c.w2;
+    const int dx = kInlet[s][0], dy = kInlet[s][1], s0 = kInlet[s][2], s1 = kInlet[s][3];
+    if (!AFTER_ODD) {
+        const T d = a.P.get(i + dx, j + dy, 0, s0, gg);
+        a.P.set(i + dx, j + dy, 0, s0, gg, keep((a.P.get(i, j, 1, s1, gg) + T(6.0) * wq * inj), d, w));
+    } else {
+        const T d = a.P.get(i, j, 1, s1, gg);
+        a.P.set(i, j, 1, s1, gg, keep((a.P.get(i + dx, j + dy, 0, s0, gg) + T(6.0) * wq * inj), d, w));
     }
+}
+template <class T, class E, bool AFTER_ODD>
+__device__ __forceinline__ void inlet_velocity_at(const BcArgs<T, E>& a, int i, int j) {
+    inlet_phi(a, i, j, a.walls[a.g.s2(i, j, 1)]);
+#pragma unroll
+    for (int gg = 0; gg < 2; ++gg)
+#pragma unroll
+        for (int s = 0; s < 5; ++s) inlet_velocity_link<T, E, AFTER_ODD>(a, i, j, gg, s);
 }
 
 // Zou-He pressure inlet per component (:1085-1241)
@@ -121,9 +124,11 @@ __device__ __forceinline__ void inlet_pressure_at(const BcArgs<T, E>& a, int i, 
     }
 }
 
-// convective outflow with the previous-step buffers (:1246-1357)
-template <class T, class E, bool AFTER_ODD>
-__device__ __forceinline__ void outlet_convective_at(const BcArgs<T, E>& a, int i, int j) {
+// convective outflow with the previous-step buffers (:1246-1357): the phi
+// ghost layers of column (i, j), and one link s (kOutlet) of component gg
+// (the links touch distinct slots and buffer entries)
+template <class T, class E>
+__device__ __forceinline__ void outlet_convective_phi(const BcArgs<T, E>& a, int i, int j) {
     const Grid& g = a.g;
     const int nz = g.nz;
     const T u = a.ph.uin_avg;
@@ -136,25 +141,35 @@ __device__ __forceinline__ void outlet_convective_at(const BcArgs<T, E>& a, int 
     a.phi[g.s4(i, j, nz + 2)] = ph;
     a.phi[g.s4(i, j, nz + 3)] = ph;
     a.phi[g.s4(i, j, nz + 4)] = ph;
-#pragma unroll
-    for (int gg = 0; gg < 2; ++gg) {
-        T* buf = gg == 0 ? a.f_cv : a.g_cv;
-#pragma unroll
-        for (int s = 0; s < 5; ++s) {
-            const int dx = kOutlet[s][0], dy = kOutlet[s][1], su = kOutlet[s][2], sd = kOutlet[s][3], sb = kOutlet[s][4];
-            T& bv = buf[g.cnv(i, j, sb)];
-            if (!AFTER_ODD) {
-                const T d = ((bv + u * a.P.get(i + dx, j + dy, nz, su, gg)) * temp) * T(1 - w) +
-                            a.P.get(i + dx, j + dy, nz + 1, su, gg) * T(w);
-                a.P.set(i + dx, j + dy, nz + 1, su, gg, d);
-                bv = d;
-            } else {
-                const T d = ((bv + u * a.P.get(i, j, nz - 1, sd, gg)) * temp) * T(1 - w) + a.P.get(i, j, nz, sd, gg) * T(w);
-                a.P.set(i, j, nz, sd, gg, d);
-                bv = d;
-            }
-        }
+}
+template <class T, class E, bool AFTER_ODD>
+__device__ __forceinline__ void outlet_convective_link(const BcArgs<T, E>& a, int i, int j, int gg, int s) {
+    const Grid& g = a.g;
+    const int nz = g.nz;
+    const T u = a.ph.uin_avg;
+    const T temp = T(1) / (T(1) + u);
+    const int w = a.walls[g.s2(i, j, nz)];
+    T* buf = gg == 0 ? a.f_cv : a.g_cv;
+    const int dx = kOutlet[s][0], dy = kOutlet[s][1], su = kOutlet[s][2], sd = kOutlet[s][3], sb = kOutlet[s][4];
+    T& bv = buf[g.cnv(i, j, sb)];
+    if (!AFTER_ODD) {
+        const T d = ((bv + u * a.P.get(i + dx, j + dy, nz, su, gg)) * temp) * T(1 - w) +
+                    a.P.get(i + dx, j + dy, nz + 1, su, gg) * T(w);
+        a.P.set(i + dx, j + dy, nz + 1, su, gg, d);
+        bv = d;
+    } else {
+        const T d = ((bv + u * a.P.get(i, j, nz - 1, sd, gg)) * temp) * T(1 - w) + a.P.get(i, j, nz, sd, gg) * T(w);
+        a.P.set(i, j, nz, sd, gg, d);
+        bv = d;
     }
+}
+template <class T, class E, bool AFTER_ODD>
+__device__ __forceinline__ void outlet_convective_at(const BcArgs<T, E>& a, int i, int j) {
+    outlet_convective_phi<T, E>(a, i, j);
+#pragma unroll
+    for (int gg = 0; gg < 2; ++gg)
+#pragma unroll
+        for (int s = 0; s < 5; ++s) outlet_convective_link<T, E, AFTER_ODD>(a, i, j, gg, s);
 }
 
 // Zou-He pressure outlet on the total density, flux split by phi (:1363-1524)
@@ -239,6 +254,31 @@ __global__ void inlet_outlet_kernel(const BcArgs<T, E> a, int inlet, int outlet)
     else if (inlet == 2) inlet_pressure_at<T, E, AFTER_ODD>(a, i, j);
     if (outlet == 1) outlet_convective_at<T, E, AFTER_ODD>(a, i, j);
     else if (outlet == 2) outlet_pressure_at<T, E, AFTER_ODD>(a, i, j);
+}
+
+// The velocity inlet and the convective outlet (the usual pair) with 11
+// threads per column: the 10 links (2 components x 5 directions) of each face
+// and the phi ghost layers.  The links of a column touch distinct slots, so
+// this gives the column kernel's results; eleven times the threads hide the
+// latency of the scattered plane accesses.  Items are link-major (a warp:
+// one link of 32 columns, 16 x 2 of them).
+template <class T, class E, bool AFTER_ODD>
+__global__ void inlet_outlet_links_kernel(const BcArgs<T, E> a, int inlet, int outlet, int ntx, int ncolp) {
+    pdl_wait();
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int item = t / ncolp, c = t - item * ncolp;
+    if (item >= 11) return;
+    const int lane = c & 31, tile = c >> 5;
+    const int i = (tile % ntx) * 16 + (lane & 15) + 1, j = (tile / ntx) * 2 + (lane >> 4) + 1;
+    if (i > a.g.nx || j > a.g.ny) return;
+    if (item == 10) {
+        if (inlet == 1) inlet_phi(a, i, j, a.walls[a.g.s2(i, j, 1)]);
+        if (outlet == 1) outlet_convective_phi<T, E>(a, i, j);
+        return;
+    }
+    const int gg = item / 5, s = item - 5 * gg;
+    if (inlet == 1) inlet_velocity_link<T, E, AFTER_ODD>(a, i, j, gg, s);
+    if (outlet == 1) outlet_convective_link<T, E, AFTER_ODD>(a, i, j, gg, s);
 }
 
 __device__ __constant__ const int kZup[5] = {6, 14, 13, 18, 17}, kZdn[5] = {5, 11, 12, 15, 16};
@@ -444,7 +484,13 @@ int launch_boundaries(mflbm_context& c, bool odd) {
     if (p.kper == 0 && p.domain_wall_status_z_min == 0 && p.domain_wall_status_z_max == 0) {
         const int in = p.inlet_BC == 1 || p.inlet_BC == 2 ? p.inlet_BC : 0;
         const int out = p.outlet_BC == 1 || p.outlet_BC == 2 ? p.outlet_BC : 0;
-        if (in || out) {
+        if ((in == 0 || in == 1) && (out == 0 || out == 1) && (in || out)) {
+            const int ntx = (g.nx + 15) / 16, ncolp = ntx * 16 * ((g.ny + 1) / 2 * 2);
+            rc = launch_pdl("inlet_outlet",
+                            odd ? inlet_outlet_links_kernel<T, E, true> : inlet_outlet_links_kernel<T, E, false>,
+                            grid_for((ll)ncolp * 11, 128), 128, s, a, in, out, ntx, ncolp);
+            if (rc != MFLBM_OK) return rc;
+        } else if (in || out) {
             rc = launch_pdl("inlet_outlet", odd ? inlet_outlet_kernel<T, E, true> : inlet_outlet_kernel<T, E, false>,
                             face_grid(g), 128, s, a, in, out);
             if (rc != MFLBM_OK) return rc;
