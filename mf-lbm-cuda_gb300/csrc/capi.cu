@@ -55,7 +55,7 @@ void free_all(mflbm_context* c) {
     void* ptrs[] = {d.pdf, d.phi, d.cn_x, d.cn_y, d.cn_z, d.c_norm, d.curv, d.W_in, d.f_cv, d.g_cv, d.phi_cv,
                     d.walls, d.walls_type, d.s_nx, d.s_ny, d.s_nz, d.fluid_list, d.list_phi_ext,
                     d.red, d.staging, d.aux, d.type8, d.cnv4, d.zpair_off,
-                    d.phi_prev, d.prof, d.dither, d.iface, d.pmask, d.fmask, d.cmask, d.tmap, d.olist, d.nlist, d.gcount,
+                    d.phi_prev, d.prof, d.dither, d.iface, d.touch, d.snb, d.pmask, d.fmask, d.cmask, d.tmap, d.olist, d.nlist, d.gcount,
                     d.sbcode, d.sbact, d.sblive, d.sbinfo, d.phioff};
     for (void* p : ptrs) if (p) cudaFree(p);
     d = DeviceState{};
@@ -217,6 +217,27 @@ int build_lists(mflbm_context* c) {
     if ((rc = upload_list(&d.list_phi_ext, &d.n_phi_ext, lphi)) != MFLBM_OK) return rc;
     d.n_cn_ext = ncn;
     {
+        // per fluid node of [-1, n+2]^3: its neighbours whose normal record
+        // the solid-normal extrapolation writes (walls_type 2 on [0, n+1]^3),
+        // for the tags of the normal pass
+        std::vector<uint32_t> nb(g.n2(), 0u);
+        for (int k = -1; k <= g.nz + 2; ++k)
+            for (int j = -1; j <= g.ny + 2; ++j)
+                for (int i = -1; i <= g.nx + 2; ++i) {
+                    if (wt[g.s4(i, j, k)] > 0) continue;
+                    uint32_t m = 0;
+                    for (int q = 1; q < 19; ++q) {
+                        const int x = i + ex(q), y = j + ey(q), z = k + ez(q);
+                        if (x >= 0 && x <= g.nx + 1 && y >= 0 && y <= g.ny + 1 && z >= 0 && z <= g.nz + 1 &&
+                            wt[g.s4(x, y, z)] == 2)
+                            m |= 1u << q;
+                    }
+                    nb[g.s2(i, j, k)] = m;
+                }
+        ll nnb = 0;
+        if ((rc = upload_list(&d.snb, &nnb, nb)) != MFLBM_OK) return rc;
+    }
+    {
         // lists of the sparse gradient passes (all records start as zero records)
         int dev = 0;
         MFLBM_CUDA(cudaGetDevice(&dev));
@@ -240,6 +261,7 @@ int build_lists(mflbm_context* c) {
     // solid nodes keep a zero normal record (only fluid nodes are rewritten per step)
     MFLBM_CUDA(cudaMemset(d.cnv4, 0, rec * g.n2()));
     MFLBM_CUDA(cudaMemset(d.iface, 0, g.n2()));
+    MFLBM_CUDA(cudaMemset(d.touch, 0, g.n2()));
     c->pair_graph_odd_first = -1;  // kernels are launched with the list sizes
     c->generation++;
     return request_full_pass(c);
@@ -652,7 +674,7 @@ int mflbm_create(const mflbm_params* params, mflbm_context** out) {
         {&d.f_cv, T * g.plane1() * 19}, {&d.g_cv, T * g.plane1() * 19}, {&d.phi_cv, T * g.plane1()},
         {(void**)&d.walls, sizeof(int32_t) * g.n2()}, {(void**)&d.walls_type, sizeof(int32_t) * g.n4()},
         {&d.s_nx, T * g.n4()}, {&d.s_ny, T * g.n4()}, {&d.s_nz, T * g.n4()},
-        {(void**)&d.dither, 2 * sizeof(uint32_t)}, {(void**)&d.iface, (size_t)g.n2()},
+        {(void**)&d.dither, 2 * sizeof(uint32_t)}, {(void**)&d.iface, (size_t)g.n2()}, {(void**)&d.touch, (size_t)g.n2()},
         {(void**)&d.pmask, sizeof(uint16_t) * (size_t)d.SX * (g.ny + 8) * (g.nz + 8)},
         {(void**)&d.sbcode, nsb}, {(void**)&d.sbact, nsb}, {(void**)&d.sblive, sizeof(uint32_t) * nsb},
         {(void**)&d.sbinfo, 4 * sizeof(int)}};

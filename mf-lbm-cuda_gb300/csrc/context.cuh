@@ -54,6 +54,9 @@ struct DeviceState {
     ll prof_len = 0;
     uint32_t* dither = nullptr;        // step counter of 16-bit stochastic rounding: [0] read by odd, [1] by even steps
     int8_t* iface = nullptr;           // s2: 1 where the normal record may be non-zero (|grad phi| >= 1e-6, type <= 0)
+    uint8_t* touch = nullptr;          // s2 (solid boundary nodes): tag of the last gradient pass that found a
+                                       // non-zero record at one of the node's fluid neighbours, 0 when cleared
+    uint32_t* snb = nullptr;           // s2 (fluid nodes): bit q where x + e_q is a solid boundary node of [0, n+1]^3
     uint16_t* pmask = nullptr;         // s4 rows x super-block columns: phi near +1 / -1 bits (gradient.cuh)
     uint8_t* fmask = nullptr;          // the same rows: fluid nodes of [1, n]^3
     uint8_t* cmask = nullptr;          // the same rows: walls_type <= 0 on [-1, n+2]^3

@@ -48,6 +48,9 @@ template <class T> struct GradArgs {
     V4* cn;    // s2: (n_x, n_y, n_z, |grad phi|)
     V4* aux;   // fluid-list order: (n_x, n_y, n_z, 0.5 * gamma * curv * c_norm)
     int8_t* iface;  // s2 (fluid nodes): 1 where the record may be non-zero; 0: the zero record
+    uint8_t* touch;        // s2 (solid boundary nodes): tag of the last pass with a non-zero record next to it
+    const uint32_t* snb;   // s2 (fluid nodes): bit q where x + e_q is a solid boundary node of [0, n+1]^3
+    int tag;               // this pass's tag, 1 or 2 (alternating); the previous pass had the other
     uint16_t* pmask;       // s4 rows (y, z) x super-block columns: phi near +1 bits (low byte), near -1 (high byte)
     const uint8_t* fmask;  // the same rows: fluid nodes of [1, n]^3
     const uint8_t* cmask;  // the same rows: walls_type <= 0 on [-1, n+2]^3 (the nodes whose normal may be non-zero)
@@ -55,7 +58,7 @@ template <class T> struct GradArgs {
     uint32_t* olist;       // packed coordinates of the nodes whose record is non-zero (interface flag set)
     uint32_t* nlist;       // packed fluid nodes whose normal this pass recomputes
     int* gcount;           // [0] olist, [2] nlist lengths, [1] solid nodes given a non-zero normal by this
-                           // pass; [4] the previous pass's [0]
+                           // pass; [4] the previous pass's [0]; [5] 1: this pass processes every node
     T *cnx, *cny, *cnz, *cnorm, *curv;  // reference-layout arrays (export / pack)
     const uint2* l_phi;
     const uint32_t* l_fluid;
@@ -185,6 +188,7 @@ __global__ void __launch_bounds__(256) sb_live_kernel(const GradArgs<T> a) {
         // reset of its records (clear_records)
         a.gcount[4] = a.gcount[0];
         a.gcount[0] = a.gcount[1] = a.gcount[2] = 0;
+        a.gcount[5] = a.sbinfo[1] != 0 ? 1 : 0;
     }
     warp_append(live, (uint32_t)s, a.sblive, a.live_n, a.SX * a.SY * a.SZ);
 }
@@ -449,7 +453,8 @@ __device__ __forceinline__ bool normal_at(const GradArgs<T>& a, int i, int j, in
 
 // unit interface normal and |grad phi| (:757-807) + wetting (:809-878) at the
 // nodes of nlist; nodes with a non-zero record are appended to olist (one
-// atomic per warp).
+// atomic per warp) and give their solid boundary neighbours (snb) this
+// pass's tag: plain byte stores of one value, so concurrent writers agree.
 template <class T>
 __global__ void __launch_bounds__(256, 8) normals_kernel(const GradArgs<T> a) {
     pdl_wait();
@@ -465,6 +470,16 @@ __global__ void __launch_bounds__(256, 8) normals_kernel(const GradArgs<T> a) {
             packed = a.nlist[p];
             unpack_xyz(packed, i, j, k);
             on = normal_at<T>(a, i, j, k, a.type8[g.s4(i, j, k)]);
+            if (on) {
+                const ll n2 = g.s2(i, j, k);
+                const uint32_t m = a.snb[n2];
+                if (m) {
+                    const ll sy = g.nx + 4, sz = (ll)(g.nx + 4) * (g.ny + 4);
+#pragma unroll
+                    for (int q = 1; q < 19; ++q)
+                        if (m & (1u << q)) a.touch[n2 + ex(q) + ey(q) * sy + ez(q) * sz] = (uint8_t)a.tag;
+                }
+            }
         }
         warp_append(on, packed, a.olist, &a.gcount[0], a.n_norm);
     }
@@ -479,7 +494,16 @@ __global__ void __launch_bounds__(256, 8) normals_kernel(const GradArgs<T> a) {
 // phi that changed: within three nodes of a flagged super-block, inside the
 // processed ones.  Neighbours whose interface flag is clear hold the zero
 // record: their +0 terms are skipped (only their weights are summed), which
-// leaves every sum bit-identical.  One block per super-block of this pass;
+// leaves every sum bit-identical.
+// The non-zero fluid records after a pass are exactly those of its olist, so
+// a solid node's record can differ from its last written value only if a
+// fluid neighbour is in this pass's olist (the normal pass tagged it with
+// this pass's tag) or in the previous one's (the previous tag).  Only those
+// are recomputed; a node that carries the previous tag has no non-zero
+// neighbour left, so it gets the zero record and its tag is cleared.  A node
+// tagged two passes ago and not since carries the current tag value again
+// and is recomputed once more, which is harmless.  A pass after the host set
+// the state recomputes every node.  One block per super-block of this pass;
 // gcount[1] counts the non-zero results.
 template <class T>
 __global__ void __launch_bounds__(256) extrapolate_normal_kernel(const GradArgs<T> a) {
@@ -487,6 +511,8 @@ __global__ void __launch_bounds__(256) extrapolate_normal_kernel(const GradArgs<
     const Grid& g = a.g;
     const int sy = g.nx + 4, sz = (g.nx + 4) * (g.ny + 4);
     const int nl = min(*a.live_n, a.SX * a.SY * a.SZ);
+    const bool all = a.gcount[5] != 0;
+    const uint8_t tag = (uint8_t)a.tag, prev = (uint8_t)(3 - a.tag);
     int nonzero = 0;
     for (int w = blockIdx.x; w < nl; w += gridDim.x) {
         const uint32_t sb = a.sblive[w];
@@ -496,6 +522,18 @@ __global__ void __launch_bounds__(256) extrapolate_normal_kernel(const GradArgs<
             unpack_xyz(e.x, i, j, k);
             if (i < 0 || j < 0 || k < 0 || i > g.nx + 1 || j > g.ny + 1 || k > g.nz + 1) continue;
             const int n = (int)g.s2(i, j, k);
+            if (!all) {
+                const uint8_t tv = a.touch[n];
+                if (tv != tag) {
+                    if (tv == prev) {
+                        typename Vec4<T>::type z;
+                        z.x = T(0); z.y = T(0); z.z = T(0); z.w = T(0);
+                        a.cn[n] = z;
+                        a.touch[n] = 0;
+                    }
+                    continue;
+                }
+            }
             T sx = T(0), syy = T(0), szz = T(0), ws = T(0);
 #pragma unroll
             for (int q = 1; q < 19; ++q) {
@@ -648,6 +686,7 @@ GradArgs<T> grad_args(const mflbm_context& c) {
     a.cn = (typename Vec4<T>::type*)d.cnv4;
     a.aux = (typename Vec4<T>::type*)d.aux;
     a.iface = d.iface;
+    a.touch = d.touch; a.snb = d.snb; a.tag = 1;
     a.pmask = d.pmask; a.fmask = d.fmask; a.cmask = d.cmask;
     a.tmap = d.tmap;
     a.olist = d.olist; a.nlist = d.nlist; a.gcount = d.gcount;
@@ -679,6 +718,7 @@ int launch_gradient(mflbm_context& c) {
     GradArgs<T> a = grad_args<T>(c);
     a.live_n = c.d.sbinfo + (c.d.grad_parity ? 2 : 0);
     a.live_next = c.d.sbinfo + (c.d.grad_parity ? 0 : 2);
+    a.tag = 1 + c.d.grad_parity;
     c.d.grad_parity ^= 1;
     const Tuning& tn = c.d.tune;
     cudaStream_t s = c.stream;
