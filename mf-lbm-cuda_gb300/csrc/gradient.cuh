@@ -503,57 +503,112 @@ __global__ void __launch_bounds__(256, 8) normals_kernel(const GradArgs<T> a) {
 // neighbour left, so it gets the zero record and its tag is cleared.  A node
 // tagged two passes ago and not since carries the current tag value again
 // and is recomputed once more, which is harmless.  A pass after the host set
-// the state recomputes every node.  One block per super-block of this pass;
-// gcount[1] counts the non-zero results.
+// the state recomputes every node.  Each block takes a run of consecutive
+// live super-blocks (about live / grid of them) and lays their solid nodes
+// out as one index range (offsets in shared memory); a thread loads the list
+// entries and then the tags of kNodes nodes before it handles any of them,
+// so the loads of a block overlap instead of following each other per
+// super-block.  gcount[1] counts the non-zero results.
 template <class T>
 __global__ void __launch_bounds__(256) extrapolate_normal_kernel(const GradArgs<T> a) {
     pdl_wait();
+    typedef typename Vec4<T>::type V4;
+    constexpr int kMaxSB = 32;   // super-blocks per batch (one warp's scan)
+    constexpr int kNodes = 4;    // list entries per thread per round
+    __shared__ int s_beg[kMaxSB + 1], s_off[kMaxSB];
+    __shared__ int s_dn[19];     // s2 offset of direction q
     const Grid& g = a.g;
     const int sy = g.nx + 4, sz = (g.nx + 4) * (g.ny + 4);
+    if (threadIdx.x < 19) {
+        const int q = threadIdx.x;
+        s_dn[q] = ex(q) + ey(q) * sy + ez(q) * sz;
+    }
     const int nl = min(*a.live_n, a.SX * a.SY * a.SZ);
     const bool all = a.gcount[5] != 0;
     const uint8_t tag = (uint8_t)a.tag, prev = (uint8_t)(3 - a.tag);
+    const int per = min(kMaxSB, max(1, (nl + (int)gridDim.x - 1) / (int)gridDim.x));
     int nonzero = 0;
-    for (int w = blockIdx.x; w < nl; w += gridDim.x) {
-        const uint32_t sb = a.sblive[w];
-        for (int t = a.phioff[sb] + threadIdx.x; t < a.phioff[sb + 1]; t += blockDim.x) {
-            const uint2 e = a.l_phi[t];
-            int i, j, k;
-            unpack_xyz(e.x, i, j, k);
-            if (i < 0 || j < 0 || k < 0 || i > g.nx + 1 || j > g.ny + 1 || k > g.nz + 1) continue;
-            const int n = (int)g.s2(i, j, k);
-            if (!all) {
-                const uint8_t tv = a.touch[n];
-                if (tv != tag) {
-                    if (tv == prev) {
-                        typename Vec4<T>::type z;
+    for (int w0 = blockIdx.x * per; w0 < nl; w0 += gridDim.x * per) {
+        if (threadIdx.x < 32) {
+            const int lane = threadIdx.x;
+            int cnt = 0, off = 0;
+            if (lane < per && w0 + lane < nl) {
+                const uint32_t sb = a.sblive[w0 + lane];
+                off = a.phioff[sb];
+                cnt = a.phioff[sb + 1] - off;
+            }
+            int incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += v;
+            }
+            if (lane < per) { s_off[lane] = off; s_beg[lane + 1] = incl; }
+            if (lane == 0) s_beg[0] = 0;
+        }
+        __syncthreads();
+        const int total = s_beg[per];
+        for (int t0 = threadIdx.x; t0 < total; t0 += kNodes * blockDim.x) {
+            int n[kNodes];
+            uint32_t nb[kNodes];
+#pragma unroll
+            for (int u = 0; u < kNodes; ++u) {
+                const int t = t0 + u * (int)blockDim.x;
+                n[u] = -1;
+                nb[u] = 0;
+                if (t < total) {
+                    int lo = 0, hi = per;   // s_beg[lo] <= t < s_beg[hi]
+                    while (hi - lo > 1) {
+                        const int mid = (lo + hi) >> 1;
+                        if (s_beg[mid] <= t) lo = mid; else hi = mid;
+                    }
+                    const uint2 e = a.l_phi[s_off[lo] + t - s_beg[lo]];
+                    int i, j, k;
+                    unpack_xyz(e.x, i, j, k);
+                    if (i >= 0 && j >= 0 && k >= 0 && i <= g.nx + 1 && j <= g.ny + 1 && k <= g.nz + 1) {
+                        n[u] = (int)g.s2(i, j, k);
+                        nb[u] = e.y;
+                    }
+                }
+            }
+            uint8_t tv[kNodes];
+#pragma unroll
+            for (int u = 0; u < kNodes; ++u) tv[u] = (n[u] >= 0 && !all) ? a.touch[n[u]] : tag;
+#pragma unroll
+            for (int u = 0; u < kNodes; ++u) {
+                if (n[u] < 0) continue;
+                if (tv[u] != tag) {
+                    if (tv[u] == prev) {
+                        V4 z;
                         z.x = T(0); z.y = T(0); z.z = T(0); z.w = T(0);
-                        a.cn[n] = z;
-                        a.touch[n] = 0;
+                        a.cn[n[u]] = z;
+                        a.touch[n[u]] = 0;
                     }
                     continue;
                 }
-            }
-            T sx = T(0), syy = T(0), szz = T(0), ws = T(0);
-#pragma unroll
-            for (int q = 1; q < 19; ++q) {
-                if (e.y & (1u << q)) {
-                    const int m = n + ex(q) + ey(q) * sy + ez(q) * sz;
+                // the fluid neighbours in direction order (lowest bit first)
+                T sx = T(0), syy = T(0), szz = T(0), ws = T(0);
+                uint32_t m = nb[u] & 0x7FFFEu;
+                while (m) {
+                    const int q = __ffs(m) - 1;
+                    m &= m - 1;
+                    const int mm = n[u] + s_dn[q];
                     const T wq = wq_of(a.ph.c, q);
-                    if (a.iface[m]) {
-                        const typename Vec4<T>::type v = a.cn[m];
+                    if (a.iface[mm]) {
+                        const V4 v = a.cn[mm];
                         sx += v.x * wq;
                         syy += v.y * wq;
                         szz += v.z * wq;
                     }
                     ws += wq;
                 }
+                V4 r;
+                r.x = sx / ws; r.y = syy / ws; r.z = szz / ws; r.w = T(0);
+                a.cn[n[u]] = r;
+                nonzero += (r.x != T(0) || r.y != T(0) || r.z != T(0)) ? 1 : 0;
             }
-            typename Vec4<T>::type r;
-            r.x = sx / ws; r.y = syy / ws; r.z = szz / ws; r.w = T(0);
-            a.cn[n] = r;
-            nonzero += (r.x != T(0) || r.y != T(0) || r.z != T(0)) ? 1 : 0;
         }
+        __syncthreads();   // s_beg / s_off of the next batch
     }
     // one atomic per warp
 #pragma unroll
