@@ -451,6 +451,15 @@ int mflbm_unet_set_params(mflbm_unet* net, const float* params);
 int mflbm_unet_conv_check(int D, int H, int W, int cin, int cout, const float* x,
                           const float* w, const float* b, int relu, const float* gy,
                           float* y, float* gx, float* gw, float* gb);
+/* Network inputs of a pore geometry (no counterpart in the reference):
+ * walls nz*ny*nx (x fastest, non-zero = solid, at least one solid and one
+ * fluid voxel); x nz*ny*nx*2: the solid mask (1 / 0) and the signed
+ * Euclidean distance between voxel centres to the nearest voxel of the other
+ * kind (positive in the fluid, negative in solids), times sdf_scale.  Bit 0,
+ * 1, 2 of periodic_xyz make x, y, z periodic (distances by the minimum
+ * image).  Exact distances, computed on the device. */
+int mflbm_unet_features(const int32_t* walls, int nx, int ny, int nz, int periodic_xyz,
+                        float sdf_scale, float* x);
 /* Bound of the tensor-core convolutions' waits for their pipeline stages,
  * in mbarrier polls (default 1048576).  A wait that runs out makes the call
  * return MFLBM_E_CUDA; the copies and MMAs still in flight are waited for

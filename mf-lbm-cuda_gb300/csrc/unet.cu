@@ -627,6 +627,36 @@ int mflbm_unet_gradients(mflbm_unet* n, const float* x, const float* target, con
 // One convolution and its gradients on host arrays (checks against a CPU
 // restatement): x D*H*W*cin, w cout*27*cin, b cout, gy D*H*W*cout, all FP32
 // (rounded to BF16 on the device); outputs y (FP32 before rounding), gx, gw, gb.
+// Network inputs of a geometry (solid mask, signed distance times sdf_scale)
+// from its wall array, on the device: three separable passes of the exact
+// distance transform (both signs at once) and one pass forming the inputs.
+// All work is on the legacy default stream, in order with the allocations.
+int mflbm_unet_features(const int32_t* walls, int nx, int ny, int nz, int periodic_xyz, float sdf_scale, float* x) {
+    if (!walls || !x) return fail(MFLBM_E_ARG, "mflbm_unet_features: null argument");
+    if (nx < 1 || ny < 1 || nz < 1 || nx > 4096 || ny > 4096 || nz > 4096)
+        return fail(MFLBM_E_ARG, "mflbm_unet_features: extents must be in [1, 4096]");
+    const U::Dims d{nz, ny, nx};
+    const size_t V = (size_t)nx * ny * nz;
+    size_t solids = 0;
+    for (size_t i = 0; i < V; ++i) solids += walls[i] != 0;
+    if (solids == 0 || solids == V)
+        return fail(MFLBM_E_ARG, "mflbm_unet_features: the geometry needs both solid and fluid voxels");
+    DevBuf w, a, b, out;
+    int rc;
+    if ((rc = w.alloc(V * sizeof(int32_t))) != MFLBM_OK || (rc = a.alloc(V * sizeof(int2))) != MFLBM_OK ||
+        (rc = b.alloc(V * sizeof(int2))) != MFLBM_OK || (rc = out.alloc(V * 2 * sizeof(float))) != MFLBM_OK)
+        return rc;
+    MFLBM_CUDA(cudaMemcpy(w.p, walls, V * sizeof(int32_t), cudaMemcpyHostToDevice));
+    const unsigned g = nblk(V, 128);
+    U::edt_axis_kernel<<<g, 128>>>(w.as<int32_t>(), nullptr, a.as<int2>(), d, 0, periodic_xyz & 1);
+    U::edt_axis_kernel<<<g, 128>>>(w.as<int32_t>(), a.as<int2>(), b.as<int2>(), d, 1, (periodic_xyz >> 1) & 1);
+    U::edt_axis_kernel<<<g, 128>>>(w.as<int32_t>(), b.as<int2>(), a.as<int2>(), d, 2, (periodic_xyz >> 2) & 1);
+    U::edt_features_kernel<<<nblk(V), 256>>>(w.as<int32_t>(), a.as<int2>(), V, (double)sdf_scale, out.as<float>());
+    MFLBM_CUDA(cudaGetLastError());
+    MFLBM_CUDA(cudaMemcpy(x, out.p, V * 2 * sizeof(float), cudaMemcpyDeviceToHost));
+    return MFLBM_OK;
+}
+
 int mflbm_unet_set_wait_limit(unsigned int polls) {
     MFLBM_CUDA(cudaMemcpyToSymbol(U::g_tc_stage_wait, &polls, sizeof(polls)));
     return MFLBM_OK;

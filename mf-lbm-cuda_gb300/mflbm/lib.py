@@ -69,6 +69,7 @@ SIGNATURES = {
     "mflbm_unet_set_params": (I, [VP, VP]),
     "mflbm_unet_conv_check": (I, [I, I, I, I, I, VP, VP, VP, I, VP, VP, VP, VP, VP]),
     "mflbm_unet_set_wait_limit": (I, [C.c_uint]),
+    "mflbm_unet_features": (I, [VP, I, I, I, I, C.c_float, VP]),
     "mflbm_node_counts": (I, [VP, C.POINTER(LL)]),
     "mflbm_stream": (VP, [VP]),
     "mflbm_set_kernel_timing": (I, [VP, I]),

@@ -119,24 +119,17 @@ def conv_check(x, w, b, gy=None, relu=False):
 # ---------------------------------------------------------------------------
 def features(walls_global, shape, periodic=(False, True, True), sdf_scale=0.125):
     """Inputs of the network for a wall array (the s0 layout of
-    ``lib.set_walls``: nz x ny x nx, non-zero = solid): channel 0 the solid
-    mask, channel 1 the signed Euclidean distance to the nearest solid-fluid
-    boundary (positive in the fluid), times sdf_scale.  periodic: per axis
-    (x, y, z) whether distances wrap around."""
-    from scipy import ndimage
-
+    ``lib.set_walls``: nz x ny x nx, non-zero = solid), computed on the
+    device by ``mflbm_unet_features``: channel 0 the solid mask, channel 1
+    the signed Euclidean distance to the nearest voxel of the other kind
+    (positive in the fluid), times sdf_scale.  periodic: per axis (x, y, z)
+    whether distances wrap around (minimum image)."""
     nx, ny, nz = shape
-    solid = (np.asarray(walls_global).reshape(nz, ny, nx) != 0)
-    pad = 16
-    pw = [(pad if periodic[2] else 0,) * 2, (pad if periodic[1] else 0,) * 2, (pad if periodic[0] else 0,) * 2]
-    s = np.pad(solid, pw, mode="wrap")
-    d_f = ndimage.distance_transform_edt(~s)
-    d_s = ndimage.distance_transform_edt(s)
-    sl = tuple(slice(p[0], p[0] + n) for p, n in zip(pw, (nz, ny, nx)))
-    sdf = (d_f - d_s)[sl]
+    w = np.ascontiguousarray(np.asarray(walls_global).reshape(nz, ny, nx), dtype=np.int32)
     x = np.empty((nz, ny, nx, N_IN), np.float32)
-    x[..., 0] = solid
-    x[..., 1] = sdf * sdf_scale
+    bits = int(bool(periodic[0])) | int(bool(periodic[1])) << 1 | int(bool(periodic[2])) << 2
+    lib.check(lib.load().mflbm_unet_features(ptr(w), nx, ny, nz, bits, C.c_float(sdf_scale), ptr(x)),
+              "mflbm_unet_features")
     return x
 
 

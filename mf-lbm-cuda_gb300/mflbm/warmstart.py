@@ -6,21 +6,26 @@ warm and cold starts on held-out samples.
         --json out.json [--model unet.npz] [--load unet.npz]
 
 Training samples are seeded single-phase grain packs (porosity uniform in
-0.3-0.7) run to a converged permeability by ``mflbm_batch`` (FP32).  For each
-held-out sample the study runs
+0.3-0.7) run to a converged permeability by ``mflbm_batch`` (FP32); the
+network's inputs come from the device (``mflbm_unet_features``).  Held-out
+samples may be larger than the training ones (``--n-eval``: the network is
+fully convolutional).  For each held-out sample the study runs
   * the FP64 cold start (rest equilibrium; the accuracy reference),
-  * the plain FP32 cold start,
-  * the warm starts: network inference and equilibrium fill, with FP32 and
-    with FP16 population storage, falling back to the cold start when the
-    permeability after the first check interval differs from the prediction
-    by more than ``--fallback`` (relative),
+  * the plain FP32 cold start, and the cold start with 16-bit storage,
+  * the warm starts: features, network inference and equilibrium fill, with
+    FP32 and with 16-bit population storage, falling back to the cold start
+    when the permeability after the first check interval differs from the
+    prediction by more than ``--fallback`` (relative),
   * the oracle starts: the fill from the converged FP64 field itself (the
     bound on what a surrogate can give), with the collision's equilibrium
     (as the warm start) and with the reference's a17 lattice-weight
-    equilibrium,
-each to the same convergence criterion (k changes by less than ``--tol``,
-relative, over ``--interval`` steps), and reports steps, wall time
-(inference included) and the permeability error against the FP64 cold start.
+    equilibrium.
+Each start is run once with k recorded every ``--every`` steps.  Two stopping
+rules are read from that record: convergence (k changes by less than
+``--tol``, relative, over ``--interval`` steps) and the band (k stays within
+``--band``, relative, of the FP64 cold start's converged k from that step
+on: "time to a converged k within 1 % of FP64").  The wall time to each is
+then measured in a run of its own without checks, start-up included.
 """
 from __future__ import annotations
 
@@ -157,17 +162,62 @@ def transient(ctx, case, walls, t_ref, k_ref, nu, g):
     return {"steps": list(CHECKPOINTS), "k_over_kref": ks, "uz_rel_err": errs}
 
 
-def evaluate(ws, case, tol, interval, max_steps, fallback, storage=abi.MFLBM_STORE_F16, with_transient=False):
+def record_run(ctx, case, tol, interval, max_steps, every, check=None, on_fallback=None):
+    """Steps one context and records k every `every` steps until k changes by
+    <= tol (relative) over `interval` steps (or max_steps).  check(k) after
+    the first `interval` steps may return False: then on_fallback() restarts
+    the context (the cold start) and the run goes on from there.  Returns the
+    trajectory [(steps, k)], the step of the first check after the
+    fallback (or None) and the steps to the tol criterion."""
+    traj, nt, steps, fell = [], 1, 0, None
+    back = interval // every
+    while steps < max_steps:
+        ctx.run(nt, every)
+        nt += every
+        steps += every
+        k = permeability(ctx, case)
+        traj.append((steps, k))
+        if check is not None and fell is None and steps == interval and not check(k):
+            on_fallback()
+            fell, nt = steps, 1
+            continue
+        if len(traj) > back and (fell is None or steps - fell >= interval):
+            k_old = traj[-1 - back][1]
+            if abs(k - k_old) <= tol * abs(k):
+                return traj, fell, steps
+    return traj, fell, steps
+
+
+def band_steps(traj, k_ref, band):
+    """First recorded step from which every later k lies within `band`
+    (relative) of k_ref; None if the last one does not."""
+    first = None
+    for s, k in traj:
+        if abs(k - k_ref) <= band * abs(k_ref):
+            if first is None:
+                first = s
+        else:
+            first = None
+    return first
+
+
+def evaluate(ws, case, tol, interval, max_steps, fallback, storage=abi.MFLBM_STORE_F16, with_transient=False,
+             band=0.01, every=50):
     """One held-out sample: the FP64 cold start (the accuracy reference, and
-    the converged field of the oracle start), the FP32 cold start, the warm
-    starts (FP32 and, unless `storage` is native, 16-bit storage) and the
-    oracle start (equilibrium fill from the converged FP64 field: the best
-    any surrogate could give through the equilibrium fill).  Steps and wall
-    time to convergence, k errors against the FP64 cold start; optionally
-    the transients of the cold, warm and oracle starts (untimed runs)."""
+    the converged field of the oracle start), the FP32 cold start, the cold
+    start with 16-bit storage, the warm starts (FP32 and, unless `storage` is
+    native, 16-bit storage) and the oracle start (equilibrium fill from the
+    converged FP64 field: the best any surrogate could give through the
+    equilibrium fill).  Each start is run once with k recorded every `every`
+    steps, which gives the steps to the convergence criterion (tol over
+    interval) and the steps after which k stays within `band` of the FP64
+    cold start's converged k; each of the two step counts is then timed in
+    a run of its own without checks (start-up, features and inference of the
+    warm starts included).  Optionally the transients of the cold, warm and
+    oracle starts (untimed runs)."""
     nu, g = nu_g(case)
     nx, ny, nz = case.shape
-    rec = {"case": case.name, "porosity_target": case.geometry.porosity}
+    rec = {"case": case.name, "porosity_target": case.geometry.porosity, "n": [nx, ny, nz]}
     ctx, info = lib.setup_case(case, abi.MFLBM_FP64, abi.MFLBM_FAST)
     walls = info["walls_global"]
     cold_start(ctx, info)
@@ -181,7 +231,7 @@ def evaluate(ws, case, tol, interval, max_steps, fallback, storage=abi.MFLBM_STO
     variants = [("fp32_cold", abi.MFLBM_STORE_NATIVE, "cold"), ("warm_fp32", abi.MFLBM_STORE_NATIVE, "warm"),
                 ("oracle_fp32", abi.MFLBM_STORE_NATIVE, "oracle"), ("oracle_a17", abi.MFLBM_STORE_NATIVE, "oracle_a17")]
     if storage != abi.MFLBM_STORE_NATIVE:
-        variants.append(("warm", storage, "warm"))
+        variants += [("cold", storage, "cold"), ("warm", storage, "warm")]
     k_pred = None
 
     def start(ctx, info, how):
@@ -195,6 +245,26 @@ def evaluate(ws, case, tol, interval, max_steps, fallback, storage=abi.MFLBM_STO
         elif how == "oracle_a17":
             unet.fill_from_prediction(ctx, t_ref / ws.scales, walls, nu, g, ws.scales, mrt=False)
 
+    def timed(st, how, n_steps, fell):
+        """Wall seconds of the start plus n_steps steps (the fallback, if the
+        recorded run took it, at the same step), no checks in between."""
+        ctx, info = lib.setup_case(case, abi.MFLBM_FP32, abi.MFLBM_FAST, storage=st)
+        cold_start(ctx, info)
+        ctx.sync()
+        t0 = time.perf_counter()
+        start(ctx, info, how)
+        if fell is not None and n_steps > fell:
+            ctx.run(1, fell)
+            permeability(ctx, case)
+            cold_start(ctx, info, capture=False)
+            ctx.run(1, n_steps - fell)
+        else:
+            ctx.run(1, n_steps)
+        ctx.sync()
+        sec = time.perf_counter() - t0
+        ctx.close()
+        return sec
+
     for name, st, how in variants:
         ctx, info = lib.setup_case(case, abi.MFLBM_FP32, abi.MFLBM_FAST, storage=st)
         cold_start(ctx, info)
@@ -205,14 +275,16 @@ def evaluate(ws, case, tol, interval, max_steps, fallback, storage=abi.MFLBM_STO
         if how == "warm":
             kp = k_pred
             check = lambda k1: abs(k1 - kp) <= fallback * abs(k1)
-        k, steps, ok = run_until_converged(ctx, case, tol, interval, max_steps, check=check)
-        if not ok:
-            cold_start(ctx, info, capture=False)
-            k, s2, _ = run_until_converged(ctx, case, tol, interval, max_steps)
-            steps += s2
-        rec[name] = {"k": k, "steps": steps, "seconds": time.perf_counter() - t0, "start_seconds": t_start,
-                     "fallback": not ok, "storage": names[st], "k_rel_err": abs(k - k_ref) / abs(k_ref)}
+        traj, fell, steps = record_run(ctx, case, tol, interval, max_steps, every, check,
+                                       on_fallback=lambda: cold_start(ctx, info, capture=False))
         ctx.close()
+        k = traj[-1][1]
+        nb = band_steps(traj, k_ref, band)
+        r = {"k": k, "steps": steps, "seconds": timed(st, how, steps, fell), "start_seconds": t_start,
+             "fallback": fell is not None, "storage": names[st], "k_rel_err": abs(k - k_ref) / abs(k_ref),
+             "band_steps": nb, "band_seconds": timed(st, how, nb, fell) if nb else None,
+             "k_traj": [round(kk / k_ref, 5) for _, kk in traj[:40]]}
+        rec[name] = r
         if with_transient and st == abi.MFLBM_STORE_NATIVE:
             ctx, info = lib.setup_case(case, abi.MFLBM_FP32, abi.MFLBM_FAST)
             start(ctx, info, how)
@@ -240,6 +312,8 @@ def main():
     ap.add_argument("--model", default="", help="write the trained parameters here (.npz)")
     ap.add_argument("--load", default="", help="skip data generation and training: use these parameters")
     ap.add_argument("--transient", type=int, default=0, help="record the transients of the first N held-out samples")
+    ap.add_argument("--band", type=float, default=0.01, help="k within this of the FP64 cold start's (relative)")
+    ap.add_argument("--every", type=int, default=50, help="steps between recorded k")
     ap.add_argument("--json", default="")
     a = ap.parse_args()
     st = {"native": abi.MFLBM_STORE_NATIVE, "f16": abi.MFLBM_STORE_F16, "bf16": abi.MFLBM_STORE_BF16}[a.storage]
@@ -264,21 +338,29 @@ def main():
     ws = WarmStarter(params, scales)
     recs = []
     for i, c in enumerate(sample_cases(a.eval, a.n_eval or a.n, a.seed + 100000)):
-        r = evaluate(ws, c, a.tol, a.interval, a.max_steps, a.fallback, st, with_transient=i < a.transient)
+        r = evaluate(ws, c, a.tol, a.interval, a.max_steps, a.fallback, st, with_transient=i < a.transient,
+                     band=a.band, every=a.every)
         log(json.dumps(r))
         recs.append(r)
     ws.close()
     tot = lambda key, f: float(sum(r[key][f] for r in recs))
     out["samples"] = recs
-    summ = {"samples": len(recs), "fp64_cold_seconds": tot("fp64_cold", "seconds"),
+    summ = {"samples": len(recs), "band": a.band, "fp64_cold_seconds": tot("fp64_cold", "seconds"),
             "fp32_cold_seconds": tot("fp32_cold", "seconds"), "fp32_cold_steps": tot("fp32_cold", "steps"),
             "max_k_rel_err_fp32_cold": max(r["fp32_cold"]["k_rel_err"] for r in recs),
             "median_k_pred_rel_err": float(np.median([r["k_pred_rel_err"] for r in recs]))}
-    for v in [k for k in ("warm_fp32", "oracle_fp32", "oracle_a17", "warm") if k in recs[0]]:
+    in_band = all(r["fp32_cold"]["band_steps"] for r in recs)
+    if in_band:
+        summ["fp32_cold_band_seconds"] = tot("fp32_cold", "band_seconds")
+        summ["fp32_cold_band_steps"] = tot("fp32_cold", "band_steps")
+    for v in [k for k in ("warm_fp32", "oracle_fp32", "oracle_a17", "cold", "warm") if k in recs[0]]:
         summ[v] = {"seconds": tot(v, "seconds"), "steps": tot(v, "steps"),
                    "speedup_vs_fp32_cold": tot("fp32_cold", "seconds") / max(tot(v, "seconds"), 1e-12),
                    "max_k_rel_err": max(r[v]["k_rel_err"] for r in recs),
                    "fallbacks": sum(r[v]["fallback"] for r in recs), "storage": recs[0][v]["storage"]}
+        if in_band and all(r[v]["band_steps"] for r in recs):
+            summ[v].update({"band_seconds": tot(v, "band_seconds"), "band_steps": tot(v, "band_steps"),
+                            "band_speedup_vs_fp32_cold": tot("fp32_cold", "band_seconds") / tot(v, "band_seconds")})
     out["summary"] = summ
     log(json.dumps(out["summary"]))
     if a.json:

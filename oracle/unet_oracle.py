@@ -233,3 +233,24 @@ def init_params(seed):
         b[:real_out] = rng.normal(0, 0.05, real_out)
         out += [w.ravel(), b]
     return np.concatenate(out).astype(np.float32)
+
+
+def features(walls, periodic=(False, True, True), sdf_scale=0.125):
+    """Network inputs of a wall array [nz, ny, nx] (non-zero = solid), the
+    CPU restatement of mflbm_unet_features: solid mask and the signed exact
+    Euclidean distance to the nearest voxel of the other kind (scipy's
+    distance transform, positive in the fluid) times sdf_scale.  A periodic
+    axis is padded by a full period on both sides, so that every minimum
+    image lies inside the padded volume."""
+    from scipy import ndimage
+    solid = np.asarray(walls) != 0
+    nz, ny, nx = solid.shape
+    pw = [(n if p else 0,) * 2 for n, p in zip((nz, ny, nx), periodic[::-1])]
+    s = np.pad(solid, pw, mode="wrap")
+    d_f = ndimage.distance_transform_edt(~s)
+    d_s = ndimage.distance_transform_edt(s)
+    sl = tuple(slice(p[0], p[0] + n) for p, n in zip(pw, (nz, ny, nx)))
+    x = np.empty((nz, ny, nx, 2), np.float32)
+    x[..., 0] = solid
+    x[..., 1] = (d_f - d_s)[sl] * sdf_scale
+    return x

@@ -174,3 +174,39 @@ def test_init_flow_fills_the_equilibrium(mflbm_lib):
     assert np.allclose(np.tensordot(b, f, 1), -475.0 / 63.0 * j2, rtol=1e-9, atol=1e-13)
     ctx.close()
 
+
+
+def _grains(shape, frac, seed, walls_x=False):
+    from scipy import ndimage
+    rng = np.random.default_rng(seed)
+    s = ndimage.binary_dilation(rng.random(shape) < frac, iterations=2)
+    if walls_x:
+        s[:, :, 0] = s[:, :, -1] = True
+    return s.astype(np.int32)
+
+
+# Network inputs on the device (mflbm_unet_features) against scipy's exact
+# distance transform: bit-identical (both take the FP64 square root of the
+# same integer squared distance, scale by a power of two and round once).
+# The lone-grain cases have fluid voxels more than half a period from the
+# grain, so the minimum image decides their distance.
+@pytest.mark.parametrize("shape,frac,periodic,walls_x", [
+    ((32, 16, 24), 0.01, (False, True, True), True),
+    ((20, 28, 36), 0.004, (True, True, True), False),
+    ((17, 9, 23), 0.02, (False, False, False), False),
+    ((40, 40, 40), 0.0, (True, True, True), False),
+    ((40, 36, 44), 0.0, (False, True, True), True)])
+def test_features_match_oracle(mflbm_lib, shape, frac, periodic, walls_x):
+    w = _grains(shape, frac, 7, walls_x)
+    if w.sum() == 0:
+        w[shape[0] // 3, shape[1] // 2, shape[2] // 4] = 1   # one lone grain voxel
+    nz, ny, nx = shape
+    x = unet.features(w, (nx, ny, nz), periodic)
+    ref = UO.features(w, periodic)
+    assert x.tobytes() == ref.tobytes()
+
+
+def test_features_reject_uniform_geometry(mflbm_lib):
+    from mflbm import lib
+    with pytest.raises(lib.MflbmError, match="both solid and fluid"):
+        unet.features(np.zeros((8, 8, 8), np.int32), (8, 8, 8))
