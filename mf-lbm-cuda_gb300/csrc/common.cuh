@@ -147,12 +147,23 @@ template <class T, class E> struct PopCodec {  // native storage: identity
 template <> struct PopCodec<float, __half> {
     __device__ __forceinline__ static float dec(__half e, float w, float) { return w + w * __half2float(e); }
     __device__ __forceinline__ static __half enc(float v, float, float winv) { return __float2half_rn(v * winv - 1.0f); }
+    // Stochastic rounding on the bits.  Half-normal range: a half keeps the
+    // top 10 of the 23 mantissa bits; adding a 13-bit variate to the FP32
+    // bits and truncating (rz) rounds the magnitude up with probability equal
+    // to the dropped fraction (a carry into the exponent gives the next
+    // binade's value).  Half-subnormal range (|x| < 2^-14, spacing 2^-24):
+    // |x| * 2^40 (exact) plus a 16-bit variate, shifted down by 16, is the
+    // subnormal's integer mantissa, which is also its bit pattern (1024 gives
+    // 2^-14).  At or above the largest half: round to nearest.
     __device__ __forceinline__ static __half enc_dither(float v, float, float winv, uint32_t r16) {
         const float x = v * winv - 1.0f;
-        const __half lo = __float2half_rd(x), hi = __float2half_ru(x);
-        const float flo = __half2float(lo), fhi = __half2float(hi);
-        if (!(fhi > flo)) return lo;
-        return (float)r16 * (1.0f / 65536.0f) * (fhi - flo) < x - flo ? hi : lo;
+        const uint32_t b = __float_as_uint(x), mag = b & 0x7fffffffu;
+        if (mag < 0x38800000u) {
+            const uint32_t t = (uint32_t)(__uint_as_float(mag) * 1099511627776.0f);
+            return __ushort_as_half((unsigned short)(((b >> 16) & 0x8000u) | ((t + r16) >> 16)));
+        }
+        if (mag >= 0x477fe000u) return __float2half_rn(x);
+        return __float2half_rz(__uint_as_float(b + (r16 >> 3)));
     }
 };
 template <> struct PopCodec<float, __nv_bfloat16> {
@@ -160,12 +171,15 @@ template <> struct PopCodec<float, __nv_bfloat16> {
     __device__ __forceinline__ static __nv_bfloat16 enc(float v, float, float winv) {
         return __float2bfloat16_rn(v * winv - 1.0f);
     }
+    // Stochastic rounding on the bits: a BF16 is the top half of an FP32, so
+    // adding a 16-bit variate to the magnitude and keeping the top half rounds
+    // it up with probability equal to the dropped fraction.  Inf / NaN: round
+    // to nearest.
     __device__ __forceinline__ static __nv_bfloat16 enc_dither(float v, float, float winv, uint32_t r16) {
         const float x = v * winv - 1.0f;
-        const __nv_bfloat16 lo = __float2bfloat16_rd(x), hi = __float2bfloat16_ru(x);
-        const float flo = __bfloat162float(lo), fhi = __bfloat162float(hi);
-        if (!(fhi > flo)) return lo;
-        return (float)r16 * (1.0f / 65536.0f) * (fhi - flo) < x - flo ? hi : lo;
+        const uint32_t b = __float_as_uint(x);
+        if ((b & 0x7f800000u) == 0x7f800000u) return __float2bfloat16_rn(x);
+        return __ushort_as_bfloat16((unsigned short)((b + r16) >> 16));
     }
 };
 // integer hash for the dither (a 32-bit avalanche mixer)
