@@ -224,6 +224,17 @@ int mflbm_init_flow(mflbm_context* ctx, const void* rho, const void* u,
  * relaxing that moment in the first steps -- the warm start's fill. */
 int mflbm_init_flow_mrt(mflbm_context* ctx, const void* rho, const void* u,
                         const void* v, const void* w);
+/* No counterpart in the reference: the warm start's fill from a prediction
+ * in the U-Net's output format, formed on the device.  y: host array of
+ * nx*ny*nz*4 floats (x fastest, 4 values per node): u nu/g, v nu/g, w nu/g
+ * and (rho - <rho>)/(3 g), each divided by scales[c].  Fluid nodes get
+ * u = y scale g/nu and rho = 1 + 3 g y scale, solid nodes rest; the halo
+ * layers repeat the opposite interior layer along periodic y (jper) and z
+ * (kper) and rest elsewhere; FP32 arithmetic (g/nu and 3 g rounded to
+ * FP32).  Then the equilibrium fill of mflbm_init_flow (mrt = 0) or
+ * mflbm_init_flow_mrt (mrt = 1). */
+int mflbm_init_flow_predicted(mflbm_context* ctx, const float* y, double nu, double g,
+                              const float* scales, int mrt);
 
 /* Reference: MemAllocate_multi_GPU(1) (src/Init_multiphase_GPU.cu:73-104):
  * upload a full host state.  Any pointer except pdf and phi may be NULL

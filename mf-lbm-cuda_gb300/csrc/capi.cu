@@ -1,5 +1,6 @@
 // The C ABI of libmflbm (include/mflbm.h).
 #include <algorithm>
+#include <cmath>
 #include <atomic>
 #include <cstring>
 #include <string>
@@ -807,6 +808,26 @@ static int init_flow_entry(mflbm_context* c, const void* rho, const void* u, con
         dev[a] = dst;
     }
     if ((rc = init_flow(*c, dev[0], dev[1], dev[2], dev[3], mrt)) != MFLBM_OK) return rc;
+    MFLBM_CUDA(cudaStreamSynchronize(c->stream));
+    c->d.arrays_stale = true;
+    return request_full_pass(c);
+}
+
+int mflbm_init_flow_predicted(mflbm_context* c, const float* y, double nu, double g, const float* scales, int mrt) {
+    if (!c || !y || !scales) return fail(MFLBM_E_ARG, "mflbm_init_flow_predicted: null argument");
+    if (!c->have_fields)
+        return fail(MFLBM_E_STATE, "mflbm_init_flow_predicted needs phi (mflbm_init_fields or mflbm_upload_fields first)");
+    if (!(nu > 0) || !std::isfinite(g)) return fail(MFLBM_E_ARG, "mflbm_init_flow_predicted: nu must be > 0, g finite");
+    const Grid& gr = c->d.g;
+    int rc = ensure_staging(c);
+    if (rc != MFLBM_OK) return rc;
+    // the staging buffer (38 n1 values) holds the prediction (4 floats per
+    // interior node) and, 256-byte aligned after it, the four fields
+    const size_t ybytes = sizeof(float) * 4 * (size_t)gr.n0();
+    float* ydev = (float*)c->d.staging;
+    void* work = (char*)c->d.staging + ((ybytes + 255) / 256) * 256;
+    MFLBM_CUDA(cudaMemcpyAsync(ydev, y, ybytes, cudaMemcpyHostToDevice, c->stream));
+    if ((rc = init_flow_predicted(*c, ydev, nu, g, scales, mrt ? 1 : 0, work)) != MFLBM_OK) return rc;
     MFLBM_CUDA(cudaStreamSynchronize(c->stream));
     c->d.arrays_stale = true;
     return request_full_pass(c);

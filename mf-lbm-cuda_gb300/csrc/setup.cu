@@ -366,6 +366,53 @@ int init_flow_t(mflbm_context& c, const void* rho, const void* u, const void* v,
     return MFLBM_OK;
 }
 
+// Warm-start fields from a prediction in the network's output format (no
+// counterpart in the reference): y holds, per interior node (x fastest, 4
+// values per node), u nu/g, v nu/g, w nu/g and (rho - <rho>)/(3g), each
+// divided by its scale.  A fluid node gets u = (y * scale) * (g/nu) and
+// rho = 1 + (3g) * (y * scale); a solid node rests (rho = 1, u = 0).  Halo
+// nodes of [0, n+1]^3 repeat the opposite interior layer along periodic
+// axes (y: jper, z: kper) and rest elsewhere.  The prediction is FP32, and so
+// is the arithmetic: the constants g/nu and 3g rounded to FP32, each product
+// and sum rounded (no contraction), the result widened to T.
+template <class T>
+__global__ void predicted_fields_kernel(Grid g, const int32_t* __restrict__ walls, const float* __restrict__ y,
+                                        float4 sc, float c_u, float c_rho, int per_y, int per_z, T* rho, T* u, T* v,
+                                        T* w) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+    if (i > g.nx + 1) return;
+    const ll o = g.s1(i, j, k);
+    int jj = j, kk = k;
+    bool rest = i == 0 || i == g.nx + 1;
+    if (j == 0 || j == g.ny + 1) { if (per_y) jj = j == 0 ? g.ny : 1; else rest = true; }
+    if (k == 0 || k == g.nz + 1) { if (per_z) kk = k == 0 ? g.nz : 1; else rest = true; }
+    if (rest || walls[g.s2(i, jj, kk)] != 0) {
+        rho[o] = T(1); u[o] = T(0); v[o] = T(0); w[o] = T(0);
+        return;
+    }
+    const float* p = y + 4 * ((i - 1) + (ll)g.nx * ((jj - 1) + (ll)g.ny * (kk - 1)));
+    u[o] = (T)__fmul_rn(__fmul_rn(p[0], sc.x), c_u);
+    v[o] = (T)__fmul_rn(__fmul_rn(p[1], sc.y), c_u);
+    w[o] = (T)__fmul_rn(__fmul_rn(p[2], sc.z), c_u);
+    rho[o] = (T)__fadd_rn(1.0f, __fmul_rn(c_rho, __fmul_rn(p[3], sc.w)));
+}
+
+// the fields into `work` (4 arrays of n1 T), then the equilibrium fill
+template <class T, class E>
+int init_flow_predicted_t(mflbm_context& c, const float* y, double nu, double gf, const float* scales, int mrt,
+                          void* work) {
+    const Grid g = c.d.g;
+    T* f = (T*)work;
+    const ll n1 = g.n1();
+    const float4 sc = make_float4(scales[0], scales[1], scales[2], scales[3]);
+    predicted_fields_kernel<T><<<dim3(grid_for(g.nx + 2, 128), g.ny + 2, g.nz + 2), 128, 0, c.stream>>>(
+        g, c.d.walls, y, sc, (float)(gf / nu), (float)(3.0 * gf), c.params.jper != 0, c.params.kper != 0, f, f + n1,
+        f + 2 * n1, f + 3 * n1);
+    int rc = after_launch("predicted_fields");
+    if (rc != MFLBM_OK) return rc;
+    return init_flow_t<T, E>(c, f, f + n1, f + 2 * n1, f + 3 * n1, mrt);
+}
+
 // ---------------------------------------------------------------------------
 // FP64 monitor reductions (quantities of src/Monitor.cpp:17-140, 472-495)
 // over the fluid-node list, on post-even populations: per-block partials with
@@ -815,6 +862,10 @@ int preprocess_geometry(mflbm_context& c, const int32_t* walls_global, int iper)
 int init_fields(mflbm_context& c, int option, double z0) { return MFLBM_POP(init_fields_t, c, option, z0); }
 int init_flow(mflbm_context& c, const void* rho, const void* u, const void* v, const void* w, int mrt) {
     return MFLBM_POP(init_flow_t, c, rho, u, v, w, mrt);
+}
+int init_flow_predicted(mflbm_context& c, const float* y, double nu, double g, const float* scales, int mrt,
+                        void* work) {
+    return MFLBM_POP(init_flow_predicted_t, c, y, nu, g, scales, mrt, work);
 }
 
 int monitor(mflbm_context& c, int nex_in, int nex_out, mflbm_monitor* out) {

@@ -6,6 +6,10 @@ namespace mflbm {
 int preprocess_geometry(mflbm_context& c, const int32_t* walls_global_host, int iper);
 int init_fields(mflbm_context& c, int option, double z0);
 int init_flow(mflbm_context& c, const void* rho, const void* u, const void* v, const void* w, int mrt);
+// the fill from a normalised prediction y (device, nx*ny*nz*4 floats); work:
+// device space for 4 arrays of n1 values of the context's precision
+int init_flow_predicted(mflbm_context& c, const float* y, double nu, double g, const float* scales, int mrt,
+                        void* work);
 int monitor(mflbm_context& c, int nex_in, int nex_out, mflbm_monitor* out);
 // per-slice monitor sums and the extra monitor scalars
 int monitor_profile(mflbm_context& c, double* slices, mflbm_monitor_ext* ext, bool track_phi);

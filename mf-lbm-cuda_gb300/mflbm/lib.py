@@ -59,6 +59,7 @@ SIGNATURES = {
     "mflbm_read_checkpoint": (I, [VP, C.c_char_p, VP, C.POINTER(I)]),
     "mflbm_init_flow": (I, [VP, VP, VP, VP, VP]),
     "mflbm_init_flow_mrt": (I, [VP, VP, VP, VP, VP]),
+    "mflbm_init_flow_predicted": (I, [VP, VP, C.c_double, C.c_double, VP, I]),
     "mflbm_unet_create": (I, [I, I, I, C.c_ulonglong, C.POINTER(VP)]),
     "mflbm_unet_destroy": (I, [VP]),
     "mflbm_unet_param_count": (I, [VP, C.POINTER(LL)]),
@@ -213,6 +214,17 @@ class Context:
                 raise ValueError(f"init_flow: expected {n} values per field, got {f.size}")
         fn = self.lib.mflbm_init_flow_mrt if mrt else self.lib.mflbm_init_flow
         check(fn(self.h, *[ptr(f) for f in a]), "mflbm_init_flow")
+
+    def init_flow_predicted(self, y, nu, g, scales, mrt=True):
+        """mflbm_init_flow_predicted: the equilibrium fill from a normalised
+        prediction y [nz, ny, nx, 4] (float32), formed on the device."""
+        L = self.L
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        if y.shape != (L.nz, L.ny, L.nx, 4):
+            raise ValueError(f"init_flow_predicted: expected shape {(L.nz, L.ny, L.nx, 4)}, got {y.shape}")
+        sc = np.ascontiguousarray(scales, dtype=np.float32)
+        check(self.lib.mflbm_init_flow_predicted(self.h, ptr(y), float(nu), float(g), ptr(sc), int(bool(mrt))),
+              "mflbm_init_flow_predicted")
 
     def step(self, ntime):
         check(self.lib.mflbm_step(self.h, int(ntime)), "mflbm_step")

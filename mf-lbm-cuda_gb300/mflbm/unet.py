@@ -169,26 +169,14 @@ def flow_target(ctx, walls_global, nu, g):
 
 
 def fill_from_prediction(ctx, y, walls_global, nu, g, scales, mrt=True):
-    """Equilibrium populations from a normalised prediction y [nz, ny, nx, 4];
-    velocity zero in solids, halos periodic in y and z.  mrt: the collision's
-    own equilibrium (mflbm_init_flow_mrt), else the reference's a17 formula
-    with the lattice weights (mflbm_init_flow)."""
-    L = ctx.L
-    nx, ny, nz = L.nx, L.ny, L.nz
-    solid = (np.asarray(walls_global).reshape(nz, ny, nx) != 0)
-    phys = y * np.asarray(scales, np.float32)
-    c = g / nu
-    fields = []
-    for a in range(3):
-        f = np.where(solid, 0.0, phys[..., a] * c)
-        fields.append(f)
-    fields.insert(0, np.where(solid, 1.0, 1.0 + 3.0 * g * phys[..., 3]))
-
-    def halo(f, fill):
-        p = np.pad(f, ((1, 1), (1, 1), (0, 0)), mode="wrap")        # z, y periodic
-        return np.pad(p, ((0, 0), (0, 0), (1, 1)), constant_values=fill)
-    rho, u, v, w = halo(fields[0], 1.0), halo(fields[1], 0.0), halo(fields[2], 0.0), halo(fields[3], 0.0)
-    ctx.init_flow(rho, u, v, w, mrt=mrt)
+    """Equilibrium populations from a normalised prediction y [nz, ny, nx, 4]:
+    velocity zero in solids, halos periodic along the context's periodic
+    axes, formed on the device (mflbm_init_flow_predicted).  mrt: the
+    collision's own equilibrium (as mflbm_init_flow_mrt), else the
+    reference's a17 formula with the lattice weights (as mflbm_init_flow).
+    walls_global is not needed (the context holds the walls); it is kept
+    for the callers' symmetry with features()."""
+    ctx.init_flow_predicted(y, nu, g, scales, mrt=mrt)
 
 
 def predicted_permeability(y, scales, nx, ny, nz):

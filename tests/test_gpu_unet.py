@@ -210,3 +210,46 @@ def test_features_reject_uniform_geometry(mflbm_lib):
     from mflbm import lib
     with pytest.raises(lib.MflbmError, match="both solid and fluid"):
         unet.features(np.zeros((8, 8, 8), np.int32), (8, 8, 8))
+
+
+def _host_fields(y, walls_global, shape, nu, g, scales):
+    """The warm-start fields of a normalised prediction, restated in numpy
+    (periodic y and z halos, resting x halos): the formula of
+    mflbm_init_flow_predicted, in FP32 (numpy keeps a float32 array float32
+    against Python scalars, which it rounds to float32)."""
+    nx, ny, nz = shape
+    solid = (np.asarray(walls_global).reshape(nz, ny, nx) != 0)
+    phys = y * np.asarray(scales, np.float32)
+    c = g / nu
+    fields = [np.where(solid, 1.0, 1.0 + 3.0 * g * phys[..., 3])]
+    fields += [np.where(solid, 0.0, phys[..., a] * c) for a in range(3)]
+
+    def halo(f, fill):
+        p = np.pad(f, ((1, 1), (1, 1), (0, 0)), mode="wrap")
+        return np.pad(p, ((0, 0), (0, 0), (1, 1)), constant_values=fill)
+    return [halo(fields[0], 1.0)] + [halo(f, 0.0) for f in fields[1:]]
+
+
+# The device fill from a prediction equals the host formula followed by
+# mflbm_init_flow(_mrt), byte for byte, in FP32 and FP64 (a 24 x 24 x 32
+# permeability sample, periodic in y and z).
+@pytest.mark.parametrize("precision", ["f32", "f64"])
+@pytest.mark.parametrize("mrt", [False, True])
+def test_predicted_fill_matches_host_formula(mflbm_lib, precision, mrt):
+    from mflbm import abi, cases, lib
+    prec = abi.MFLBM_FP32 if precision == "f32" else abi.MFLBM_FP64
+    case = cases.permeability_sample(16, 0.55, 11, body_force=1e-4)
+    case.keys.update({"nxGlobal": 24, "nyGlobal": 24, "nzGlobal": 32})
+    nx, ny, nz = case.shape
+    rng = np.random.default_rng(4)
+    y = rng.normal(size=(nz, ny, nx, 4)).astype(np.float32)
+    scales = np.array([0.8, 0.8, 2.1, 6.0], np.float32)
+    nu, g = 1.0 / 6.0, 1e-4
+    dev, info = lib.setup_case(case, prec, abi.MFLBM_FAST)
+    host, _ = lib.setup_case(case, prec, abi.MFLBM_FAST)
+    dev.init_flow_predicted(y, nu, g, scales, mrt=mrt)
+    host.init_flow(*_host_fields(y, info["walls_global"], (nx, ny, nz), nu, g, scales), mrt=mrt)
+    a, b = dev.download(("pdf",))["pdf"], host.download(("pdf",))["pdf"]
+    assert a.tobytes() == b.tobytes()
+    dev.close()
+    host.close()
