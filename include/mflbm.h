@@ -464,7 +464,7 @@ int mflbm_unet_conv_check(int D, int H, int W, int cin, int cout, const float* x
                           float* y, float* gx, float* gw, float* gb);
 /* Network inputs of a pore geometry (no counterpart in the reference):
  * walls nz*ny*nx (x fastest, non-zero = solid, at least one solid and one
- * fluid voxel); x nz*ny*nx*2: the solid mask (1 / 0) and the signed
+ * fluid voxel, fewer than 2^31 voxels); x nz*ny*nx*2: the solid mask (1 / 0) and the signed
  * Euclidean distance between voxel centres to the nearest voxel of the other
  * kind (positive in the fluid, negative in solids), times sdf_scale.  Bit 0,
  * 1, 2 of periodic_xyz make x, y, z periodic (distances by the minimum

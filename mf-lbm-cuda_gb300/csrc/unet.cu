@@ -635,8 +635,9 @@ int mflbm_unet_features(const int32_t* walls, int nx, int ny, int nz, int period
     if (!walls || !x) return fail(MFLBM_E_ARG, "mflbm_unet_features: null argument");
     if (nx < 1 || ny < 1 || nz < 1 || nx > 4096 || ny > 4096 || nz > 4096)
         return fail(MFLBM_E_ARG, "mflbm_unet_features: extents must be in [1, 4096]");
-    const U::Dims d{nz, ny, nx};
     const size_t V = (size_t)nx * ny * nz;
+    if (V >= (size_t)1 << 31) return fail(MFLBM_E_ARG, "mflbm_unet_features: at most 2^31 - 1 voxels");
+    const U::Dims d{nz, ny, nx};
     size_t solids = 0;
     for (size_t i = 0; i < V; ++i) solids += walls[i] != 0;
     if (solids == 0 || solids == V)
