@@ -154,16 +154,16 @@ template <> struct PopCodec<float, __half> {
     // binade's value).  Half-subnormal range (|x| < 2^-14, spacing 2^-24):
     // |x| * 2^40 (exact) plus a 16-bit variate, shifted down by 16, is the
     // subnormal's integer mantissa, which is also its bit pattern (1024 gives
-    // 2^-14).  At or above the largest half: round to nearest.
+    // 2^-14).  Both are formed and one is selected (values of a warp straddle
+    // 2^-14, so a branch would run both anyway); at or above the largest half
+    // the truncation saturates at 65504.
     __device__ __forceinline__ static __half enc_dither(float v, float, float winv, uint32_t r16) {
         const float x = v * winv - 1.0f;
         const uint32_t b = __float_as_uint(x), mag = b & 0x7fffffffu;
-        if (mag < 0x38800000u) {
-            const uint32_t t = (uint32_t)(__uint_as_float(mag) * 1099511627776.0f);
-            return __ushort_as_half((unsigned short)(((b >> 16) & 0x8000u) | ((t + r16) >> 16)));
-        }
-        if (mag >= 0x477fe000u) return __float2half_rn(x);
-        return __float2half_rz(__uint_as_float(b + (r16 >> 3)));
+        const uint32_t t = (uint32_t)(__uint_as_float(min(mag, 0x387fffffu)) * 1099511627776.0f);
+        const unsigned short hs = (unsigned short)(((b >> 16) & 0x8000u) | ((t + r16) >> 16));
+        const unsigned short hn = __half_as_ushort(__float2half_rz(__uint_as_float(b + (r16 >> 3))));
+        return __ushort_as_half(mag < 0x38800000u ? hs : hn);
     }
 };
 template <> struct PopCodec<float, __nv_bfloat16> {

@@ -18,10 +18,10 @@ def half_sr(x, r16):
         t = np.uint32(np.float32(np.uint32(mag).view(np.float32)) * np.float32(1099511627776.0))
         bits = ((b >> np.uint32(16)) & np.uint32(0x8000)) | ((t + r16) >> np.uint32(16))
         return bits.astype(np.uint16).view(np.float16)
-    if mag >= 0x477FE000:
-        return np.full(r16.shape, np.float16(x))
     b2 = (b + (r16 >> np.uint32(3))) & np.uint32(0xFFFFE000)      # rz: drop the 13 low bits
-    return b2.view(np.float32).astype(np.float16)                  # exactly representable now
+    with np.errstate(over="ignore"):
+        h = b2.view(np.float32).astype(np.float16)                 # exactly representable below 65520
+    return np.where(np.isinf(h), np.copysign(np.float16(65504), h), h)   # rz saturates
 
 
 def bf16_sr(x, r16):
