@@ -103,3 +103,23 @@ def test_invalid_input_is_rejected_with_a_message(mflbm_lib):
     p.nx = 2000
     assert mflbm_lib.mflbm_create(C.byref(p), C.byref(h)) == -1
     assert not h.value
+
+
+def test_warm_start_entries_reject_bad_arguments_before_device_work(mflbm_lib):
+    """mflbm_unet_features and mflbm_init_flow_predicted check their
+    arguments on the host (no device is touched for these calls)."""
+    import numpy as np
+    from mflbm.abi import ptr
+    x = np.empty((4, 4, 4, 2), np.float32)
+    fluid = np.zeros((4, 4, 4), np.int32)
+    assert mflbm_lib.mflbm_unet_features(None, 4, 4, 4, 0, C.c_float(0.125), ptr(x)) == -1
+    assert b"null argument" in mflbm_lib.mflbm_last_error()
+    assert mflbm_lib.mflbm_unet_features(ptr(fluid), 0, 4, 4, 0, C.c_float(0.125), ptr(x)) == -1
+    assert b"extents" in mflbm_lib.mflbm_last_error()
+    assert mflbm_lib.mflbm_unet_features(ptr(fluid), 4, 4, 4, 0, C.c_float(0.125), ptr(x)) == -1
+    assert b"both solid and fluid" in mflbm_lib.mflbm_last_error()
+    assert mflbm_lib.mflbm_unet_features(ptr(fluid), 4096, 4096, 4096, 0, C.c_float(0.125), ptr(x)) == -1
+    assert b"2^31" in mflbm_lib.mflbm_last_error()
+    y = np.zeros(4, np.float32)
+    assert mflbm_lib.mflbm_init_flow_predicted(None, ptr(y), 1.0 / 6.0, 1e-4, ptr(y), 1) == -1
+    assert b"null argument" in mflbm_lib.mflbm_last_error()
