@@ -179,9 +179,12 @@ def fill_from_prediction(ctx, y, walls_global, nu, g, scales, mrt=True):
     ctx.init_flow_predicted(y, nu, g, scales, mrt=mrt)
 
 
-def predicted_permeability(y, scales, nx, ny, nz):
-    """k of the predicted field: the mean of u_z nu / g over (nx - 2) ny nz."""
-    return float(y[..., 2].astype(np.float64).sum() * scales[2] / ((nx - 2) * ny * nz))
+def predicted_permeability(y, scales, nx, ny, nz, walls_global):
+    """k of the predicted field: the sum of u_z nu / g over the fluid voxels
+    (walls_global == 0; the network's outputs at solid voxels are not
+    trained and the fill sets them to rest) divided by (nx - 2) ny nz."""
+    fluid = np.asarray(walls_global).reshape(nz, ny, nx) == 0
+    return float(y[..., 2].astype(np.float64)[fluid].sum() * scales[2] / ((nx - 2) * ny * nz))
 
 
 # ---------------------------------------------------------------------------

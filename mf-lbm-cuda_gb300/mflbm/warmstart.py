@@ -238,7 +238,7 @@ def evaluate(ws, case, tol, interval, max_steps, fallback, storage=abi.MFLBM_STO
         nonlocal k_pred
         if how == "warm":
             y = ws.predict(case, walls)
-            k_pred = unet.predicted_permeability(y, ws.scales, nx, ny, nz)
+            k_pred = unet.predicted_permeability(y, ws.scales, nx, ny, nz, walls)
             unet.fill_from_prediction(ctx, y, walls, nu, g, ws.scales)
         elif how == "oracle":
             unet.fill_from_prediction(ctx, t_ref / ws.scales, walls, nu, g, ws.scales)
