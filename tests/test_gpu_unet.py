@@ -87,8 +87,11 @@ def _check_conv(shape, cin, cout, relu):
     assert np.all(np.abs(gx - gx_ref) <= 2 ** -8 * np.abs(gx_ref) + 2e-5 * gx_scale + 1e-6)
 
 
-def test_network_gradients_match_oracle(mflbm_lib):
-    D = 16
+# 16^3: every convolution on the gather kernels; 64^3 (the training size of
+# the warm-start study): levels 0 and 1 on the halo-tiled kernels (at least
+# one tile per multiprocessor), forward and data gradients.
+@pytest.mark.parametrize("D", [16, 64])
+def test_network_gradients_match_oracle(mflbm_lib, D):
     rng = np.random.default_rng(7)
     net = unet.UNet(D, D, D, seed=3)
     assert net.n_params == UO.param_count()
@@ -104,14 +107,18 @@ def test_network_gradients_match_oracle(mflbm_lib):
     loss_ref, g_ref = UO.loss_and_gradients(p, x, t, m)
     assert abs(loss - loss_ref) <= 1e-3 * loss_ref
     o = 0
+    errs = []
     for li, (ci, co, _) in enumerate(UO.layer_shapes()):
         n = co * 27 * ci + co
         a, r = g[o:o + n].astype(np.float64), g_ref[o:o + n].astype(np.float64)
         o += n
         err = np.linalg.norm(a - r) / max(np.linalg.norm(r), 1e-30)
-        assert err <= 3e-2, (li, err)
+        errs.append(err)
     y = net.forward(x)
     y_ref, _, _ = UO.forward(p, x)
+    print("layer gradient errors", [round(e, 4) for e in errs],
+          "forward", float(np.max(np.abs(y - y_ref)) / np.max(np.abs(y_ref))))
+    assert max(errs) <= 3e-2, errs
     assert np.max(np.abs(y - y_ref)) <= 2e-2 * np.max(np.abs(y_ref))
     net.close()
 
