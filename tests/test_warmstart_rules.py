@@ -59,3 +59,22 @@ def test_record_run_falls_back_and_restarts_the_window(scripted):
     assert steps - fell >= 500
     # the record after the fallback is the cold start's from its own step 50
     assert dict(traj)[550] == pytest.approx(1.0 - 0.5 ** 0.5)
+
+
+def test_predicted_permeability_sums_fluid_voxels_only():
+    """The network's outputs at solid voxels are untrained (the loss masks
+    them) and the fill sets them to rest: they must not enter the predicted
+    permeability."""
+    import numpy as np
+    from mflbm import unet
+    nx, ny, nz = 6, 4, 5
+    walls = np.zeros((nz, ny, nx), np.int32)
+    walls[:, :, 0] = walls[:, :, -1] = 1          # the x walls
+    walls[2, 1, 3] = 1                             # one grain voxel
+    y = np.zeros((nz, ny, nx, 4), np.float32)
+    y[..., 2] = 0.5
+    y[walls != 0, 2] = 1e6                         # garbage where the network is not trained
+    scales = np.array([1, 1, 2, 1], np.float32)
+    k = unet.predicted_permeability(y, scales, nx, ny, nz, walls)
+    fluid = int((walls == 0).sum())
+    assert k == pytest.approx(0.5 * 2 * fluid / ((nx - 2) * ny * nz))
